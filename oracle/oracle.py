@@ -1,0 +1,239 @@
+"""ctypes binding of the AO-path oracle (test infrastructure only).
+
+Loads ``oracle/librn_oracle.so`` (the C restatement in ``rn_oracle.c``) and, where it was
+built, ``oracle/_ref/libref_ao.so`` (the reference's own sources). Only the tests, the
+smoke check and the benchmark's CPU-baseline leg import this module: it is the checker,
+never the thing measured or shipped.
+
+File encodings follow src/core/image.cpp:34-106 of the reference: ``Pf`` PFM with rows
+bottom-to-top, the coverage mask as P5 PGM 255/0, and 8-bit previews ``v*255+0.5``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "librn_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref_ao.so")
+
+# The CLI's fixed sampling (raw/renderer/render.hpp:25-27) and its default camera
+# (raw/tools/cli_params.hpp:16-21).
+RT_SAMPLES, SS_SAMPLES, AO_RADIUS, TOLERANCE = 64, 24, 2.0, 0.12
+DEFAULT_CAMERA = (4.0, 4.0, 6.0, 0.0, 1.0, 0.0, 0.0, 1.0, 0.0, 0.9)
+
+_F = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_U8 = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_I32 = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_U64 = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+
+
+def build(with_ref: bool | None = None) -> None:
+    """Compile the oracle (and the reference harness when the raw-native tree exists)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    ref_dir = os.environ.get("RN_REFERENCE_DIR", "/root/reference")
+    if with_ref is None:
+        with_ref = os.path.isdir(os.path.join(ref_dir, "src", "renderer"))
+    if with_ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_dir}"], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build(with_ref=False)
+        L = C.CDLL(LIB)
+        L.rno_hash01.restype = C.c_float
+        L.rno_hash01.argtypes = [C.c_uint32] * 3
+        L.rno_intersect.argtypes = [_F, _F, C.POINTER(C.c_float)]
+        L.rno_accel_build.restype = C.c_void_p
+        L.rno_accel_build.argtypes = [_F, C.c_int]
+        L.rno_accel_free.argtypes = [C.c_void_p]
+        L.rno_accel_nodes.argtypes = [C.c_void_p]
+        L.rno_occluded.argtypes = [C.c_void_p, _F, C.c_float]
+        L.rno_occluded_scan.argtypes = [_F, C.c_int, _F, C.c_float]
+        L.rno_trace.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_void_p, _F, C.c_int, C.c_int,
+                                C.c_float, C.c_void_p, C.c_int, _F, C.c_void_p, C.c_void_p,
+                                C.c_int, C.c_int, C.c_int]
+        L.rno_ssao.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_int, C.c_float, _F, C.c_int]
+        L.rno_reconcile.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_float, _F,
+                                    C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int), C.POINTER(C.c_double)]
+        L.rno_test_scene.restype = C.c_int
+        L.rno_test_scene.argtypes = [_F, _F, _F]
+        L.rno_rasterize.argtypes = [_F, _F, C.c_int, _F, C.c_int, C.c_int, _F, _F, _F, _U8]
+        L.rno_morton_keys.argtypes = [_F, C.c_int, _U64]
+        L.rno_ploc_build.restype = C.c_int
+        L.rno_ploc_build.argtypes = [_F, C.c_int, C.c_int, _I32, C.POINTER(C.c_uint32)]
+        L.rno_tree_hash.restype = C.c_uint64
+        L.rno_tree_hash.argtypes = [_I32, C.c_int]
+        L.rno_soup.argtypes = [C.c_int, C.c_uint64, _F]
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def ref() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        R = C.CDLL(REF_LIB)
+        R.ref_render_default.argtypes = [C.c_int, C.c_int, _F, C.c_int, C.c_float, C.c_int, C.c_float,
+                                         C.c_int, _F, _F, _U8, _F, _F, _F, _F, _F, _F]
+        R.ref_trace.argtypes = [C.c_int, C.c_int, _F, _F, _U8, _F, C.c_int, C.c_int, C.c_float,
+                                C.c_void_p, _F, C.c_void_p, C.c_void_p, C.c_int]
+        R.ref_ssao.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_int, C.c_float, _F, C.c_int]
+        R.ref_reconcile.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_float, _F, _F]
+        R.ref_ploc.restype = C.c_int
+        R.ref_ploc.argtypes = [_F, C.c_int, C.c_int, _I32, C.POINTER(C.c_uint32)]
+        _ref = R
+    return _ref
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+# ---------------------------------------------------------------- scene and G-buffer
+def test_scene():
+    """The built-in scene (src/scene/scene.cpp:18-32): tris (14, 9), corner normals, light."""
+    tris = np.zeros((14, 9), np.float32)
+    nrm = np.zeros((14, 9), np.float32)
+    light = np.zeros(3, np.float32)
+    n = lib().rno_test_scene(tris, nrm, light)
+    return tris[:n], nrm[:n], light
+
+
+def rasterize(tris, nrm, cam, w: int, h: int):
+    """G-buffer (depth, position (h,w,3), normal (h,w,3), mask (h,w) u8) of a triangle list."""
+    tris, nrm = _f32(tris).reshape(-1, 9), _f32(nrm).reshape(-1, 9)
+    depth = np.empty((h, w), np.float32)
+    pos = np.empty((h, w, 3), np.float32)
+    nr = np.empty((h, w, 3), np.float32)
+    mask = np.empty((h, w), np.uint8)
+    lib().rno_rasterize(tris, nrm, len(tris), _f32(cam), w, h, depth, pos, nr, mask)
+    return depth, pos, nr, mask
+
+
+# ---------------------------------------------------------------- the three passes
+def trace(pos, nrm, mask, tris, spp, radius, to_light=None, accel="bvh", threads=1,
+          row0=0, row_stride=1):
+    """computeRTAO (to_light None) or computeRTVisibility; returns ao or (ao, sky, sun)."""
+    pos, nrm = _f32(pos), _f32(nrm)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    tris = _f32(tris).reshape(-1, 9)
+    h, w = mask.shape
+    ao = np.zeros((h, w), np.float32)
+    sky = np.zeros((h, w), np.float32) if to_light is not None else None
+    sun = np.zeros((h, w), np.float32) if to_light is not None else None
+    L = lib()
+    handle = L.rno_accel_build(tris, len(tris)) if accel == "bvh" else None
+    tl = _f32(to_light) if to_light is not None else None
+    try:
+        L.rno_trace(w, h, pos, nrm, mask, handle, tris, len(tris), int(spp), float(radius),
+                    _ptr(tl), 0, ao, _ptr(sky), _ptr(sun), int(threads), int(row0), int(row_stride))
+    finally:
+        if handle:
+            L.rno_accel_free(handle)
+    return ao if to_light is None else (ao, sky, sun)
+
+
+def ssao(pos, nrm, mask, samples=SS_SAMPLES, radius=AO_RADIUS, threads=1):
+    mask = np.ascontiguousarray(mask, np.uint8)
+    h, w = mask.shape
+    out = np.zeros((h, w), np.float32)
+    lib().rno_ssao(w, h, _f32(pos), _f32(nrm), mask, int(samples), float(radius), out, int(threads))
+    return out
+
+
+def reconcile(approx, truth, mask, tolerance=TOLERANCE):
+    """(error map, dict(rmse, maxError, pixels, within, sumSq))."""
+    mask = np.ascontiguousarray(mask, np.uint8)
+    h, w = mask.shape
+    err = np.zeros((h, w), np.float32)
+    rmse, mx, s = C.c_float(), C.c_float(), C.c_double()
+    n, within = C.c_int(), C.c_int()
+    lib().rno_reconcile(w, h, _f32(approx), _f32(truth), mask, float(tolerance), err,
+                        C.byref(rmse), C.byref(mx), C.byref(n), C.byref(within), C.byref(s))
+    return err, dict(rmse=rmse.value, maxError=mx.value, pixels=n.value, within=bool(within.value),
+                     sumSq=s.value)
+
+
+# ---------------------------------------------------------------- PLOC
+def ploc(tris, radius=16):
+    """(nodes (2n-1, 9) int32, root, rounds) as rt::buildPloc builds them."""
+    tris = _f32(tris).reshape(-1, 9)
+    n = len(tris)
+    nodes = np.zeros((max(2 * n - 1, 1), 9), np.int32)
+    rounds = C.c_uint32()
+    root = lib().rno_ploc_build(tris, n, int(radius), nodes, C.byref(rounds))
+    return nodes, root, rounds.value
+
+
+def morton_keys(tris):
+    tris = _f32(tris).reshape(-1, 9)
+    keys = np.zeros(len(tris), np.uint64)
+    lib().rno_morton_keys(tris, len(tris), keys)
+    return keys
+
+
+def tree_hash(nodes) -> str:
+    nodes = np.ascontiguousarray(nodes, np.int32)
+    return "%016x" % lib().rno_tree_hash(nodes, len(nodes))
+
+
+def soup(count: int, seed: int):
+    tris = np.zeros((count, 9), np.float32)
+    lib().rno_soup(count, seed, tris)
+    return tris
+
+
+# ---------------------------------------------------------------- file bytes and digests
+def pfm1_bytes(buf) -> bytes:
+    buf = np.asarray(buf, np.float32)
+    h, w = buf.shape
+    return b"Pf\n%d %d\n-1.0\n" % (w, h) + np.ascontiguousarray(buf[::-1]).astype("<f4").tobytes()
+
+
+def mask_pgm_bytes(mask) -> bytes:
+    mask = np.asarray(mask)
+    h, w = mask.shape
+    return b"P5\n%d %d\n255\n" % (w, h) + np.where(mask != 0, 255, 0).astype(np.uint8).tobytes()
+
+
+def pgm_bytes(buf) -> bytes:
+    buf = np.asarray(buf, np.float32)
+    h, w = buf.shape
+    v = (np.clip(buf, np.float32(0), np.float32(1)) * np.float32(255.0) + np.float32(0.5)).astype(np.uint8)
+    return b"P5\n%d %d\n255\n" % (w, h) + v.tobytes()
+
+
+def sha256(b: bytes) -> str:
+    return hashlib.sha256(b).hexdigest()
+
+
+def render_default(w, h, cam=DEFAULT_CAMERA, spp=RT_SAMPLES, radius=AO_RADIUS, ss_samples=SS_SAMPLES,
+                   tolerance=TOLERANCE, threads=1, accel="bvh"):
+    """The CLI's frame on the oracle: G-buffer, ao/sky/sun, SSAO, reconcile."""
+    tris, nrm9, light = test_scene()
+    _, pos, nrm, mask = rasterize(tris, nrm9, cam, w, h)
+    ao, sky, sun = trace(pos, nrm, mask, tris, spp, radius, to_light=-light, accel=accel, threads=threads)
+    ss = ssao(pos, nrm, mask, ss_samples, radius, threads)
+    err, st = reconcile(ss, ao, mask, tolerance)
+    return dict(tris=tris, pos=pos, nrm=nrm, mask=mask, ao=ao, sky=sky, sun=sun, ss=ss, err=err, stats=st,
+                light=light)
