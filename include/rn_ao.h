@@ -1,0 +1,169 @@
+/*
+ * rn_ao.h -- C ABI of the GB300 (sm_103a) ambient-occlusion path of raw-native.
+ *
+ * One shared library, librn_ao.so, replaces the CPU bodies of the reference's AO oracle
+ * ("raw-rt-ao-v1"), its screen-space AO pass and the reconcile between them. The C++ shim
+ * in raw-native_gb300/host/ implements the reference's own symbols (computeRTAO,
+ * computeRTVisibility, computeSSAO, reconcile, LinearAccel) over these entry points, so
+ * raw_native_cli and `raw_native_cli verify` run their AO passes on one GPU with no source
+ * change. Plain pointers and sizes only; no C++ or torch types cross this boundary.
+ *
+ * Conventions
+ *  - Every entry point returns an rn_code (0 = RN_OK) and, when `st` is not NULL, fills
+ *    it with the code and a one-line message. Nothing throws, nothing aborts, and there is
+ *    no CPU fallback: without a usable GPU every call returns RN_ERR_NO_DEVICE (the
+ *    reference maps "no device" to exit 4 and the verdict "unverifiable",
+ *    src/tools/gpu_run.cpp:52-59).
+ *  - Pointers are HOST pointers unless the call's flags include RN_DEVICE_PTRS, in which
+ *    case every buffer argument is a device pointer on the current device. Host calls copy
+ *    in, compute and copy out on the library's stream and return when the results are in
+ *    host memory. Device-pointer calls are asynchronous on the library's stream
+ *    (rn_set_stream) unless the call returns a host-side scalar result, in which case it
+ *    synchronizes that stream.
+ *  - Images are row-major, row 0 at the top, w * h pixels. A position or normal plane is
+ *    3 floats per pixel (x, y, z), as raw::Buffer<raw::Vec3> stores it
+ *    (raw/core/image.hpp:8-16). A mask is one byte per pixel, nonzero = covered.
+ *  - Triangles are 9 floats each (a, b, c), in the order raw::LinearAccel::build flattens
+ *    the scene's meshes (src/renderer/accel.cpp:13-25).
+ *  - The library keeps one process-wide device context (the reference's device is a
+ *    process singleton, src/renderer/gpu/gpu_renderer.cpp:72-77). Calls must come from one
+ *    host thread at a time.
+ */
+#ifndef RN_AO_H
+#define RN_AO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RN_AO_ABI_VERSION 1
+
+typedef enum rn_code {
+    RN_OK = 0,
+    RN_ERR_INVALID = 1,    /* bad argument: null pointer, size, spp, radius */
+    RN_ERR_NO_DEVICE = 2,  /* no CUDA device, or the device is not sm_103 */
+    RN_ERR_CUDA = 3,       /* a CUDA runtime call failed; message names it */
+    RN_ERR_NO_MEMORY = 4,  /* device or pinned-host allocation refused */
+    RN_ERR_OVERFLOW = 5,   /* a traversal stack or a build queue ran out of room */
+    RN_ERR_BUDGET = 6,     /* a device-side loop hit its iteration budget and gave up */
+    RN_ERR_STATE = 7       /* call sequence error (e.g. an accel from another context) */
+} rn_code;
+
+typedef struct rn_status {
+    int code;
+    char message[240];
+} rn_status;
+
+/* Flags shared by the entry points. */
+#define RN_DEVICE_PTRS  0x1   /* buffer arguments are device pointers */
+#define RN_SKY          0x2   /* rn_ao_visibility: also write sky (and sun) */
+#define RN_SUN_FORCED   0x4   /* rn_ao_visibility: sun = 1 everywhere (lighting v2-nosun) */
+#define RN_EXACT_TRIG   0x0   /* default: sample angles use the host libm's cosf/sinf bits */
+#define RN_DEVICE_TRIG  0x8   /* sample angles use the device sincosf alone (no calibration) */
+
+/* A G-buffer as the AO passes read it: raw::GBuffer's position, normal and mask planes
+ * (raw/renderer/gbuffer.hpp:7-21). */
+typedef struct rn_gbuf {
+    int w, h;
+    const float* position;   /* 3 floats per pixel */
+    const float* normal;     /* 3 floats per pixel */
+    const uint8_t* mask;     /* 1 byte per pixel */
+} rn_gbuf;
+
+/* The scalar half of raw::ReconcileResult (raw/cert/reconcile.hpp:6-11) plus the FP64 sum
+ * of squares it derives rmse from. */
+typedef struct rn_reconcile_result {
+    float rmse;
+    float max_error;
+    int32_t pixels;
+    int32_t within_tolerance;
+    double sum_sq;
+} rn_reconcile_result;
+
+/* Opaque occlusion accelerator: the GPU-built BVH over one triangle list. Replaces the
+ * heap Bvh inside raw::LinearAccel (raw/renderer/accel.hpp:15-23). */
+typedef struct rn_accel rn_accel;
+
+/* Library ABI version (RN_AO_ABI_VERSION). No counterpart in the reference. */
+int rn_ao_version(void);
+
+/* Open the process-wide context on the current CUDA device: checks for sm_103, creates the
+ * library stream and builds the sampler's angle table. Every other entry point calls it
+ * on first use; call it early to keep that set-up out of a timed region or a capture. */
+int rn_init(rn_status* st);
+
+/* Use `stream` (a cudaStream_t, NULL = the library's own) for all later work. */
+int rn_set_stream(void* stream, rn_status* st);
+
+/* Wait for all work queued on the library's stream. */
+int rn_synchronize(rn_status* st);
+
+/* Build the accelerator for `ntri` triangles (9 floats each). Replaces
+ * raw::LinearAccel::build + raw::Bvh::build (src/renderer/accel.cpp:13-25,
+ * src/renderer/bvh.cpp:35-92): on the GPU a PLOC binary tree (Morton codes, radix sort,
+ * nearest-neighbour merge rounds) collapsed into 4-wide nodes. ntri may be 0 (every ray
+ * is then open, as an empty Bvh answers). */
+int rn_accel_build(const float* tris, uint32_t ntri, int flags, rn_accel** out, rn_status* st);
+
+/* Release an accelerator (NULL is a no-op). */
+void rn_accel_free(rn_accel* accel);
+
+/* Node and triangle counts of an accelerator (for reports; any pointer may be NULL). */
+int rn_accel_info(const rn_accel* accel, uint32_t* wide_nodes, uint32_t* leaf_tris,
+                  uint32_t* ploc_rounds, rn_status* st);
+
+/* Ray-traced AO and lighting model 2's visibility from the same rays.
+ * Replaces raw::computeRTAO and raw::computeRTVisibility (raw/renderer/ray_ao.hpp:6-14,
+ * src/renderer/ray_ao.cpp:20-63): per covered pixel `spp` cosine-weighted hemisphere rays
+ * from p + 1e-3 n; ao = open / spp where open = no hit within `radius`. With RN_SKY also
+ * sky = free / spp (free = open and no hit at any distance) and sun = 1 when the ray
+ * towards normalize(to_light) hits nothing (or RN_SUN_FORCED). Uncovered pixels get 1.
+ * `sky` and `sun` may be NULL without RN_SKY; `to_light` is read only with RN_SKY. */
+int rn_ao_visibility(const rn_gbuf* g, const rn_accel* accel, int spp, float radius,
+                     const float* to_light, int flags, float* ao, float* sky, float* sun,
+                     rn_status* st);
+
+/* Screen-space AO. Replaces raw::computeSSAO (raw/renderer/ssao.hpp:5-6,
+ * src/renderer/ssao.cpp:11-39): `samples` taps within 6 pixels, occluded when
+ * 1e-4 <= |d| <= radius and n . d/|d| > 0.15; ao = max(0, 1 - occ/used), 1 when unused. */
+int rn_ssao(const rn_gbuf* g, int samples, float radius, int flags, float* ao_ss, rn_status* st);
+
+/* Reconcile an approximation against the truth over the mask. Replaces raw::reconcile
+ * (raw/cert/reconcile.hpp:12-13, src/cert/reconcile.cpp:4-21): err = |approx - truth| on
+ * covered pixels and 0 elsewhere; rmse = (float)sqrt(sum_sq / pixels) with sum_sq
+ * accumulated in FP64 (a fixed-order tile reduction; run-to-run deterministic);
+ * within = rmse <= tolerance. `err` may be NULL. The result is written to host memory. */
+int rn_reconcile(const float* approx, const float* truth, const uint8_t* mask, int w, int h,
+                 float tolerance, int flags, float* err, rn_reconcile_result* out, rn_status* st);
+
+/* The AO part of one CPU-reference frame in one call, the three passes of
+ * src/renderer/render.cpp:29-54 on one stream: visibility (ao, sky, sun), SSAO with the
+ * reconcile fused into its epilogue (error map, FP64 sum, max, count). Any of sky/sun/err
+ * may be NULL when not wanted (sky and sun need RN_SKY). */
+int rn_ao_frame(const rn_gbuf* g, const rn_accel* accel, int spp, float radius, int ss_samples,
+                float tolerance, const float* to_light, int flags, float* ao, float* sky,
+                float* sun, float* ao_ss, float* err, rn_reconcile_result* out, rn_status* st);
+
+/* The PLOC binary tree exactly as raw::rt::buildPloc builds it (raw/renderer/rt_bvh.hpp:45,
+ * src/renderer/rt_bvh.cpp:112-172), built on the GPU: nodes_out receives 2*ntri-1 nodes of
+ * 9 int32 {left, right, tri, bits(lo.x), bits(hi.x), bits(lo.y), bits(hi.y), bits(lo.z),
+ * bits(hi.z)} (leaves 0..n-1 in sorted order, then internal nodes in creation order).
+ * `tris` and `nodes_out` follow RN_DEVICE_PTRS; root and rounds are host pointers. */
+int rn_ploc_build(const float* tris, uint32_t ntri, int radius, int flags, int32_t* nodes_out,
+                  int32_t* root, uint32_t* rounds, rn_status* st);
+
+/* Any-hit queries for a list of rays through an accelerator: hit[i] = 1 when some
+ * triangle is hit at 1e-4 < t < t_max[i] (raw::rt::occluded / raw::Bvh::occluded,
+ * src/renderer/bvh.cpp:119-138). rays: 6 floats each (origin, direction). The ray-list
+ * mode of the rt_trace pass (src/renderer/gpu/shaders/rt.wgsl:306-446). */
+int rn_occluded(const rn_accel* accel, const float* rays, const float* t_max, uint32_t nrays,
+                int flags, uint8_t* hit, rn_status* st);
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif  /* RN_AO_H */

@@ -61,6 +61,7 @@ def lib() -> C.CDLL:
         L.rno_accel_nodes.argtypes = [C.c_void_p]
         L.rno_occluded.argtypes = [C.c_void_p, _F, C.c_float]
         L.rno_occluded_scan.argtypes = [_F, C.c_int, _F, C.c_float]
+        L.rno_occluded_scan_batch.argtypes = [_F, C.c_int, _F, _F, C.c_int, _U8, C.c_int]
         L.rno_trace.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_void_p, _F, C.c_int, C.c_int,
                                 C.c_float, C.c_void_p, C.c_int, _F, C.c_void_p, C.c_void_p,
                                 C.c_int, C.c_int, C.c_int]
@@ -151,6 +152,15 @@ def trace(pos, nrm, mask, tris, spp, radius, to_light=None, accel="bvh", threads
         if handle:
             L.rno_accel_free(handle)
     return ao if to_light is None else (ao, sky, sun)
+
+
+def occluded_scan(tris, rays, tmax, threads=1):
+    """Any-hit by scanning every triangle (the reference's test oracle) for rays (n, 6)."""
+    tris = _f32(tris).reshape(-1, 9)
+    rays = _f32(rays).reshape(-1, 6)
+    hit = np.zeros(len(rays), np.uint8)
+    lib().rno_occluded_scan_batch(tris, len(tris), rays, _f32(tmax), len(rays), hit, int(threads))
+    return hit
 
 
 def ssao(pos, nrm, mask, samples=SS_SAMPLES, radius=AO_RADIUS, threads=1):

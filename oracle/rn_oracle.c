@@ -713,3 +713,16 @@ RNO_API void rno_soup(int count, uint64_t seed, float* tris9) {
         o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = b.x; o[4] = b.y; o[5] = b.z; o[6] = d.x; o[7] = d.y; o[8] = d.z;
     }
 }
+
+/* Any-hit scan for a batch of rays (accel.cpp:31-35 per ray), rows of `threads` workers. */
+typedef struct { const tri_t* tris; int ntri; const float* rays; const float* tmax; uint8_t* hit; int n; } scan_ctx;
+static void scan_row(void* p, int i) {
+    const scan_ctx* c = (const scan_ctx*)p;
+    const float* r = c->rays + (size_t)i * 6;
+    c->hit[i] = (uint8_t)scan_occluded(c->tris, c->ntri, v3m(r[0], r[1], r[2]), v3m(r[3], r[4], r[5]), c->tmax[i]);
+}
+RNO_API void rno_occluded_scan_batch(const float* tris9, int ntri, const float* rays6, const float* tmax, int n,
+                                     uint8_t* hit, int threads) {
+    scan_ctx c = {(const tri_t*)tris9, ntri, rays6, tmax, hit, n};
+    parallel_rows(n, threads, scan_row, &c);
+}

@@ -1,0 +1,495 @@
+// capi.cu -- the C ABI of librn_ao.so (include/rn_ao.h): the process-wide device context,
+// the sampler's host-libm calibration, workspace management, and the entry points that
+// stage host buffers, launch the kernels and return results.
+#include "rn_internal.h"
+#include "rn_device.cuh"
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace rn {
+
+Context& ctx() {
+    static Context c;
+    return c;
+}
+
+int fail(rn_status* st, int code, const char* fmt, ...) {
+    if (st) {
+        st->code = code;
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(st->message, sizeof st->message, fmt, ap);
+        va_end(ap);
+    }
+    return code;
+}
+int ok(rn_status* st) {
+    if (st) { st->code = RN_OK; st->message[0] = '\0'; }
+    return RN_OK;
+}
+int cuda_fail(rn_status* st, cudaError_t e, const char* what) {
+    int code = RN_ERR_CUDA;
+    if (e == cudaErrorMemoryAllocation) code = RN_ERR_NO_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) code = RN_ERR_NO_DEVICE;
+    return fail(st, code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------- sampler calibration
+namespace {
+constexpr uint32_t kAngles = 1u << 24;
+
+// One byte per sample angle: host-minus-device bit difference of cos (low nibble) and sin
+// (high nibble). `bad` counts angles whose difference does not fit in [-8, 7].
+__global__ void trig_corr_kernel(const float2* __restrict__ host_cs, uint8_t* __restrict__ corr, uint32_t* bad) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= kAngles) return;
+    float s, c;
+    sincosf(sample_angle(k), &s, &c);
+    const float2 h = host_cs[k];
+    const int dc = __float_as_int(h.x) - __float_as_int(c);
+    const int ds = __float_as_int(h.y) - __float_as_int(s);
+    uint8_t v = 0;
+    if (dc >= -8 && dc <= 7 && ds >= -8 && ds <= 7)
+        v = (uint8_t)((dc & 15) | ((ds & 15) << 4));
+    else
+        atomicAdd(bad, 1u);
+    corr[k] = v;
+}
+}  // namespace
+
+// The reference's directions depend on the host libm's cosf/sinf at phi = 6.2831853f * k/2^24.
+// Evaluate both on every one of the 2^24 angles (host threads), upload, and let the device
+// record its own sincosf's difference from them.
+int build_trig_correction(Context& c, rn_status* st) {
+    std::vector<float> host((size_t)kAngles * 2);
+    unsigned nt = std::thread::hardware_concurrency();
+    if (nt < 1) nt = 1;
+    if (nt > 64) nt = 64;
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < nt; ++t)
+        pool.emplace_back([&host, t, nt] {
+            for (uint32_t k = t; k < kAngles; k += nt) {
+                const float u = (float)k / 16777216.0f;
+                const float phi = 6.2831853f * u;
+                host[2 * (size_t)k] = ::cosf(phi);
+                host[2 * (size_t)k + 1] = ::sinf(phi);
+            }
+        });
+    for (auto& th : pool) th.join();
+    float2* d_host = nullptr;
+    uint32_t* d_bad = nullptr;
+    RN_CUDA(cudaMalloc((void**)&c.trig_corr, kAngles), st);
+    RN_CUDA(cudaMalloc((void**)&d_host, (size_t)kAngles * sizeof(float2)), st);
+    RN_CUDA(cudaMalloc((void**)&d_bad, 4), st);
+    RN_CUDA(cudaMemsetAsync(d_bad, 0, 4, c.stream), st);
+    RN_CUDA(cudaMemcpyAsync(d_host, host.data(), (size_t)kAngles * sizeof(float2), cudaMemcpyHostToDevice, c.stream), st);
+    trig_corr_kernel<<<kAngles / 256, 256, 0, c.stream>>>(d_host, c.trig_corr, d_bad);
+    RN_CUDA(cudaGetLastError(), st);
+    uint32_t bad = 0;
+    RN_CUDA(cudaMemcpyAsync(&bad, d_bad, 4, cudaMemcpyDeviceToHost, c.stream), st);
+    RN_CUDA(cudaStreamSynchronize(c.stream), st);
+    cudaFree(d_host);
+    cudaFree(d_bad);
+    if (bad) return fail(st, RN_ERR_STATE, "sampler calibration: %u angles differ by more than 7 ulp", bad);
+    return RN_OK;
+}
+
+int ensure_ctx(rn_status* st) {
+    Context& c = ctx();
+    if (c.ready) return RN_OK;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+        return fail(st, RN_ERR_NO_DEVICE, "no CUDA device (%s)", e == cudaSuccess ? "count 0" : cudaGetErrorString(e));
+    int dev = 0;
+    RN_CUDA(cudaGetDevice(&dev), st);
+    cudaDeviceProp prop;
+    RN_CUDA(cudaGetDeviceProperties(&prop, dev), st);
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(st, RN_ERR_NO_DEVICE, "device %d (%s) is sm_%d%d; librn_ao.so is built for sm_103a", dev, prop.name,
+                    prop.major, prop.minor);
+    c.device = dev;
+    c.sm_count = prop.multiProcessorCount;
+    RN_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking), st);
+    c.stream = c.own_stream;
+    RN_CUDA(cudaMalloc((void**)&c.dev_error, 64), st);
+    RN_CUDA(cudaMemsetAsync(c.dev_error, 0, 64, c.stream), st);
+    RN_TRY(build_trig_correction(c, st));
+    c.ready = true;
+    return RN_OK;
+}
+
+int ws_get(Slot s, size_t bytes, void** out, rn_status* st) {
+    DevBuf& b = ctx().ws[s];
+    if (bytes == 0) bytes = 16;
+    if (b.cap < bytes) {
+        if (b.ptr) {
+            RN_CUDA(cudaStreamSynchronize(ctx().stream), st);
+            cudaFree(b.ptr);
+            b.ptr = nullptr;
+            b.cap = 0;
+        }
+        const size_t cap = (bytes + 4095) & ~size_t(4095);
+        RN_CUDA(cudaMalloc(&b.ptr, cap), st);
+        // reduction counters must start at zero; every kernel leaves them at zero
+        RN_CUDA(cudaMemsetAsync(b.ptr, 0, cap, ctx().stream), st);
+        b.cap = cap;
+    }
+    *out = b.ptr;
+    return RN_OK;
+}
+
+int check_device_error(rn_status* st, const char* where) {
+    Context& c = ctx();
+    uint32_t word = 0;
+    RN_CUDA(cudaMemcpyAsync(&word, c.dev_error, 4, cudaMemcpyDeviceToHost, c.stream), st);
+    RN_CUDA(cudaStreamSynchronize(c.stream), st);
+    if (word) {
+        RN_CUDA(cudaMemsetAsync(c.dev_error, 0, 4, c.stream), st);
+        const int code = (word & (DEV_STACK_OVERFLOW | DEV_QUEUE_OVERFLOW)) ? RN_ERR_OVERFLOW : RN_ERR_BUDGET;
+        return fail(st, code, "%s: device error word 0x%x (%s)", where, word,
+                    (word & DEV_STACK_OVERFLOW) ? "traversal stack overflow"
+                    : (word & DEV_GUARD)        ? "iteration budget exhausted"
+                                                : "queue overflow");
+    }
+    return RN_OK;
+}
+
+}  // namespace rn
+
+using namespace rn;
+
+namespace {
+
+// Stage a host buffer into a workspace slot (or pass a device pointer through).
+template <typename T>
+int stage_in(const T* p, size_t count, bool dev, Slot slot, const T** out, rn_status* st) {
+    if (dev || p == nullptr) { *out = p; return RN_OK; }
+    void* d = nullptr;
+    RN_TRY(ws_get(slot, count * sizeof(T), &d, st));
+    RN_CUDA(cudaMemcpyAsync(d, p, count * sizeof(T), cudaMemcpyHostToDevice, ctx().stream), st);
+    *out = (const T*)d;
+    return RN_OK;
+}
+template <typename T>
+int stage_out(T* p, size_t count, bool dev, Slot slot, T** out, rn_status* st) {
+    if (dev || p == nullptr) { *out = p; return RN_OK; }
+    void* d = nullptr;
+    RN_TRY(ws_get(slot, count * sizeof(T), &d, st));
+    *out = (T*)d;
+    return RN_OK;
+}
+template <typename T>
+int copy_back(T* host, const T* dev, size_t count, rn_status* st) {
+    if (host == nullptr || host == dev) return RN_OK;
+    RN_CUDA(cudaMemcpyAsync(host, dev, count * sizeof(T), cudaMemcpyDeviceToHost, ctx().stream), st);
+    return RN_OK;
+}
+
+int check_gbuf(const rn_gbuf* g, rn_status* st) {
+    if (!g) return fail(st, RN_ERR_INVALID, "null G-buffer");
+    if (g->w <= 0 || g->h <= 0) return fail(st, RN_ERR_INVALID, "G-buffer size %dx%d", g->w, g->h);
+    if ((size_t)g->w * (size_t)g->h > (size_t)1 << 31) return fail(st, RN_ERR_INVALID, "G-buffer larger than 2^31 pixels");
+    if (!g->position || !g->normal || !g->mask) return fail(st, RN_ERR_INVALID, "G-buffer plane is null");
+    return RN_OK;
+}
+
+struct StagedGbuf { const float* pos; const float* nrm; const uint8_t* mask; };
+
+int stage_gbuf(const rn_gbuf* g, bool dev, StagedGbuf* s, rn_status* st) {
+    const size_t np = (size_t)g->w * g->h;
+    RN_TRY(stage_in(g->position, np * 3, dev, WS_POS, &s->pos, st));
+    RN_TRY(stage_in(g->normal, np * 3, dev, WS_NRM, &s->nrm, st));
+    RN_TRY(stage_in(g->mask, np, dev, WS_MASK, &s->mask, st));
+    return RN_OK;
+}
+
+int do_visibility(const StagedGbuf& g, int w, int h, const rn_accel* accel, int spp, float radius,
+                  const float* to_light, int flags, float* ao, float* sky, float* sun, rn_status* st) {
+    Context& c = ctx();
+    TraceParams p{};
+    p.w = w; p.h = h;
+    p.pos = g.pos; p.nrm = g.nrm; p.mask = g.mask;
+    p.nodes = accel->d_nodes; p.tris = accel->d_tris;
+    p.has_geometry = accel->ntri > 0;
+    p.spp = spp; p.radius = radius;
+    p.want_sky = (flags & RN_SKY) != 0;
+    p.sun_forced = (flags & RN_SUN_FORCED) != 0;
+    if (p.want_sky) { p.lx = to_light[0]; p.ly = to_light[1]; p.lz = to_light[2]; }
+    else { p.lx = 0.0f; p.ly = 1.0f; p.lz = 0.0f; }
+    p.corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
+    p.ao = ao; p.sky = sky; p.sun = sun;
+    p.err_word = c.dev_error;
+    if (launch_trace(p, c.sm_count, c.stream) != RN_OK) return cuda_fail(st, cudaGetLastError(), "trace_kernel");
+    return RN_OK;
+}
+
+int check_vis_args(const rn_gbuf* g, const rn_accel* accel, int spp, const float* to_light, int flags, const float* ao,
+                   const float* sky, const float* sun, rn_status* st) {
+    RN_TRY(check_gbuf(g, st));
+    if (!accel) return fail(st, RN_ERR_INVALID, "null accelerator");
+    if (spp <= 0) return fail(st, RN_ERR_INVALID, "samples per pixel %d <= 0", spp);
+    if (!ao) return fail(st, RN_ERR_INVALID, "null ao output");
+    if ((flags & RN_SKY) && (!sky || !sun || !to_light)) return fail(st, RN_ERR_INVALID, "RN_SKY needs sky, sun and to_light");
+    if (accel->device != ctx().device) return fail(st, RN_ERR_STATE, "accelerator belongs to device %d", accel->device);
+    return RN_OK;
+}
+
+void fill_result(const RecOut& r, float tolerance, rn_reconcile_result* out) {
+    out->sum_sq = r.sum;
+    out->pixels = r.n;
+    out->max_error = r.max;
+    out->rmse = r.n > 0 ? (float)std::sqrt(r.sum / (double)r.n) : 0.0f;
+    out->within_tolerance = out->rmse <= tolerance ? 1 : 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rn_ao_version(void) { return RN_AO_ABI_VERSION; }
+
+int rn_init(rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    return ok(st);
+}
+
+int rn_set_stream(void* stream, rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    c.stream = stream ? (cudaStream_t)stream : c.own_stream;
+    return ok(st);
+}
+
+int rn_synchronize(rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    RN_CUDA(cudaStreamSynchronize(ctx().stream), st);
+    RN_TRY(check_device_error(st, "rn_synchronize"));
+    return ok(st);
+}
+
+int rn_accel_build(const float* tris, uint32_t ntri, int flags, rn_accel** out, rn_status* st) {
+    if (!out) return fail(st, RN_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (ntri > 0 && !tris) return fail(st, RN_ERR_INVALID, "null triangles");
+    if (ntri >= (1u << 28)) return fail(st, RN_ERR_INVALID, "%u triangles: at most 2^28 - 1", ntri);
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const float* d_tris = nullptr;
+    RN_TRY(stage_in(tris, (size_t)ntri * 9, dev, WS_TRIS_IN, &d_tris, st));
+    rn_accel* acc = new rn_accel();
+    acc->device = c.device;
+    PlocTree tree;
+    int rc = ploc_build(d_tris, ntri, 16, &tree, c.stream, st);
+    if (rc == RN_OK) rc = collapse_bvh4(tree, d_tris, acc, c.stream, st);
+    if (rc == RN_OK) {
+        cudaError_t e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) rc = cuda_fail(st, e, "rn_accel_build");
+    }
+    ploc_free(&tree);
+    if (rc == RN_OK && acc->depth * 3 + 2 > 96)
+        rc = fail(st, RN_ERR_OVERFLOW, "BVH depth %u needs more than the traversal's 96-entry stack", acc->depth);
+    if (rc != RN_OK) { rn_accel_free(acc); return rc; }
+    *out = acc;
+    return ok(st);
+}
+
+void rn_accel_free(rn_accel* accel) {
+    if (!accel) return;
+    if (accel->d_nodes) cudaFree(accel->d_nodes);
+    if (accel->d_tris) cudaFree(accel->d_tris);
+    delete accel;
+}
+
+int rn_accel_info(const rn_accel* accel, uint32_t* wide_nodes, uint32_t* leaf_tris, uint32_t* ploc_rounds, rn_status* st) {
+    if (!accel) return fail(st, RN_ERR_INVALID, "null accelerator");
+    if (wide_nodes) *wide_nodes = accel->nodes;
+    if (leaf_tris) *leaf_tris = accel->ntri;
+    if (ploc_rounds) *ploc_rounds = accel->rounds;
+    return ok(st);
+}
+
+int rn_ao_visibility(const rn_gbuf* g, const rn_accel* accel, int spp, float radius, const float* to_light, int flags,
+                     float* ao, float* sky, float* sun, rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    RN_TRY(check_vis_args(g, accel, spp, to_light, flags, ao, sky, sun, st));
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const size_t np = (size_t)g->w * g->h;
+    StagedGbuf sg;
+    RN_TRY(stage_gbuf(g, dev, &sg, st));
+    float *d_ao, *d_sky = nullptr, *d_sun = nullptr;
+    float tl[3] = {0.0f, 1.0f, 0.0f};
+    if (flags & RN_SKY) { tl[0] = to_light[0]; tl[1] = to_light[1]; tl[2] = to_light[2]; }
+    RN_TRY(stage_out(ao, np, dev, WS_AO, &d_ao, st));
+    if (flags & RN_SKY) {
+        RN_TRY(stage_out(sky, np, dev, WS_SKY, &d_sky, st));
+        RN_TRY(stage_out(sun, np, dev, WS_SUN, &d_sun, st));
+    }
+    RN_TRY(do_visibility(sg, g->w, g->h, accel, spp, radius, tl, flags, d_ao, d_sky, d_sun, st));
+    if (dev) return ok(st);
+    RN_TRY(copy_back(ao, d_ao, np, st));
+    if (flags & RN_SKY) { RN_TRY(copy_back(sky, d_sky, np, st)); RN_TRY(copy_back(sun, d_sun, np, st)); }
+    RN_TRY(check_device_error(st, "rn_ao_visibility"));
+    return ok(st);
+}
+
+int rn_ssao(const rn_gbuf* g, int samples, float radius, int flags, float* ao_ss, rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    RN_TRY(check_gbuf(g, st));
+    if (!ao_ss) return fail(st, RN_ERR_INVALID, "null output");
+    if (samples < 0) return fail(st, RN_ERR_INVALID, "samples %d < 0", samples);
+    Context& c = ctx();
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const size_t np = (size_t)g->w * g->h;
+    StagedGbuf sg;
+    RN_TRY(stage_gbuf(g, dev, &sg, st));
+    float* d_ss;
+    RN_TRY(stage_out(ao_ss, np, dev, WS_SS, &d_ss, st));
+    const uint8_t* corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
+    if (launch_ssao(g->w, g->h, sg.pos, sg.nrm, sg.mask, samples, radius, corr, d_ss, nullptr, nullptr, nullptr,
+                    nullptr, c.stream) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "ssao_kernel");
+    if (dev) return ok(st);
+    RN_TRY(copy_back(ao_ss, d_ss, np, st));
+    RN_CUDA(cudaStreamSynchronize(c.stream), st);
+    return ok(st);
+}
+
+int rn_reconcile(const float* approx, const float* truth, const uint8_t* mask, int w, int h, float tolerance, int flags,
+                 float* err, rn_reconcile_result* out, rn_status* st) {
+    if (!approx || !truth || !mask || !out) return fail(st, RN_ERR_INVALID, "null argument");
+    if (w < 0 || h < 0) return fail(st, RN_ERR_INVALID, "size %dx%d", w, h);
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const size_t np = (size_t)w * h;
+    if (np == 0) {
+        *out = rn_reconcile_result{0.0f, 0.0f, 0, 1, 0.0};
+        out->within_tolerance = 0.0f <= tolerance;
+        return ok(st);
+    }
+    const float *d_a, *d_t;
+    const uint8_t* d_m;
+    float* d_e = nullptr;
+    RN_TRY(stage_in(approx, np, dev, WS_APPROX, &d_a, st));
+    RN_TRY(stage_in(truth, np, dev, WS_TRUTH, &d_t, st));
+    RN_TRY(stage_in(mask, np, dev, WS_MASK, &d_m, st));
+    if (err) RN_TRY(stage_out(err, np, dev, WS_ERR, &d_e, st));
+    const int nb = reconcile_blocks(np);
+    void *parts = nullptr, *ro = nullptr;
+    RN_TRY(ws_get(WS_PARTIALS, (size_t)nb * sizeof(RecPartial), &parts, st));
+    RN_TRY(ws_get(WS_COUNTERS, sizeof(RecOut), &ro, st));
+    if (launch_reconcile(d_a, d_t, d_m, np, d_e, (RecPartial*)parts, nb, (RecOut*)ro, c.stream) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "reconcile_kernel");
+    RecOut r;
+    RN_CUDA(cudaMemcpyAsync(&r, ro, sizeof r, cudaMemcpyDeviceToHost, c.stream), st);
+    if (!dev) RN_TRY(copy_back(err, d_e, np, st));
+    RN_CUDA(cudaStreamSynchronize(c.stream), st);
+    fill_result(r, tolerance, out);
+    return ok(st);
+}
+
+int rn_ao_frame(const rn_gbuf* g, const rn_accel* accel, int spp, float radius, int ss_samples, float tolerance,
+                const float* to_light, int flags, float* ao, float* sky, float* sun, float* ao_ss, float* err,
+                rn_reconcile_result* out, rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    RN_TRY(check_vis_args(g, accel, spp, to_light, flags, ao, sky, sun, st));
+    if (!ao_ss || !out) return fail(st, RN_ERR_INVALID, "null ao_ss or result");
+    if (ss_samples < 0) return fail(st, RN_ERR_INVALID, "ss_samples %d < 0", ss_samples);
+    Context& c = ctx();
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const size_t np = (size_t)g->w * g->h;
+    StagedGbuf sg;
+    RN_TRY(stage_gbuf(g, dev, &sg, st));
+    float *d_ao, *d_sky = nullptr, *d_sun = nullptr, *d_ss, *d_err = nullptr;
+    float tl[3] = {0.0f, 1.0f, 0.0f};
+    if (flags & RN_SKY) { tl[0] = to_light[0]; tl[1] = to_light[1]; tl[2] = to_light[2]; }
+    RN_TRY(stage_out(ao, np, dev, WS_AO, &d_ao, st));
+    if (flags & RN_SKY) {
+        RN_TRY(stage_out(sky, np, dev, WS_SKY, &d_sky, st));
+        RN_TRY(stage_out(sun, np, dev, WS_SUN, &d_sun, st));
+    }
+    RN_TRY(stage_out(ao_ss, np, dev, WS_SS, &d_ss, st));
+    if (err) RN_TRY(stage_out(err, np, dev, WS_ERR, &d_err, st));
+    RN_TRY(do_visibility(sg, g->w, g->h, accel, spp, radius, tl, flags, d_ao, d_sky, d_sun, st));
+    const int nb = ssao_blocks(g->w, g->h);
+    void *parts = nullptr, *ro = nullptr;
+    RN_TRY(ws_get(WS_PARTIALS, (size_t)nb * sizeof(RecPartial), &parts, st));
+    RN_TRY(ws_get(WS_COUNTERS, sizeof(RecOut), &ro, st));
+    const uint8_t* corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
+    if (launch_ssao(g->w, g->h, sg.pos, sg.nrm, sg.mask, ss_samples, radius, corr, d_ss, d_ao, d_err,
+                    (RecPartial*)parts, (RecOut*)ro, c.stream) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "ssao_kernel (fused reconcile)");
+    RecOut r;
+    RN_CUDA(cudaMemcpyAsync(&r, ro, sizeof r, cudaMemcpyDeviceToHost, c.stream), st);
+    if (!dev) {
+        RN_TRY(copy_back(ao, d_ao, np, st));
+        if (flags & RN_SKY) { RN_TRY(copy_back(sky, d_sky, np, st)); RN_TRY(copy_back(sun, d_sun, np, st)); }
+        RN_TRY(copy_back(ao_ss, d_ss, np, st));
+        if (err) RN_TRY(copy_back(err, d_err, np, st));
+    }
+    RN_TRY(check_device_error(st, "rn_ao_frame"));
+    fill_result(r, tolerance, out);
+    return ok(st);
+}
+
+int rn_ploc_build(const float* tris, uint32_t ntri, int radius, int flags, int32_t* nodes_out, int32_t* root,
+                  uint32_t* rounds, rn_status* st) {
+    if ((ntri > 0 && (!tris || !nodes_out)) || !root || !rounds) return fail(st, RN_ERR_INVALID, "null argument");
+    if (ntri >= (1u << 30)) return fail(st, RN_ERR_INVALID, "%u triangles: too many", ntri);
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    *root = -1;
+    *rounds = 0;
+    if (ntri == 0) return ok(st);
+    const float* d_tris = nullptr;
+    RN_TRY(stage_in(tris, (size_t)ntri * 9, dev, WS_TRIS_IN, &d_tris, st));
+    PlocTree tree;
+    int rc = ploc_build(d_tris, ntri, radius, &tree, c.stream, st);
+    const size_t count = 2 * (size_t)ntri - 1;
+    int32_t* d_out = nodes_out;
+    if (rc == RN_OK && !dev) {
+        void* p = nullptr;
+        rc = ws_get(WS_HITS, count * 9 * 4, &p, st);
+        d_out = (int32_t*)p;
+    }
+    if (rc == RN_OK) rc = ploc_export(tree, d_out, c.stream, st);
+    if (rc == RN_OK && !dev) rc = copy_back(nodes_out, d_out, count * 9, st);
+    if (rc == RN_OK) {
+        cudaError_t e = cudaStreamSynchronize(c.stream);
+        if (e != cudaSuccess) rc = cuda_fail(st, e, "rn_ploc_build");
+    }
+    *root = tree.root;
+    *rounds = tree.rounds;
+    ploc_free(&tree);
+    return rc == RN_OK ? ok(st) : rc;
+}
+
+int rn_occluded(const rn_accel* accel, const float* rays, const float* t_max, uint32_t nrays, int flags, uint8_t* hit,
+                rn_status* st) {
+    if (!accel || (nrays > 0 && (!rays || !t_max || !hit))) return fail(st, RN_ERR_INVALID, "null argument");
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    if (accel->device != c.device) return fail(st, RN_ERR_STATE, "accelerator belongs to device %d", accel->device);
+    if (nrays == 0) return ok(st);
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const float *d_rays, *d_t;
+    uint8_t* d_hit;
+    RN_TRY(stage_in(rays, (size_t)nrays * 6, dev, WS_RAYS, &d_rays, st));
+    RN_TRY(stage_in(t_max, (size_t)nrays, dev, WS_TMAX, &d_t, st));
+    RN_TRY(stage_out(hit, (size_t)nrays, dev, WS_HITS, &d_hit, st));
+    if (launch_occluded(accel->d_nodes, accel->d_tris, accel->ntri > 0, d_rays, d_t, nrays, d_hit, c.dev_error,
+                        c.stream) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "occluded_kernel");
+    if (dev) return ok(st);
+    RN_TRY(copy_back(hit, d_hit, nrays, st));
+    RN_TRY(check_device_error(st, "rn_occluded"));
+    return ok(st);
+}
+
+}  // extern "C"

@@ -1,0 +1,169 @@
+// rn_internal.h -- host-side internals of librn_ao.so: the process-wide device context,
+// its workspace, error reporting, and the launchers each kernel file exports.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include "../../include/rn_ao.h"
+
+namespace rn {
+
+// Error word written by kernels whose device-side loops have budgets (traversal guard,
+// stack overflow, PLOC rounds). The host reads it after the work completes.
+enum DeviceError : uint32_t {
+    DEV_OK = 0,
+    DEV_STACK_OVERFLOW = 1u << 0,
+    DEV_GUARD = 1u << 1,
+    DEV_PLOC_NO_MERGE = 1u << 2,
+    DEV_QUEUE_OVERFLOW = 1u << 3,
+};
+
+// A device buffer that grows on demand and is reused across calls.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t cap = 0;
+};
+
+// Workspace slots of the context. Each entry point uses fixed slots, so repeated calls of
+// the same size allocate nothing.
+enum Slot {
+    WS_POS, WS_NRM, WS_MASK, WS_AO, WS_SKY, WS_SUN, WS_SS, WS_ERR, WS_TRUTH, WS_APPROX,
+    WS_PARTIALS, WS_WORKLIST, WS_COUNTERS, WS_RAYS, WS_TMAX, WS_HITS, WS_TRIS_IN,
+    WS_COUNT
+};
+
+struct Context {
+    bool ready = false;
+    int device = -1;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;      // the stream all work goes to
+    cudaStream_t own_stream = nullptr;  // the library's own stream
+    uint8_t* trig_corr = nullptr;       // 2^24 bytes: host-libm correction per sample angle
+    uint32_t* dev_error = nullptr;      // one DeviceError word
+    DevBuf ws[WS_COUNT];
+};
+
+Context& ctx();
+
+// Status helpers: fill `st` and return the code.
+int fail(rn_status* st, int code, const char* fmt, ...);
+int ok(rn_status* st);
+// Check a CUDA call; on failure fill `st` and return RN_ERR_CUDA (or RN_ERR_NO_MEMORY).
+int cuda_fail(rn_status* st, cudaError_t e, const char* what);
+#define RN_CUDA(call, st)                                          \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return ::rn::cuda_fail(st, e_, #call); \
+    } while (0)
+#define RN_TRY(expr)                 \
+    do {                             \
+        int rc_ = (expr);            \
+        if (rc_ != RN_OK) return rc_; \
+    } while (0)
+
+// Make sure the context is open (device, stream, sampler table).
+int ensure_ctx(rn_status* st);
+// A workspace buffer of at least `bytes`.
+int ws_get(Slot s, size_t bytes, void** out, rn_status* st);
+// Read and clear the device error word (synchronizes the stream).
+int check_device_error(rn_status* st, const char* where);
+
+// ---------------------------------------------------------------- sampler table
+int build_trig_correction(Context& c, rn_status* st);
+
+// ---------------------------------------------------------------- reconcile / SSAO
+struct RecPartial {   // one tile's share of the reconcile
+    double sum;
+    float max;
+    int32_t n;
+};
+struct RecOut {       // the reduction's device-side result
+    double sum;
+    float max;
+    int32_t n;
+    uint32_t done;    // blocks finished (the last block reduces, then resets it to 0)
+    uint32_t pad;
+};
+int launch_reconcile(const float* approx, const float* truth, const uint8_t* mask, size_t npx,
+                     float* err, RecPartial* partials, int nblocks, RecOut* out, cudaStream_t s);
+int reconcile_blocks(size_t npx);
+int launch_ssao(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, int samples,
+                float radius, const uint8_t* corr, float* ao, const float* truth, float* err,
+                RecPartial* partials, RecOut* out, cudaStream_t s);
+int ssao_blocks(int w, int h);
+
+// ---------------------------------------------------------------- accelerator
+// A 4-wide BVH node: six 4-float planes of child boxes (SoA) then the 4 child words and
+// per-node metadata. 128 bytes, 16-byte aligned for vector loads. Child word >= 0: index of
+// an interior node; < 0: leaf, ~word = first << 3 | (count - 1) into the leaf triangles.
+struct alignas(16) Node4 {
+    float lox[4], hix[4], loy[4], hiy[4], loz[4], hiz[4];
+    int32_t child[4];
+    int32_t meta[4];   // meta[0] = number of valid children
+};
+static_assert(sizeof(Node4) == 128, "Node4 layout");
+constexpr int kLeafMax = 4;
+
+// A leaf triangle: vertices a, b, c as float4 (w of a = input triangle index).
+struct alignas(16) LeafTri {
+    float ax, ay, az, id;
+    float bx, by, bz, pad0;
+    float cx, cy, cz, pad1;
+};
+
+}  // namespace rn
+
+// The accelerator handle of the C ABI.
+struct rn_accel {
+    int device = -1;
+    uint32_t ntri = 0;
+    uint32_t nodes = 0;        // wide nodes
+    uint32_t rounds = 0;       // PLOC rounds
+    uint32_t depth = 0;        // wide-tree depth (levels)
+    rn::Node4* d_nodes = nullptr;
+    rn::LeafTri* d_tris = nullptr;
+};
+
+namespace rn {
+// PLOC: build the binary tree on the device. Outputs (device): nodes9 (2n-1 x 9 int32 in
+// the reference's layout) when non-null; the binary tree in SoA form for the collapse.
+struct PlocTree {
+    uint32_t n = 0;
+    int32_t root = -1;
+    uint32_t rounds = 0;
+    float* box = nullptr;      // (2n-1) x 6: lo.x lo.y lo.z hi.x hi.y hi.z
+    int32_t* left = nullptr;   // (2n-1)
+    int32_t* right = nullptr;  // (2n-1)
+    int32_t* tri = nullptr;    // (2n-1)
+    void* mem = nullptr;       // the one allocation holding the arrays above
+};
+int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaStream_t s, rn_status* st);
+void ploc_free(PlocTree* t);
+int ploc_export(const PlocTree& t, int32_t* d_nodes9, cudaStream_t s, rn_status* st);
+int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, cudaStream_t s, rn_status* st);
+
+// ---------------------------------------------------------------- traversal
+struct TraceParams {
+    int w, h;
+    const float* pos;
+    const float* nrm;
+    const uint8_t* mask;
+    const Node4* nodes;
+    const LeafTri* tris;
+    int has_geometry;
+    int spp;
+    float radius;
+    float lx, ly, lz;     // to_light (normalized on the device)
+    int want_sky, sun_forced;
+    const uint8_t* corr;
+    float* ao;
+    float* sky;
+    float* sun;
+    uint32_t* err_word;
+};
+int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s);
+int launch_occluded(const Node4* nodes, const LeafTri* tris, int has_geometry, const float* rays,
+                    const float* tmax, uint32_t n, uint8_t* hit, uint32_t* err_word, cudaStream_t s);
+
+}  // namespace rn

@@ -1,0 +1,205 @@
+// trace.cu -- ray-traced AO and lighting model 2's visibility on the GPU: the hot loop of
+// raw-native's CPU oracle (src/renderer/ray_ao.cpp:20-51) as one persistent kernel.
+//
+// Work: the frame is cut into 8 x 4 pixel tiles; each warp takes the next tile from a global
+// counter, one pixel per lane, and walks its `spp` rays (then the sky continuation of every
+// open ray and the sun ray) through the 4-wide BVH. Neighbouring lanes trace neighbouring
+// pixels, so the warp's rays start close together and visit similar nodes.
+//
+// Exactness: ray generation (basis, origin, cosine-weighted direction) and the triangle test
+// use one IEEE rounding per operation in the reference's order; the sample angle's cos/sin
+// carry the host libm's bits (rn_device.cuh). The box test is only required to be
+// conservative, and is: padded boxes, the robust slab exit of Ize (2013) widened by
+// 1.0000008, and NaN-safe min/max, so the any-hit answer is exactly the scan-every-triangle
+// answer the reference's own BVH reproduces.
+#include "rn_internal.h"
+#include "rn_device.cuh"
+
+namespace rn {
+namespace {
+
+constexpr int kStack = 96;
+constexpr uint32_t kGuard = 1u << 24;       // node visits per ray before giving up
+constexpr int kTileW = 8, kTileH = 4;
+
+__device__ __forceinline__ float min_nan(float a, float b) {
+    float r;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float max_nan(float a, float b) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+// inverse(d) of src/renderer/bvh.cpp:29-33: 1/x, or a signed infinity for a zero component.
+__device__ __forceinline__ float safe_inv(float x) { return x != 0.0f ? fdiv(1.0f, x) : copysignf(__int_as_float(0x7f800000), x); }
+
+struct Inv { float x, y, z; };
+
+// Slab entry of one child box. An axis whose distances are NaN (origin on the plane, zero
+// direction component) constrains nothing, as in the reference's entry().
+__device__ __forceinline__ bool slab(float lox, float hix, float loy, float hiy, float loz, float hiz,
+                                     const v3& o, const Inv& iv, float tmax, float& tnear) {
+    const float ax = (lox - o.x) * iv.x, bx = (hix - o.x) * iv.x;
+    const float ay = (loy - o.y) * iv.y, by = (hiy - o.y) * iv.y;
+    const float az = (loz - o.z) * iv.z, bz = (hiz - o.z) * iv.z;
+    const float t0 = fmaxf(fmaxf(fmaxf(0.0f, min_nan(ax, bx)), min_nan(ay, by)), min_nan(az, bz));
+    const float t1 = fminf(fminf(fminf(tmax, max_nan(ax, bx)), max_nan(ay, by)), max_nan(az, bz));
+    tnear = t0;
+    return t0 <= t1 * 1.0000008f;
+}
+
+// Any hit with 1e-4 < t < tmax (raw::Bvh::occluded, src/renderer/bvh.cpp:119-138).
+__device__ bool any_hit(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, const WRay& r,
+                        const Inv& iv, float tmax, uint32_t* err) {
+    int32_t stack[kStack];
+    int sp = 0;
+    int32_t cur = 0;                     // the root is always node 0
+    for (uint32_t guard = 0; guard < kGuard; ++guard) {
+        if (cur >= 0) {
+            const float4* q = reinterpret_cast<const float4*>(nodes + cur);
+            const float4 lx = __ldg(q + 0), hx = __ldg(q + 1), ly = __ldg(q + 2), hy = __ldg(q + 3);
+            const float4 lz = __ldg(q + 4), hz = __ldg(q + 5);
+            const int4 ch = __ldg(reinterpret_cast<const int4*>(q + 6));
+            const int cnt = __ldg(reinterpret_cast<const int*>(q + 7));
+            const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
+            const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
+            const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+            const int32_t CH[4] = {ch.x, ch.y, ch.z, ch.w};
+            int32_t nearest = 0;
+            float tbest = 3.0e38f;
+            bool have = false;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float tn;
+                if (k >= cnt || !slab(LX[k], HX[k], LY[k], HY[k], LZ[k], HZ[k], r.o, iv, tmax, tn)) continue;
+                const int32_t c = CH[k];
+                if (c < 0) {
+                    // leaf: test its triangles now (an early hit ends the walk)
+                    const uint32_t w = (uint32_t)~c;
+                    const uint32_t first = w >> 3, count = (w & 7u) + 1u;
+                    for (uint32_t i = 0; i < count; ++i) {
+                        const float4* tq = reinterpret_cast<const float4*>(tris + first + i);
+                        const float4 A = __ldg(tq), B = __ldg(tq + 1), C = __ldg(tq + 2);
+                        float t;
+                        if (hit_tri(r, mk(A.x, A.y, A.z), mk(B.x, B.y, B.z), mk(C.x, C.y, C.z), t) && t < tmax)
+                            return true;
+                    }
+                    continue;
+                }
+                if (!have) { nearest = c; tbest = tn; have = true; continue; }
+                // keep the nearer child to descend into, stack the other
+                int32_t push = c;
+                if (tn < tbest) { push = nearest; nearest = c; tbest = tn; }
+                if (sp >= kStack) { atomicOr(err, DEV_STACK_OVERFLOW); return false; }
+                stack[sp++] = push;
+            }
+            if (have) { cur = nearest; continue; }
+        }
+        if (sp == 0) return false;
+        cur = stack[--sp];
+    }
+    atomicOr(err, DEV_GUARD);
+    return false;
+}
+
+__device__ __forceinline__ Inv make_inv(const v3& d) { return Inv{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)}; }
+
+// One pixel: its spp cosine-weighted rays, the sky continuation of the open ones, the sun ray.
+__device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, const v3& toLight) {
+    const float kFar = 1e30f;
+    const size_t i = (size_t)y * p.w + x;
+    if (!p.mask[i]) {
+        p.ao[i] = 1.0f;
+        if (p.want_sky) { p.sky[i] = 1.0f; p.sun[i] = 1.0f; }
+        return;
+    }
+    const v3 P = load3(p.pos + 3 * i), n = load3(p.nrm + 3 * i);
+    // basis (ray_ao.cpp:14-17)
+    const v3 a = fabsf(n.x) > 0.9f ? mk(0.0f, 1.0f, 0.0f) : mk(1.0f, 0.0f, 0.0f);
+    const v3 t = normalize(cross(a, n)), b = cross(n, t);
+    const v3 origin = add(P, scale(n, 1e-3f));
+    int open = 0, freec = 0;
+    for (int s = 0; s < p.spp; ++s) {
+        const float u1 = unit24(hash24((uint32_t)x, (uint32_t)y, (uint32_t)(2 * s)));
+        const uint32_t k2 = hash24((uint32_t)x, (uint32_t)y, (uint32_t)(2 * s + 1));
+        float c, sn;
+        sample_sincos(k2, p.corr, c, sn);
+        const float r = fsqrt(u1);
+        const float lx = fmul(r, c), ly = fmul(r, sn);
+        const float lz = fsqrt(smax(0.0f, fsub(1.0f, u1)));
+        const v3 dir = normalize(add(add(scale(t, lx), scale(b, ly)), scale(n, lz)));
+        bool occ = false;
+        WRay wr;
+        Inv iv;
+        if (p.has_geometry) {
+            wr = make_wray(origin, dir);
+            iv = make_inv(dir);
+            occ = any_hit(p.nodes, p.tris, wr, iv, p.radius, p.err_word);
+        }
+        if (!occ) {
+            ++open;
+            if (p.want_sky && !(p.has_geometry && any_hit(p.nodes, p.tris, wr, iv, kFar, p.err_word))) ++freec;
+        }
+    }
+    p.ao[i] = fdiv((float)open, (float)p.spp);
+    if (p.want_sky) {
+        p.sky[i] = fdiv((float)freec, (float)p.spp);
+        bool lit = true;
+        if (!p.sun_forced && p.has_geometry) {
+            const WRay wr = make_wray(origin, toLight);
+            lit = !any_hit(p.nodes, p.tris, wr, make_inv(toLight), kFar, p.err_word);
+        }
+        p.sun[i] = lit ? 1.0f : 0.0f;
+    }
+}
+
+__global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ TraceParams p, uint32_t* tile_ctr) {
+    const int tiles_x = (p.w + kTileW - 1) / kTileW, tiles_y = (p.h + kTileH - 1) / kTileH;
+    const uint32_t ntiles = (uint32_t)tiles_x * tiles_y;
+    const unsigned lane = threadIdx.x & 31u;
+    // lighting model 2's sun direction, normalized on the device as computeRTVisibility does
+    const v3 toLight = normalize(mk(p.lx, p.ly, p.lz));
+    while (true) {
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(tile_ctr, 1u);
+        tile = __shfl_sync(0xffffffffu, tile, 0);
+        if (tile >= ntiles) return;
+        const int x = (int)(tile % tiles_x) * kTileW + (int)(lane % kTileW);
+        const int y = (int)(tile / tiles_x) * kTileH + (int)(lane / kTileW);
+        // no lane leaves the loop body early: the next tile fetch is a full-warp shuffle
+        if (x < p.w && y < p.h) trace_pixel(p, x, y, toLight);
+    }
+}
+
+__global__ void occluded_kernel(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, int has_geometry,
+                                const float* __restrict__ rays, const float* __restrict__ tmax, uint32_t n,
+                                uint8_t* __restrict__ hit, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const v3 o = load3(rays + (size_t)i * 6), d = load3(rays + (size_t)i * 6 + 3);
+    bool h = false;
+    if (has_geometry) h = any_hit(nodes, tris, make_wray(o, d), make_inv(d), tmax[i], err);
+    hit[i] = h ? 1 : 0;
+}
+
+}  // namespace
+
+int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s) {
+    // the tile counter sits in the word after the error word
+    uint32_t* tile_ctr = p.err_word + 1;
+    cudaMemsetAsync(tile_ctr, 0, 4, s);
+    const int blocks = sm_count * 4;
+    trace_kernel<<<blocks, 256, 0, s>>>(p, tile_ctr);
+    return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
+}
+
+int launch_occluded(const Node4* nodes, const LeafTri* tris, int has_geometry, const float* rays, const float* tmax,
+                    uint32_t n, uint8_t* hit, uint32_t* err_word, cudaStream_t s) {
+    if (n == 0) return RN_OK;
+    occluded_kernel<<<(n + 255) / 256, 256, 0, s>>>(nodes, tris, has_geometry, rays, tmax, n, hit, err_word);
+    return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
+}
+
+}  // namespace rn

@@ -1,0 +1,318 @@
+"""Python face of librn_ao.so, the sm_103a AO path of raw-native.
+
+The names follow the reference's C++ API so a test reads like the reference's own:
+``LinearAccel`` (raw/renderer/accel.hpp:15-23), ``compute_rtao`` / ``compute_rt_visibility``
+(raw/renderer/ray_ao.hpp:6-14), ``compute_ssao`` (raw/renderer/ssao.hpp:5-6), ``reconcile``
+(raw/cert/reconcile.hpp:12-13) and ``build_ploc`` (raw/renderer/rt_bvh.hpp:45).
+
+Arrays may be numpy arrays (host: the library copies in and out) or CUDA tensors (device:
+the work is queued on torch's current stream and nothing is copied). Every call goes to the
+GPU library; there is no CPU path, and a missing library or device raises ``RnError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librn_ao.so")
+
+RN_DEVICE_PTRS, RN_SKY, RN_SUN_FORCED, RN_DEVICE_TRIG = 0x1, 0x2, 0x4, 0x8
+RT_SAMPLES, SS_SAMPLES, AO_RADIUS, TOLERANCE = 64, 24, 2.0, 0.12
+
+ERROR_NAMES = {0: "RN_OK", 1: "RN_ERR_INVALID", 2: "RN_ERR_NO_DEVICE", 3: "RN_ERR_CUDA", 4: "RN_ERR_NO_MEMORY",
+               5: "RN_ERR_OVERFLOW", 6: "RN_ERR_BUDGET", 7: "RN_ERR_STATE"}
+
+# Every symbol include/rn_ao.h declares.
+EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_accel_build", "rn_accel_free",
+           "rn_accel_info", "rn_ao_visibility", "rn_ssao", "rn_reconcile", "rn_ao_frame", "rn_ploc_build",
+           "rn_occluded")
+
+
+class RnError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__("%s: %s" % (ERROR_NAMES.get(code, str(code)), message))
+        self.code = code
+        self.message = message
+
+
+class Status(C.Structure):
+    _fields_ = [("code", C.c_int), ("message", C.c_char * 240)]
+
+
+class GBuf(C.Structure):
+    _fields_ = [("w", C.c_int), ("h", C.c_int), ("position", C.c_void_p), ("normal", C.c_void_p),
+                ("mask", C.c_void_p)]
+
+
+class ReconcileOut(C.Structure):
+    _fields_ = [("rmse", C.c_float), ("max_error", C.c_float), ("pixels", C.c_int32),
+                ("within_tolerance", C.c_int32), ("sum_sq", C.c_double)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load librn_ao.so; raise when it is not built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RnError(2, "librn_ao.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        vp, st = C.c_void_p, C.POINTER(Status)
+        L.rn_ao_version.restype = C.c_int
+        L.rn_init.argtypes = [st]
+        L.rn_set_stream.argtypes = [vp, st]
+        L.rn_synchronize.argtypes = [st]
+        L.rn_accel_build.argtypes = [vp, C.c_uint32, C.c_int, C.POINTER(vp), st]
+        L.rn_accel_free.argtypes = [vp]
+        L.rn_accel_free.restype = None
+        L.rn_accel_info.argtypes = [vp, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), st]
+        L.rn_ao_visibility.argtypes = [C.POINTER(GBuf), vp, C.c_int, C.c_float, vp, C.c_int, vp, vp, vp, st]
+        L.rn_ssao.argtypes = [C.POINTER(GBuf), C.c_int, C.c_float, C.c_int, vp, st]
+        L.rn_reconcile.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, C.c_int, vp, C.POINTER(ReconcileOut), st]
+        L.rn_ao_frame.argtypes = [C.POINTER(GBuf), vp, C.c_int, C.c_float, C.c_int, C.c_float, vp, C.c_int, vp, vp,
+                                  vp, vp, vp, C.POINTER(ReconcileOut), st]
+        L.rn_ploc_build.argtypes = [vp, C.c_uint32, C.c_int, C.c_int, vp, C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_uint32), st]
+        L.rn_occluded.argtypes = [vp, vp, vp, C.c_uint32, C.c_int, vp, st]
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, st: Status) -> None:
+    if rc != 0:
+        raise RnError(rc, st.message.decode(errors="replace"))
+
+
+def init() -> None:
+    st = Status()
+    _check(lib().rn_init(C.byref(st)), st)
+
+
+def synchronize() -> None:
+    st = Status()
+    _check(lib().rn_synchronize(C.byref(st)), st)
+
+
+# ---------------------------------------------------------------- array plumbing
+def _is_cuda(a) -> bool:
+    return hasattr(a, "is_cuda") and a.is_cuda
+
+
+def _use_torch_stream() -> None:
+    import torch
+    st = Status()
+    _check(lib().rn_set_stream(C.c_void_p(torch.cuda.current_stream().cuda_stream), C.byref(st)), st)
+
+
+class _Args:
+    """Collects pointers for one call; all arrays are either host or CUDA."""
+
+    def __init__(self, *arrays):
+        present = [a for a in arrays if a is not None]
+        self.device = bool(present) and _is_cuda(present[0])
+        for a in present:
+            if _is_cuda(a) != self.device:
+                raise RnError(1, "mix of host and CUDA arrays in one call")
+        self.keep = []
+        if self.device:
+            _use_torch_stream()
+
+    def ptr(self, a, dtype):
+        if a is None:
+            return None
+        if self.device:
+            import torch
+            tdt = {np.float32: torch.float32, np.uint8: torch.uint8, np.int32: torch.int32}[dtype]
+            if a.dtype != tdt or not a.is_contiguous():
+                raise RnError(1, "CUDA array must be contiguous %s" % tdt)
+            return C.c_void_p(a.data_ptr())
+        arr = np.ascontiguousarray(a, dtype=dtype)
+        self.keep.append(arr)
+        return C.c_void_p(arr.ctypes.data)
+
+    def out(self, like, shape, dtype):
+        if self.device:
+            import torch
+            tdt = {np.float32: torch.float32, np.uint8: torch.uint8, np.int32: torch.int32}[dtype]
+            return torch.empty(shape, dtype=tdt, device=like.device)
+        return np.empty(shape, dtype)
+
+    @property
+    def flags(self) -> int:
+        return RN_DEVICE_PTRS if self.device else 0
+
+
+@dataclasses.dataclass
+class GBuffer:
+    """raw::GBuffer's AO inputs (raw/renderer/gbuffer.hpp:7-21): position and normal as
+    (h, w, 3) float32, mask as (h, w) uint8."""
+    position: object
+    normal: object
+    mask: object
+
+    @property
+    def shape(self):
+        return tuple(self.mask.shape)
+
+
+def _gbuf(g: GBuffer, args: _Args) -> GBuf:
+    h, w = g.shape
+    return GBuf(w, h, args.ptr(g.position, np.float32), args.ptr(g.normal, np.float32), args.ptr(g.mask, np.uint8))
+
+
+# ---------------------------------------------------------------- accelerator
+class LinearAccel:
+    """The occlusion accelerator over a triangle list (n, 9) float32, built on the GPU
+    (PLOC, collapsed to 4-wide nodes). Replaces raw::LinearAccel::build."""
+
+    def __init__(self, tris):
+        args = _Args(tris)
+        n = int(tris.shape[0]) if tris is not None else 0
+        self._h = C.c_void_p()
+        st = Status()
+        _check(lib().rn_accel_build(args.ptr(tris, np.float32), n, args.flags, C.byref(self._h), C.byref(st)), st)
+        self.ntri = n
+
+    def info(self) -> dict:
+        a, b, c = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        st = Status()
+        _check(lib().rn_accel_info(self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(st)), st)
+        return dict(wide_nodes=a.value, leaf_tris=b.value, ploc_rounds=c.value)
+
+    def close(self) -> None:
+        if self._h:
+            lib().rn_accel_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+
+# ---------------------------------------------------------------- the three passes
+def compute_rt_visibility(g: GBuffer, accel: LinearAccel, samples: int, radius: float, to_light=None,
+                          sun_forced: bool = False, device_trig: bool = False):
+    """computeRTVisibility when to_light is given: (ao, sky, sun); computeRTAO otherwise: ao."""
+    args = _Args(g.position, g.normal, g.mask)
+    gb = _gbuf(g, args)
+    h, w = g.shape
+    ao = args.out(g.mask, (h, w), np.float32)
+    sky = sun = None
+    flags = args.flags | (RN_DEVICE_TRIG if device_trig else 0)
+    tl = None
+    if to_light is not None:
+        flags |= RN_SKY | (RN_SUN_FORCED if sun_forced else 0)
+        sky = args.out(g.mask, (h, w), np.float32)
+        sun = args.out(g.mask, (h, w), np.float32)
+        tl = (C.c_float * 3)(*[float(v) for v in to_light])
+    st = Status()
+    rc = lib().rn_ao_visibility(C.byref(gb), accel.handle, int(samples), float(radius),
+                                C.cast(tl, C.c_void_p) if tl is not None else None, flags,
+                                args.ptr(ao, np.float32), args.ptr(sky, np.float32), args.ptr(sun, np.float32),
+                                C.byref(st))
+    _check(rc, st)
+    return ao if to_light is None else (ao, sky, sun)
+
+
+def compute_rtao(g: GBuffer, accel: LinearAccel, samples: int, radius: float, device_trig: bool = False):
+    return compute_rt_visibility(g, accel, samples, radius, None, device_trig=device_trig)
+
+
+def compute_ssao(g: GBuffer, samples: int = SS_SAMPLES, radius: float = AO_RADIUS, device_trig: bool = False):
+    args = _Args(g.position, g.normal, g.mask)
+    gb = _gbuf(g, args)
+    out = args.out(g.mask, g.shape, np.float32)
+    st = Status()
+    flags = args.flags | (RN_DEVICE_TRIG if device_trig else 0)
+    _check(lib().rn_ssao(C.byref(gb), int(samples), float(radius), flags, args.ptr(out, np.float32), C.byref(st)), st)
+    return out
+
+
+@dataclasses.dataclass
+class ReconcileResult:
+    """raw::ReconcileResult (raw/cert/reconcile.hpp:6-11) plus the FP64 sum it came from."""
+    error_map: object
+    rmse: float
+    max_error: float
+    pixels: int
+    within_tolerance: bool
+    sum_sq: float
+
+
+def _result(err, r: ReconcileOut) -> ReconcileResult:
+    return ReconcileResult(err, r.rmse, r.max_error, r.pixels, bool(r.within_tolerance), r.sum_sq)
+
+
+def reconcile(approx, truth, mask, tolerance: float = TOLERANCE, error_map: bool = True) -> ReconcileResult:
+    args = _Args(approx, truth, mask)
+    h, w = tuple(mask.shape)
+    err = args.out(mask, (h, w), np.float32) if error_map else None
+    r = ReconcileOut()
+    st = Status()
+    _check(lib().rn_reconcile(args.ptr(approx, np.float32), args.ptr(truth, np.float32), args.ptr(mask, np.uint8),
+                              w, h, float(tolerance), args.flags, args.ptr(err, np.float32), C.byref(r),
+                              C.byref(st)), st)
+    return _result(err, r)
+
+
+def ao_frame(g: GBuffer, accel: LinearAccel, samples: int = RT_SAMPLES, radius: float = AO_RADIUS,
+             ss_samples: int = SS_SAMPLES, tolerance: float = TOLERANCE, to_light=None, sun_forced=False,
+             outputs=None, device_trig: bool = False):
+    """The AO passes of one frame (render.cpp:29-54): returns dict(ao, sky, sun, ss, err, rec).
+    `outputs` may pass preallocated arrays under the same keys."""
+    args = _Args(g.position, g.normal, g.mask)
+    gb = _gbuf(g, args)
+    h, w = g.shape
+    o = dict(outputs or {})
+    for k in ("ao", "ss", "err") + (("sky", "sun") if to_light is not None else ()):
+        if o.get(k) is None:
+            o[k] = args.out(g.mask, (h, w), np.float32)
+    flags = args.flags | (RN_DEVICE_TRIG if device_trig else 0)
+    tl = None
+    if to_light is not None:
+        flags |= RN_SKY | (RN_SUN_FORCED if sun_forced else 0)
+        tl = (C.c_float * 3)(*[float(v) for v in to_light])
+    r = ReconcileOut()
+    st = Status()
+    p = {k: (args.ptr(v, np.float32) if v is not None else None) for k, v in o.items()}
+    rc = lib().rn_ao_frame(C.byref(gb), accel.handle, int(samples), float(radius), int(ss_samples), float(tolerance),
+                           C.cast(tl, C.c_void_p) if tl is not None else None, flags, p["ao"], p.get("sky"),
+                           p.get("sun"), p["ss"], p["err"], C.byref(r), C.byref(st))
+    _check(rc, st)
+    o["rec"] = _result(o["err"], r)
+    return o
+
+
+def build_ploc(tris, radius: int = 16):
+    """rt::buildPloc on the GPU: (nodes (2n-1, 9) int32, root, rounds)."""
+    args = _Args(tris)
+    n = int(tris.shape[0])
+    nodes = args.out(tris, (max(2 * n - 1, 1), 9), np.int32)
+    root, rounds = C.c_int32(), C.c_uint32()
+    st = Status()
+    _check(lib().rn_ploc_build(args.ptr(tris, np.float32), n, int(radius), args.flags, args.ptr(nodes, np.int32),
+                               C.byref(root), C.byref(rounds), C.byref(st)), st)
+    return nodes, root.value, rounds.value
+
+
+def occluded(accel: LinearAccel, rays, t_max):
+    """Any-hit for a list of rays (n, 6): uint8 hit flags."""
+    args = _Args(rays, t_max)
+    n = int(rays.shape[0])
+    hit = args.out(rays, (n,), np.uint8)
+    st = Status()
+    _check(lib().rn_occluded(accel.handle, args.ptr(rays, np.float32), args.ptr(t_max, np.float32), n, args.flags,
+                             args.ptr(hit, np.uint8), C.byref(st)), st)
+    return hit

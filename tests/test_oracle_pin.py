@@ -1,0 +1,138 @@
+"""The oracle is pinned before it is trusted: its C restatement must reproduce the
+reference's committed SHA-256 goldens (tests/golden/identity.json, taken from the
+reference's evidence/identity-golden.json) byte for byte, the reference's exact reconcile
+numbers, and the PLOC tree hashes of the reference's GPU evidence. Where the reference's
+own sources were compiled here (oracle/_ref), the restatement is also compared with them.
+
+The goldens were made on x86-64 with glibc's libm; a host whose libm rounds cosf, sinf or
+tanf differently reproduces the algorithm but not those bytes, and says so by skipping.
+"""
+import json
+import os
+import platform
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+IDENT = json.load(open(os.path.join(HERE, "golden", "identity.json")))
+PLOC = json.load(open(os.path.join(HERE, "golden", "ploc.json")))
+X86 = platform.machine() in ("x86_64", "AMD64")
+
+
+def _digests(O, r, w, h):
+    return {"ao_rt.pfm": O.sha256(O.pfm1_bytes(r["ao"])), "ao_ss.pfm": O.sha256(O.pfm1_bytes(r["ss"])),
+            "mask.pgm": O.sha256(O.mask_pgm_bytes(r["mask"])), "ao_error.pgm": O.sha256(O.pgm_bytes(r["err"]))}
+
+
+@pytest.mark.parametrize("case", sorted(IDENT["cases"]))
+def test_oracle_reproduces_reference_goldens(oracle, case):
+    c = IDENT["cases"][case]
+    r = oracle.render_default(c["width"], c["height"], c["camera"], threads=os.cpu_count() or 1)
+    got = _digests(oracle, r, c["width"], c["height"])
+    if got != c["files"] and not X86:
+        pytest.skip("host libm differs from the x86-64 golden host (%s)" % platform.machine())
+    assert got == c["files"]
+    assert oracle.sha256(oracle.pfm1_bytes(r["sky"])) == c["sky_sha256"]
+    assert oracle.sha256(oracle.pfm1_bytes(r["sun"])) == c["sun_sha256"]
+    st = r["stats"]
+    assert st["pixels"] == c["exact"]["pixels"]
+    assert np.float32(st["rmse"]) == np.float32(c["exact"]["rmse"])
+    assert np.float32(st["maxError"]) == np.float32(c["exact"]["maxError"])
+    assert st["within"] == c["exact"]["within"]
+
+
+def test_default_certificate_numbers(oracle):
+    # docs/examples/default-certificate.json: pixels 151984, rmse 0.134912357, maxError 0.640625
+    c = IDENT["cases"]["default-512"]["exact"]
+    assert c["pixels"] == 151984 and "%.9g" % c["rmse"] == "0.134912357" and c["maxError"] == 0.640625
+    assert not c["within"]
+
+
+def test_ploc_soup_tree_hash(oracle):
+    s = PLOC["scenes"]["soup"]
+    tris = oracle.soup(s["count"], s["seed"])
+    nodes, root, rounds = oracle.ploc(tris)
+    assert oracle.tree_hash(nodes) == s["tree_hash"]
+    assert rounds == s["rounds"]
+    assert root == 2 * s["count"] - 2
+
+
+def test_ploc_test_scene_tree_hash(oracle):
+    s = PLOC["scenes"]["test_scene"]
+    tris, _, _ = oracle.test_scene()
+    nodes, root, rounds = oracle.ploc(tris)
+    assert (oracle.tree_hash(nodes), root, rounds) == (s["tree_hash"], s["root"], s["rounds"])
+
+
+def test_ploc_radius_control_changes_tree(oracle):
+    # the reference's false-success control: radius 8 must give another tree
+    tris = oracle.soup(2000, 3)
+    assert oracle.tree_hash(oracle.ploc(tris, 16)[0]) != oracle.tree_hash(oracle.ploc(tris, 8)[0])
+
+
+def test_reconcile_two_pixels(oracle):
+    # tests/test_reconcile.cpp:4-19
+    a = np.array([[0.5, 0.8]], np.float32)
+    b = np.array([[0.5, 0.4]], np.float32)
+    m = np.ones((1, 2), np.uint8)
+    err, st = oracle.reconcile(a, b, m, 0.1)
+    assert abs(err[0, 0]) < 1e-6 and abs(err[0, 1] - 0.4) < 1e-6
+    assert abs(st["maxError"] - 0.4) < 1e-6 and st["pixels"] == 2 and not st["within"]
+    _, st2 = oracle.reconcile(a, a, m, 0.1)
+    assert st2["rmse"] == 0.0 and st2["within"]
+
+
+def test_bvh_equals_scan_on_random_rays(oracle):
+    # tests/test_bvh.cpp: seeded rays, the BVH's any-hit answer equals the scan's
+    tris = oracle.soup(3000, 11)
+    rng = np.random.default_rng(5)
+    import ctypes as C
+    L = oracle.lib()
+    h = L.rno_accel_build(np.ascontiguousarray(tris), len(tris))
+    try:
+        bad = 0
+        for _ in range(4000):
+            o = rng.uniform(-14, 14, 3).astype(np.float32)
+            d = rng.normal(size=3).astype(np.float32)
+            d /= np.float32(np.linalg.norm(d))
+            ray = np.concatenate([o, d]).astype(np.float32)
+            for tmax in (np.float32(2.0), np.float32(1e30)):
+                bad += L.rno_occluded(h, ray, tmax) != L.rno_occluded_scan(np.ascontiguousarray(tris), len(tris), ray, tmax)
+        assert bad == 0
+    finally:
+        L.rno_accel_free(h)
+
+
+def test_thread_count_invariance(oracle):
+    # tests/test_verify.cpp:40-43: output identical for any thread count
+    a = oracle.render_default(128, 96, threads=1)
+    b = oracle.render_default(128, 96, threads=5)
+    for k in ("ao", "sky", "sun", "ss", "err"):
+        assert np.array_equal(a[k], b[k])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libref_ao.so")),
+                    reason="the reference's own sources are not compiled on this host")
+def test_restatement_equals_reference_build(oracle):
+    import ctypes as C
+    R = oracle.ref()
+    rng = np.random.default_rng(1)
+    for cam in ([4, 4, 6, 0, 1, 0, 0, 1, 0, 0.9], [3, 1.2, -4, 0, 0.5, 0, 0, 1, 0, 1.1]):
+        w, h = 160, 120
+        r = oracle.render_default(w, h, cam, spp=13, radius=1.5, threads=4)
+        n = w * h
+        b = {k: np.zeros(n * (3 if k in ("pos", "nrm") else 1), np.uint8 if k == "mask" else np.float32)
+             for k in ("pos", "nrm", "mask", "ao", "sky", "sun", "ss", "err")}
+        st = np.zeros(4, np.float32)
+        R.ref_render_default(w, h, np.array(cam, np.float32), 13, 1.5, 24, 0.12, 4, b["pos"], b["nrm"], b["mask"],
+                             b["ao"], b["sky"], b["sun"], b["ss"], b["err"], st)
+        for k in ("ao", "sky", "sun", "ss", "err"):
+            assert np.array_equal(r[k].ravel(), b[k]), k
+        assert np.array_equal(r["mask"].ravel(), b["mask"])
+    tris = oracle.soup(5000, int(rng.integers(1, 1000)))
+    nodes, root, rounds = oracle.ploc(tris)
+    out = np.zeros((2 * len(tris) - 1, 9), np.int32)
+    rr = C.c_uint32()
+    assert R.ref_ploc(tris, len(tris), 16, out, C.byref(rr)) == root
+    assert np.array_equal(out, nodes) and rr.value == rounds
