@@ -1,0 +1,355 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 AO path on the 4K workload.
+
+Workload: the reference's built-in scene and default camera at 3840 x 2160, ray-traced AO at
+256 cosine-weighted rays per pixel with lighting model 2's sky and sun visibility (radius 2),
+SSAO with 24 taps, and the reconcile (tolerance 0.12): one "step" is one such AO frame, the
+three passes of src/renderer/render.cpp:29-54. Inputs are synthetic (the built-in scene,
+rasterized on the GPU by this library); no dataset is involved.
+
+  value    AO Grays/s over all ranks, G-buffer resident in HBM, device pointers (the 207 MB
+           G-buffer exceeds the 129 MB L2, so no flush is needed between steps)
+  e2e      the same metric through the C ABI with pinned host buffers: the G-buffer copied
+           in and ao, sky, sun, ss and the error map copied out every step
+  roofline the traversal kernel (trace_kernel): algorithmic bytes per launch = 4-wide node
+           fetches x 128 B + leaf-triangle fetches x 48 B, from the library's traversal
+           counters over the whole frame, divided by the kernel's CUDA-event time
+  cpu_baseline  the oracle (a C restatement of the reference's CPU path) on this host's
+           cores, on every 4th row of the same frame
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "raw-native_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+W_PX, H_PX, SPP, RADIUS, SS_SAMPLES, TOL = 3840, 2160, 256, 2.0, 24, 0.12
+METRIC = "4K AO ms/frame at RMSE<=0.02 vs 1024-spp: surrogate vs plain GPU RT; AO Grays/s"
+WORKLOAD = ("plain GPU RT AO frame, built-in scene (14 triangles), default camera, 3840x2160, 256 spp, "
+            "sky+sun visibility, SSAO 24 taps, reconcile")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--cpu-row-stride", type=int, default=4, help="rows of the CPU sample: every n-th")
+    p.add_argument("--profile", choices=["frame", "trace", "ssao", "reconcile", "build"],
+                   help="run only this pass `--steps` times after `--warmup` (for ncu), print nothing")
+    p.add_argument("--spp", type=int, default=SPP, help="samples per pixel (the benchmark uses 256)")
+    p.add_argument("--tris", type=int, default=1000000, help="--profile build: soup triangles")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+# ---------------------------------------------------------------- clocks during the timed region
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r for r in csv.reader(io.StringIO(self.file.read())) if len(r) >= 9]
+        os.unlink(self.file.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "", 1).isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "", 1).isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    try:
+        mp = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(mp["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """dram bytes per trace_kernel launch from the committed ncu summary (bytes, or None)."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "trace_kernel_4k_256spp.json")))
+        return float(d["dram_bytes_per_launch"])
+    except Exception:
+        return None
+
+
+# ---------------------------------------------------------------- CPU (oracle) timing
+def cpu_frame_sample(row_stride: int, threads: int):
+    """The oracle's AO frame on every row_stride-th row: (AO rays traced, seconds)."""
+    from oracle import oracle as O
+    import numpy as np
+    import ctypes as C
+    tris, nrm9, light = O.test_scene()
+    _, pos, nrm, mask = O.rasterize(tris, nrm9, O.DEFAULT_CAMERA, W_PX, H_PX)
+    L = O.lib()
+    ao = np.zeros((H_PX, W_PX), np.float32)
+    sky = np.zeros_like(ao)
+    sun = np.zeros_like(ao)
+    tl = (C.c_float * 3)(*(-light))
+    acc = L.rno_accel_build(np.ascontiguousarray(tris), len(tris))
+    rows = np.arange(0, H_PX, row_stride)
+    t0 = time.perf_counter()
+    L.rno_trace(W_PX, H_PX, pos, nrm, mask, acc, tris, len(tris), SPP, RADIUS, C.cast(tl, C.c_void_p), 0, ao,
+                sky.ctypes.data_as(C.c_void_p), sun.ctypes.data_as(C.c_void_p), threads, 0, row_stride)
+    sub = np.ascontiguousarray(mask[rows])
+    ss = O.ssao(np.ascontiguousarray(pos[rows]), np.ascontiguousarray(nrm[rows]), sub, SS_SAMPLES, RADIUS, threads)
+    O.reconcile(ss, np.ascontiguousarray(ao[rows]), sub, TOL)
+    dt = time.perf_counter() - t0
+    L.rno_accel_free(acc)
+    return int(sub.sum()) * SPP, dt, len(rows)
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    stride = max(args.cpu_row_stride * 2, 1)
+    for _ in range(args.warmup):
+        cpu_frame_sample(stride * 4, threads)
+    rays, secs = 0, 0.0
+    for _ in range(args.steps):
+        r, dt, nrows = cpu_frame_sample(stride, threads)
+        rays += r
+        secs += dt
+    v = rays / secs / 1e9
+    sample = "every %dth row of the 4K frame (%d rows), visibility + SSAO + reconcile, oracle port (SAH BVH)" % (
+        stride, nrows)
+    print(json.dumps({
+        "metric": METRIC, "value": v, "unit": "Grays/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "width": W_PX, "height": H_PX, "spp": SPP, "radius": RADIUS,
+                   "ss_samples": SS_SAMPLES, "tolerance": TOL, "sample": sample},
+        "cpu_baseline": {"value": v, "unit": "Grays/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "Grays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ---------------------------------------------------------------- GPU
+def run_ours(args):
+    import numpy as np
+    import torch
+    import rn_ao as rn
+    import scene as scenes
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    rn.init()
+    sc = scenes.build_test_scene()
+    tris = torch.from_numpy(sc.tris).cuda()
+    nrms = torch.from_numpy(sc.normals).cuda()
+    g = rn.rasterize(tris, nrms, sc.camera, W_PX, H_PX)
+    t0 = time.perf_counter()
+    acc = rn.LinearAccel(tris)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    covered = int(g.mask.sum().item())
+    rays = covered * SPP
+    outs = {k: torch.empty(H_PX, W_PX, device="cuda") for k in ("ao", "sky", "sun", "ss", "err")}
+    tl = sc.to_light
+
+    def frame():
+        return rn.ao_frame(g, acc, SPP, RADIUS, SS_SAMPLES, TOL, to_light=tl, outputs=outs)
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if not pg:
+            return x
+        t = torch.tensor([x], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
+    stream = torch.cuda.current_stream()
+    # ---- resident: device pointers
+    for _ in range(args.warmup):
+        frame()
+    torch.cuda.synchronize()
+    barrier()
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            last = frame()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    clocks = clk.summary()
+    value = world * rays / (ms * 1e-3) / 1e9
+    rec = last["rec"]
+
+    # ---- end to end: pinned host buffers through the C ABI
+    hpos = g.position.cpu().pin_memory()
+    hnrm = g.normal.cpu().pin_memory()
+    hmask = g.mask.cpu().pin_memory()
+    hg = rn.GBuffer(hpos.numpy(), hnrm.numpy(), hmask.numpy())
+    houts = {k: torch.empty(H_PX, W_PX).pin_memory().numpy() for k in ("ao", "sky", "sun", "ss", "err")}
+    for _ in range(args.warmup):
+        rn.ao_frame(hg, acc, SPP, RADIUS, SS_SAMPLES, TOL, to_light=tl, outputs=houts)
+    torch.cuda.synchronize()
+    barrier()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for _ in range(args.steps):
+        rn.ao_frame(hg, acc, SPP, RADIUS, SS_SAMPLES, TOL, to_light=tl, outputs=houts)
+    e3.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = max_over_ranks(e2.elapsed_time(e3) / args.steps)
+    h2d = hpos.numel() * 4 + hnrm.numel() * 4 + hmask.numel()
+    d2h = 5 * H_PX * W_PX * 4 + 24
+    same = np.array_equal(houts["ao"], outs["ao"].cpu().numpy()) and np.array_equal(houts["err"], outs["err"].cpu().numpy())
+
+    # ---- roofline of the dominant kernel: the traversal
+    stats = rn.trace_stats(g, acc, SPP, RADIUS, to_light=tl, tile_stride=1)
+    alg_bytes = stats["nodes"] * 128 + stats["tris"] * 48
+    for _ in range(2):
+        rn.compute_rt_visibility(g, acc, SPP, RADIUS, tl)
+    torch.cuda.synchronize()
+    e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nvis = max(3, args.steps // 2)
+    e4.record(stream)
+    for _ in range(nvis):
+        rn.compute_rt_visibility(g, acc, SPP, RADIUS, tl)
+    e5.record(stream)
+    torch.cuda.synchronize()
+    trace_ms = e4.elapsed_time(e5) / nvis
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / (trace_ms * 1e-3) / 1e9
+    traffic = committed_traffic()
+
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1:
+        r, dt, nrows = cpu_frame_sample(args.cpu_row_stride, os.cpu_count() or 1)
+        cpu = {"value": r / dt / 1e9, "unit": "Grays/s", "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": "every %dth row of the same 4K frame (%d rows, %.1f s): visibility + SSAO + reconcile, "
+                         "oracle port with its SAH BVH" % (args.cpu_row_stride, nrows, dt)}
+    out = {
+        "metric": METRIC, "value": value, "unit": "Grays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "width": W_PX, "height": H_PX, "spp": SPP, "radius": RADIUS,
+                   "ss_samples": SS_SAMPLES, "tolerance": TOL, "covered_px": covered, "ao_rays_per_step": rays,
+                   "parallelism": "replicas (one full frame per GPU)" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2: 207 MB G-buffer > 129 MB L2, no flush",
+                   "bvh_build_ms": round(build_ms, 3)},
+        "ms_per_frame": ms,
+        "frame_result": {"rmse": rec.rmse, "max_error": rec.max_error, "pixels": rec.pixels,
+                         "within_tolerance": rec.within_tolerance},
+        "e2e": {"value": world * rays / (e2e_ms * 1e-3) / 1e9, "unit": "Grays/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "matches_resident": bool(same)},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "trace_kernel", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": trace_ms,
+                     "rays_per_launch": stats["rays"], "sky_rays_per_launch": stats["sky_rays"],
+                     "node_fetches_per_ray": stats["nodes"] / max(1, stats["rays"] + stats["sky_rays"]),
+                     "tri_fetches_per_ray": stats["tris"] / max(1, stats["rays"] + stats["sky_rays"])},
+        "clocks": clocks,
+    }
+    if cpu:
+        out["cpu_baseline"] = cpu
+    print(json.dumps(out), flush=True)
+
+
+def run_profile(args):
+    """One pass, repeated, for a profiler: the 4K G-buffer and accelerator are built first."""
+    import torch
+    import rn_ao as rn
+    import scene as scenes
+    torch.cuda.set_device(0)
+    rn.init()
+    sc = scenes.build_test_scene()
+    tris = torch.from_numpy(sc.tris).cuda()
+    g = rn.rasterize(tris, torch.from_numpy(sc.normals).cuda(), sc.camera, W_PX, H_PX)
+    acc = rn.LinearAccel(tris)
+    outs = {k: torch.empty(H_PX, W_PX, device="cuda") for k in ("ao", "sky", "sun", "ss", "err")}
+    if args.profile == "build":
+        import numpy as np
+        rng = np.random.default_rng(1)
+        c = rng.uniform(-50, 50, (args.tris, 1, 3)).astype(np.float32)
+        t = (c + rng.uniform(-1, 1, (args.tris, 3, 3)).astype(np.float32)).reshape(args.tris, 9)
+        soup = torch.from_numpy(np.ascontiguousarray(t)).cuda()
+    fn = {"frame": lambda: rn.ao_frame(g, acc, args.spp, RADIUS, SS_SAMPLES, TOL, to_light=sc.to_light, outputs=outs),
+          "trace": lambda: rn.compute_rt_visibility(g, acc, args.spp, RADIUS, sc.to_light),
+          "ssao": lambda: rn.compute_ssao(g, SS_SAMPLES, RADIUS),
+          "reconcile": lambda: rn.reconcile(outs["ss"], outs["ao"], g.mask, TOL),
+          "build": lambda: rn.LinearAccel(soup)}[args.profile]
+    for _ in range(args.warmup + args.steps):
+        fn()
+    torch.cuda.synchronize()
+
+
+def main():
+    args = parse()
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -95,7 +95,8 @@ int rn_ao_version(void);
  * on first use; call it early to keep that set-up out of a timed region or a capture. */
 int rn_init(rn_status* st);
 
-/* Use `stream` (a cudaStream_t, NULL = the library's own) for all later work. */
+/* Use `stream` (a cudaStream_t; NULL = the library's own non-blocking stream; pass
+ * cudaStreamLegacy to order with the legacy default stream) for all later work. */
 int rn_set_stream(void* stream, rn_status* st);
 
 /* Wait for all work queued on the library's stream. */
@@ -161,6 +162,25 @@ int rn_ploc_build(const float* tris, uint32_t ntri, int radius, int flags, int32
  * mode of the rt_trace pass (src/renderer/gpu/shaders/rt.wgsl:306-446). */
 int rn_occluded(const rn_accel* accel, const float* rays, const float* t_max, uint32_t nrays,
                 int flags, uint8_t* hit, rn_status* st);
+
+/* The G-buffer planes the AO passes read, rasterized on the GPU. Replaces raw::rasterize
+ * (raw/renderer/raster.hpp:9, src/renderer/raster.cpp:92-126) with its default options:
+ * `tris` and `nrm` hold 9 floats per triangle (the corners' positions and vertex normals,
+ * in scene order); `cam` (host, 10 floats) = eye, target, up, fovy, with aspect w / h and
+ * near/far 0.1/100 as raw::Camera (raw/scene/scene.hpp:12-17). Bit-identical to the CPU
+ * rasterizer: the winner per pixel, its screen-linear depth, position and normal. Uncovered
+ * pixels: depth +inf, position and normal 0, mask 0. `depth` may be NULL. */
+int rn_raster_gbuffer(const float* tris, const float* nrm, uint32_t ntri, const float* cam, int w, int h,
+                      int flags, float* depth, float* position, float* normal, uint8_t* mask,
+                      rn_status* st);
+
+/* Traversal counters for roofline accounting (no counterpart in the reference): runs the
+ * visibility pass with per-ray counting on every `tile_stride`-th 8x4 tile and writes
+ * counts[0] = hemisphere rays, [1] = 4-wide node fetches (128 B each), [2] = leaf-triangle
+ * fetches (48 B each), [3] = sky continuation rays. Writes no image outputs. */
+int rn_ao_trace_stats(const rn_gbuf* g, const rn_accel* accel, int spp, float radius,
+                      const float* to_light, int flags, uint32_t tile_stride, uint64_t* counts,
+                      rn_status* st);
 
 #ifdef __cplusplus
 }  /* extern "C" */

@@ -238,6 +238,53 @@ int check_vis_args(const rn_gbuf* g, const rn_accel* accel, int spp, const float
     return RN_OK;
 }
 
+// raw/math/mat.hpp:9-35 and raw/scene/scene.hpp:12-17 on the host: the view-projection
+// matrix of a camera (eye, target, up, fovy; aspect = w / h; near 0.1, far 100), in the
+// reference's float operation order (this file's host code builds with -ffp-contract=off).
+struct M4 { float m[16]; };
+M4 m4_mul(const M4& a, const M4& b) {
+    M4 r{};
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            float s = 0;
+            for (int k = 0; k < 4; ++k) s += a.m[i * 4 + k] * b.m[k * 4 + j];
+            r.m[i * 4 + j] = s;
+        }
+    return r;
+}
+void h_norm(const float v[3], float o[3]) {
+    const float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (l > 0) { const float i = 1.0f / l; o[0] = v[0] * i; o[1] = v[1] * i; o[2] = v[2] * i; }
+    else { o[0] = v[0]; o[1] = v[1]; o[2] = v[2]; }
+}
+void h_cross(const float a[3], const float b[3], float o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+}
+float h_dot(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+M4 view_proj(const float* cam, int w, int h, float nearZ, float farZ) {
+    const float eye[3] = {cam[0], cam[1], cam[2]}, ctr[3] = {cam[3], cam[4], cam[5]}, up[3] = {cam[6], cam[7], cam[8]};
+    const float d[3] = {ctr[0] - eye[0], ctr[1] - eye[1], ctr[2] - eye[2]};
+    float f[3], s0[3], sv[3], u[3];
+    h_norm(d, f);
+    h_cross(f, up, s0);
+    h_norm(s0, sv);
+    h_cross(sv, f, u);
+    M4 view{};
+    view.m[0] = view.m[5] = view.m[10] = view.m[15] = 1;
+    view.m[0] = sv[0]; view.m[1] = sv[1]; view.m[2] = sv[2]; view.m[3] = -h_dot(sv, eye);
+    view.m[4] = u[0]; view.m[5] = u[1]; view.m[6] = u[2]; view.m[7] = -h_dot(u, eye);
+    view.m[8] = -f[0]; view.m[9] = -f[1]; view.m[10] = -f[2]; view.m[11] = h_dot(f, eye);
+    const float aspect = h > 0 ? (float)w / (float)h : 1.0f;
+    const float t = 1.0f / ::tanf(cam[9] * 0.5f);
+    M4 proj{};
+    proj.m[0] = t / aspect; proj.m[5] = t;
+    proj.m[10] = (farZ + nearZ) / (nearZ - farZ); proj.m[11] = (2 * farZ * nearZ) / (nearZ - farZ);
+    proj.m[14] = -1;
+    return m4_mul(proj, view);
+}
+
 void fill_result(const RecOut& r, float tolerance, rn_reconcile_result* out) {
     out->sum_sq = r.sum;
     out->pixels = r.n;
@@ -468,6 +515,88 @@ int rn_ploc_build(const float* tris, uint32_t ntri, int radius, int flags, int32
     *rounds = tree.rounds;
     ploc_free(&tree);
     return rc == RN_OK ? ok(st) : rc;
+}
+
+int rn_raster_gbuffer(const float* tris, const float* nrm, uint32_t ntri, const float* cam, int w, int h, int flags,
+                      float* depth, float* position, float* normal, uint8_t* mask, rn_status* st) {
+    if ((ntri > 0 && (!tris || !nrm)) || !cam || !position || !normal || !mask)
+        return fail(st, RN_ERR_INVALID, "null argument");
+    if (w <= 0 || h <= 0 || (size_t)w * (size_t)h > ((size_t)1 << 31)) return fail(st, RN_ERR_INVALID, "size %dx%d", w, h);
+    if (ntri >= (1u << 28)) return fail(st, RN_ERR_INVALID, "%u triangles: too many", ntri);
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const size_t np = (size_t)w * h;
+    const float *d_tris = nullptr, *d_nin = nullptr;
+    RN_TRY(stage_in(tris, (size_t)ntri * 9, dev, WS_TRIS_IN, &d_tris, st));
+    RN_TRY(stage_in(nrm, (size_t)ntri * 9, dev, WS_NRM_IN, &d_nin, st));
+    float *d_depth, *d_pos, *d_nrm;
+    uint8_t* d_mask;
+    float* scratch_depth = nullptr;
+    if (depth) RN_TRY(stage_out(depth, np, dev, WS_DEPTH, &d_depth, st));
+    else { void* p; RN_TRY(ws_get(WS_DEPTH, np * 4, &p, st)); d_depth = scratch_depth = (float*)p; }
+    RN_TRY(stage_out(position, np * 3, dev, WS_POS, &d_pos, st));
+    RN_TRY(stage_out(normal, np * 3, dev, WS_NRM, &d_nrm, st));
+    RN_TRY(stage_out(mask, np, dev, WS_MASK, &d_mask, st));
+    const float nearZ = 0.1f, farZ = 100.0f;
+    const M4 vp = view_proj(cam, w, h, nearZ, farZ);
+    void* rec = nullptr;
+    RN_TRY(ws_get(WS_RASTER, raster_records_bytes(ntri) + 64 + 256, &rec, st));
+    float* d_vp = (float*)rec;                                  // 16 floats, then the records
+    void* records = (char*)rec + 256;
+    RN_CUDA(cudaMemcpyAsync(d_vp, vp.m, sizeof vp.m, cudaMemcpyHostToDevice, c.stream), st);
+    if (launch_raster(d_tris, d_nin, ntri, d_vp, nearZ, w, h, records, d_depth, d_pos, d_nrm, d_mask, c.stream) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "raster kernels");
+    if (dev) {
+        // the matrix lives in host memory until the copy runs: wait for it
+        RN_CUDA(cudaStreamSynchronize(c.stream), st);
+        return ok(st);
+    }
+    if (depth) RN_TRY(copy_back(depth, d_depth, np, st));
+    RN_TRY(copy_back(position, d_pos, np * 3, st));
+    RN_TRY(copy_back(normal, d_nrm, np * 3, st));
+    RN_TRY(copy_back(mask, d_mask, np, st));
+    RN_CUDA(cudaStreamSynchronize(c.stream), st);
+    (void)scratch_depth;
+    return ok(st);
+}
+
+int rn_ao_trace_stats(const rn_gbuf* g, const rn_accel* accel, int spp, float radius, const float* to_light, int flags,
+                      uint32_t tile_stride, uint64_t* counts, rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    void* scratch[3];
+    if (!counts) return fail(st, RN_ERR_INVALID, "null counts");
+    const size_t np = g ? (size_t)g->w * g->h : 0;
+    RN_TRY(ws_get(WS_AO, np * 4, &scratch[0], st));
+    RN_TRY(check_vis_args(g, accel, spp, to_light, flags, (float*)scratch[0], (float*)scratch[0], (float*)scratch[0], st));
+    Context& c = ctx();
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    StagedGbuf sg;
+    RN_TRY(stage_gbuf(g, dev, &sg, st));
+    RN_TRY(ws_get(WS_SKY, np * 4, &scratch[1], st));
+    RN_TRY(ws_get(WS_SUN, np * 4, &scratch[2], st));
+    void* cnt = nullptr;
+    RN_TRY(ws_get(WS_STATS, 4 * sizeof(unsigned long long), &cnt, st));
+    RN_CUDA(cudaMemsetAsync(cnt, 0, 4 * sizeof(unsigned long long), c.stream), st);
+    TraceParams p{};
+    p.w = g->w; p.h = g->h;
+    p.pos = sg.pos; p.nrm = sg.nrm; p.mask = sg.mask;
+    p.nodes = accel->d_nodes; p.tris = accel->d_tris;
+    p.has_geometry = accel->ntri > 0;
+    p.spp = spp; p.radius = radius;
+    p.want_sky = (flags & RN_SKY) != 0;
+    p.sun_forced = (flags & RN_SUN_FORCED) != 0;
+    if (p.want_sky) { p.lx = to_light[0]; p.ly = to_light[1]; p.lz = to_light[2]; } else { p.lx = 0; p.ly = 1; p.lz = 0; }
+    p.corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
+    p.ao = (float*)scratch[0]; p.sky = (float*)scratch[1]; p.sun = (float*)scratch[2];
+    p.err_word = c.dev_error;
+    if (launch_trace(p, c.sm_count, c.stream, (unsigned long long*)cnt, tile_stride) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "trace_kernel (counting)");
+    unsigned long long h[4];
+    RN_CUDA(cudaMemcpyAsync(h, cnt, sizeof h, cudaMemcpyDeviceToHost, c.stream), st);
+    RN_TRY(check_device_error(st, "rn_ao_trace_stats"));
+    for (int k = 0; k < 4; ++k) counts[k] = h[k];
+    return ok(st);
 }
 
 int rn_occluded(const rn_accel* accel, const float* rays, const float* t_max, uint32_t nrays, int flags, uint8_t* hit,

@@ -30,6 +30,7 @@ struct DevBuf {
 enum Slot {
     WS_POS, WS_NRM, WS_MASK, WS_AO, WS_SKY, WS_SUN, WS_SS, WS_ERR, WS_TRUTH, WS_APPROX,
     WS_PARTIALS, WS_WORKLIST, WS_COUNTERS, WS_RAYS, WS_TMAX, WS_HITS, WS_TRIS_IN,
+    WS_NRM_IN, WS_RASTER, WS_DEPTH, WS_STATS,
     WS_COUNT
 };
 
@@ -162,7 +163,13 @@ struct TraceParams {
     float* sun;
     uint32_t* err_word;
 };
-int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s);
+int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned long long* counts = nullptr,
+                 uint32_t stride = 1);
+
+// ---------------------------------------------------------------- G-buffer
+size_t raster_records_bytes(uint32_t ntri);
+int launch_raster(const float* tris, const float* nrm, uint32_t ntri, const float* d_vp, float nearZ, int w, int h,
+                  void* records, float* depth, float* pos, float* nrm_out, uint8_t* mask, cudaStream_t s);
 int launch_occluded(const Node4* nodes, const LeafTri* tris, int has_geometry, const float* rays,
                     const float* tmax, uint32_t n, uint8_t* hit, uint32_t* err_word, cudaStream_t s);
 

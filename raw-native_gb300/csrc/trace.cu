@@ -50,14 +50,19 @@ __device__ __forceinline__ bool slab(float lox, float hix, float loy, float hiy,
     return t0 <= t1 * 1.0000008f;
 }
 
+// Per-thread traversal counters (the measurement build; compiled out otherwise).
+struct Counts { unsigned long long rays = 0, nodes = 0, tris = 0, sky = 0; };
+
 // Any hit with 1e-4 < t < tmax (raw::Bvh::occluded, src/renderer/bvh.cpp:119-138).
+template <bool kCount>
 __device__ bool any_hit(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, const WRay& r,
-                        const Inv& iv, float tmax, uint32_t* err) {
+                        const Inv& iv, float tmax, uint32_t* err, Counts& cn) {
     int32_t stack[kStack];
     int sp = 0;
     int32_t cur = 0;                     // the root is always node 0
     for (uint32_t guard = 0; guard < kGuard; ++guard) {
         if (cur >= 0) {
+            if (kCount) ++cn.nodes;
             const float4* q = reinterpret_cast<const float4*>(nodes + cur);
             const float4 lx = __ldg(q + 0), hx = __ldg(q + 1), ly = __ldg(q + 2), hy = __ldg(q + 3);
             const float4 lz = __ldg(q + 4), hz = __ldg(q + 5);
@@ -80,6 +85,7 @@ __device__ bool any_hit(const Node4* __restrict__ nodes, const LeafTri* __restri
                     const uint32_t w = (uint32_t)~c;
                     const uint32_t first = w >> 3, count = (w & 7u) + 1u;
                     for (uint32_t i = 0; i < count; ++i) {
+                        if (kCount) ++cn.tris;
                         const float4* tq = reinterpret_cast<const float4*>(tris + first + i);
                         const float4 A = __ldg(tq), B = __ldg(tq + 1), C = __ldg(tq + 2);
                         float t;
@@ -107,7 +113,8 @@ __device__ bool any_hit(const Node4* __restrict__ nodes, const LeafTri* __restri
 __device__ __forceinline__ Inv make_inv(const v3& d) { return Inv{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)}; }
 
 // One pixel: its spp cosine-weighted rays, the sky continuation of the open ones, the sun ray.
-__device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, const v3& toLight) {
+template <bool kCount>
+__device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, const v3& toLight, Counts& cn) {
     const float kFar = 1e30f;
     const size_t i = (size_t)y * p.w + x;
     if (!p.mask[i]) {
@@ -136,11 +143,13 @@ __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, 
         if (p.has_geometry) {
             wr = make_wray(origin, dir);
             iv = make_inv(dir);
-            occ = any_hit(p.nodes, p.tris, wr, iv, p.radius, p.err_word);
+            occ = any_hit<kCount>(p.nodes, p.tris, wr, iv, p.radius, p.err_word, cn);
         }
+        if (kCount) ++cn.rays;
         if (!occ) {
             ++open;
-            if (p.want_sky && !(p.has_geometry && any_hit(p.nodes, p.tris, wr, iv, kFar, p.err_word))) ++freec;
+            if (kCount && p.want_sky) ++cn.sky;
+            if (p.want_sky && !(p.has_geometry && any_hit<kCount>(p.nodes, p.tris, wr, iv, kFar, p.err_word, cn))) ++freec;
         }
     }
     p.ao[i] = fdiv((float)open, (float)p.spp);
@@ -149,27 +158,40 @@ __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, 
         bool lit = true;
         if (!p.sun_forced && p.has_geometry) {
             const WRay wr = make_wray(origin, toLight);
-            lit = !any_hit(p.nodes, p.tris, wr, make_inv(toLight), kFar, p.err_word);
+            lit = !any_hit<kCount>(p.nodes, p.tris, wr, make_inv(toLight), kFar, p.err_word, cn);
         }
         p.sun[i] = lit ? 1.0f : 0.0f;
     }
 }
 
-__global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ TraceParams p, uint32_t* tile_ctr) {
+// kCount: trace only every `stride`-th tile and add the rays, node fetches and triangle
+// fetches to counts[0..3] (rays, nodes, tris, sky rays); the outputs of the other tiles are
+// left unwritten.
+template <bool kCount>
+__global__ void __launch_bounds__(256) trace_kernel(const __grid_constant__ TraceParams p, uint32_t* tile_ctr,
+                                                    unsigned long long* counts, uint32_t stride) {
     const int tiles_x = (p.w + kTileW - 1) / kTileW, tiles_y = (p.h + kTileH - 1) / kTileH;
     const uint32_t ntiles = (uint32_t)tiles_x * tiles_y;
     const unsigned lane = threadIdx.x & 31u;
+    Counts cn;
     // lighting model 2's sun direction, normalized on the device as computeRTVisibility does
     const v3 toLight = normalize(mk(p.lx, p.ly, p.lz));
     while (true) {
         uint32_t tile = 0;
         if (lane == 0) tile = atomicAdd(tile_ctr, 1u);
         tile = __shfl_sync(0xffffffffu, tile, 0);
-        if (tile >= ntiles) return;
+        if (tile >= ntiles) break;
         const int x = (int)(tile % tiles_x) * kTileW + (int)(lane % kTileW);
         const int y = (int)(tile / tiles_x) * kTileH + (int)(lane / kTileW);
         // no lane leaves the loop body early: the next tile fetch is a full-warp shuffle
-        if (x < p.w && y < p.h) trace_pixel(p, x, y, toLight);
+        if (kCount && tile % stride != 0) continue;
+        if (x < p.w && y < p.h) trace_pixel<kCount>(p, x, y, toLight, cn);
+    }
+    if (kCount) {
+        atomicAdd(counts, cn.rays);
+        atomicAdd(counts + 1, cn.nodes);
+        atomicAdd(counts + 2, cn.tris);
+        atomicAdd(counts + 3, cn.sky);
     }
 }
 
@@ -180,18 +202,22 @@ __global__ void occluded_kernel(const Node4* __restrict__ nodes, const LeafTri* 
     if (i >= n) return;
     const v3 o = load3(rays + (size_t)i * 6), d = load3(rays + (size_t)i * 6 + 3);
     bool h = false;
-    if (has_geometry) h = any_hit(nodes, tris, make_wray(o, d), make_inv(d), tmax[i], err);
+    Counts cn;
+    if (has_geometry) h = any_hit<false>(nodes, tris, make_wray(o, d), make_inv(d), tmax[i], err, cn);
     hit[i] = h ? 1 : 0;
 }
 
 }  // namespace
 
-int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s) {
+int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned long long* counts, uint32_t stride) {
     // the tile counter sits in the word after the error word
     uint32_t* tile_ctr = p.err_word + 1;
     cudaMemsetAsync(tile_ctr, 0, 4, s);
     const int blocks = sm_count * 4;
-    trace_kernel<<<blocks, 256, 0, s>>>(p, tile_ctr);
+    if (counts)
+        trace_kernel<true><<<blocks, 256, 0, s>>>(p, tile_ctr, counts, stride < 1 ? 1 : stride);
+    else
+        trace_kernel<false><<<blocks, 256, 0, s>>>(p, tile_ctr, nullptr, 1);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 

@@ -29,7 +29,7 @@ ERROR_NAMES = {0: "RN_OK", 1: "RN_ERR_INVALID", 2: "RN_ERR_NO_DEVICE", 3: "RN_ER
 # Every symbol include/rn_ao.h declares.
 EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_accel_build", "rn_accel_free",
            "rn_accel_info", "rn_ao_visibility", "rn_ssao", "rn_reconcile", "rn_ao_frame", "rn_ploc_build",
-           "rn_occluded")
+           "rn_occluded", "rn_raster_gbuffer", "rn_ao_trace_stats")
 
 
 class RnError(RuntimeError):
@@ -80,6 +80,9 @@ def lib() -> C.CDLL:
         L.rn_ploc_build.argtypes = [vp, C.c_uint32, C.c_int, C.c_int, vp, C.POINTER(C.c_int32),
                                     C.POINTER(C.c_uint32), st]
         L.rn_occluded.argtypes = [vp, vp, vp, C.c_uint32, C.c_int, vp, st]
+        L.rn_raster_gbuffer.argtypes = [vp, vp, C.c_uint32, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, st]
+        L.rn_ao_trace_stats.argtypes = [C.POINTER(GBuf), vp, C.c_int, C.c_float, vp, C.c_int, C.c_uint32,
+                                        C.POINTER(C.c_uint64), st]
         _lib = L
     return _lib
 
@@ -105,9 +108,12 @@ def _is_cuda(a) -> bool:
 
 
 def _use_torch_stream() -> None:
+    """Queue the library's work on torch's current stream. torch's default stream has handle
+    0, the legacy default stream: pass cudaStreamLegacy (1) so the work orders with it."""
     import torch
+    handle = torch.cuda.current_stream().cuda_stream or 1
     st = Status()
-    _check(lib().rn_set_stream(C.c_void_p(torch.cuda.current_stream().cuda_stream), C.byref(st)), st)
+    _check(lib().rn_set_stream(C.c_void_p(handle), C.byref(st)), st)
 
 
 class _Args:
@@ -293,6 +299,43 @@ def ao_frame(g: GBuffer, accel: LinearAccel, samples: int = RT_SAMPLES, radius: 
     _check(rc, st)
     o["rec"] = _result(o["err"], r)
     return o
+
+
+def rasterize(tris, normals, camera, w: int, h: int, want_depth: bool = False):
+    """raw::rasterize on the GPU: GBuffer (and depth when asked). tris/normals (n, 9) float32;
+    camera = eye(3), target(3), up(3), fovy."""
+    args = _Args(tris, normals)
+    n = int(tris.shape[0])
+    like = tris
+    pos = args.out(like, (h, w, 3), np.float32)
+    nrm = args.out(like, (h, w, 3), np.float32)
+    mask = args.out(like, (h, w), np.uint8)
+    depth = args.out(like, (h, w), np.float32) if want_depth else None
+    cam = (C.c_float * 10)(*[float(v) for v in camera])
+    st = Status()
+    _check(lib().rn_raster_gbuffer(args.ptr(tris, np.float32), args.ptr(normals, np.float32), n,
+                                   C.cast(cam, C.c_void_p), int(w), int(h), args.flags, args.ptr(depth, np.float32),
+                                   args.ptr(pos, np.float32), args.ptr(nrm, np.float32), args.ptr(mask, np.uint8),
+                                   C.byref(st)), st)
+    g = GBuffer(pos, nrm, mask)
+    return (g, depth) if want_depth else g
+
+
+def trace_stats(g: GBuffer, accel: LinearAccel, samples: int, radius: float, to_light=None, tile_stride: int = 1):
+    """Traversal counters of the visibility pass: dict(rays, nodes, tris, sky_rays)."""
+    args = _Args(g.position, g.normal, g.mask)
+    gb = _gbuf(g, args)
+    flags = args.flags
+    tl = None
+    if to_light is not None:
+        flags |= RN_SKY
+        tl = (C.c_float * 3)(*[float(v) for v in to_light])
+    counts = (C.c_uint64 * 4)()
+    st = Status()
+    _check(lib().rn_ao_trace_stats(C.byref(gb), accel.handle, int(samples), float(radius),
+                                   C.cast(tl, C.c_void_p) if tl is not None else None, flags, int(tile_stride),
+                                   counts, C.byref(st)), st)
+    return dict(rays=counts[0], nodes=counts[1], tris=counts[2], sky_rays=counts[3])
 
 
 def build_ploc(tris, radius: int = 16):

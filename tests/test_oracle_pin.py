@@ -136,3 +136,10 @@ def test_restatement_equals_reference_build(oracle):
     rr = C.c_uint32()
     assert R.ref_ploc(tris, len(tris), 16, out, C.byref(rr)) == root
     assert np.array_equal(out, nodes) and rr.value == rounds
+
+
+def test_product_scene_equals_reference_scene(oracle):
+    import scene as scenes
+    sc = scenes.build_test_scene()
+    tris, nrm, light = oracle.test_scene()
+    assert np.array_equal(sc.tris, tris) and np.array_equal(sc.normals, nrm) and np.array_equal(sc.light, light)
