@@ -304,8 +304,9 @@ def run_ours(args):
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": trace_ms,
                      "rays_per_launch": stats["rays"], "sky_rays_per_launch": stats["sky_rays"],
-                     "node_fetches_per_ray": stats["nodes"] / max(1, stats["rays"] + stats["sky_rays"]),
-                     "tri_fetches_per_ray": stats["tris"] / max(1, stats["rays"] + stats["sky_rays"])},
+                     "walks_per_launch": stats["rays"] + covered,
+                     "node_fetches_per_walk": stats["nodes"] / max(1, stats["rays"] + covered),
+                     "tri_fetches_per_walk": stats["tris"] / max(1, stats["rays"] + covered)},
         "clocks": clocks,
     }
     if cpu:

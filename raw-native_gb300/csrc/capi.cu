@@ -5,6 +5,7 @@
 #include "rn_device.cuh"
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <thread>
 #include <vector>
@@ -47,7 +48,7 @@ __global__ void trig_corr_kernel(const float2* __restrict__ host_cs, uint8_t* __
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= kAngles) return;
     float s, c;
-    sincosf(sample_angle(k), &s, &c);
+    angle_sincos(sample_angle(k), s, c);
     const float2 h = host_cs[k];
     const int dc = __float_as_int(h.x) - __float_as_int(c);
     const int ds = __float_as_int(h.y) - __float_as_int(s);
@@ -62,7 +63,7 @@ __global__ void trig_corr_kernel(const float2* __restrict__ host_cs, uint8_t* __
 
 // The reference's directions depend on the host libm's cosf/sinf at phi = 6.2831853f * k/2^24.
 // Evaluate both on every one of the 2^24 angles (host threads), upload, and let the device
-// record its own sincosf's difference from them.
+// record its own angle_sincos's difference from them.
 int build_trig_correction(Context& c, rn_status* st) {
     std::vector<float> host((size_t)kAngles * 2);
     unsigned nt = std::thread::hardware_concurrency();
@@ -113,6 +114,10 @@ int ensure_ctx(rn_status* st) {
                     prop.major, prop.minor);
     c.device = dev;
     c.sm_count = prop.multiProcessorCount;
+    if (const char* v = getenv("RN_TUNE_TRACE_MIN_BLOCKS")) {
+        const int mb = atoi(v);
+        if (mb >= 2 && mb <= 4) c.tune.trace_min_blocks = mb;
+    }
     RN_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking), st);
     c.stream = c.own_stream;
     RN_CUDA(cudaMalloc((void**)&c.dev_error, 64), st);

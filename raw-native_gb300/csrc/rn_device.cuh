@@ -47,26 +47,56 @@ __device__ __forceinline__ uint32_t hash24(uint32_t x, uint32_t y, uint32_t s) {
     h ^= h >> 16;
     return h & 0xFFFFFFu;
 }
-__device__ __forceinline__ float unit24(uint32_t k) { return fdiv((float)k, 16777216.0f); }
+// (h & 0xFFFFFF) / 2^24: the division by a power of two is exact, so a multiply by 2^-24 is
+// the same value.
+__device__ __forceinline__ float unit24(uint32_t k) { return fmul((float)k, 5.9604644775390625e-8f); }
 
 // The sample angle of 24-bit index k: phi = 6.2831853f * (k / 2^24), as both passes form it.
 __device__ __forceinline__ float sample_angle(uint32_t k) { return fmul(6.2831853f, unit24(k)); }
 
+// sin and cos of an angle in [0, 2 pi) on the device: a three-constant Cody-Waite reduction
+// by pi/2 (1.5703125 + 4.838267923e-4 + 2.563344068e-12; the first product is exact) to
+// |r| <= pi/4, then the Taylor series of sin to r^11 and of cos to r^12 in Horner form
+// (truncation below 2e-10). About one unit in the last place; the correction table below
+// supplies the host's last bits. No slow path: the argument range is fixed.
+__device__ __forceinline__ void angle_sincos(float phi, float& s, float& c) {
+    const float j = rintf(phi * 0.636619772f);
+    float r = __fmaf_rn(-j, 1.5703125f, phi);
+    r = __fmaf_rn(-j, 4.838267923e-4f, r);
+    r = __fmaf_rn(-j, 2.563344068e-12f, r);
+    const float r2 = r * r;
+    float ps = __fmaf_rn(r2, -2.50521084e-8f, 2.75573192e-6f);
+    ps = __fmaf_rn(r2, ps, -1.98412698e-4f);
+    ps = __fmaf_rn(r2, ps, 8.33333333e-3f);
+    ps = __fmaf_rn(r2, ps, -1.66666667e-1f);
+    const float sr = __fmaf_rn(r * r2, ps, r);
+    float pc = __fmaf_rn(r2, 2.08767570e-9f, -2.75573192e-7f);
+    pc = __fmaf_rn(r2, pc, 2.48015873e-5f);
+    pc = __fmaf_rn(r2, pc, -1.38888889e-3f);
+    pc = __fmaf_rn(r2, pc, 4.16666667e-2f);
+    pc = __fmaf_rn(r2, pc, -0.5f);
+    const float cr = __fmaf_rn(r2, pc, 1.0f);
+    const int q = (int)j & 3;
+    s = q == 0 ? sr : q == 1 ? cr : q == 2 ? -sr : -cr;
+    c = q == 0 ? cr : q == 1 ? -sr : q == 2 ? -cr : sr;
+}
+
 // cos and sin of the sample angle with the host C library's bits. The reference takes
 // std::cos/std::sin of a float (the host libm's cosf/sinf), which differ from the correctly
-// rounded value on about 1.3% of these 2^24 angles; the device sincosf differs from both.
-// `corr` holds one byte per angle, cos delta in the low nibble and sin delta in the high
-// nibble (two's complement, in units in the last place), built once per process by
-// comparing the two libraries on every angle; adding it to the bit pattern gives the host's
-// value exactly. corr == nullptr selects the plain device sincosf.
+// rounded value on about 1.3% of these 2^24 angles. `corr` holds one byte per angle, the
+// cos difference in the low nibble and the sin difference in the high nibble (two's
+// complement, in units in the last place) between the host's value and angle_sincos's,
+// built once per process over every angle; adding it to the bit pattern gives the host's
+// value exactly (a caller may fetch the byte ahead and use apply_corr). corr == nullptr
+// selects the device function alone.
 __device__ __forceinline__ float bump_ulps(float v, int d) { return __int_as_float(__float_as_int(v) + d); }
+__device__ __forceinline__ void apply_corr(int d, float& c, float& s) {
+    c = bump_ulps(c, ((d & 15) ^ 8) - 8);
+    s = bump_ulps(s, ((d >> 4) ^ 8) - 8);
+}
 __device__ __forceinline__ void sample_sincos(uint32_t k, const uint8_t* __restrict__ corr, float& c, float& s) {
-    sincosf(sample_angle(k), &s, &c);
-    if (corr) {
-        const int d = __ldg(corr + k);
-        c = bump_ulps(c, ((d & 15) ^ 8) - 8);
-        s = bump_ulps(s, ((d >> 4) ^ 8) - 8);
-    }
+    angle_sincos(sample_angle(k), s, c);
+    if (corr) apply_corr(__ldg(corr + k), c, s);
 }
 
 // ------------------------------------------------------------------ rays

@@ -34,8 +34,14 @@ enum Slot {
     WS_COUNT
 };
 
+// Launch shapes the autotuner may change (rn_tune_* and RN_TUNE_* environment variables).
+struct Tune {
+    int trace_min_blocks = 3;   // resident 256-thread traversal blocks per SM: 2, 3 or 4
+};
+
 struct Context {
     bool ready = false;
+    Tune tune;
     int device = -1;
     int sm_count = 0;
     cudaStream_t stream = nullptr;      // the stream all work goes to
