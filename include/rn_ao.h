@@ -182,6 +182,20 @@ int rn_ao_trace_stats(const rn_gbuf* g, const rn_accel* accel, int spp, float ra
                       const float* to_light, int flags, uint32_t tile_stride, uint64_t* counts,
                       rn_status* st);
 
+/* rn_reconcile without any allocation, for callers that cannot let this library allocate
+ * GPU memory: a host that budgets all device memory up front and refuses growth (as
+ * raw-native's fail-closed frame arena does), a frame loop that must not stall on
+ * cudaMalloc/cudaFree, or code that owns the device's memory through its own pool. No
+ * counterpart in the reference. Same results as rn_reconcile; every buffer is a DEVICE
+ * pointer (err may be NULL); work goes to `stream` (NULL = the legacy default stream) and
+ * the call returns when `out` is filled. Scratch comes from a fixed 33 KiB device array in
+ * the library, held on every GPU that loads it until exit; at most 2^31-1 pixels. The first
+ * call on a device looks the array's address up (make it before any stream capture). Calls
+ * share the array: calls that overlap on the GPU race and must be serialized. */
+int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t* mask, int w, int h,
+                         float tolerance, void* stream, float* err, rn_reconcile_result* out,
+                         rn_status* st);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

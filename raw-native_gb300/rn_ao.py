@@ -29,7 +29,7 @@ ERROR_NAMES = {0: "RN_OK", 1: "RN_ERR_INVALID", 2: "RN_ERR_NO_DEVICE", 3: "RN_ER
 # Every symbol include/rn_ao.h declares.
 EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_accel_build", "rn_accel_free",
            "rn_accel_info", "rn_ao_visibility", "rn_ssao", "rn_reconcile", "rn_ao_frame", "rn_ploc_build",
-           "rn_occluded", "rn_raster_gbuffer", "rn_ao_trace_stats")
+           "rn_occluded", "rn_raster_gbuffer", "rn_ao_trace_stats", "rn_reconcile_noalloc")
 
 
 class RnError(RuntimeError):
@@ -81,6 +81,8 @@ def lib() -> C.CDLL:
                                     C.POINTER(C.c_uint32), st]
         L.rn_occluded.argtypes = [vp, vp, vp, C.c_uint32, C.c_int, vp, st]
         L.rn_raster_gbuffer.argtypes = [vp, vp, C.c_uint32, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, st]
+        L.rn_reconcile_noalloc.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, vp, vp,
+                                           C.POINTER(ReconcileOut), st]
         L.rn_ao_trace_stats.argtypes = [C.POINTER(GBuf), vp, C.c_int, C.c_float, vp, C.c_int, C.c_uint32,
                                         C.POINTER(C.c_uint64), st]
         _lib = L
