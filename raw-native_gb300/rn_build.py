@@ -71,15 +71,17 @@ def build_library(verbose: bool = False) -> str:
 
 
 def build_shim(verbose: bool = False) -> str:
-    """The reference-facing C++23 shim (computeRTAO & co. over the C ABI)."""
-    srcs = sorted(os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".cpp"))
+    """The reference-facing C++23 shim (computeRTAO & co. over the C ABI), built stand-alone
+    against host/mirror's headers with a C test API (librn_ao_shim.so). Inside a raw-native
+    build the same ao_shim.cpp compiles against the reference's headers."""
+    mirror = os.path.join(HOST, "mirror")
+    srcs = [os.path.join(HOST, "ao_shim.cpp")] + sorted(
+        os.path.join(mirror, f) for f in os.listdir(mirror) if f.endswith(".cpp"))
     hdrs = [os.path.join(dp, f) for dp, _, fs in os.walk(HOST) for f in fs if f.endswith(".hpp")]
-    if not srcs:
-        return ""
     if _stale(SHIM, srcs + hdrs + [LIB]):
         cxx = shutil.which("g++") or "g++"
-        _run([cxx, "-std=c++23", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-I" + os.path.join(HOST, "include"),
-              "-I" + os.path.join(ROOT, "include"), "-o", SHIM] + srcs +
+        _run([cxx, "-std=c++23", "-O2", "-fPIC", "-ffp-contract=off", "-shared", "-I" + mirror,
+              "-I" + os.path.join(ROOT, "include"), "-I" + HOST, "-o", SHIM] + srcs +
              ["-L" + HERE, "-lrn_ao", "-Wl,-rpath,$ORIGIN"])
     return SHIM
 
