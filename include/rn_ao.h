@@ -163,6 +163,48 @@ int rn_ploc_build(const float* tris, uint32_t ntri, int radius, int flags, int32
 int rn_occluded(const rn_accel* accel, const float* rays, const float* t_max, uint32_t nrays,
                 int flags, uint8_t* hit, rn_status* st);
 
+/* One view of a batch: its G-buffer and outputs, all DEVICE pointers. `sky`/`sun` are used
+ * with RN_SKY; `ao_ss` (and `err`, optional) turn on SSAO and the reconcile for the view. */
+typedef struct rn_view {
+    int w, h;
+    int spp;
+    float radius;
+    const float* position;
+    const float* normal;
+    const uint8_t* mask;
+    float* ao;
+    float* sky;
+    float* sun;
+    float* ao_ss;
+    float* err;
+} rn_view;
+
+/* A prepared batch of views over one accelerator. */
+typedef struct rn_batch rn_batch;
+
+/* Prepare a batch (no counterpart in the reference; the batched multi-view form): up to 256
+ * views of uneven size and spp over one scene. One frame of the batch is one persistent
+ * traversal launch fed by a device-side tile queue over all views, one SSAO launch with each
+ * view's reconcile fused in, and the copy of the per-view results; the sequence is captured
+ * once into a CUDA graph here and replayed by rn_batch_run. Each view's outputs equal those
+ * of rn_ao_frame on that view alone. */
+int rn_batch_create(const rn_accel* accel, const rn_view* views, int nviews, int ss_samples, float tolerance,
+                    const float* to_light, int flags, rn_batch** out, rn_status* st);
+
+/* Run one frame of the batch on the library's stream and wait for it; `results` (host,
+ * nviews entries, may be NULL) receives each view's reconcile. */
+int rn_batch_run(rn_batch* batch, rn_reconcile_result* results, rn_status* st);
+
+/* Traversal tiles and pixel-samples (w * h * spp summed over views) of a batch. */
+int rn_batch_info(const rn_batch* batch, uint64_t* tiles, uint64_t* pixel_samples, rn_status* st);
+
+/* Release a batch (NULL is a no-op). */
+void rn_batch_free(rn_batch* batch);
+
+/* rn_batch_create + rn_batch_run + rn_batch_free. */
+int rn_ao_batch(const rn_accel* accel, const rn_view* views, int nviews, int ss_samples, float tolerance,
+                const float* to_light, int flags, rn_reconcile_result* results, rn_status* st);
+
 /* The G-buffer planes the AO passes read, rasterized on the GPU. Replaces raw::rasterize
  * (raw/renderer/raster.hpp:9, src/renderer/raster.cpp:92-126) with its default options:
  * `tris` and `nrm` hold 9 floats per triangle (the corners' positions and vertex normals,

@@ -535,34 +535,37 @@ int rn_raster_gbuffer(const float* tris, const float* nrm, uint32_t ntri, const 
     const float *d_tris = nullptr, *d_nin = nullptr;
     RN_TRY(stage_in(tris, (size_t)ntri * 9, dev, WS_TRIS_IN, &d_tris, st));
     RN_TRY(stage_in(nrm, (size_t)ntri * 9, dev, WS_NRM_IN, &d_nin, st));
-    float *d_depth, *d_pos, *d_nrm;
+    float *d_depth = nullptr, *d_pos, *d_nrm;
     uint8_t* d_mask;
-    float* scratch_depth = nullptr;
     if (depth) RN_TRY(stage_out(depth, np, dev, WS_DEPTH, &d_depth, st));
-    else { void* p; RN_TRY(ws_get(WS_DEPTH, np * 4, &p, st)); d_depth = scratch_depth = (float*)p; }
     RN_TRY(stage_out(position, np * 3, dev, WS_POS, &d_pos, st));
     RN_TRY(stage_out(normal, np * 3, dev, WS_NRM, &d_nrm, st));
     RN_TRY(stage_out(mask, np, dev, WS_MASK, &d_mask, st));
     const float nearZ = 0.1f, farZ = 100.0f;
     const M4 vp = view_proj(cam, w, h, nearZ, farZ);
-    void* rec = nullptr;
-    RN_TRY(ws_get(WS_RASTER, raster_records_bytes(ntri) + 64 + 256, &rec, st));
-    float* d_vp = (float*)rec;                                  // 16 floats, then the records
-    void* records = (char*)rec + 256;
-    RN_CUDA(cudaMemcpyAsync(d_vp, vp.m, sizeof vp.m, cudaMemcpyHostToDevice, c.stream), st);
-    if (launch_raster(d_tris, d_nin, ntri, d_vp, nearZ, w, h, records, d_depth, d_pos, d_nrm, d_mask, c.stream) != RN_OK)
-        return cuda_fail(st, cudaGetLastError(), "raster kernels");
-    if (dev) {
-        // the matrix lives in host memory until the copy runs: wait for it
-        RN_CUDA(cudaStreamSynchronize(c.stream), st);
-        return ok(st);
+    void* vpbuf = nullptr;
+    RN_TRY(ws_get(WS_STATS, 256, &vpbuf, st));
+    RN_CUDA(cudaMemcpyAsync(vpbuf, vp.m, sizeof vp.m, cudaMemcpyHostToDevice, c.stream), st);
+    // first guess: four bins per triangle record; grown once if the scene needs more
+    size_t pairs = (size_t)8 * ntri + 1024;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        const size_t bytes = raster_scratch_bytes(ntri, np, pairs);
+        void* scratch = nullptr;
+        RN_TRY(ws_get(WS_RASTER, bytes, &scratch, st));
+        size_t needed = 0;
+        const int rc = launch_raster(d_tris, d_nin, ntri, (const float*)vpbuf, nearZ, w, h, (char*)scratch,
+                                     ctx().ws[WS_RASTER].cap, d_depth, d_pos, d_nrm, d_mask, c.stream, &needed);
+        if (rc == RN_OK) break;
+        if (rc == RN_ERR_NO_MEMORY && attempt == 0) { pairs = needed + needed / 8 + 1024; continue; }
+        return rc == RN_ERR_NO_MEMORY ? fail(st, rc, "raster: %zu bin pairs", needed)
+                                      : cuda_fail(st, cudaGetLastError(), "raster kernels");
     }
+    if (dev) return ok(st);
     if (depth) RN_TRY(copy_back(depth, d_depth, np, st));
     RN_TRY(copy_back(position, d_pos, np * 3, st));
     RN_TRY(copy_back(normal, d_nrm, np * 3, st));
     RN_TRY(copy_back(mask, d_mask, np, st));
     RN_CUDA(cudaStreamSynchronize(c.stream), st);
-    (void)scratch_depth;
     return ok(st);
 }
 

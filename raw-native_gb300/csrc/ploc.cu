@@ -100,16 +100,6 @@ __global__ void scan_down_u32(const uint32_t* __restrict__ in, uint32_t n, const
         run += v[k];
     }
 }
-int scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* bsum, uint32_t* total,
-                       cudaStream_t s) {
-    const uint32_t nb = (n + kTile - 1) / kTile;
-    if (nb == 0) return RN_OK;
-    scan_reduce_u32<<<nb, kThreads, 0, s>>>(in, n, bsum);
-    scan_top_u32<<<1, kThreads, 0, s>>>(bsum, nb, total);
-    scan_down_u32<<<nb, kThreads, 0, s>>>(in, n, bsum, out);
-    return RN_OK;
-}
-
 // ------------------------------------------------------------------ centroids and codes
 struct Bounds { unsigned lo[3], hi[3]; };
 
@@ -572,6 +562,18 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
 inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 
 }  // namespace
+
+// Exclusive prefix sum of n u32 values (three launches: block sums, one-block scan of the
+// sums, block scans plus offsets); `total` (device) receives the sum when not null.
+int scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* bsum, uint32_t* total,
+                       cudaStream_t s) {
+    const uint32_t nb = (n + kTile - 1) / kTile;
+    if (nb == 0) return RN_OK;
+    scan_reduce_u32<<<nb, kThreads, 0, s>>>(in, n, bsum);
+    scan_top_u32<<<1, kThreads, 0, s>>>(bsum, nb, total);
+    scan_down_u32<<<nb, kThreads, 0, s>>>(in, n, bsum, out);
+    return RN_OK;
+}
 
 // ------------------------------------------------------------------ host drivers
 int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaStream_t s, rn_status* st) {

@@ -1,21 +1,31 @@
 // raster.cu -- the G-buffer the AO passes read, on the GPU: raw-native's CPU rasterizer
-// (src/renderer/raster.cpp:9-126, default RasterOptions) restated per pixel.
+// (src/renderer/raster.cpp:9-126, default RasterOptions), bit for bit, for any triangle count.
 //
-// The reference walks triangles in scene order and, inside each triangle's pixel box,
-// keeps a fragment when its screen-linear depth is below the pixel's current one. A pixel's
-// final state depends only on that order and those comparisons, so here one thread per
-// pixel walks the same triangle list in the same order: the winner, its depth, and the
-// position and normal interpolated for it are the reference's, bit for bit (every
-// operation is one IEEE rounding in the reference's order).
+// The reference walks triangles in scene order and, inside each triangle's pixel box, keeps
+// a fragment when its screen-linear depth is below the pixel's current one. The surviving
+// fragment of a pixel is therefore the first triangle, in scene order, among those with the
+// smallest depth there: the minimum of the key (depth bits, record index), since positive
+// floats order like their bit patterns. That minimum does not depend on the order fragments
+// arrive in, so the GPU rasterizes in bins and keeps it with a 64-bit atomicMin:
 //
-// Triangle set-up (clip-space transform, near-plane clip into at most two triangles,
-// perspective divide, screen mapping, area, pixel box) runs once per triangle into two
-// fixed record slots, so record order is scene order.
+//   1. set-up, one thread per triangle: clip-space transform, near-plane clip into at most
+//      two triangles, perspective divide, screen mapping, area, pixel box -> two record
+//      slots per triangle (slot order = scene order);
+//   2. count each record's 8 x 8 pixel tiles, prefix sum, emit (record, tile) pairs;
+//   3. one thread per pixel of each pair: edge weights, depth, atomicMin(key);
+//   4. resolve, one thread per pixel: the winning record's weights again, then position and
+//      normal interpolated exactly as the reference does.
+// Every float operation of steps 1, 3 and 4 is one IEEE rounding in the reference's order.
 #include "rn_internal.h"
 #include "rn_device.cuh"
 
 namespace rn {
+
+int scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* bsum, uint32_t* total, cudaStream_t s);
+
 namespace {
+
+constexpr int kBin = 8;     // bin edge in pixels
 
 struct ClipV { float cs[4]; v3 wp, wn; };
 
@@ -100,42 +110,88 @@ __global__ void raster_setup(const float* __restrict__ tris, const float* __rest
     }
 }
 
-// raster.cpp:58-81 per pixel, triangles in scene order.
-__global__ void raster_pixels(const RasterTri* __restrict__ recs, uint32_t nrec, int w, int h, float* __restrict__ depth,
-                              float* __restrict__ pos, float* __restrict__ nrm, uint8_t* __restrict__ mask) {
+__device__ __forceinline__ uint32_t tiles_of(const RasterTri& T) {
+    if (T.minx > T.maxx || T.miny > T.maxy) return 0;
+    return (uint32_t)((T.maxx / kBin - T.minx / kBin + 1) * (T.maxy / kBin - T.miny / kBin + 1));
+}
+
+__global__ void count_tiles(const RasterTri* __restrict__ recs, uint32_t nrec, uint32_t* __restrict__ cnt) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < nrec) cnt[r] = tiles_of(recs[r]);
+}
+
+// One (record, bin) pair per entry: bin index in the low 32 bits of the pair's tile word.
+__global__ void emit_pairs(const RasterTri* __restrict__ recs, uint32_t nrec, const uint32_t* __restrict__ off,
+                           uint2* __restrict__ pairs, uint32_t cap) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrec) return;
+    const RasterTri& T = recs[r];
+    const uint32_t n = tiles_of(T);
+    if (!n) return;
+    const int bx0 = T.minx / kBin, bx1 = T.maxx / kBin, by0 = T.miny / kBin, by1 = T.maxy / kBin;
+    uint32_t o = off[r];
+    for (int by = by0; by <= by1; ++by)
+        for (int bx = bx0; bx <= bx1; ++bx) {
+            if (o < cap) pairs[o] = make_uint2(r, ((uint32_t)by << 16) | (uint32_t)bx);
+            ++o;
+        }
+}
+
+// raster.cpp:58-63: the edge weights of pixel (x, y) in record T; false when outside.
+__device__ __forceinline__ bool weights(const RasterTri& T, int x, int y, float& w0, float& w1, float& w2) {
+    const float px = fadd((float)x, 0.5f), py = fadd((float)y, 0.5f);
+    w0 = fdiv(fsub(fmul(fsub(T.sx[1], px), fsub(T.sy[2], py)), fmul(fsub(T.sy[1], py), fsub(T.sx[2], px))), T.area);
+    w1 = fdiv(fsub(fmul(fsub(T.sx[2], px), fsub(T.sy[0], py)), fmul(fsub(T.sy[2], py), fsub(T.sx[0], px))), T.area);
+    w2 = fsub(fsub(1.0f, w0), w1);
+    return !(w0 < 0.0f || w1 < 0.0f || w2 < 0.0f);
+}
+__device__ __forceinline__ float frag_depth(const RasterTri& T, float w0, float w1, float w2) {
+    return fadd(fadd(fmul(w0, T.sz[0]), fmul(w1, T.sz[1])), fmul(w2, T.sz[2]));
+}
+
+// 64 threads per pair (one per pixel of the 8 x 8 bin), four pairs per block.
+__global__ void raster_pairs(const RasterTri* __restrict__ recs, const uint2* __restrict__ pairs, uint32_t npairs,
+                             int w, unsigned long long* __restrict__ keys) {
+    const uint32_t pi = blockIdx.x * 4 + threadIdx.x / 64;
+    if (pi >= npairs) return;
+    const uint2 pr = pairs[pi];
+    const RasterTri& T = recs[pr.x];
+    const int x = (int)(pr.y & 0xFFFFu) * kBin + (int)(threadIdx.x & 7u);
+    const int y = (int)(pr.y >> 16) * kBin + (int)((threadIdx.x >> 3) & 7u);
+    if (x < T.minx || x > T.maxx || y < T.miny || y > T.maxy) return;
+    float w0, w1, w2;
+    if (!weights(T, x, y, w0, w1, w2)) return;
+    const float d = frag_depth(T, w0, w1, w2);
+    const unsigned long long key = ((unsigned long long)__float_as_uint(d) << 32) | pr.x;
+    atomicMin(keys + (size_t)y * w + x, key);
+}
+
+// raster.cpp:64-80 for the surviving fragment of each pixel.
+__global__ void raster_resolve(const RasterTri* __restrict__ recs, const unsigned long long* __restrict__ keys, int w,
+                               int h, float* __restrict__ depth, float* __restrict__ pos, float* __restrict__ nrm,
+                               uint8_t* __restrict__ mask) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
-    const float px = fadd((float)x, 0.5f), py = fadd((float)y, 0.5f);
-    float best = __int_as_float(0x7f800000);
-    int win = -1;
-    float bw0 = 0.0f, bw1 = 0.0f, bw2 = 0.0f;
-    for (uint32_t r = 0; r < nrec; ++r) {
-        const RasterTri& T = recs[r];
-        if (x < T.minx || x > T.maxx || y < T.miny || y > T.maxy) continue;
-        const float w0 = fdiv(fsub(fmul(fsub(T.sx[1], px), fsub(T.sy[2], py)), fmul(fsub(T.sy[1], py), fsub(T.sx[2], px))), T.area);
-        const float w1 = fdiv(fsub(fmul(fsub(T.sx[2], px), fsub(T.sy[0], py)), fmul(fsub(T.sy[2], py), fsub(T.sx[0], px))), T.area);
-        const float w2 = fsub(fsub(1.0f, w0), w1);
-        if (w0 < 0.0f || w1 < 0.0f || w2 < 0.0f) continue;
-        const float d = fadd(fadd(fmul(w0, T.sz[0]), fmul(w1, T.sz[1])), fmul(w2, T.sz[2]));
-        if (d >= best) continue;
-        best = d; win = (int)r; bw0 = w0; bw1 = w1; bw2 = w2;
-    }
     const size_t i = (size_t)y * w + x;
-    depth[i] = best;
-    if (win < 0) {
+    const unsigned long long key = keys[i];
+    if (key == ~0ull) {
+        if (depth) depth[i] = __int_as_float(0x7f800000);
         pos[3 * i] = pos[3 * i + 1] = pos[3 * i + 2] = 0.0f;
         nrm[3 * i] = nrm[3 * i + 1] = nrm[3 * i + 2] = 0.0f;
         mask[i] = 0;
         return;
     }
-    const RasterTri& T = recs[win];
-    const float iw = fadd(fadd(fmul(bw0, T.invw[0]), fmul(bw1, T.invw[1])), fmul(bw2, T.invw[2]));
+    const RasterTri& T = recs[(uint32_t)(key & 0xFFFFFFFFull)];
+    float w0, w1, w2;
+    weights(T, x, y, w0, w1, w2);
+    if (depth) depth[i] = frag_depth(T, w0, w1, w2);
+    const float iw = fadd(fadd(fmul(w0, T.invw[0]), fmul(w1, T.invw[1])), fmul(w2, T.invw[2]));
     float P[3], N[3];
     for (int a = 0; a < 3; ++a) {
-        P[a] = fdiv(fadd(fadd(fmul(fmul(bw0, T.wp[a]), T.invw[0]), fmul(fmul(bw1, T.wp[3 + a]), T.invw[1])),
-                         fmul(fmul(bw2, T.wp[6 + a]), T.invw[2])), iw);
-        N[a] = fdiv(fadd(fadd(fmul(fmul(bw0, T.wn[a]), T.invw[0]), fmul(fmul(bw1, T.wn[3 + a]), T.invw[1])),
-                         fmul(fmul(bw2, T.wn[6 + a]), T.invw[2])), iw);
+        P[a] = fdiv(fadd(fadd(fmul(fmul(w0, T.wp[a]), T.invw[0]), fmul(fmul(w1, T.wp[3 + a]), T.invw[1])),
+                         fmul(fmul(w2, T.wp[6 + a]), T.invw[2])), iw);
+        N[a] = fdiv(fadd(fadd(fmul(fmul(w0, T.wn[a]), T.invw[0]), fmul(fmul(w1, T.wn[3 + a]), T.invw[1])),
+                         fmul(fmul(w2, T.wn[6 + a]), T.invw[2])), iw);
     }
     const v3 nn = normalize(mk(N[0], N[1], N[2]));
     pos[3 * i] = P[0]; pos[3 * i + 1] = P[1]; pos[3 * i + 2] = P[2];
@@ -143,16 +199,48 @@ __global__ void raster_pixels(const RasterTri* __restrict__ recs, uint32_t nrec,
     mask[i] = 1;
 }
 
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
 }  // namespace
 
-size_t raster_records_bytes(uint32_t ntri) { return (size_t)2 * ntri * sizeof(RasterTri); }
+// Scratch layout: records (2 per triangle), tile counts and offsets, scan block sums, the
+// pair total, the per-pixel keys, then the pairs.
+size_t raster_scratch_bytes(uint32_t ntri, size_t npx, size_t npairs) {
+    const size_t nrec = 2 * (size_t)ntri;
+    return align256(nrec * sizeof(RasterTri)) + 2 * align256(nrec * 4 + 4) + align256(((nrec + 2047) / 2048 + 1) * 8) +
+           256 + align256(npx * 8) + align256(npairs * sizeof(uint2));
+}
 
 int launch_raster(const float* tris, const float* nrm, uint32_t ntri, const float* d_vp, float nearZ, int w, int h,
-                  void* records, float* depth, float* pos, float* nrmo, uint8_t* mask, cudaStream_t s) {
-    RasterTri* recs = (RasterTri*)records;
-    if (ntri) raster_setup<<<(ntri + 127) / 128, 128, 0, s>>>(tris, nrm, ntri, d_vp, nearZ, w, h, recs);
+                  char* scratch, size_t scratch_bytes, float* depth, float* pos, float* nrmo, uint8_t* mask,
+                  cudaStream_t s, size_t* pairs_needed) {
+    const uint32_t nrec = 2 * ntri;
+    const size_t npx = (size_t)w * h;
+    size_t off = 0;
+    auto take = [&](size_t b) { char* p = scratch + off; off += align256(b); return p; };
+    RasterTri* recs = (RasterTri*)take((size_t)nrec * sizeof(RasterTri));
+    uint32_t* cnt = (uint32_t*)take((size_t)nrec * 4 + 4);
+    uint32_t* ofs = (uint32_t*)take((size_t)nrec * 4 + 4);
+    uint32_t* bsum = (uint32_t*)take(((size_t)(nrec + 2047) / 2048 + 1) * 8);
+    uint32_t* total = (uint32_t*)take(256);
+    unsigned long long* keys = (unsigned long long*)take(npx * 8);
+    uint2* pairs = (uint2*)(scratch + off);
+    const size_t cap = off < scratch_bytes ? (scratch_bytes - off) / sizeof(uint2) : 0;
+    uint32_t npairs = 0;
+    cudaMemsetAsync(keys, 0xFF, npx * 8, s);
+    if (ntri) {
+        raster_setup<<<(ntri + 127) / 128, 128, 0, s>>>(tris, nrm, ntri, d_vp, nearZ, w, h, recs);
+        count_tiles<<<(nrec + 255) / 256, 256, 0, s>>>(recs, nrec, cnt);
+        scan_exclusive_u32(cnt, ofs, nrec, bsum, total, s);
+        cudaMemcpyAsync(&npairs, total, 4, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return RN_ERR_CUDA;
+        if (npairs > cap) { *pairs_needed = npairs; return RN_ERR_NO_MEMORY; }
+        emit_pairs<<<(nrec + 255) / 256, 256, 0, s>>>(recs, nrec, ofs, pairs, (uint32_t)cap);
+        if (npairs) raster_pairs<<<(npairs + 3) / 4, 256, 0, s>>>(recs, pairs, npairs, w, keys);
+    }
     const dim3 blk(32, 8), grid((w + 31) / 32, (h + 7) / 8);
-    raster_pixels<<<grid, blk, 0, s>>>(recs, 2 * ntri, w, h, depth, pos, nrmo, mask);
+    raster_resolve<<<grid, blk, 0, s>>>(recs, keys, w, h, depth, pos, nrmo, mask);
+    *pairs_needed = npairs;
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 

@@ -173,9 +173,13 @@ int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned lo
                  uint32_t stride = 1);
 
 // ---------------------------------------------------------------- G-buffer
-size_t raster_records_bytes(uint32_t ntri);
+// Scratch bytes for ntri triangles, npx pixels and npairs (record, 8x8 bin) pairs.
+size_t raster_scratch_bytes(uint32_t ntri, size_t npx, size_t npairs);
+// RN_ERR_NO_MEMORY with *pairs_needed set when the scratch holds too few pairs.
 int launch_raster(const float* tris, const float* nrm, uint32_t ntri, const float* d_vp, float nearZ, int w, int h,
-                  void* records, float* depth, float* pos, float* nrm_out, uint8_t* mask, cudaStream_t s);
+                  char* scratch, size_t scratch_bytes, float* depth, float* pos, float* nrm_out, uint8_t* mask,
+                  cudaStream_t s, size_t* pairs_needed);
+int scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* bsum, uint32_t* total, cudaStream_t s);
 int launch_occluded(const Node4* nodes, const LeafTri* tris, int has_geometry, const float* rays,
                     const float* tmax, uint32_t n, uint8_t* hit, uint32_t* err_word, cudaStream_t s);
 

@@ -1,0 +1,181 @@
+// trace_device.cuh -- the AO walk and the per-pixel loop of the ray-traced pass, shared by
+// the single-frame kernel (trace.cu) and the batched multi-view kernel (batch.cu). See
+// trace.cu for the design and the exactness argument.
+#pragma once
+#include "rn_internal.h"
+#include "rn_device.cuh"
+
+namespace rn {
+namespace trace_dev {
+
+
+constexpr int kStack = 96;
+constexpr uint32_t kGuard = 1u << 24;       // node visits per ray before giving up
+constexpr int kTileW = 8, kTileH = 4;
+
+__device__ __forceinline__ float min_nan(float a, float b) {
+    float r;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float max_nan(float a, float b) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+// inverse(d) of src/renderer/bvh.cpp:29-33: 1/x, or a signed infinity for a zero component.
+__device__ __forceinline__ float safe_inv(float x) { return x != 0.0f ? __frcp_rn(x) : copysignf(__int_as_float(0x7f800000), x); }
+
+struct Inv { float x, y, z; };
+__device__ __forceinline__ Inv make_inv(const v3& d) { return Inv{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)}; }
+
+// Slab entry of one child box. An axis whose distances are NaN (origin on the plane, zero
+// direction component) constrains nothing, as in the reference's entry().
+__device__ __forceinline__ bool slab(float lox, float hix, float loy, float hiy, float loz, float hiz,
+                                     const v3& o, const Inv& iv, float tmax, float& tnear) {
+    const float ax = (lox - o.x) * iv.x, bx = (hix - o.x) * iv.x;
+    const float ay = (loy - o.y) * iv.y, by = (hiy - o.y) * iv.y;
+    const float az = (loz - o.z) * iv.z, bz = (hiz - o.z) * iv.z;
+    const float t0 = fmaxf(fmaxf(fmaxf(0.0f, min_nan(ax, bx)), min_nan(ay, by)), min_nan(az, bz));
+    const float t1 = fminf(fminf(fminf(tmax, max_nan(ax, bx)), max_nan(ay, by)), max_nan(az, bz));
+    tnear = t0;
+    return t0 <= t1 * 1.0000008f;
+}
+
+// Per-thread traversal counters (the measurement build; compiled out otherwise).
+struct Counts { unsigned long long rays = 0, nodes = 0, tris = 0, sky = 0; };
+
+enum : int { HIT_NEAR = 1, HIT_FAR = 2 };
+
+// One walk, two limits (tnear <= tfar): HIT_NEAR | HIT_FAR when some triangle is hit at
+// 1e-4 < t < tnear; HIT_FAR alone when the nearest hit it needed to find lies in
+// [tnear, tfar); 0 when nothing is hit before tfar. The any-hit query of raw::Bvh::occluded
+// (src/renderer/bvh.cpp:119-138) is tnear == tfar.
+template <bool kCount>
+__device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, const v3& o, const v3& d,
+                    float tnear, float tfar, uint32_t* err, Counts& cn) {
+    const Inv iv = make_inv(d);
+    WRay wr;                             // the watertight set-up: formed at the first leaf
+    bool wr_ready = false;
+    float tmax = tfar;
+    int far_hit = 0;
+    int32_t stack[kStack];
+    int sp = 0;
+    int32_t cur = 0;                     // the root is always node 0
+    for (uint32_t guard = 0; guard < kGuard; ++guard) {
+        if (kCount) ++cn.nodes;
+        const float4* q = reinterpret_cast<const float4*>(nodes + cur);
+        const float4 lx = __ldg(q + 0), hx = __ldg(q + 1), ly = __ldg(q + 2), hy = __ldg(q + 3);
+        const float4 lz = __ldg(q + 4), hz = __ldg(q + 5);
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(q + 6));
+        const int cnt = __ldg(reinterpret_cast<const int*>(q + 7));
+        const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
+        const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
+        const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+        const int32_t CH[4] = {ch.x, ch.y, ch.z, ch.w};
+        int32_t nearest = -1;
+        float tbest = 3.0e38f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float tn;
+            if (k >= cnt || !slab(LX[k], HX[k], LY[k], HY[k], LZ[k], HZ[k], o, iv, tmax, tn)) continue;
+            const int32_t c = CH[k];
+            if (c < 0) {
+                // a leaf: test its triangles now (a near hit ends the walk)
+                if (!wr_ready) { wr = make_wray(o, d); wr_ready = true; }
+                const uint32_t w = (uint32_t)~c;
+                const uint32_t first = w >> 3, count = (w & 7u) + 1u;
+                for (uint32_t i = 0; i < count; ++i) {
+                    if (kCount) ++cn.tris;
+                    const float4* tq = reinterpret_cast<const float4*>(tris + first + i);
+                    const float4 A = __ldg(tq), B = __ldg(tq + 1), C = __ldg(tq + 2);
+                    float t;
+                    if (!hit_tri(wr, mk(A.x, A.y, A.z), mk(B.x, B.y, B.z), mk(C.x, C.y, C.z), t)) continue;
+                    if (t < tnear) return HIT_NEAR | HIT_FAR;
+                    if (t < tmax) { far_hit = HIT_FAR; tmax = tnear; }
+                }
+                continue;
+            }
+            if (nearest < 0) { nearest = c; tbest = tn; continue; }
+            // keep the nearer child to descend into, stack the other
+            int32_t push = c;
+            if (tn < tbest) { push = nearest; nearest = c; tbest = tn; }
+            if (sp >= kStack) { atomicOr(err, DEV_STACK_OVERFLOW); return far_hit; }
+            stack[sp++] = push;
+        }
+        if (nearest >= 0) { cur = nearest; continue; }
+        if (sp == 0) return far_hit;
+        cur = stack[--sp];
+    }
+    atomicOr(err, DEV_GUARD);
+    return far_hit;
+}
+
+// One pixel: its spp cosine-weighted rays (AO and, when asked, the sky), then the sun ray.
+template <bool kCount>
+__device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, const v3& toLight, Counts& cn) {
+    const float kFar = 1e30f;
+    const size_t i = (size_t)y * p.w + x;
+    if (!p.mask[i]) {
+        p.ao[i] = 1.0f;
+        if (p.want_sky) { p.sky[i] = 1.0f; p.sun[i] = 1.0f; }
+        return;
+    }
+    const v3 P = load3(p.pos + 3 * i), n = load3(p.nrm + 3 * i);
+    // basis (ray_ao.cpp:14-17)
+    const v3 a = fabsf(n.x) > 0.9f ? mk(0.0f, 1.0f, 0.0f) : mk(1.0f, 0.0f, 0.0f);
+    const v3 t = normalize(cross(a, n)), b = cross(n, t);
+    const v3 origin = add(P, scale(n, 1e-3f));
+    const uint32_t ux = (uint32_t)x, uy = (uint32_t)y;
+    const float tfar_h = p.want_sky ? kFar : p.radius;
+    const int slots = p.spp + ((p.want_sky && !p.sun_forced) ? 1 : 0);
+    int open = 0, freec = 0;
+    bool lit = true;
+    // the correction byte of the next sample is fetched one iteration ahead
+    uint32_t k2n = hash24(ux, uy, 1u);
+    int cbn = p.corr ? __ldg(p.corr + k2n) : 0;
+    for (int s = 0; s < slots; ++s) {
+        v3 dir;
+        float tn, tf;
+        if (s < p.spp) {
+            const uint32_t k2 = k2n;
+            const int cb = cbn;
+            if (s + 1 < p.spp) {
+                k2n = hash24(ux, uy, (uint32_t)(2 * s + 3));
+                cbn = p.corr ? __ldg(p.corr + k2n) : 0;
+            }
+            const float u1 = unit24(hash24(ux, uy, (uint32_t)(2 * s)));
+            float c, sn;
+            angle_sincos(sample_angle(k2), sn, c);
+            if (p.corr) apply_corr(cb, c, sn);
+            const float r = fsqrt(u1);
+            const float lx = fmul(r, c), ly = fmul(r, sn);
+            const float lz = fsqrt(smax(0.0f, fsub(1.0f, u1)));
+            dir = normalize(add(add(scale(t, lx), scale(b, ly)), scale(n, lz)));
+            tn = p.radius;
+            tf = tfar_h;
+        } else {
+            dir = toLight;
+            tn = tf = kFar;
+        }
+        const int h = p.has_geometry ? walk<kCount>(p.nodes, p.tris, origin, dir, tn, tf, p.err_word, cn) : 0;
+        if (s < p.spp) {
+            if (kCount) { ++cn.rays; if (p.want_sky && !(h & HIT_NEAR)) ++cn.sky; }
+            if (!(h & HIT_NEAR)) {
+                ++open;
+                if (!(h & HIT_FAR)) ++freec;
+            }
+        } else {
+            lit = h == 0;
+        }
+    }
+    p.ao[i] = fdiv((float)open, (float)p.spp);
+    if (p.want_sky) {
+        p.sky[i] = fdiv((float)freec, (float)p.spp);
+        p.sun[i] = lit ? 1.0f : 0.0f;
+    }
+}
+
+
+}  // namespace trace_dev
+}  // namespace rn

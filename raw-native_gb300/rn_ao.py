@@ -29,7 +29,8 @@ ERROR_NAMES = {0: "RN_OK", 1: "RN_ERR_INVALID", 2: "RN_ERR_NO_DEVICE", 3: "RN_ER
 # Every symbol include/rn_ao.h declares.
 EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_accel_build", "rn_accel_free",
            "rn_accel_info", "rn_ao_visibility", "rn_ssao", "rn_reconcile", "rn_ao_frame", "rn_ploc_build",
-           "rn_occluded", "rn_raster_gbuffer", "rn_ao_trace_stats", "rn_reconcile_noalloc")
+           "rn_occluded", "rn_raster_gbuffer", "rn_ao_trace_stats", "rn_reconcile_noalloc", "rn_batch_create",
+           "rn_batch_run", "rn_batch_info", "rn_batch_free", "rn_ao_batch")
 
 
 class RnError(RuntimeError):
@@ -46,6 +47,12 @@ class Status(C.Structure):
 class GBuf(C.Structure):
     _fields_ = [("w", C.c_int), ("h", C.c_int), ("position", C.c_void_p), ("normal", C.c_void_p),
                 ("mask", C.c_void_p)]
+
+
+class View(C.Structure):
+    _fields_ = [("w", C.c_int), ("h", C.c_int), ("spp", C.c_int), ("radius", C.c_float), ("position", C.c_void_p),
+                ("normal", C.c_void_p), ("mask", C.c_void_p), ("ao", C.c_void_p), ("sky", C.c_void_p),
+                ("sun", C.c_void_p), ("ao_ss", C.c_void_p), ("err", C.c_void_p)]
 
 
 class ReconcileOut(C.Structure):
@@ -83,6 +90,14 @@ def lib() -> C.CDLL:
         L.rn_raster_gbuffer.argtypes = [vp, vp, C.c_uint32, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, st]
         L.rn_reconcile_noalloc.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, vp, vp,
                                            C.POINTER(ReconcileOut), st]
+        L.rn_batch_create.argtypes = [vp, C.POINTER(View), C.c_int, C.c_int, C.c_float, vp, C.c_int,
+                                      C.POINTER(vp), st]
+        L.rn_batch_run.argtypes = [vp, C.POINTER(ReconcileOut), st]
+        L.rn_batch_info.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64), st]
+        L.rn_batch_free.argtypes = [vp]
+        L.rn_batch_free.restype = None
+        L.rn_ao_batch.argtypes = [vp, C.POINTER(View), C.c_int, C.c_int, C.c_float, vp, C.c_int,
+                                  C.POINTER(ReconcileOut), st]
         L.rn_ao_trace_stats.argtypes = [C.POINTER(GBuf), vp, C.c_int, C.c_float, vp, C.c_int, C.c_uint32,
                                         C.POINTER(C.c_uint64), st]
         _lib = L
@@ -338,6 +353,71 @@ def trace_stats(g: GBuffer, accel: LinearAccel, samples: int, radius: float, to_
                                    C.cast(tl, C.c_void_p) if tl is not None else None, flags, int(tile_stride),
                                    counts, C.byref(st)), st)
     return dict(rays=counts[0], nodes=counts[1], tris=counts[2], sky_rays=counts[3])
+
+
+class Batch:
+    """A prepared batch of views over one accelerator (CUDA tensors only). `views` is a list of
+    dicts with keys g (GBuffer), spp, radius and, optionally, ssao=True and sky=True
+    (the batch-wide to_light). Outputs are allocated here: batch.outputs[i] holds the view's
+    ao (and ss, err, sky, sun). run() replays the captured frame and returns the per-view
+    ReconcileResults (error maps are in outputs)."""
+
+    def __init__(self, accel: LinearAccel, views, ss_samples: int = SS_SAMPLES, tolerance: float = TOLERANCE,
+                 to_light=None, device_trig: bool = False):
+        import torch
+        _use_torch_stream()
+        self.accel = accel
+        self.n = len(views)
+        self.outputs = []
+        arr = (View * self.n)()
+        for k, v in enumerate(views):
+            g = v["g"]
+            h, w = g.shape
+            o = {"ao": torch.empty(h, w, device=g.mask.device)}
+            if v.get("ssao", True):
+                o["ss"] = torch.empty_like(o["ao"])
+                o["err"] = torch.empty_like(o["ao"])
+            if to_light is not None:
+                o["sky"] = torch.empty_like(o["ao"])
+                o["sun"] = torch.empty_like(o["ao"])
+            self.outputs.append(o)
+            ptr = lambda t: t.data_ptr() if t is not None else None
+            arr[k] = View(w, h, int(v["spp"]), float(v["radius"]), g.position.data_ptr(), g.normal.data_ptr(),
+                          g.mask.data_ptr(), o["ao"].data_ptr(), ptr(o.get("sky")), ptr(o.get("sun")),
+                          ptr(o.get("ss")), ptr(o.get("err")))
+        self._views = views                 # keep the G-buffers alive
+        flags = (RN_SKY if to_light is not None else 0) | (RN_DEVICE_TRIG if device_trig else 0)
+        tl = (C.c_float * 3)(*[float(x) for x in to_light]) if to_light is not None else None
+        self._h = C.c_void_p()
+        st = Status()
+        _check(lib().rn_batch_create(accel.handle, arr, self.n, int(ss_samples), float(tolerance),
+                                     C.cast(tl, C.c_void_p) if tl is not None else None, flags, C.byref(self._h),
+                                     C.byref(st)), st)
+        self.tolerance = tolerance
+
+    def info(self) -> dict:
+        t, r = C.c_uint64(), C.c_uint64()
+        st = Status()
+        _check(lib().rn_batch_info(self._h, C.byref(t), C.byref(r), C.byref(st)), st)
+        return dict(tiles=t.value, pixel_samples=r.value)
+
+    def run(self):
+        _use_torch_stream()
+        res = (ReconcileOut * self.n)()
+        st = Status()
+        _check(lib().rn_batch_run(self._h, res, C.byref(st)), st)
+        return [_result(self.outputs[k].get("err"), res[k]) for k in range(self.n)]
+
+    def close(self):
+        if self._h:
+            lib().rn_batch_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def build_ploc(tris, radius: int = 16):

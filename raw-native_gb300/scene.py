@@ -61,3 +61,113 @@ def build_test_scene(camera=DEFAULT_CAMERA) -> Scene:
     _quad(tris, nrms, (p0[0], p0[1], p0[2]), (p0[0], p0[1], p1[2]), (p0[0], p1[1], p1[2]), (p0[0], p1[1], p0[2]), (-1, 0, 0))
     return Scene(np.ascontiguousarray(np.stack(tris)), np.ascontiguousarray(np.stack(nrms)),
                  _normalize((-0.4, -1.0, -0.3)), tuple(camera))
+
+
+# ------------------------------------------------------------------ seeded synthetic scenes
+# The large workloads use scenes this project generates (the reference has none): a ground
+# grid, yawed boxes and subdivided icospheres resting on it, placed by a seeded PCG64.
+#   build_synthetic_scene(seed, 2000, 500)    ~744,000 triangles (batched views)
+#   build_synthetic_scene(seed, 200, 50)      146,400 triangles (surrogate training scenes)
+#   build_synthetic_scene(seed, 10000, 6000)  ~7,880,000 triangles (4K head-to-head)
+
+def _icosphere(subdiv: int):
+    """Unit icosphere: 20 * 4^subdiv triangles (vertices, faces), outward winding."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = np.array([(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t),
+                  (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)], np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    f = np.array([(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+                  (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+                  (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)], np.int64)
+    verts = list(map(tuple, v))
+    for _ in range(subdiv):
+        cache = {}
+
+        def mid(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in cache:
+                m = (np.array(verts[a]) + np.array(verts[b])) / 2.0
+                verts.append(tuple(m / np.linalg.norm(m)))
+                cache[key] = len(verts) - 1
+            return cache[key]
+        nf = []
+        for a, b, c in f:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        f = np.array(nf, np.int64)
+    return np.array(verts, np.float64), f
+
+
+def _box_tris(c, s, yaw):
+    """12 triangles of a box with footprint centre c=(x, z), sides s=(sx, sy, sz), resting on
+    y = 0, rotated by `yaw` about the vertical axis; face normals."""
+    hx, hz = s[0] / 2.0, s[2] / 2.0
+    corners = np.array([[x, y, z] for y in (0.0, s[1]) for z in (-hz, hz) for x in (-hx, hx)])
+    cy, sy = np.cos(yaw), np.sin(yaw)
+    rot = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+    p = corners @ rot.T + np.array([c[0], 0.0, c[1]])
+    faces = [((0, 1, 3, 2), (0, -1, 0)), ((4, 6, 7, 5), (0, 1, 0)), ((0, 4, 5, 1), (0, 0, -1)),
+             ((2, 3, 7, 6), (0, 0, 1)), ((0, 2, 6, 4), (-1, 0, 0)), ((1, 5, 7, 3), (1, 0, 0))]
+    tris, nrms = [], []
+    for (a, b, cc, d), n in faces:
+        nr = rot @ np.array(n, np.float64)
+        for t3 in ((a, b, cc), (a, cc, d)):
+            tris.append(np.concatenate([p[t3[0]], p[t3[1]], p[t3[2]]]))
+            nrms.append(np.concatenate([nr, nr, nr]))
+    return np.array(tris), np.array(nrms)
+
+
+def build_synthetic_scene(seed: int, n_boxes: int, n_spheres: int, grid: int = 200, half: float = 50.0,
+                          subdiv: int = 3) -> Scene:
+    rng = np.random.Generator(np.random.PCG64(seed))
+    # ground: grid x grid quads on [-half, half]^2 at y = 0
+    xs = np.linspace(-half, half, grid + 1)
+    i, j = np.meshgrid(np.arange(grid), np.arange(grid), indexing="ij")
+    x0, x1, z0, z1 = xs[i].ravel(), xs[i + 1].ravel(), xs[j].ravel(), xs[j + 1].ravel()
+    zero = np.zeros_like(x0)
+    a = np.stack([x0, zero, z0], 1); b = np.stack([x1, zero, z0], 1)
+    c = np.stack([x1, zero, z1], 1); d = np.stack([x0, zero, z1], 1)
+    ground = np.stack([np.concatenate([a, b, c], 1), np.concatenate([a, c, d], 1)], 1).reshape(-1, 9)
+    gnrm = np.tile(np.array([0, 1, 0] * 3, np.float64), (len(ground), 1))
+    parts, nparts = [ground], [gnrm]
+    # boxes
+    centres = rng.uniform(-half, half, (n_boxes, 2))
+    sides = rng.uniform(0.2, 3.0, (n_boxes, 3))
+    yaws = rng.uniform(0.0, 2.0 * np.pi, n_boxes)
+    for k in range(n_boxes):
+        t, n = _box_tris(centres[k], sides[k], yaws[k])
+        parts.append(t); nparts.append(n)
+    # icospheres resting on the ground
+    if n_spheres:
+        v, f = _icosphere(subdiv)
+        unit = v[f].reshape(-1, 9)                    # (faces, 9) corner positions on the unit sphere
+        sc = rng.uniform(-half, half, (n_spheres, 2))
+        r = np.clip(rng.lognormal(0.0, 0.5, n_spheres), 0.2, 4.0)
+        off = np.stack([sc[:, 0], r, sc[:, 1]], 1)    # centres at height r
+        sph = unit[None, :, :] * r[:, None, None] + np.tile(off, 3)[:, None, :]
+        parts.append(sph.reshape(-1, 9))
+        nparts.append(np.tile(unit, (n_spheres, 1)))
+    tris = np.ascontiguousarray(np.concatenate(parts).astype(np.float32))
+    nrms = np.ascontiguousarray(np.concatenate(nparts).astype(np.float32))
+    return Scene(tris, nrms, _normalize((-0.4, -1.0, -0.3)), (40.0, 12.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.9))
+
+
+RESOLUTIONS = ((512, 512), (1280, 720), (1920, 1080), (2560, 1440))
+SPPS = (16, 64, 256)
+
+
+def orbit_views(seed: int, n: int, radius: float = 40.0, heights=(3.0, 20.0), fovy: float = 0.9,
+                resolutions=RESOLUTIONS, spps=SPPS):
+    """n cameras evenly around an orbit of `radius`, heights uniform in `heights`, looking at
+    the origin; each draws a resolution and an spp. Returns [(w, h, spp, camera10)]."""
+    rng = np.random.Generator(np.random.PCG64(seed ^ 0x5EED))
+    hs = rng.uniform(heights[0], heights[1], n)
+    ri = rng.integers(0, len(resolutions), n)
+    si = rng.integers(0, len(spps), n)
+    views = []
+    for k in range(n):
+        th = 2.0 * np.pi * k / n
+        cam = (float(radius * np.cos(th)), float(hs[k]), float(radius * np.sin(th)), 0.0, 0.0, 0.0, 0.0, 1.0, 0.0, fovy)
+        w, h = resolutions[ri[k]]
+        views.append((w, h, int(spps[si[k]]), cam))
+    return views

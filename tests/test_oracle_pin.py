@@ -143,3 +143,15 @@ def test_product_scene_equals_reference_scene(oracle):
     sc = scenes.build_test_scene()
     tris, nrm, light = oracle.test_scene()
     assert np.array_equal(sc.tris, tris) and np.array_equal(sc.normals, nrm) and np.array_equal(sc.light, light)
+
+
+def test_synthetic_scenes_are_seeded_and_sized():
+    import scene as scenes
+    a = scenes.build_synthetic_scene(1, 2000, 500)
+    b = scenes.build_synthetic_scene(1, 2000, 500)
+    assert a.tris.shape == (744000, 9) and np.array_equal(a.tris, b.tris)
+    assert scenes.build_synthetic_scene(7, 200, 50).tris.shape == (146400, 9)
+    assert not np.array_equal(a.tris, scenes.build_synthetic_scene(2, 2000, 500).tris)
+    v = scenes.orbit_views(1, 64)
+    assert len(v) == 64 and {(w, h) for w, h, _, _ in v} <= set(scenes.RESOLUTIONS)
+    assert {s for _, _, s, _ in v} <= set(scenes.SPPS)
