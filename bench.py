@@ -55,6 +55,10 @@ def parse():
                    help="run only this pass `--steps` times after `--warmup` (for ncu), print nothing")
     p.add_argument("--spp", type=int, default=SPP, help="samples per pixel (the benchmark uses 256)")
     p.add_argument("--tris", type=int, default=1000000, help="--profile build: soup triangles")
+    p.add_argument("--workload", default="4k", choices=["4k", "batch", "large"],
+                   help="4k: the benchmark (built-in scene, 3840x2160, 256 spp); batch: 64 orbit views of the "
+                        "seeded 744k-triangle scene in one batch; large: 16 4K views of the 7.88M-triangle scene")
+    p.add_argument("--views", type=int, default=0, help="batch/large: number of views (default 64 / 16)")
     return p.parse_args()
 
 
@@ -321,20 +325,34 @@ def run_profile(args):
     import scene as scenes
     torch.cuda.set_device(0)
     rn.init()
-    sc = scenes.build_test_scene()
+    radius = RADIUS
+    if args.workload == "4k":
+        sc = scenes.build_test_scene()
+        cam, w, h = sc.camera, W_PX, H_PX
+    else:
+        # one 1920x1080 orbit view of the large scene (or of the batched-views scene)
+        sc = (scenes.build_synthetic_scene(5, 10000, 6000) if args.workload == "large"
+              else scenes.build_synthetic_scene(1, 2000, 500))
+        cam, w, h, radius = scenes.orbit_views(5, 16)[0][3], 1920, 1080, 1.0
     tris = torch.from_numpy(sc.tris).cuda()
-    g = rn.rasterize(tris, torch.from_numpy(sc.normals).cuda(), sc.camera, W_PX, H_PX)
+    g = rn.rasterize(tris, torch.from_numpy(sc.normals).cuda(), cam, w, h)
     acc = rn.LinearAccel(tris)
-    outs = {k: torch.empty(H_PX, W_PX, device="cuda") for k in ("ao", "sky", "sun", "ss", "err")}
+    if os.environ.get("RN_PRINT_STATS"):
+        st = rn.trace_stats(g, acc, args.spp, radius, tile_stride=1)
+        print(json.dumps({"workload": args.workload, "spp": args.spp, "radius": radius, **st,
+                          "nodes_per_ray": st["nodes"] / max(1, st["rays"]), "tris_per_ray": st["tris"] / max(1, st["rays"]),
+                          "accel": acc.info()}), flush=True)
+    outs = {k: torch.empty(h, w, device="cuda") for k in ("ao", "sky", "sun", "ss", "err")}
     if args.profile == "build":
         import numpy as np
         rng = np.random.default_rng(1)
         c = rng.uniform(-50, 50, (args.tris, 1, 3)).astype(np.float32)
         t = (c + rng.uniform(-1, 1, (args.tris, 3, 3)).astype(np.float32)).reshape(args.tris, 9)
         soup = torch.from_numpy(np.ascontiguousarray(t)).cuda()
-    fn = {"frame": lambda: rn.ao_frame(g, acc, args.spp, RADIUS, SS_SAMPLES, TOL, to_light=sc.to_light, outputs=outs),
-          "trace": lambda: rn.compute_rt_visibility(g, acc, args.spp, RADIUS, sc.to_light),
-          "ssao": lambda: rn.compute_ssao(g, SS_SAMPLES, RADIUS),
+    tl = sc.to_light if args.workload == "4k" else None
+    fn = {"frame": lambda: rn.ao_frame(g, acc, args.spp, radius, SS_SAMPLES, TOL, to_light=tl, outputs=outs),
+          "trace": lambda: rn.compute_rt_visibility(g, acc, args.spp, radius, tl),
+          "ssao": lambda: rn.compute_ssao(g, SS_SAMPLES, radius),
           "reconcile": lambda: rn.reconcile(outs["ss"], outs["ao"], g.mask, TOL),
           "build": lambda: rn.LinearAccel(soup)}[args.profile]
     for _ in range(args.warmup + args.steps):
@@ -342,8 +360,66 @@ def run_profile(args):
     torch.cuda.synchronize()
 
 
+def run_views(args):
+    """The batched-views and large-scene workloads: one batch frame = every view's AO (radius 1),
+    SSAO and reconcile, from one traversal launch and one SSAO launch (a CUDA graph)."""
+    import numpy as np
+    import torch
+    import rn_ao as rn
+    import scene as scenes
+    torch.cuda.set_device(0)
+    rn.init()
+    if args.workload == "batch":
+        sc = scenes.build_synthetic_scene(1, 2000, 500)
+        specs = scenes.orbit_views(1, args.views or 64)
+        name = "batched views: seeded 744k-triangle scene, %d orbit views, resolutions/spp as drawn, radius 1" % len(specs)
+    else:
+        sc = scenes.build_synthetic_scene(5, 10000, 6000)
+        n = args.views or 16
+        specs = [(3840, 2160, args.spp if args.spp != SPP else 64, cam)
+                 for (_, _, _, cam) in scenes.orbit_views(5, n)]
+        name = "large: seeded 7.88M-triangle scene, %d 4K orbit views, %d spp, radius 1" % (n, specs[0][2])
+    tris = torch.from_numpy(sc.tris).cuda()
+    nrms = torch.from_numpy(sc.normals).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    acc = rn.LinearAccel(tris)
+    build_ms = (time.perf_counter() - t0) * 1e3
+    views = []
+    for w, h, spp, cam in specs:
+        views.append(dict(g=rn.rasterize(tris, nrms, cam, w, h), spp=spp, radius=1.0))
+    covered_rays = sum(int(v["g"].mask.sum().item()) * v["spp"] for v in views)
+    b = rn.Batch(acc, views, ss_samples=SS_SAMPLES, tolerance=TOL)
+    for _ in range(args.warmup):
+        b.run()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    with Clocks(0) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            res = b.run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    info = acc.info()
+    out = {"metric": METRIC, "value": covered_rays / (ms * 1e-3) / 1e9, "unit": "Grays/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": name, "triangles": int(len(sc.tris)), "views": len(views),
+                      "ao_rays_per_step": covered_rays, "bvh_build_ms": round(build_ms, 1),
+                      "bvh_wide_nodes": info["wide_nodes"], "ploc_rounds": info["ploc_rounds"]},
+           "ms_per_view": ms / len(views),
+           "rmse_mean": float(np.mean([r.rmse for r in res])), "clocks": clk.summary(),
+           "gpu_launches": 2 * args.steps}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload != "4k" and not args.profile:
+        run_views(args)
+        return
     if args.profile:
         run_profile(args)
     elif args.impl == "reference":
