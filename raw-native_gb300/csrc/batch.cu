@@ -56,6 +56,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_batch_kernel(const Batc
     for (int v = threadIdx.x; v < nviews; v += blockDim.x) { sp[v] = views[v].tp; begins[v] = views[v].tile_begin; }
     __syncthreads();
     const unsigned lane = threadIdx.x & 31u;
+    __shared__ trace_dev::FrontierEntry frontier[8][trace_dev::kFrontier];
+    trace_dev::FrontierEntry* F = frontier[threadIdx.x >> 5];
     Counts cn;
     while (true) {
         uint32_t tile = 0;
@@ -69,7 +71,10 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_batch_kernel(const Batc
         const int x = (int)(local % tiles_x) * kTileW + (int)(lane % kTileW);
         const int y = (int)(local / tiles_x) * kTileH + (int)(lane / kTileW);
         const v3 toLight = normalize(mk(p.lx, p.ly, p.lz));
-        if (x < p.w && y < p.h) trace_dev::trace_pixel<false>(p, x, y, toLight, cn);
+        const int fn = (!p.want_sky && p.has_geometry && p.frontier)
+                            ? trace_dev::tile_frontier(p, x, y, x < p.w && y < p.h, F) : 0;
+        if (x < p.w && y < p.h) trace_dev::trace_pixel<false>(p, x, y, toLight, cn, F, fn);
+        __syncwarp();
     }
 }
 
@@ -160,6 +165,7 @@ int rn_batch_create(const rn_accel* accel, const rn_view* views, int nviews, int
         p.corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
         p.ao = in.ao; p.sky = in.sky; p.sun = in.sun;
         p.err_word = c.dev_error;
+        p.frontier = c.tune.trace_frontier;
         b.tile_begin = tiles;
         tiles += (uint32_t)(((in.w + 7) / 8) * ((in.h + 3) / 4));
         b.ssao_begin = ssao_blocks_total;

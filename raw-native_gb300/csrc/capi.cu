@@ -118,6 +118,7 @@ int ensure_ctx(rn_status* st) {
         const int mb = atoi(v);
         if (mb >= 2 && mb <= 4) c.tune.trace_min_blocks = mb;
     }
+    if (const char* v = getenv("RN_TUNE_TRACE_FRONTIER")) c.tune.trace_frontier = atoi(v) != 0;
     RN_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking), st);
     c.stream = c.own_stream;
     RN_CUDA(cudaMalloc((void**)&c.dev_error, 64), st);
@@ -228,6 +229,7 @@ int do_visibility(const StagedGbuf& g, int w, int h, const rn_accel* accel, int 
     p.corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
     p.ao = ao; p.sky = sky; p.sun = sun;
     p.err_word = c.dev_error;
+    p.frontier = c.tune.trace_frontier;
     if (launch_trace(p, c.sm_count, c.stream) != RN_OK) return cuda_fail(st, cudaGetLastError(), "trace_kernel");
     return RN_OK;
 }
@@ -598,6 +600,7 @@ int rn_ao_trace_stats(const rn_gbuf* g, const rn_accel* accel, int spp, float ra
     p.corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
     p.ao = (float*)scratch[0]; p.sky = (float*)scratch[1]; p.sun = (float*)scratch[2];
     p.err_word = c.dev_error;
+    p.frontier = c.tune.trace_frontier;
     if (launch_trace(p, c.sm_count, c.stream, (unsigned long long*)cnt, tile_stride) != RN_OK)
         return cuda_fail(st, cudaGetLastError(), "trace_kernel (counting)");
     unsigned long long h[4];

@@ -37,6 +37,7 @@ enum Slot {
 // Launch shapes the autotuner may change (rn_tune_* and RN_TUNE_* environment variables).
 struct Tune {
     int trace_min_blocks = 3;   // resident 256-thread traversal blocks per SM: 2, 3 or 4
+    int trace_frontier = 1;     // per-warp frontier for AO-only walks
 };
 
 struct Context {
@@ -168,6 +169,7 @@ struct TraceParams {
     float* sky;
     float* sun;
     uint32_t* err_word;
+    int frontier;         // AO-only walks start from a per-warp frontier (0: from the root)
 };
 int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned long long* counts = nullptr,
                  uint32_t stride = 1);

@@ -36,6 +36,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
     const int tiles_x = (p.w + kTileW - 1) / kTileW, tiles_y = (p.h + kTileH - 1) / kTileH;
     const uint32_t ntiles = (uint32_t)tiles_x * tiles_y;
     const unsigned lane = threadIdx.x & 31u;
+    __shared__ FrontierEntry frontier[8][kFrontier];
+    FrontierEntry* F = frontier[threadIdx.x >> 5];
     Counts cn;
     // lighting model 2's sun direction, normalized on the device as computeRTVisibility does
     const v3 toLight = normalize(mk(p.lx, p.ly, p.lz));
@@ -48,7 +50,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         const int y = (int)(tile / tiles_x) * kTileH + (int)(lane / kTileW);
         // no lane leaves the loop body early: the next tile fetch is a full-warp shuffle
         if (kCount && tile % stride != 0) continue;
-        if (x < p.w && y < p.h) trace_pixel<kCount>(p, x, y, toLight, cn);
+        const int fn = (!p.want_sky && p.has_geometry && p.frontier) ? tile_frontier(p, x, y, x < p.w && y < p.h, F) : 0;
+        if (x < p.w && y < p.h) trace_pixel<kCount>(p, x, y, toLight, cn, F, fn);
+        __syncwarp();                              // the frontier is rebuilt for the next tile
     }
     if (kCount) {
         atomicAdd(counts, cn.rays);

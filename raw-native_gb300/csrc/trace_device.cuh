@@ -47,13 +47,69 @@ struct Counts { unsigned long long rays = 0, nodes = 0, tris = 0, sky = 0; };
 
 enum : int { HIT_NEAR = 1, HIT_FAR = 2 };
 
+// A warp's frontier: BVH entries (a child word and its padded box) that together hold every
+// triangle a short ray of the warp's tile can reach. A triangle hit at t < radius lies within
+// radius of its ray's origin, so its leaf box, and every ancestor's, overlaps the box Q of
+// the tile's origins grown by the radius; the frontier is the set of Q-overlapping nodes
+// reached by expanding Q-overlapping nodes from the root (largest box first) while at most
+// kFrontier entries result. AO walks start from it instead of re-descending from the root.
+constexpr int kFrontier = 16;
+struct FrontierEntry {
+    float lo[3], hi[3];
+    int32_t word;
+    int32_t pad;
+};
+
+__device__ __forceinline__ bool box_overlaps(float lx, float ly, float lz, float hx, float hy, float hz,
+                                             const float* qlo, const float* qhi) {
+    return lx <= qhi[0] && hx >= qlo[0] && ly <= qhi[1] && hy >= qlo[1] && lz <= qhi[2] && hz >= qlo[2];
+}
+
+// Lane 0 builds the frontier of box [qlo, qhi] into F; returns its size (0: start at the root).
+__device__ inline int build_frontier(const Node4* __restrict__ nodes, const float* qlo, const float* qhi,
+                              FrontierEntry* F) {
+    int n = 0;
+    auto expand = [&](int32_t node, int slot) -> bool {
+        // replace F[slot] (or append when slot < 0) by node's Q-overlapping children
+        const Node4& N = nodes[node];
+        int add[4], na = 0;
+        for (int k = 0; k < N.meta[0]; ++k)
+            if (box_overlaps(N.lox[k], N.loy[k], N.loz[k], N.hix[k], N.hiy[k], N.hiz[k], qlo, qhi)) add[na++] = k;
+        if (n - (slot >= 0 ? 1 : 0) + na > kFrontier) return false;
+        for (int j = 0; j < na; ++j) {
+            const int k = add[j];
+            FrontierEntry e;
+            e.lo[0] = N.lox[k]; e.lo[1] = N.loy[k]; e.lo[2] = N.loz[k];
+            e.hi[0] = N.hix[k]; e.hi[1] = N.hiy[k]; e.hi[2] = N.hiz[k];
+            e.word = N.child[k];
+            e.pad = 0;
+            if (j == 0 && slot >= 0) F[slot] = e; else F[n++] = e;
+        }
+        if (na == 0 && slot >= 0) F[slot] = F[--n];
+        return true;
+    };
+    expand(0, -1);
+    for (int iter = 0; iter < 4 * kFrontier; ++iter) {
+        int pick = -1;
+        float best = -1.0f;
+        for (int e = 0; e < n; ++e) {
+            if (F[e].word < 0) continue;
+            const float ext = fmaxf(fmaxf(F[e].hi[0] - F[e].lo[0], F[e].hi[1] - F[e].lo[1]), F[e].hi[2] - F[e].lo[2]);
+            if (ext > best) { best = ext; pick = e; }
+        }
+        if (pick < 0 || !expand(F[pick].word, pick)) break;
+    }
+    return n;
+}
+
 // One walk, two limits (tnear <= tfar): HIT_NEAR | HIT_FAR when some triangle is hit at
 // 1e-4 < t < tnear; HIT_FAR alone when the nearest hit it needed to find lies in
 // [tnear, tfar); 0 when nothing is hit before tfar. The any-hit query of raw::Bvh::occluded
 // (src/renderer/bvh.cpp:119-138) is tnear == tfar.
 template <bool kCount>
 __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, const v3& o, const v3& d,
-                    float tnear, float tfar, uint32_t* err, Counts& cn) {
+                    float tnear, float tfar, uint32_t* err, Counts& cn, const FrontierEntry* F = nullptr,
+                    int fn = 0) {
     const Inv iv = make_inv(d);
     WRay wr;                             // the watertight set-up: formed at the first leaf
     bool wr_ready = false;
@@ -62,6 +118,38 @@ __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__
     int32_t stack[kStack];
     int sp = 0;
     int32_t cur = 0;                     // the root is always node 0
+    if (fn > 0) {
+        // start from the frontier: its entries are the root's stand-ins
+        int32_t nearest = -1;
+        float tbest = 3.0e38f;
+        for (int e = 0; e < fn; ++e) {
+            float tn;
+            if (!slab(F[e].lo[0], F[e].hi[0], F[e].lo[1], F[e].hi[1], F[e].lo[2], F[e].hi[2], o, iv, tmax, tn)) continue;
+            const int32_t c = F[e].word;
+            if (c < 0) {
+                if (!wr_ready) { wr = make_wray(o, d); wr_ready = true; }
+                const uint32_t w = (uint32_t)~c;
+                const uint32_t first = w >> 3, count = (w & 7u) + 1u;
+                for (uint32_t i = 0; i < count; ++i) {
+                    if (kCount) ++cn.tris;
+                    const float4* tq = reinterpret_cast<const float4*>(tris + first + i);
+                    const float4 A = __ldg(tq), B = __ldg(tq + 1), C = __ldg(tq + 2);
+                    float t;
+                    if (!hit_tri(wr, mk(A.x, A.y, A.z), mk(B.x, B.y, B.z), mk(C.x, C.y, C.z), t)) continue;
+                    if (t < tnear) return HIT_NEAR | HIT_FAR;
+                    if (t < tmax) { far_hit = HIT_FAR; tmax = tnear; }
+                }
+                continue;
+            }
+            if (nearest < 0) { nearest = c; tbest = tn; continue; }
+            int32_t push = c;
+            if (tn < tbest) { push = nearest; nearest = c; tbest = tn; }
+            stack[sp++] = push;                  // fn <= kFrontier < kStack
+        }
+        if (nearest >= 0) cur = nearest;
+        else if (sp > 0) cur = stack[--sp];
+        else return far_hit;
+    }
     for (uint32_t guard = 0; guard < kGuard; ++guard) {
         if (kCount) ++cn.nodes;
         const float4* q = reinterpret_cast<const float4*>(nodes + cur);
@@ -111,9 +199,40 @@ __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__
     return far_hit;
 }
 
+// The frontier of the warp's tile for AO walks of `radius` (all 32 lanes call it; lane 0
+// builds, the others wait). Returns its size, 0 when the tile has no covered pixel.
+__device__ __forceinline__ int tile_frontier(const TraceParams& p, int x, int y, bool valid, FrontierEntry* F) {
+    float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f}, mag = 0.0f;
+    if (valid) {
+        const size_t i = (size_t)y * p.w + x;
+        if (p.mask[i]) {
+            const v3 P = load3(p.pos + 3 * i), n = load3(p.nrm + 3 * i);
+            const v3 o = add(P, scale(n, 1e-3f));
+            lo[0] = hi[0] = o.x; lo[1] = hi[1] = o.y; lo[2] = hi[2] = o.z;
+            mag = fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z));
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1)
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], off));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], off));
+        }
+    for (int off = 16; off > 0; off >>= 1) mag = fmaxf(mag, __shfl_xor_sync(0xffffffffu, mag, off));
+    if (lo[0] > hi[0]) return 0;
+    // grow by the radius with margin for the rounding of t, |d| and the hit point
+    const float g = p.radius * 1.0001f + 1e-5f * (mag + 1.0f);
+    for (int a = 0; a < 3; ++a) { lo[a] -= g; hi[a] += g; }
+    int n = 0;
+    if ((threadIdx.x & 31u) == 0) n = build_frontier(p.nodes, lo, hi, F);
+    n = __shfl_sync(0xffffffffu, n, 0);
+    __syncwarp();
+    return n;
+}
+
 // One pixel: its spp cosine-weighted rays (AO and, when asked, the sky), then the sun ray.
 template <bool kCount>
-__device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, const v3& toLight, Counts& cn) {
+__device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, const v3& toLight, Counts& cn,
+                                            const FrontierEntry* F = nullptr, int fn = 0) {
     const float kFar = 1e30f;
     const size_t i = (size_t)y * p.w + x;
     if (!p.mask[i]) {
@@ -158,7 +277,11 @@ __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, 
             dir = toLight;
             tn = tf = kFar;
         }
-        const int h = p.has_geometry ? walk<kCount>(p.nodes, p.tris, origin, dir, tn, tf, p.err_word, cn) : 0;
+        // AO-only walks may start from the warp's frontier; the sky and the sun need the root
+        const bool local = s < p.spp && tf == p.radius;
+        const int h = p.has_geometry ? walk<kCount>(p.nodes, p.tris, origin, dir, tn, tf, p.err_word, cn,
+                                                    local ? F : nullptr, local ? fn : 0)
+                                     : 0;
         if (s < p.spp) {
             if (kCount) { ++cn.rays; if (p.want_sky && !(h & HIT_NEAR)) ++cn.sky; }
             if (!(h & HIT_NEAR)) {

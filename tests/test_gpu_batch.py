@@ -107,3 +107,16 @@ def test_config3_batch_on_big_scene(rn, oracle, big_scene):
         L.rno_accel_free(hnd)
     rows = np.arange(0, h, 16)
     assert np.array_equal(b.outputs[0]["ao"].cpu().numpy()[rows], ao[rows])
+
+
+def test_big_scene_ao_only_walks_match_oracle(rn, oracle, big_scene):
+    """AO-only walks start from each warp's frontier; the answer must still be the oracle's."""
+    import scene as scenes
+    for k, radius in ((3, 1.0), (40, 2.5)):
+        _, _, _, cam = scenes.orbit_views(1, 64)[k]
+        w, h = 160, 120
+        g = rn.rasterize(big_scene.tris, big_scene.normals, cam, w, h)
+        acc = rn.LinearAccel(big_scene.tris)
+        ao = rn.compute_rtao(g, acc, 32, radius)
+        ref = oracle.trace(g.position, g.normal, g.mask, big_scene.tris, 32, radius, threads=THREADS)
+        assert np.array_equal(ao, ref), (k, int((ao != ref).sum()))
