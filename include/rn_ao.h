@@ -238,6 +238,15 @@ int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t*
                          float tolerance, void* stream, float* err, rn_reconcile_result* out,
                          rn_status* st);
 
+/* The learned surrogate's tensor-core GEMM (no counterpart in the reference): C = P * Q^T,
+ * P (M x K) and Q (N x K) BF16 row-major with K contiguous (row strides ldp, ldq, multiples
+ * of 8), FP32 accumulation on tcgen05 with TMEM, output FP32 (`c32`) and/or BF16 (`c16`) with
+ * row stride ldc, optional bias[N] and ReLU. M % 128 == 0; N one of 32, 64, 128, 256 or a
+ * multiple of 128; K % (64 * splits) == 0; splits > 1 adds FP32 partials atomically into c32
+ * (which the caller zeroes). Device pointers, the library's stream, asynchronous. */
+int rn_tc_gemm(const void* P, int ldp, const void* Q, int ldq, int M, int N, int K, int splits, float* c32,
+               void* c16, int ldc, const float* bias, int relu, rn_status* st);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -30,7 +30,7 @@ ERROR_NAMES = {0: "RN_OK", 1: "RN_ERR_INVALID", 2: "RN_ERR_NO_DEVICE", 3: "RN_ER
 EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_accel_build", "rn_accel_free",
            "rn_accel_info", "rn_ao_visibility", "rn_ssao", "rn_reconcile", "rn_ao_frame", "rn_ploc_build",
            "rn_occluded", "rn_raster_gbuffer", "rn_ao_trace_stats", "rn_reconcile_noalloc", "rn_batch_create",
-           "rn_batch_run", "rn_batch_info", "rn_batch_free", "rn_ao_batch")
+           "rn_batch_run", "rn_batch_info", "rn_batch_free", "rn_ao_batch", "rn_tc_gemm")
 
 
 class RnError(RuntimeError):
@@ -98,6 +98,8 @@ def lib() -> C.CDLL:
         L.rn_batch_free.restype = None
         L.rn_ao_batch.argtypes = [vp, C.POINTER(View), C.c_int, C.c_int, C.c_float, vp, C.c_int,
                                   C.POINTER(ReconcileOut), st]
+        L.rn_tc_gemm.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, vp,
+                                 C.c_int, st]
         L.rn_ao_trace_stats.argtypes = [C.POINTER(GBuf), vp, C.c_int, C.c_float, vp, C.c_int, C.c_uint32,
                                         C.POINTER(C.c_uint64), st]
         _lib = L
@@ -418,6 +420,23 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def tc_gemm(P, Q, out_dtype=None, bias=None, relu=False, splits=1):
+    """C = P @ Q.T on the tensor cores (CUDA bf16 tensors, K contiguous). FP32 output, or bf16
+    when out_dtype is torch.bfloat16; splits > 1 reduces K in slices with FP32 atomics."""
+    import torch
+    M, K = P.shape
+    N = Q.shape[0]
+    _use_torch_stream()
+    c32 = torch.zeros(M, N, device=P.device) if (out_dtype in (None, torch.float32) or splits > 1) else None
+    c16 = torch.empty(M, N, device=P.device, dtype=torch.bfloat16) if out_dtype == torch.bfloat16 else None
+    st = Status()
+    _check(lib().rn_tc_gemm(C.c_void_p(P.data_ptr()), P.stride(0), C.c_void_p(Q.data_ptr()), Q.stride(0), M, N, K,
+                            int(splits), C.c_void_p(c32.data_ptr()) if c32 is not None else None,
+                            C.c_void_p(c16.data_ptr()) if c16 is not None else None, N,
+                            C.c_void_p(bias.data_ptr()) if bias is not None else None, int(relu), C.byref(st)), st)
+    return c16 if c16 is not None else c32
 
 
 def build_ploc(tris, radius: int = 16):
