@@ -247,6 +247,30 @@ int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t*
 int rn_tc_gemm(const void* P, int ldp, const void* Q, int ldq, int M, int N, int K, int splits, float* c32,
                void* c16, int ldc, const float* bias, int relu, rn_status* st);
 
+/* The learned AO surrogate (no counterpart in the reference): a BF16 U-Net, 4 levels of
+ * 32/64/128/256 channels, two 3x3 convolutions + ReLU per level, average-pool down, nearest up
+ * with skip concatenation, a 1x1 sigmoid head; every convolution (forward, data gradient,
+ * weight gradient) on the tcgen05 GEMM, FP32 accumulation, Adam on FP32 master weights.
+ * A network is created for one input shape: batch x height x width, height and width
+ * multiples of 16 and batch * (height/8) * (width/8) a multiple of 128. Inputs are DEVICE
+ * FP32 [batch][height][width][5] (depth / radius, normal xyz, 4-spp AO); outputs and targets
+ * DEVICE FP32 [batch][height][width]. */
+typedef struct rn_unet rn_unet;
+int rn_unet_create(int batch, int height, int width, uint64_t seed, rn_unet** out, rn_status* st);
+void rn_unet_free(rn_unet* net);
+int rn_unet_param_count(const rn_unet* net, uint64_t* count, rn_status* st);
+/* Predicted AO into `output` (asynchronous on the library's stream). */
+int rn_unet_forward(rn_unet* net, const float* input, int batch, float* output, rn_status* st);
+/* One Adam step on the mean squared error against `target` (lr 0: gradients only); writes
+ * the batch's loss to *loss (host). */
+int rn_unet_train_step(rn_unet* net, const float* input, const float* target, int batch, float lr, float* loss,
+                       rn_status* st);
+/* Parameters / last gradients as FP32 host arrays: per convolution w[cout][9 cin] (tap-major,
+ * input channel fastest) then b[cout], then the head's w[32] and b. */
+int rn_unet_get_params(rn_unet* net, float* host, rn_status* st);
+int rn_unet_set_params(rn_unet* net, const float* host, rn_status* st);
+int rn_unet_get_grads(rn_unet* net, float* host, rn_status* st);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -14,7 +14,7 @@
 //     ReLU-backward gate, and stores BF16 or FP32 (or adds FP32 atomically for split K).
 // Every mbarrier wait is bounded; on a timeout the kernel sets the error word, waits
 // (bounded) for its own copies in flight, frees its TMEM and returns.
-#include "rn_internal.h"
+#include "gemm_tc.h"
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -23,20 +23,8 @@
 namespace rn {
 namespace tc {
 
-constexpr int kBM = 128, kBK = 64, kStages = 4, kThreads = 128;
+constexpr int kStages = 4, kThreads = 128;
 constexpr uint32_t kSpin = 1u << 24;      // try_wait rounds before a wait gives up
-
-struct Epilogue {
-    int ldc;                         // row stride of C in elements
-    float* c32;                      // FP32 output (split K: accumulated with atomics)
-    __nv_bfloat16* c16;              // BF16 output
-    const float* bias;               // [N] or null
-    const __nv_bfloat16* gate;       // [M][ldc]: output zeroed where gate <= 0 (ReLU backward), or null
-    int relu;
-    int atomic;
-    int k_per_split;                 // K range of one grid.z slice (a multiple of 64)
-    uint32_t* err;
-};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 

@@ -30,7 +30,9 @@ ERROR_NAMES = {0: "RN_OK", 1: "RN_ERR_INVALID", 2: "RN_ERR_NO_DEVICE", 3: "RN_ER
 EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_accel_build", "rn_accel_free",
            "rn_accel_info", "rn_ao_visibility", "rn_ssao", "rn_reconcile", "rn_ao_frame", "rn_ploc_build",
            "rn_occluded", "rn_raster_gbuffer", "rn_ao_trace_stats", "rn_reconcile_noalloc", "rn_batch_create",
-           "rn_batch_run", "rn_batch_info", "rn_batch_free", "rn_ao_batch", "rn_tc_gemm")
+           "rn_batch_run", "rn_batch_info", "rn_batch_free", "rn_ao_batch", "rn_tc_gemm", "rn_unet_create",
+           "rn_unet_free", "rn_unet_param_count", "rn_unet_forward", "rn_unet_train_step", "rn_unet_get_params",
+           "rn_unet_set_params", "rn_unet_get_grads")
 
 
 class RnError(RuntimeError):
@@ -100,6 +102,14 @@ def lib() -> C.CDLL:
                                   C.POINTER(ReconcileOut), st]
         L.rn_tc_gemm.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, vp,
                                  C.c_int, st]
+        L.rn_unet_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(vp), st]
+        L.rn_unet_free.argtypes = [vp]
+        L.rn_unet_free.restype = None
+        L.rn_unet_param_count.argtypes = [vp, C.POINTER(C.c_uint64), st]
+        L.rn_unet_forward.argtypes = [vp, vp, C.c_int, vp, st]
+        L.rn_unet_train_step.argtypes = [vp, vp, vp, C.c_int, C.c_float, C.POINTER(C.c_float), st]
+        for f in (L.rn_unet_get_params, L.rn_unet_set_params, L.rn_unet_get_grads):
+            f.argtypes = [vp, vp, st]
         L.rn_ao_trace_stats.argtypes = [C.POINTER(GBuf), vp, C.c_int, C.c_float, vp, C.c_int, C.c_uint32,
                                         C.POINTER(C.c_uint64), st]
         _lib = L
@@ -437,6 +447,69 @@ def tc_gemm(P, Q, out_dtype=None, bias=None, relu=False, splits=1):
                             C.c_void_p(c16.data_ptr()) if c16 is not None else None, N,
                             C.c_void_p(bias.data_ptr()) if bias is not None else None, int(relu), C.byref(st)), st)
     return c16 if c16 is not None else c32
+
+
+class UNet:
+    """The learned AO surrogate network for one input shape (see rn_unet_create). Inputs,
+    targets and outputs are CUDA float32 tensors: x [B, H, W, 5], y [B, H, W]."""
+
+    def __init__(self, batch: int, height: int, width: int, seed: int = 0):
+        self._h = C.c_void_p()
+        st = Status()
+        _check(lib().rn_unet_create(batch, height, width, seed, C.byref(self._h), C.byref(st)), st)
+        self.shape = (batch, height, width)
+        n = C.c_uint64()
+        _check(lib().rn_unet_param_count(self._h, C.byref(n), C.byref(st)), st)
+        self.param_count = n.value
+
+    def forward(self, x):
+        import torch
+        _use_torch_stream()
+        out = torch.empty(self.shape, device=x.device)
+        st = Status()
+        _check(lib().rn_unet_forward(self._h, C.c_void_p(x.data_ptr()), self.shape[0], C.c_void_p(out.data_ptr()),
+                                     C.byref(st)), st)
+        return out
+
+    def train_step(self, x, y, lr: float) -> float:
+        _use_torch_stream()
+        loss = C.c_float()
+        st = Status()
+        _check(lib().rn_unet_train_step(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), self.shape[0],
+                                        float(lr), C.byref(loss), C.byref(st)), st)
+        return loss.value
+
+    def _io(self, fn, arr=None):
+        out = np.empty(self.param_count, np.float32) if arr is None else np.ascontiguousarray(arr, np.float32)
+        st = Status()
+        _check(fn(self._h, C.c_void_p(out.ctypes.data), C.byref(st)), st)
+        return out
+
+    def get_params(self):
+        return self._io(lib().rn_unet_get_params)
+
+    def set_params(self, p):
+        self._io(lib().rn_unet_set_params, p)
+
+    def get_grads(self):
+        return self._io(lib().rn_unet_get_grads)
+
+    def close(self):
+        if self._h:
+            lib().rn_unet_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# The surrogate's layer table, for code that restates the network (tests): (cin, cout) of
+# each 3x3 convolution in parameter order.
+UNET_CONVS = [(8, 32), (32, 32), (32, 64), (64, 64), (64, 128), (128, 128), (128, 256), (256, 256), (384, 128),
+              (128, 128), (192, 64), (64, 64), (96, 32), (32, 32)]
 
 
 def build_ploc(tris, radius: int = 16):

@@ -5,8 +5,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-CASES = [(128, 32, 64, 1), (256, 64, 256, 1), (512, 128, 1152, 1), (1024, 256, 2304, 1), (384, 96, 320, 1),
-         (128, 128, 4096, 8)]
+CASES = [(128, 32, 64, 1), (256, 64, 256, 1), (512, 128, 1152, 1), (1024, 256, 2304, 1), (384, 32, 320, 1),
+         (256, 384, 3456, 1), (128, 128, 4096, 8)]
 
 
 @pytest.mark.parametrize("M,N,K,splits", CASES)
@@ -33,3 +33,12 @@ def test_tc_gemm_bf16_bias_relu(rn):
     got = rn.tc_gemm(P, Q, out_dtype=torch.bfloat16, bias=b, relu=True)
     torch.cuda.synchronize()
     assert torch.allclose(got.float(), ref.to(torch.bfloat16).float(), rtol=1e-2, atol=1e-2)
+
+
+def test_tc_gemm_rejects_unsupported_shapes(rn):
+    import torch
+    P = torch.zeros(128, 64, device="cuda", dtype=torch.bfloat16)
+    with pytest.raises(rn.RnError):
+        rn.tc_gemm(P, torch.zeros(96, 64, device="cuda", dtype=torch.bfloat16))     # N 96
+    with pytest.raises(rn.RnError):
+        rn.tc_gemm(torch.zeros(100, 64, device="cuda", dtype=torch.bfloat16), P[:32])   # M not a multiple of 128
