@@ -55,7 +55,7 @@ def parse():
                    help="run only this pass `--steps` times after `--warmup` (for ncu), print nothing")
     p.add_argument("--spp", type=int, default=SPP, help="samples per pixel (the benchmark uses 256)")
     p.add_argument("--tris", type=int, default=1000000, help="--profile build: soup triangles")
-    p.add_argument("--workload", default="4k", choices=["4k", "batch", "large"],
+    p.add_argument("--workload", default="4k", choices=["4k", "batch", "large", "surrogate"],
                    help="4k: the benchmark (built-in scene, 3840x2160, 256 spp); batch: 64 orbit views of the "
                         "seeded 744k-triangle scene in one batch; large: 16 4K views of the 7.88M-triangle scene")
     p.add_argument("--views", type=int, default=0, help="batch/large: number of views (default 64 / 16)")
@@ -415,8 +415,88 @@ def run_views(args):
     print(json.dumps(out), flush=True)
 
 
+SURROGATE_WEIGHTS = os.path.join(PKG, "weights", "surrogate_bf16.npz")
+
+
+def run_surrogate(args):
+    """The 4K head-to-head: 16 orbit views at 3840 x 2160 of the seeded 7.88M-triangle scene,
+    AO radius 1. Truth: the 1024-spp trace of each view. Plain GPU RT runs at the smallest
+    spp of {16, 32, 64, 128, 256} whose RMSE against the truth is <= 0.02 on every view; the
+    surrogate (4-spp trace + U-Net + fallback tiles traced at that same spp) is timed on the
+    same views. Both are timed per frame with CUDA events, G-buffers resident."""
+    import numpy as np
+    import torch
+    import rn_ao as rn
+    import scene as scenes
+    import surrogate as S
+    torch.cuda.set_device(0)
+    rn.init()
+    n_views = args.views or 16
+    sc = scenes.build_synthetic_scene(5, 10000, 6000)
+    tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+    acc = rn.LinearAccel(tris)
+    W, H, R = 3840, 2160, 1.0
+    net = rn.UNet(1, *S.padded_shape(H, W), inference=True)
+    meta = S.load_weights(net, SURROGATE_WEIGHTS)
+    frames = []
+    spps = (16, 32, 64, 128, 256)
+    for (_, _, _, cam) in scenes.orbit_views(5, n_views):
+        g, depth = rn.rasterize(tris, nrms, cam, W, H, want_depth=True)
+        truth = rn.compute_rtao(g, acc, S.SPP_TARGET, R)
+        rm = {s: S.rmse(rn.compute_rtao(g, acc, s, R), truth, g.mask) for s in spps}
+        frames.append(dict(g=g, depth=depth, truth=truth, rmse_rt=rm, covered=int(g.mask.sum().item())))
+    ok_spp = [s for s in spps if all(f["rmse_rt"][s] <= 0.02 for f in frames)]
+    spp_rt = ok_spp[0] if ok_spp else spps[-1]
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, out
+
+    rt_ms, sur_ms, sur_rmse, fb = [], [], [], []
+    with Clocks(0) as clk:
+        for f in frames:
+            ms, _ = timed(lambda: rn.compute_rtao(f["g"], acc, spp_rt, R), args.steps)
+            rt_ms.append(ms)
+            ms, (ao, frac) = timed(lambda: S.surrogate_ao(net, f["g"], f["depth"], acc, spp_rt, R), args.steps)
+            sur_ms.append(ms)
+            sur_rmse.append(S.rmse(ao, f["truth"], f["g"].mask))
+            fb.append(frac)
+    rays_rt = sum(f["covered"] for f in frames) * spp_rt
+    out = {
+        "metric": METRIC, "value": float(np.mean(sur_ms)), "unit": "ms/frame (surrogate)", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(sur_ms)), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, f32 trace", "data": "synthetic",
+        "config": {"workload": "surrogate vs plain GPU RT: seeded 7.88M-triangle scene, %d orbit views at 3840x2160, "
+                               "radius 1, truth 1024 spp" % n_views, "triangles": int(len(sc.tris)),
+                   "views": n_views, "weights": os.path.relpath(SURROGATE_WEIGHTS, ROOT),
+                   "trained": {k: meta.get(k) for k in ("steps", "batch", "lr", "data_digest")}},
+        "plain_rt": {"spp": spp_rt, "ms_per_frame": float(np.mean(rt_ms)),
+                     "grays_per_s": rays_rt / (sum(rt_ms) * 1e-3) / 1e9,
+                     "rmse_by_spp_max_over_views": {s: max(f["rmse_rt"][s] for f in frames) for s in spps}},
+        "surrogate": {"ms_per_frame": float(np.mean(sur_ms)), "rmse_max_over_views": max(sur_rmse),
+                      "rmse_mean": float(np.mean(sur_rmse)), "fallback_fraction_mean": float(np.mean(fb)),
+                      "spp_input": S.SPP_IN, "fallback_spp": spp_rt},
+        "speedup_vs_plain_rt": float(np.mean(rt_ms) / np.mean(sur_ms)),
+        "surrogate_meets_rmse": bool(max(sur_rmse) <= 0.02),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "surrogate" and not args.profile:
+        run_surrogate(args)
+        return
     if args.workload != "4k" and not args.profile:
         run_views(args)
         return

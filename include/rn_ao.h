@@ -238,6 +238,20 @@ int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t*
                          float tolerance, void* stream, float* err, rn_reconcile_result* out,
                          rn_status* st);
 
+/* Launch-shape tuning (no counterpart in the reference; no key changes a per-pixel result).
+ * Keys and values:
+ *   trace_min_blocks  2 | 3 | 4      resident traversal blocks per SM (register budget)
+ *   trace_frontier    0 | 1          per-warp frontier for AO-only walks
+ *   trace_packet      4 | 8 | 16     a warp's pixel packet: packet x (32 / packet)
+ *   trace_stack       48 | 96        traversal stack entries (48 only where the tree allows)
+ *   ssao_tile_h       4 | 8 | 16     SSAO tile 32 x h (the fused FP64 sum follows the tiling)
+ *   conv_bn_max       64 | 128 | 256 widest GEMM tile of the surrogate's convolutions
+ * Process-wide; RN_TUNE_<KEY> environment variables apply before the first call.
+ * rn_tune_load reads "key = value" lines ('#' comments), all or nothing. */
+int rn_tune_set(const char* key, int value, rn_status* st);
+int rn_tune_get(const char* key, int* value, rn_status* st);
+int rn_tune_load(const char* path, rn_status* st);
+
 /* The learned surrogate's tensor-core GEMM (no counterpart in the reference): C = P * Q^T,
  * P (M x K) and Q (N x K) BF16 row-major with K contiguous (row strides ldp, ldq, multiples
  * of 8), FP32 accumulation on tcgen05 with TMEM, output FP32 (`c32`) and/or BF16 (`c16`) with
@@ -246,6 +260,17 @@ int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t*
  * (which the caller zeroes). Device pointers, the library's stream, asynchronous. */
 int rn_tc_gemm(const void* P, int ldp, const void* Q, int ldq, int M, int N, int K, int splits, float* c32,
                void* c16, int ldc, const float* bias, int relu, rn_status* st);
+
+/* The surrogate's implicit-GEMM 3x3 convolution (no counterpart in the reference), stride 1,
+ * zero padding 1: out[b,y,x,n] = bias[n] + sum over taps t = 3 (dy+1) + (dx+1) and input
+ * channels ci of in[b, y+dy, x+dx, ci] * w[n][t * Cin + ci], the input being src0's c0
+ * channels followed by src1's c1 (src1 may be null). Sources are NHWC BF16 [B][H][W][c],
+ * c a multiple of 32; w is BF16 [N][ldw], ldw >= 9 Cin; outputs [B][H][W][N] as FP32 (c32)
+ * and/or BF16 (c16), optional ReLU; up16 (with c16) also receives the BF16 output upsampled
+ * 2x by nearest neighbour, [B][2H][2W][N]. W's largest power-of-two divisor (at most 128),
+ * TW, sets the tile (128 / TW rows must divide H). Device pointers, the library's stream. */
+int rn_tc_conv3x3(const void* src0, int c0, const void* src1, int c1, int B, int H, int W, const void* w, int ldw,
+                  int N, float* c32, void* c16, void* up16, const float* bias, int relu, rn_status* st);
 
 /* The learned AO surrogate (no counterpart in the reference): a BF16 U-Net, 4 levels of
  * 32/64/128/256 channels, two 3x3 convolutions + ReLU per level, average-pool down, nearest up
@@ -256,7 +281,13 @@ int rn_tc_gemm(const void* P, int ldp, const void* Q, int ldq, int M, int N, int
  * FP32 [batch][height][width][5] (depth / radius, normal xyz, 4-spp AO); outputs and targets
  * DEVICE FP32 [batch][height][width]. */
 typedef struct rn_unet rn_unet;
-int rn_unet_create(int batch, int height, int width, uint64_t seed, rn_unet** out, rn_status* st);
+/* flags: RN_UNET_INFERENCE creates a forward-only network (no gradient storage;
+ * rn_unet_train_step is refused). Convolutions with >= 32 input channels run as implicit
+ * GEMMs (rn_tc_conv3x3) when every level's size can be tiled, else on explicit im2col rows
+ * and the GEMM; RN_UNET_EXPLICIT forces the latter (same arithmetic, for comparison). */
+#define RN_UNET_INFERENCE 1u
+#define RN_UNET_EXPLICIT 2u
+int rn_unet_create(int batch, int height, int width, uint64_t seed, uint32_t flags, rn_unet** out, rn_status* st);
 void rn_unet_free(rn_unet* net);
 int rn_unet_param_count(const rn_unet* net, uint64_t* count, rn_status* st);
 /* Predicted AO into `output` (asynchronous on the library's stream). */
@@ -270,6 +301,15 @@ int rn_unet_train_step(rn_unet* net, const float* input, const float* target, in
 int rn_unet_get_params(rn_unet* net, float* host, rn_status* st);
 int rn_unet_set_params(rn_unet* net, const float* host, rn_status* st);
 int rn_unet_get_grads(rn_unet* net, float* host, rn_status* st);
+/* Adaptive gradient clipping for later train steps: the global gradient norm is limited to
+ * ratio x a running mean of the past clipped norms (0, the default, turns it off); a
+ * non-finite gradient skips the update. The last step's norm and applied factor: */
+int rn_unet_set_clip(rn_unet* net, float ratio, rn_status* st);
+int rn_unet_last_grad_norm(const rn_unet* net, float* norm, float* scale, rn_status* st);
+/* Training state for checkpoints: 3 x param_count FP32 host values (master weights, Adam's
+ * first moments, second moments, each in the parameters' layout) and the step count. */
+int rn_unet_get_state(rn_unet* net, float* host, uint64_t* step, rn_status* st);
+int rn_unet_set_state(rn_unet* net, const float* host, uint64_t step, rn_status* st);
 
 #ifdef __cplusplus
 }  /* extern "C" */

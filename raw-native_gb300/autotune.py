@@ -1,0 +1,191 @@
+"""Autotuner for the library's launch shapes (rn_tune_* keys): the traversal's packet shape,
+stack depth, residency and frontier; the SSAO tile; the convolution GEMM's tile width.
+
+Every candidate is timed with CUDA events on the library's stream over representative
+workloads, after a check that it reproduces the default configuration's outputs bit for bit
+(the keys change launch shapes, never results). The winners are written as a tune file
+("key = value" lines) that rn_tune_load reads; rn_ao.init() loads the package's
+tune_sm103.txt when it exists.
+
+  python autotune.py --out tune_sm103.txt [--report report.json] [--quick]
+
+Workloads:
+  trace/model2   the reference's built-in scene and default camera at 3840 x 2160, 64 spp,
+                 AO + sky + sun (lighting model 2, radius 2)
+  trace/ao       a seeded synthetic scene (2,000 boxes, 500 spheres; 744k triangles),
+                 1920 x 1080 orbit view, 64 spp AO only (radius 1)
+  ssao           the built-in scene at 4K: SSAO, 24 taps
+  conv           the surrogate U-Net: a forward at 1088 x 1920 and a training step on
+                 64 crops of 128 x 128
+The traversal keys are searched jointly (every combination); the SSAO and GEMM keys alone.
+"""
+from __future__ import annotations
+
+import argparse
+import itertools
+import json
+import sys
+import time
+
+import numpy as np
+
+import rn_ao as rn
+import scene as scenes
+
+TRACE_KEYS = ("trace_min_blocks", "trace_packet", "trace_stack", "trace_frontier")
+
+
+def _time(fn, reps: int) -> float:
+    """Mean ms of fn() over reps runs on the current stream, after one warm-up run."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _apply(cfg: dict) -> None:
+    for k, v in cfg.items():
+        rn.tune_set(k, v)
+
+
+def trace_workloads(quick: bool):
+    import torch
+    out = []
+    sc = scenes.build_test_scene()
+    tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+    w, h = (1920, 1080) if quick else (3840, 2160)
+    g = rn.rasterize(tris, nrms, sc.camera, w, h)
+    acc = rn.LinearAccel(tris)
+    tl = sc.to_light
+    out.append(("trace/model2", lambda: rn.compute_rt_visibility(g, acc, 64, 2.0, tl)[0], (g, acc)))
+    big = scenes.build_synthetic_scene(7, 500 if quick else 2000, 100 if quick else 500)
+    bt, bn = torch.from_numpy(big.tris).cuda(), torch.from_numpy(big.normals).cuda()
+    cam = scenes.orbit_views(7, 8)[0][3]
+    g2 = rn.rasterize(bt, bn, cam, 1920, 1080)
+    acc2 = rn.LinearAccel(bt)
+    out.append(("trace/ao", lambda: rn.compute_rtao(g2, acc2, 64, 1.0), (g2, acc2)))
+    return out
+
+
+def tune_trace(quick: bool, reps: int, log):
+    defaults = {k: rn.tune_get(k) for k in TRACE_KEYS}
+    wls = trace_workloads(quick)
+    _apply(defaults)
+    ref = [fn().clone() for _, fn, _ in wls]
+    rows = []
+    for combo in itertools.product(*(rn.TUNE_KEYS[k] for k in TRACE_KEYS)):
+        cfg = dict(zip(TRACE_KEYS, combo))
+        _apply(cfg)
+        same = all(bool((fn() == r).all()) for (_, fn, _), r in zip(wls, ref))
+        if not same:
+            raise RuntimeError("tuning changed a traced result: %s" % cfg)
+        ms = {name: _time(fn, reps) for name, fn, _ in wls}
+        rows.append(dict(cfg=cfg, ms=ms))
+        log("trace %s  %s" % (cfg, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    base = next(r for r in rows if r["cfg"] == defaults)["ms"]
+    # score: geometric mean of the time ratios to the defaults
+    for r in rows:
+        r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
+    best = min(rows, key=lambda r: r["score"])
+    _apply(best["cfg"])
+    return best["cfg"], rows
+
+
+def tune_ssao(quick: bool, reps: int, log):
+    import torch
+    sc = scenes.build_test_scene()
+    tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+    w, h = (1920, 1080) if quick else (3840, 2160)
+    g = rn.rasterize(tris, nrms, sc.camera, w, h)
+    rows = []
+    ref = None
+    for v in rn.TUNE_KEYS["ssao_tile_h"]:
+        rn.tune_set("ssao_tile_h", v)
+        ao = rn.compute_ssao(g)
+        if ref is None:
+            ref = ao.clone()
+        elif not bool((ao == ref).all()):
+            raise RuntimeError("ssao_tile_h %d changed the SSAO image" % v)
+        ms = _time(lambda: rn.compute_ssao(g), reps)
+        rows.append(dict(cfg={"ssao_tile_h": v}, ms={"ssao": ms}))
+        log("ssao_tile_h %d  %.3f ms" % (v, ms))
+    best = min(rows, key=lambda r: r["ms"]["ssao"])
+    rn.tune_set("ssao_tile_h", best["cfg"]["ssao_tile_h"])
+    return best["cfg"], rows
+
+
+def tune_conv(quick: bool, reps: int, log):
+    import torch
+    H, W = (544, 960) if quick else (1088, 1920)
+    inf = rn.UNet(1, H, W, seed=1, inference=True)
+    trn = rn.UNet(16 if quick else 64, 128, 128, seed=1)
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.rand(1, H, W, 5, device="cuda", generator=g)
+    xb = torch.rand(trn.shape[0], 128, 128, 5, device="cuda", generator=g)
+    yb = torch.rand(trn.shape[0], 128, 128, device="cuda", generator=g)
+    rows = []
+    ref = None
+    for v in rn.TUNE_KEYS["conv_bn_max"]:
+        rn.tune_set("conv_bn_max", v)
+        out = inf.forward(x)
+        if ref is None:
+            ref = out.clone()
+        elif not bool((out == ref).all()):
+            raise RuntimeError("conv_bn_max %d changed the network's output" % v)
+        ms_f = _time(lambda: inf.forward(x), reps)
+        ms_t = _time(lambda: trn.train_step(xb, yb, 0.0), max(2, reps // 2))
+        rows.append(dict(cfg={"conv_bn_max": v}, ms={"forward": ms_f, "train_step": ms_t}))
+        log("conv_bn_max %d  forward %.3f ms  train step %.3f ms" % (v, ms_f, ms_t))
+    base = rows[-1]["ms"]
+    for r in rows:
+        r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
+    best = min(rows, key=lambda r: r["score"])
+    rn.tune_set("conv_bn_max", best["cfg"]["conv_bn_max"])
+    inf.close()
+    trn.close()
+    return best["cfg"], rows
+
+
+def write_tune_file(path: str, cfg: dict, note: str) -> None:
+    with open(path, "w") as f:
+        f.write("# launch shapes picked by autotune.py: %s\n" % note)
+        for k in rn.TUNE_KEYS:
+            if k in cfg:
+                f.write("%s = %d\n" % (k, cfg[k]))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--out", required=True, help="tune file to write")
+    ap.add_argument("--report", default=None, help="JSON with every candidate's timings")
+    ap.add_argument("--quick", action="store_true", help="smaller workloads (a test run)")
+    ap.add_argument("--reps", type=int, default=5)
+    a = ap.parse_args(argv)
+    import torch
+    rn.init(load_tune=False)
+    t0 = time.time()
+    log = lambda m: print(m, flush=True)
+    cfg, report = {}, {}
+    c, report["trace"] = tune_trace(a.quick, a.reps, log)
+    cfg.update(c)
+    c, report["ssao"] = tune_ssao(a.quick, a.reps, log)
+    cfg.update(c)
+    c, report["conv"] = tune_conv(a.quick, a.reps, log)
+    cfg.update(c)
+    dev = torch.cuda.get_device_name(0)
+    note = "%s, %d SMs, %s workloads, %.0f s" % (dev, torch.cuda.get_device_properties(0).multi_processor_count,
+                                                 "quick" if a.quick else "full", time.time() - t0)
+    write_tune_file(a.out, cfg, note)
+    log("picked %s" % json.dumps(cfg))
+    if a.report:
+        json.dump(dict(picked=cfg, note=note, candidates=report), open(a.report, "w"), indent=1)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

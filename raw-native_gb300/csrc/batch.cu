@@ -165,7 +165,8 @@ int rn_batch_create(const rn_accel* accel, const rn_view* views, int nviews, int
         p.corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
         p.ao = in.ao; p.sky = in.sky; p.sun = in.sun;
         p.err_word = c.dev_error;
-        p.frontier = c.tune.trace_frontier;
+        apply_tune(p, accel);
+        p.packet_log2 = 3;                       // the batch's work queue uses 8 x 4 packets
         b.tile_begin = tiles;
         tiles += (uint32_t)(((in.w + 7) / 8) * ((in.h + 3) / 4));
         b.ssao_begin = ssao_blocks_total;

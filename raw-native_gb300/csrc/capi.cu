@@ -6,7 +6,10 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
+#include <string>
+#include <utility>
 #include <thread>
 #include <vector>
 
@@ -98,6 +101,64 @@ int build_trig_correction(Context& c, rn_status* st) {
     return RN_OK;
 }
 
+// ------------------------------------------------------------------ launch-shape tuning
+namespace {
+struct TuneKey {
+    const char* name;
+    const char* env;
+    int Tune::*field;
+    int allowed[4];
+    int nallowed;
+};
+const TuneKey kTuneKeys[] = {
+    {"trace_min_blocks", "RN_TUNE_TRACE_MIN_BLOCKS", &Tune::trace_min_blocks, {2, 3, 4}, 3},
+    {"trace_frontier", "RN_TUNE_TRACE_FRONTIER", &Tune::trace_frontier, {0, 1}, 2},
+    {"trace_packet", "RN_TUNE_TRACE_PACKET", &Tune::trace_packet, {4, 8, 16}, 3},
+    {"trace_stack", "RN_TUNE_TRACE_STACK", &Tune::trace_stack, {48, 96}, 2},
+    {"ssao_tile_h", "RN_TUNE_SSAO_TILE_H", &Tune::ssao_tile_h, {4, 8, 16}, 3},
+    {"conv_bn_max", "RN_TUNE_CONV_BN_MAX", &Tune::conv_bn_max, {64, 128, 256}, 3},
+};
+
+const TuneKey* find_tune_key(const char* name) {
+    for (const TuneKey& k : kTuneKeys)
+        if (std::strcmp(k.name, name) == 0) return &k;
+    return nullptr;
+}
+
+int tune_assign(const char* name, int value, rn_status* st) {
+    const TuneKey* k = find_tune_key(name);
+    if (!k) return fail(st, RN_ERR_INVALID, "unknown tuning key '%s'", name);
+    for (int i = 0; i < k->nallowed; ++i)
+        if (k->allowed[i] == value) {
+            ctx().tune.*(k->field) = value;
+            return RN_OK;
+        }
+    return fail(st, RN_ERR_INVALID, "tuning key '%s' does not take %d", name, value);
+}
+
+// RN_TUNE_<KEY> environment variables, applied once before any other tuning call.
+void tune_env_once() {
+    static bool done = false;
+    if (done) return;
+    done = true;
+    for (const TuneKey& k : kTuneKeys)
+        if (const char* v = getenv(k.env)) {
+            rn_status ignored;
+            tune_assign(k.name, atoi(v), &ignored);
+        }
+}
+
+int packet_log2(int packet) { return packet == 4 ? 2 : packet == 16 ? 4 : 3; }
+
+}  // namespace
+
+void apply_tune(TraceParams& p, const rn_accel* accel) {
+    const Tune& t = ctx().tune;
+    p.frontier = t.trace_frontier;
+    p.packet_log2 = packet_log2(t.trace_packet);
+    p.stack_need = 16 + 3 * (int)(accel ? accel->depth : 0);
+}
+
 int ensure_ctx(rn_status* st) {
     Context& c = ctx();
     if (c.ready) return RN_OK;
@@ -114,11 +175,7 @@ int ensure_ctx(rn_status* st) {
                     prop.major, prop.minor);
     c.device = dev;
     c.sm_count = prop.multiProcessorCount;
-    if (const char* v = getenv("RN_TUNE_TRACE_MIN_BLOCKS")) {
-        const int mb = atoi(v);
-        if (mb >= 2 && mb <= 4) c.tune.trace_min_blocks = mb;
-    }
-    if (const char* v = getenv("RN_TUNE_TRACE_FRONTIER")) c.tune.trace_frontier = atoi(v) != 0;
+    tune_env_once();
     RN_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking), st);
     c.stream = c.own_stream;
     RN_CUDA(cudaMalloc((void**)&c.dev_error, 64), st);
@@ -229,7 +286,7 @@ int do_visibility(const StagedGbuf& g, int w, int h, const rn_accel* accel, int 
     p.corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
     p.ao = ao; p.sky = sky; p.sun = sun;
     p.err_word = c.dev_error;
-    p.frontier = c.tune.trace_frontier;
+    apply_tune(p, accel);
     if (launch_trace(p, c.sm_count, c.stream) != RN_OK) return cuda_fail(st, cudaGetLastError(), "trace_kernel");
     return RN_OK;
 }
@@ -305,6 +362,56 @@ void fill_result(const RecOut& r, float tolerance, rn_reconcile_result* out) {
 extern "C" {
 
 int rn_ao_version(void) { return RN_AO_ABI_VERSION; }
+
+int rn_tune_set(const char* key, int value, rn_status* st) {
+    if (!key) return fail(st, RN_ERR_INVALID, "null key");
+    tune_env_once();
+    RN_TRY(tune_assign(key, value, st));
+    return ok(st);
+}
+
+int rn_tune_get(const char* key, int* value, rn_status* st) {
+    if (!key || !value) return fail(st, RN_ERR_INVALID, "null argument");
+    tune_env_once();
+    const TuneKey* k = find_tune_key(key);
+    if (!k) return fail(st, RN_ERR_INVALID, "unknown tuning key '%s'", key);
+    *value = ctx().tune.*(k->field);
+    return ok(st);
+}
+
+// "key = value" lines; '#' starts a comment. Every line is checked before any is applied; a
+// key whose RN_TUNE_<KEY> environment variable is set keeps the variable's value.
+int rn_tune_load(const char* path, rn_status* st) {
+    if (!path) return fail(st, RN_ERR_INVALID, "null path");
+    tune_env_once();
+    FILE* f = std::fopen(path, "r");
+    if (!f) return fail(st, RN_ERR_INVALID, "cannot open %s", path);
+    std::vector<std::pair<std::string, int>> kv;
+    char line[256];
+    int lineno = 0, rc = RN_OK;
+    while (rc == RN_OK && std::fgets(line, sizeof line, f)) {
+        ++lineno;
+        if (char* h = std::strchr(line, '#')) *h = 0;
+        char key[64];
+        int value = 0;
+        char extra[8];
+        const int n = std::sscanf(line, " %63[a-z0-9_] = %d %7s", key, &value, extra);
+        if (n == EOF || (n <= 0 && std::strspn(line, " \t\r\n") == std::strlen(line))) continue;
+        if (n != 2) { rc = fail(st, RN_ERR_INVALID, "%s:%d: expected 'key = value'", path, lineno); break; }
+        const TuneKey* k = find_tune_key(key);
+        if (!k) { rc = fail(st, RN_ERR_INVALID, "%s:%d: unknown tuning key '%s'", path, lineno, key); break; }
+        kv.emplace_back(key, value);
+    }
+    std::fclose(f);
+    if (rc != RN_OK) return rc;
+    const Tune saved = ctx().tune;
+    for (auto& e : kv)
+        if (!getenv(find_tune_key(e.first.c_str())->env) && tune_assign(e.first.c_str(), e.second, st) != RN_OK) {
+            ctx().tune = saved;
+            return st ? st->code : RN_ERR_INVALID;
+        }
+    return ok(st);
+}
 
 int rn_init(rn_status* st) {
     RN_TRY(ensure_ctx(st));
@@ -600,7 +707,7 @@ int rn_ao_trace_stats(const rn_gbuf* g, const rn_accel* accel, int spp, float ra
     p.corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
     p.ao = (float*)scratch[0]; p.sky = (float*)scratch[1]; p.sun = (float*)scratch[2];
     p.err_word = c.dev_error;
-    p.frontier = c.tune.trace_frontier;
+    apply_tune(p, accel);
     if (launch_trace(p, c.sm_count, c.stream, (unsigned long long*)cnt, tile_stride) != RN_OK)
         return cuda_fail(st, cudaGetLastError(), "trace_kernel (counting)");
     unsigned long long h[4];

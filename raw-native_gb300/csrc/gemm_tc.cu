@@ -60,6 +60,21 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     d |= (uint64_t)2 << 61;                                   // 128-byte swizzle
     return d;
 }
+// The same for rows of 64 bytes (32 BF16): 64-byte swizzle, 8-row atoms 512 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc64(uint32_t addr) {
+    uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((512u >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)4 << 61;                                   // 64-byte swizzle
+    return d;
+}
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c, int x, int y, int b,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c), "r"(x), "r"(y), "r"(b), "r"(bar)
+        : "memory");
+}
 // Instruction descriptor of tcgen05.mma.kind::f16: FP32 accumulator, BF16 A and B, both
 // K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t instr_desc(int n) {
@@ -212,6 +227,154 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
 }
 
+
+// ------------------------------------------------------------------ implicit 3x3 convolution
+// Same roles as tc_gemm_kernel. CB is the channel block of one K step (64: 128-byte rows and
+// swizzle; 32: 64-byte rows and swizzle); a K step is (tap, source, channel block), taps
+// outermost, matching the weights' column order tap * Cin + ci.
+struct ConvArgs {
+    int nsrc;
+    int C0, C1;                 // channels of the sources
+    int B, H, W, tw_log2;       // output (= input) geometry and tiling
+    int tiles_x, tiles_y;       // tiles per image row / column
+    int cin;                    // C0 + C1
+    __nv_bfloat16* up16;        // optional 2x nearest-upsampled copy of the BF16 output
+};
+
+template <int BN, int CB>
+__global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const __grid_constant__ CUtensorMap map0,
+                                                              const __grid_constant__ CUtensorMap map1,
+                                                              const __grid_constant__ CUtensorMap mapW,
+                                                              const ConvArgs a, const Epilogue e) {
+    constexpr int kSt = CB == 32 ? 8 : 4;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    constexpr uint32_t kABytes = kBM * CB * 2, kBBytes = BN * CB * 2;
+    constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+    uint8_t* sA = smem;
+    uint8_t* sB = smem + kSt * kABytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kSt * kBBytes);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 1);
+    __shared__ int s_abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tw = 1 << a.tw_log2, th = kBM >> a.tw_log2;
+    const int tile = blockIdx.x;
+    const int tx = tile % a.tiles_x, ty = (tile / a.tiles_x) % a.tiles_y, b = tile / (a.tiles_x * a.tiles_y);
+    const int x0 = tx * tw, y0 = ty * th, n0 = blockIdx.y * BN;
+    const int nb0 = a.C0 / CB, nb1 = a.nsrc > 1 ? a.C1 / CB : 0, per_tap = nb0 + nb1;
+    const int nkb = 9 * per_tap;
+    auto full = [&](int s) { return smem_u32(&bars[s]); };
+    auto empty = [&](int s) { return smem_u32(&bars[kSt + s]); };
+    const uint32_t done = smem_u32(&bars[2 * kSt]);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kSt; ++s) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0) {
+        int issued = 0;
+        for (int kb = 0; kb < nkb; ++kb) {
+            const int s = kb % kSt;
+            const uint32_t ph = (uint32_t)(kb / kSt) & 1u;
+            if (!mbar_wait(empty(s), ph ^ 1u)) { atomicOr(e.err, DEV_GUARD); s_abort = 1; break; }
+            const int tap = kb / per_tap, r = kb % per_tap;
+            const bool second = r >= nb0;
+            const int cb = second ? r - nb0 : r;
+            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            mbar_expect_tx(full(s), kABytes + kBBytes);
+            tma_load_4d(smem_u32(sA + s * kABytes), second ? &map1 : &map0, cb * CB, x0 + dx, y0 + dy, b, full(s));
+            tma_load_2d(smem_u32(sB + s * kBBytes), &mapW, tap * a.cin + (second ? a.C0 : 0) + cb * CB, n0, full(s));
+            ++issued;
+        }
+        for (int kb = issued > kSt ? issued - kSt : 0; kb < issued; ++kb)
+            mbar_wait(full(kb % kSt), (uint32_t)(kb / kSt) & 1u);
+    } else if (warp == 1 && lane == 0) {
+        const uint32_t idesc = instr_desc(BN);
+        for (int kb = 0; kb < nkb; ++kb) {
+            const int s = kb % kSt;
+            const uint32_t ph = (uint32_t)(kb / kSt) & 1u;
+            if (!mbar_wait(full(s), ph)) { atomicOr(e.err, DEV_GUARD); s_abort = 1; break; }
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(sA + s * kABytes), b0 = smem_u32(sB + s * kBBytes);
+#pragma unroll
+            for (int k = 0; k < CB / 16; ++k) {
+                const uint64_t da = CB == 64 ? smem_desc(a0 + k * 32) : smem_desc64(a0 + k * 32);
+                const uint64_t db = CB == 64 ? smem_desc(b0 + k * 32) : smem_desc64(b0 + k * 32);
+                tc_mma(tmem, da, db, idesc, (kb | k) != 0 ? 1u : 0u);
+            }
+            tc_commit(empty(s));
+        }
+        tc_commit(done);
+    }
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
+    tc_fence_after();
+    if (!ok && lane == 0) atomicOr(e.err, DEV_GUARD);
+    const int abort_warp = __shfl_sync(0xffffffffu, *(volatile int*)&s_abort, 0);
+    if (ok && !abort_warp) {
+        const int r = warp * 32 + lane;
+        const int y = y0 + (r >> a.tw_log2), x = x0 + (r & (tw - 1));
+        const size_t pix = ((size_t)b * a.H + y) * a.W + x;
+        const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            uint32_t v[16];
+            tmem_ld16(tbase + (uint32_t)c0, v);
+            float f[16];
+            const int col = n0 + c0;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                float q = __uint_as_float(v[j]);
+                if (e.bias) q += e.bias[col + j];
+                if (e.relu) q = fmaxf(q, 0.0f);
+                f[j] = q;
+            }
+            const size_t o = pix * e.ldc + col;
+            if (e.c16 || a.up16) {
+                uint4 out[2];
+                __nv_bfloat16* ob = reinterpret_cast<__nv_bfloat16*>(out);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) ob[j] = __float2bfloat16_rn(f[j]);
+                if (e.c16) {
+                    uint4* d4 = reinterpret_cast<uint4*>(e.c16 + o);
+                    d4[0] = out[0];
+                    d4[1] = out[1];
+                }
+                if (a.up16) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const size_t up = ((size_t)b * 2 * a.H + 2 * y + (q >> 1)) * (2 * a.W) + 2 * x + (q & 1);
+                        uint4* d4 = reinterpret_cast<uint4*>(a.up16 + up * e.ldc + col);
+                        d4[0] = out[0];
+                        d4[1] = out[1];
+                    }
+                }
+            }
+            if (e.c32) {
+                float4* d4 = reinterpret_cast<float4*>(e.c32 + o);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+}
+
 // ------------------------------------------------------------------ host side
 PFN_cuTensorMapEncodeTiled_v12000 encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -238,6 +401,62 @@ bool make_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, ui
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, elem,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+
+// A 2-D weight map [rows][ld] read in boxes of cb x box_rows (128- or 64-byte swizzle).
+bool make_map_cb(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint64_t ld, uint32_t box_rows, int cb) {
+    auto fn = encoder();
+    if (!fn) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)cb, box_rows};
+    const cuuint32_t elem[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, elem,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, cb == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// A 4-D map of an NHWC BF16 tensor [B][H][W][C], boxes of cb x tw x th x 1; coordinates
+// outside the tensor read zeros (the convolution's padding).
+bool make_map_nhwc(CUtensorMap* m, const void* base, int B, int H, int W, int C, int tw, int th, int cb) {
+    auto fn = encoder();
+    if (!fn) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)C, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B};
+    const cuuint64_t strides[3] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)cb, (cuuint32_t)tw, (cuuint32_t)th, 1};
+    const cuuint32_t elem[4] = {1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(base), dims, strides, box, elem,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, cb == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN, int CB>
+int launch_conv(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap& mw, const ConvArgs& a,
+                const Epilogue& e, int N, cudaStream_t s) {
+    constexpr int kSt = CB == 32 ? 8 : 4;
+    const size_t smem = 1024 + kSt * (kBM * CB * 2 + BN * CB * 2) + (2 * kSt + 1) * 8 + 16;
+    static bool attr = false;
+    if (!attr) {
+        if (cudaFuncSetAttribute(tc_conv_kernel<BN, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return RN_ERR_CUDA;
+        attr = true;
+    }
+    const dim3 grid((unsigned)(a.tiles_x * a.tiles_y * a.B), (unsigned)(N / BN));
+    tc_conv_kernel<BN, CB><<<grid, kThreads, smem, s>>>(m0, m1, mw, a, e);
+    return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
+}
+
+ConvTiling conv_tiling(int H, int W) {
+    ConvTiling t{0, false};
+    if (H <= 0 || W <= 0) return t;
+    int lg = 0;
+    while (lg < 7 && (W % (2 << lg)) == 0) ++lg;            // TW = 2^lg <= 128 divides W
+    const int th = kBM >> lg;
+    t.tw_log2 = lg;
+    t.ok = (H % th) == 0;
+    return t;
 }
 
 template <int BN>
@@ -267,8 +486,9 @@ int tc_gemm(const __nv_bfloat16* P, int ldp, const __nv_bfloat16* Q, int ldq, in
     if ((ldp % 8) || (ldq % 8) || ((uintptr_t)P % 16) || ((uintptr_t)Q % 16))
         return fail(st, RN_ERR_INVALID, "tc_gemm operands must be 16-byte aligned rows");
     if (splits > 1 && !(epi.c32 && epi.atomic)) return fail(st, RN_ERR_INVALID, "split K needs an atomic FP32 output");
-    const int bn = (N == 32 || N == 64 || N == 128 || N == 256) ? N : 128;
+    int bn = (N == 32 || N == 64 || N == 128 || N == 256) ? N : 128;
     if (N % bn) return fail(st, RN_ERR_INVALID, "tc_gemm N %d", N);
+    while (bn > ctx().tune.conv_bn_max && bn > 32) bn /= 2;     // the tuned tile width (divides N)
     tc::Epilogue e = epi;
     e.k_per_split = K / splits;
     CUtensorMap mp, mq;
@@ -283,6 +503,60 @@ int tc_gemm(const __nv_bfloat16* P, int ldp, const __nv_bfloat16* Q, int ldq, in
         default: rc = tc::launch_bn<128>(mp, mq, e, M, N, splits, s); break;
     }
     if (rc != RN_OK) return cuda_fail(st, cudaGetLastError(), "tc_gemm_kernel");
+    return RN_OK;
+}
+
+
+int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv_bfloat16* w, int ldw, int N,
+               const tc::Epilogue& epi, __nv_bfloat16* up16, cudaStream_t s, rn_status* st) {
+    if (nsrc < 1 || nsrc > 2 || !src) return fail(st, RN_ERR_INVALID, "tc_conv3x3: %d sources", nsrc);
+    const tc::ConvTiling t = tc::conv_tiling(H, W);
+    if (!t.ok || B <= 0) return fail(st, RN_ERR_INVALID, "tc_conv3x3: %dx%d cannot be tiled", H, W);
+    int cin = 0;
+    bool all64 = true;
+    for (int i = 0; i < nsrc; ++i) {
+        if (!src[i].ptr || src[i].C <= 0 || src[i].C % 32 || ((uintptr_t)src[i].ptr % 16))
+            return fail(st, RN_ERR_INVALID, "tc_conv3x3: source %d (C %d)", i, src[i].C);
+        all64 = all64 && src[i].C % 64 == 0;
+        cin += src[i].C;
+    }
+    if (ldw < 9 * cin || ldw % 8 || ((uintptr_t)w % 16)) return fail(st, RN_ERR_INVALID, "tc_conv3x3: weight stride %d", ldw);
+    if (epi.atomic || epi.gate) return fail(st, RN_ERR_INVALID, "tc_conv3x3: no atomic or gated epilogue");
+    int bn = (N == 32 || N == 64 || N == 128 || N == 256) ? N : 128;
+    if (N % bn) return fail(st, RN_ERR_INVALID, "tc_conv3x3 N %d", N);
+    while (bn > ctx().tune.conv_bn_max && bn > 32) bn /= 2;
+    if (up16 && !epi.c16) return fail(st, RN_ERR_INVALID, "tc_conv3x3: the upsampled copy needs a BF16 output");
+    const int cb = all64 ? 64 : 32;
+    const int tw = 1 << t.tw_log2, th = tc::kBM >> t.tw_log2;
+    CUtensorMap m[2], mw;
+    for (int i = 0; i < nsrc; ++i)
+        if (!tc::make_map_nhwc(&m[i], src[i].ptr, B, H, W, src[i].C, tw, th, cb))
+            return fail(st, RN_ERR_CUDA, "cuTensorMapEncodeTiled (activation) failed");
+    if (nsrc == 1) m[1] = m[0];
+    if (!tc::make_map_cb(&mw, w, (uint64_t)N, (uint64_t)ldw, (uint64_t)ldw, (uint32_t)bn, cb))
+        return fail(st, RN_ERR_CUDA, "cuTensorMapEncodeTiled (weights) failed");
+    tc::ConvArgs a{};
+    a.nsrc = nsrc;
+    a.C0 = src[0].C;
+    a.C1 = nsrc > 1 ? src[1].C : 0;
+    a.B = B; a.H = H; a.W = W; a.tw_log2 = t.tw_log2;
+    a.tiles_x = W / tw; a.tiles_y = H / th;
+    a.cin = cin;
+    a.up16 = up16;
+    int rc;
+#define RN_CONV_CASE(BNV)                                                                             \
+    case BNV:                                                                                         \
+        rc = cb == 64 ? tc::launch_conv<BNV, 64>(m[0], m[1], mw, a, epi, N, s)                        \
+                      : tc::launch_conv<BNV, 32>(m[0], m[1], mw, a, epi, N, s);                       \
+        break;
+    switch (bn) {
+        RN_CONV_CASE(32)
+        RN_CONV_CASE(64)
+        RN_CONV_CASE(256)
+        default: RN_CONV_CASE(128)
+    }
+#undef RN_CONV_CASE
+    if (rc != RN_OK) return cuda_fail(st, cudaGetLastError(), "tc_conv_kernel");
     return RN_OK;
 }
 
@@ -303,5 +577,24 @@ extern "C" int rn_tc_gemm(const void* P, int ldp, const void* Q, int ldq, int M,
     e.atomic = splits > 1;
     e.err = ctx().dev_error;
     RN_TRY(tc_gemm((const __nv_bfloat16*)P, ldp, (const __nv_bfloat16*)Q, ldq, M, N, K, splits, e, ctx().stream, st));
+    return ok(st);
+}
+
+// Test and measurement entry of the implicit 3x3 convolution (device pointers, NHWC BF16
+// sources, the library's stream).
+extern "C" int rn_tc_conv3x3(const void* src0, int c0, const void* src1, int c1, int B, int H, int W, const void* w,
+                             int ldw, int N, float* c32, void* c16, void* up16, const float* bias, int relu,
+                             rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    tc::ConvSrc src[2] = {{(const __nv_bfloat16*)src0, c0}, {(const __nv_bfloat16*)src1, c1}};
+    tc::Epilogue e{};
+    e.ldc = N;
+    e.c32 = c32;
+    e.c16 = (__nv_bfloat16*)c16;
+    e.bias = bias;
+    e.relu = relu;
+    e.err = ctx().dev_error;
+    RN_TRY(tc_conv3x3(src, src1 ? 2 : 1, B, H, W, (const __nv_bfloat16*)w, ldw, N, e, (__nv_bfloat16*)up16,
+                      ctx().stream, st));
     return ok(st);
 }

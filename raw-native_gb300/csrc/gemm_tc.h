@@ -21,7 +21,33 @@ struct Epilogue {
     uint32_t* err;
 };
 
+// One input of an implicit-GEMM 3x3 convolution: an NHWC BF16 tensor at the output's
+// resolution with C channels (C a multiple of 32).
+struct ConvSrc {
+    const __nv_bfloat16* ptr;
+    int C;
+};
+
+// Output tiling of the implicit convolution: 128 output pixels per CTA as a TH x TW block
+// (TW = the largest power of two <= 128 dividing W, TH = 128 / TW; H % TH == 0).
+struct ConvTiling {
+    int tw_log2;
+    bool ok;
+};
+ConvTiling conv_tiling(int H, int W);
+
 }  // namespace tc
+
+// Implicit-GEMM 3x3 convolution, stride 1, zero padding 1 (no im2col in memory):
+//   out[b, y, x, n] = sum over taps (dy, dx) and input channels ci of
+//                     in[b, y + dy - 1, x + dx - 1, ci] * w[n][tap * Cin + ci]
+// with the inputs' channels concatenated (src[0] first), Cin = sum of src[i].C, w [N][ldw]
+// BF16 (ldw >= 9 Cin, a multiple of 8). Per K step the producer loads, by TMA, the
+// (channels x TW x TH) box of one source at the tap's offset (the border reads zeros) and
+// the matching weight columns. The epilogue's ldc/c16/c32/bias/relu apply per pixel row;
+// up16, when set, also receives the output upsampled 2x (nearest) at (2H, 2W).
+int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv_bfloat16* w, int ldw, int N,
+               const tc::Epilogue& epi, __nv_bfloat16* up16, cudaStream_t s, rn_status* st);
 
 // C (M x N, row stride ldc) = P (M x K, row stride ldp) * Q (N x K, row stride ldq)^T.
 // M % 128 == 0, N in {32, 64, 128, 256} or a multiple of 128, K % (64 * splits) == 0;

@@ -34,10 +34,15 @@ enum Slot {
     WS_COUNT
 };
 
-// Launch shapes the autotuner may change (rn_tune_* and RN_TUNE_* environment variables).
+// Launch shapes the autotuner may change (rn_tune_set / rn_tune_load, and RN_TUNE_<KEY>
+// environment variables at the first rn_init). None of them changes a result bit.
 struct Tune {
     int trace_min_blocks = 3;   // resident 256-thread traversal blocks per SM: 2, 3 or 4
     int trace_frontier = 1;     // per-warp frontier for AO-only walks
+    int trace_packet = 8;       // a warp's pixel packet: trace_packet x (32 / trace_packet); 4, 8 or 16
+    int trace_stack = 96;       // traversal stack entries: 48 or 96 (48 only where the tree's depth allows)
+    int ssao_tile_h = 8;        // SSAO tile: 32 x ssao_tile_h pixels, one thread each; 4, 8 or 16
+    int conv_bn_max = 256;      // largest GEMM tile width (columns of C per CTA): 64, 128 or 256
 };
 
 struct Context {
@@ -170,7 +175,11 @@ struct TraceParams {
     float* sun;
     uint32_t* err_word;
     int frontier;         // AO-only walks start from a per-warp frontier (0: from the root)
+    int packet_log2;      // log2 of the packet width (pixels per warp row): 2, 3 or 4
+    int stack_need;       // entries the walk can push on this tree: 16 + 3 x wide depth
 };
+// The tuned trace fields of p (frontier, packet, stack bound for this tree).
+void apply_tune(TraceParams& p, const rn_accel* accel);
 int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned long long* counts = nullptr,
                  uint32_t stride = 1);
 

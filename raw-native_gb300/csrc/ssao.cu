@@ -18,33 +18,51 @@ namespace {
 
 using namespace ssao_dev;
 
-template <bool kFused>
-__global__ void __launch_bounds__(kThreads) ssao_kernel(int w, int h, const float* __restrict__ pos,
-                                                        const float* __restrict__ nrm, const uint8_t* __restrict__ mask,
-                                                        int samples, float radius, const uint8_t* __restrict__ corr,
-                                                        float* __restrict__ ao, const float* __restrict__ truth,
-                                                        float* __restrict__ err, RecPartial* parts, RecOut* out) {
-    __shared__ float4 win[kSH][kSW];
+template <bool kFused, int TY>
+__global__ void __launch_bounds__(Tile<TY>::kThreads) ssao_kernel(int w, int h, const float* __restrict__ pos,
+                                                                  const float* __restrict__ nrm,
+                                                                  const uint8_t* __restrict__ mask, int samples,
+                                                                  float radius, const uint8_t* __restrict__ corr,
+                                                                  float* __restrict__ ao, const float* __restrict__ truth,
+                                                                  float* __restrict__ err, RecPartial* parts, RecOut* out) {
+    __shared__ float4 win[Tile<TY>::kH][kSW];
     RecAcc acc;
-    ssao_tile<kFused>(win, blockIdx.x, blockIdx.y, w, h, pos, nrm, mask, samples, radius, corr, ao, truth, err, acc);
+    ssao_tile<kFused, TY>(win, blockIdx.x, blockIdx.y, w, h, pos, nrm, mask, samples, radius, corr, ao, truth, err, acc);
     if (kFused)
-        rec_block_finish<kThreads>(acc, parts, out, blockIdx.y * gridDim.x + blockIdx.x, gridDim.x * gridDim.y);
+        rec_block_finish<Tile<TY>::kThreads>(acc, parts, out, blockIdx.y * gridDim.x + blockIdx.x, gridDim.x * gridDim.y);
+}
+
+template <int TY>
+void launch_tile(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, int samples, float radius,
+                 const uint8_t* corr, float* ao, const float* truth, float* err, RecPartial* partials, RecOut* out,
+                 cudaStream_t s) {
+    const dim3 grid((w + kTX - 1) / kTX, (h + TY - 1) / TY);
+    if (truth)
+        ssao_kernel<true, TY><<<grid, Tile<TY>::kThreads, 0, s>>>(w, h, pos, nrm, mask, samples, radius, corr, ao, truth,
+                                                                   err, partials, out);
+    else
+        ssao_kernel<false, TY><<<grid, Tile<TY>::kThreads, 0, s>>>(w, h, pos, nrm, mask, samples, radius, corr, ao,
+                                                                    nullptr, nullptr, nullptr, nullptr);
+}
+
+int tile_h() {
+    const int t = ctx().tune.ssao_tile_h;
+    return t == 4 || t == 16 ? t : 8;
 }
 
 }  // namespace
 
-int ssao_blocks(int w, int h) { return ((w + kTX - 1) / kTX) * ((h + kTY - 1) / kTY); }
+// Blocks of one SSAO launch (the fused reconcile keeps one partial per block).
+int ssao_blocks(int w, int h) { return ((w + kTX - 1) / kTX) * ((h + tile_h() - 1) / tile_h()); }
 
 int launch_ssao(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, int samples, float radius,
                 const uint8_t* corr, float* ao, const float* truth, float* err, RecPartial* partials, RecOut* out,
                 cudaStream_t s) {
-    const dim3 grid((w + kTX - 1) / kTX, (h + kTY - 1) / kTY);
-    if (truth)
-        ssao_kernel<true><<<grid, kThreads, 0, s>>>(w, h, pos, nrm, mask, samples, radius, corr, ao, truth, err,
-                                                     partials, out);
-    else
-        ssao_kernel<false><<<grid, kThreads, 0, s>>>(w, h, pos, nrm, mask, samples, radius, corr, ao, nullptr,
-                                                      nullptr, nullptr, nullptr);
+    switch (tile_h()) {
+        case 4: launch_tile<4>(w, h, pos, nrm, mask, samples, radius, corr, ao, truth, err, partials, out, s); break;
+        case 16: launch_tile<16>(w, h, pos, nrm, mask, samples, radius, corr, ao, truth, err, partials, out, s); break;
+        default: launch_tile<8>(w, h, pos, nrm, mask, samples, radius, corr, ao, truth, err, partials, out, s); break;
+    }
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 

@@ -9,9 +9,15 @@
 namespace rn {
 namespace ssao_dev {
 
+// A tile is kTX x TY pixels, one thread each (TY = 8 by default; 4 and 16 are the
+// autotuner's alternatives), with a window of (TY + 2R) x (kTX + 2R) positions.
 constexpr int kTX = 32, kTY = 8, kR = 6;
 constexpr int kSW = kTX + 2 * kR, kSH = kTY + 2 * kR;
 constexpr int kThreads = kTX * kTY;
+template <int TY> struct Tile {
+    static constexpr int kH = TY + 2 * kR;
+    static constexpr int kThreads = kTX * TY;
+};
 
 __device__ __forceinline__ bool near_half(float v) {
     const float a = fabsf(v);
@@ -21,14 +27,14 @@ __device__ __forceinline__ bool near_half(float v) {
 // Tile (bx, by) of a w x h frame: SSAO into ao, and with kFused the error against `truth`
 // into err (may be null) with this thread's share of the reconcile in `acc`. `win` is the
 // block's shared window. Every thread of the block must call it.
-template <bool kFused>
-__device__ __forceinline__ void ssao_tile(float4 (&win)[kSH][kSW], int bx, int by, int w, int h,
+template <bool kFused, int TY = kTY>
+__device__ __forceinline__ void ssao_tile(float4 (&win)[Tile<TY>::kH][kSW], int bx, int by, int w, int h,
                                           const float* __restrict__ pos, const float* __restrict__ nrm,
                                           const uint8_t* __restrict__ mask, int samples, float radius,
                                           const uint8_t* __restrict__ corr, float* __restrict__ ao,
                                           const float* __restrict__ truth, float* __restrict__ err, RecAcc& acc) {
-    const int x0 = bx * kTX, y0 = by * kTY;
-    for (int q = threadIdx.x; q < kSH * kSW; q += kThreads) {
+    const int x0 = bx * kTX, y0 = by * TY;
+    for (int q = threadIdx.x; q < Tile<TY>::kH * kSW; q += Tile<TY>::kThreads) {
         const int wy = q / kSW, wx = q % kSW;
         const int gx = x0 - kR + wx, gy = y0 - kR + wy;
         float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);

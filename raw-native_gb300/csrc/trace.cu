@@ -1,8 +1,9 @@
 // trace.cu -- ray-traced AO and lighting model 2's visibility on the GPU: the hot loop of
 // raw-native's CPU oracle (src/renderer/ray_ao.cpp:20-51) as one persistent kernel.
 //
-// Work: the frame is cut into 8 x 4 pixel tiles; each warp takes the next tile from a global
-// counter, one pixel per lane, and walks its `spp` hemisphere rays, then the sun ray,
+// Work: the frame is cut into packets of 32 pixels (8 x 4 by default; 4 x 8 and 16 x 2 are
+// the autotuner's alternatives); each warp takes the next packet from a global counter, one
+// pixel per lane, and walks its `spp` hemisphere rays, then the sun ray,
 // through the 4-wide BVH. Neighbouring lanes trace neighbouring pixels, so the warp's rays
 // start close together and visit similar nodes.
 //
@@ -30,10 +31,11 @@ using namespace trace_dev;
 // fetches to counts[0..3] (hemisphere rays, nodes, tris, sky continuations); the outputs of
 // the other tiles are left unwritten. "Sky continuations" are the open hemisphere rays whose
 // walk went on past the radius: the same walk serves both queries.
-template <bool kCount, int kMinBlocks>
+template <bool kCount, int kMinBlocks, int kStackN>
 __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_constant__ TraceParams p, uint32_t* tile_ctr,
                                                                 unsigned long long* counts, uint32_t stride) {
-    const int tiles_x = (p.w + kTileW - 1) / kTileW, tiles_y = (p.h + kTileH - 1) / kTileH;
+    const int pl = p.packet_log2, tw = 1 << pl, th = 32 >> pl;
+    const int tiles_x = (p.w + tw - 1) >> pl, tiles_y = (p.h + th - 1) / th;
     const uint32_t ntiles = (uint32_t)tiles_x * tiles_y;
     const unsigned lane = threadIdx.x & 31u;
     __shared__ FrontierEntry frontier[8][kFrontier];
@@ -46,12 +48,12 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         if (lane == 0) tile = atomicAdd(tile_ctr, 1u);
         tile = __shfl_sync(0xffffffffu, tile, 0);
         if (tile >= ntiles) break;
-        const int x = (int)(tile % tiles_x) * kTileW + (int)(lane % kTileW);
-        const int y = (int)(tile / tiles_x) * kTileH + (int)(lane / kTileW);
+        const int x = ((int)(tile % tiles_x) << pl) + (int)(lane & (tw - 1));
+        const int y = (int)(tile / tiles_x) * th + (int)(lane >> pl);
         // no lane leaves the loop body early: the next tile fetch is a full-warp shuffle
         if (kCount && tile % stride != 0) continue;
         const int fn = (!p.want_sky && p.has_geometry && p.frontier) ? tile_frontier(p, x, y, x < p.w && y < p.h, F) : 0;
-        if (x < p.w && y < p.h) trace_pixel<kCount>(p, x, y, toLight, cn, F, fn);
+        if (x < p.w && y < p.h) trace_pixel<kCount, kStackN>(p, x, y, toLight, cn, F, fn);
         __syncwarp();                              // the frontier is rebuilt for the next tile
     }
     if (kCount) {
@@ -78,25 +80,36 @@ __global__ void occluded_kernel(const Node4* __restrict__ nodes, const LeafTri* 
 // Residency variants: the register budget decides how many 256-thread blocks share an SM
 // (2: up to 128 registers, 3: 80, 4: 64, with spills to L1). The launch uses enough
 // blocks to fill every SM at that residency; ctx().tune.trace_min_blocks picks the variant.
-template <int kMB>
+// Stack variants: 48 entries where the tree's bound (16 + 3 x wide depth) fits, else 96.
+// The counting build (traversal statistics) always uses the 96-entry stack.
+template <int kMB, int kStackN>
 void launch_variant(const TraceParams& p, int sm_count, cudaStream_t s, uint32_t* tile_ctr, unsigned long long* counts,
                     uint32_t stride) {
     const int blocks = sm_count * kMB;
     if (counts)
-        trace_kernel<true, kMB><<<blocks, 256, 0, s>>>(p, tile_ctr, counts, stride < 1 ? 1 : stride);
+        trace_kernel<true, kMB, kStack><<<blocks, 256, 0, s>>>(p, tile_ctr, counts, stride < 1 ? 1 : stride);
     else
-        trace_kernel<false, kMB><<<blocks, 256, 0, s>>>(p, tile_ctr, nullptr, 1);
+        trace_kernel<false, kMB, kStackN><<<blocks, 256, 0, s>>>(p, tile_ctr, nullptr, 1);
+}
+
+template <int kStackN>
+void launch_stack(const TraceParams& p, int sm_count, cudaStream_t s, uint32_t* tile_ctr, unsigned long long* counts,
+                  uint32_t stride) {
+    switch (ctx().tune.trace_min_blocks) {
+        case 2: launch_variant<2, kStackN>(p, sm_count, s, tile_ctr, counts, stride); break;
+        case 4: launch_variant<4, kStackN>(p, sm_count, s, tile_ctr, counts, stride); break;
+        default: launch_variant<3, kStackN>(p, sm_count, s, tile_ctr, counts, stride); break;
+    }
 }
 
 int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned long long* counts, uint32_t stride) {
     // the tile counter sits in the word after the error word
     uint32_t* tile_ctr = p.err_word + 1;
     cudaMemsetAsync(tile_ctr, 0, 4, s);
-    switch (ctx().tune.trace_min_blocks) {
-        case 2: launch_variant<2>(p, sm_count, s, tile_ctr, counts, stride); break;
-        case 4: launch_variant<4>(p, sm_count, s, tile_ctr, counts, stride); break;
-        default: launch_variant<3>(p, sm_count, s, tile_ctr, counts, stride); break;
-    }
+    if (ctx().tune.trace_stack <= 48 && p.stack_need <= 48)
+        launch_stack<48>(p, sm_count, s, tile_ctr, counts, stride);
+    else
+        launch_stack<kStack>(p, sm_count, s, tile_ctr, counts, stride);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 

@@ -106,7 +106,7 @@ __device__ inline int build_frontier(const Node4* __restrict__ nodes, const floa
 // 1e-4 < t < tnear; HIT_FAR alone when the nearest hit it needed to find lies in
 // [tnear, tfar); 0 when nothing is hit before tfar. The any-hit query of raw::Bvh::occluded
 // (src/renderer/bvh.cpp:119-138) is tnear == tfar.
-template <bool kCount>
+template <bool kCount, int kStackN = kStack>
 __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, const v3& o, const v3& d,
                     float tnear, float tfar, uint32_t* err, Counts& cn, const FrontierEntry* F = nullptr,
                     int fn = 0) {
@@ -115,7 +115,7 @@ __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__
     bool wr_ready = false;
     float tmax = tfar;
     int far_hit = 0;
-    int32_t stack[kStack];
+    int32_t stack[kStackN];
     int sp = 0;
     int32_t cur = 0;                     // the root is always node 0
     if (fn > 0) {
@@ -144,7 +144,7 @@ __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__
             if (nearest < 0) { nearest = c; tbest = tn; continue; }
             int32_t push = c;
             if (tn < tbest) { push = nearest; nearest = c; tbest = tn; }
-            stack[sp++] = push;                  // fn <= kFrontier < kStack
+            stack[sp++] = push;                  // fn <= kFrontier < kStackN
         }
         if (nearest >= 0) cur = nearest;
         else if (sp > 0) cur = stack[--sp];
@@ -188,7 +188,7 @@ __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__
             // keep the nearer child to descend into, stack the other
             int32_t push = c;
             if (tn < tbest) { push = nearest; nearest = c; tbest = tn; }
-            if (sp >= kStack) { atomicOr(err, DEV_STACK_OVERFLOW); return far_hit; }
+            if (sp >= kStackN) { atomicOr(err, DEV_STACK_OVERFLOW); return far_hit; }
             stack[sp++] = push;
         }
         if (nearest >= 0) { cur = nearest; continue; }
@@ -230,7 +230,7 @@ __device__ __forceinline__ int tile_frontier(const TraceParams& p, int x, int y,
 }
 
 // One pixel: its spp cosine-weighted rays (AO and, when asked, the sky), then the sun ray.
-template <bool kCount>
+template <bool kCount, int kStackN = kStack>
 __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, const v3& toLight, Counts& cn,
                                             const FrontierEntry* F = nullptr, int fn = 0) {
     const float kFar = 1e30f;
@@ -279,7 +279,7 @@ __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, 
         }
         // AO-only walks may start from the warp's frontier; the sky and the sun need the root
         const bool local = s < p.spp && tf == p.radius;
-        const int h = p.has_geometry ? walk<kCount>(p.nodes, p.tris, origin, dir, tn, tf, p.err_word, cn,
+        const int h = p.has_geometry ? walk<kCount, kStackN>(p.nodes, p.tris, origin, dir, tn, tf, p.err_word, cn,
                                                     local ? F : nullptr, local ? fn : 0)
                                      : 0;
         if (s < p.spp) {

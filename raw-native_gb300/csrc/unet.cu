@@ -210,19 +210,21 @@ __global__ void input_kernel(const float* __restrict__ in, size_t M, bf16* __res
     }
 }
 
-struct AdamArgs { float lr, b1, b2, eps, c1, c2; };
+struct AdamArgs { float lr, b1, b2, eps, c1, c2; const float* scale; };
 
-// Adam on one convolution's weights (master [cout][kpad], gradient stored [kpad][cout]),
-// then its BF16 copies: wq [cout][kpad] and the flipped, transposed wt [cin_pad][kpad_t].
+// Adam on one convolution's weights (master [cout][kpad], gradient stored [kpad][cout],
+// multiplied by the clip factor *a.scale), then its BF16 copies: wq [cout][kpad] and the
+// flipped, transposed wt [cin_pad][kpad_t].
 __global__ void adam_conv_kernel(float* __restrict__ w, float* __restrict__ m, float* __restrict__ v,
                                  const float* __restrict__ g, int cout, int cin, int kpad, int kpad_t, AdamArgs a,
                                  bf16* __restrict__ wq, bf16* __restrict__ wt) {
     const int total = cout * 9 * cin;
+    const float sc = g ? *a.scale : 0.0f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         const int co = i / (9 * cin), k = i % (9 * cin);
         const size_t wi = (size_t)co * kpad + k;
         if (g) {
-            const float gr = g[(size_t)k * cout + co];
+            const float gr = g[(size_t)k * cout + co] * sc;
             const float mm = a.b1 * m[wi] + (1.0f - a.b1) * gr;
             const float vv = a.b2 * v[wi] + (1.0f - a.b2) * gr * gr;
             m[wi] = mm;
@@ -239,12 +241,47 @@ __global__ void adam_vec_kernel(float* __restrict__ w, float* __restrict__ m, fl
                                 const float* __restrict__ g, int n, AdamArgs a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const float gr = g[i];
+    const float gr = g[i] * *a.scale;
     const float mm = a.b1 * m[i] + (1.0f - a.b1) * gr;
     const float vv = a.b2 * v[i] + (1.0f - a.b2) * gr * gr;
     m[i] = mm;
     v[i] = vv;
     w[i] -= a.lr * (mm * a.c1) / (sqrtf(vv * a.c2) + a.eps);
+}
+
+// The squared global gradient norm: blockIdx.y picks one gradient array of the table.
+struct GradSeg { const float* p; unsigned n; };
+__global__ void grad_sumsq_kernel(const GradSeg* __restrict__ segs, float* __restrict__ sumsq) {
+    const GradSeg sg = segs[blockIdx.y];
+    float s = 0.0f;
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < sg.n; i += gridDim.x * blockDim.x) s += sg.p[i] * sg.p[i];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ float part[8];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.0f;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += part[k];
+        atomicAdd(sumsq, t);
+    }
+}
+
+// Adaptive clipping: the norm is limited to ratio x a running mean of the (clipped) norms.
+// stats: [0] sum of squares (input), [1] norm, [2] scale applied, [3] running mean.
+__global__ void clip_kernel(float* __restrict__ stats, float ratio) {
+    const float norm = sqrtf(stats[0]);
+    float ema = stats[3];
+    float scale = 1.0f;
+    if (ratio > 0.0f && isfinite(norm)) {
+        if (ema <= 0.0f) ema = norm;
+        const float thr = ratio * ema;
+        if (norm > thr) scale = thr / norm;
+        ema = 0.99f * ema + 0.01f * fminf(norm, thr);
+    }
+    if (!isfinite(norm)) scale = 0.0f;             // a non-finite gradient skips the step's update
+    stats[1] = norm;
+    stats[2] = scale;
+    stats[3] = ema;
 }
 
 inline unsigned grid_for(size_t n, int block = 256) {
@@ -260,6 +297,9 @@ using namespace rn;
 struct rn_unet {
     int B = 0, H = 0, W = 0;
     int step = 0;
+    bool inference = false;       // forward only: one shared im2col buffer, no gradient storage
+    bool implicit = false;        // 3x3 convolutions of >= 32 input channels on the implicit GEMM
+    bf16* UT[T_COUNT] = {};       // implicit: 2x upsampled copies of the tensors read upsampled
     // per layer
     struct Layer {
         int level, cin, cout, kpad, kpad_t, cin_pad;
@@ -275,7 +315,11 @@ struct rn_unet {
     bf16 *at, *dzt, *dz, *bcol;   // scratch: A^T, dZ^T, dZ, im2col(dZ)
     float* dx;                    // scratch: dgrad output [M][cin_pad]
     float* loss;                  // device scalar
-    float* host_loss;             // pinned
+    float* host_loss;             // pinned: loss, gradient norm, clip scale
+    float* gstats;                // device: see clip_kernel
+    GradSeg* segs;                // device table of the gradient arrays
+    int nsegs = 0;
+    float clip_ratio = 0.0f;
     std::vector<void*> allocs;
     size_t param_count = 0;
 };
@@ -290,11 +334,25 @@ int ualloc(rn_unet* u, void** p, size_t bytes, rn_status* st) {
 }
 size_t pixels(const rn_unet* u, int level) { return (size_t)u->B * (u->H >> level) * (u->W >> level); }
 
+// The upsampled copy a layer's output feeds (implicit path), or null.
+bf16* up_target(rn_unet* u, int l) { return u->implicit ? u->UT[l + 1] : nullptr; }
+
 int conv_forward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
     auto& Ly = u->L[l];
     const LayerSpec& sp = kSpec[l];
     const int H = u->H >> Ly.level, W = u->W >> Ly.level;
     const size_t M = pixels(u, Ly.level);
+    if (u->implicit && l > 0) {
+        tc::ConvSrc src[2] = {{u->T[sp.s0.tensor], u->TC[sp.s0.tensor]}, {nullptr, 0}};
+        if (sp.nsrc == 2) src[1] = {sp.s1.up ? u->UT[sp.s1.tensor] : u->T[sp.s1.tensor], u->TC[sp.s1.tensor]};
+        tc::Epilogue e{};
+        e.ldc = Ly.cout;
+        e.c16 = u->T[l + 1];
+        e.bias = Ly.b;
+        e.relu = 1;
+        e.err = ctx().dev_error;
+        return tc_conv3x3(src, sp.nsrc, u->B, H, W, Ly.wq, Ly.kpad, Ly.cout, e, up_target(u, l), s, st);
+    }
     Im2col a{u->T[sp.s0.tensor], u->TC[sp.s0.tensor], sp.s0.up, nullptr, 0, 0, u->B, H, W, Ly.kpad, Ly.A};
     if (sp.nsrc == 2) { a.s1 = u->T[sp.s1.tensor]; a.c1 = u->TC[sp.s1.tensor]; a.up1 = sp.s1.up; }
     im2col_kernel<<<grid_for(M * (Ly.kpad / 8)), 256, 0, s>>>(a);
@@ -325,6 +383,12 @@ int conv_backward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
     // dZ: the gradient at the pre-activation
     gate_kernel<<<grid_for(M * Ly.cout), 256, 0, s>>>(u->dT[l + 1], u->T[l + 1], M * Ly.cout, u->dz);
     colsum_kernel<<<256, 256, 0, s>>>(u->dz, M, Ly.cout, Ly.gb);
+    if (u->implicit) {
+        // the forward left no im2col rows: form this layer's now (one shared buffer)
+        Im2col a{u->T[sp.s0.tensor], u->TC[sp.s0.tensor], sp.s0.up, nullptr, 0, 0, u->B, H, W, Ly.kpad, Ly.A};
+        if (sp.nsrc == 2) { a.s1 = u->T[sp.s1.tensor]; a.c1 = u->TC[sp.s1.tensor]; a.up1 = sp.s1.up; }
+        im2col_kernel<<<grid_for(M * (Ly.kpad / 8)), 256, 0, s>>>(a);
+    }
     // wgrad: dW^T [kpad][cout] = A^T (kpad x M) * (dZ^T (cout x M))^T
     transpose_kernel<<<dim3(Ly.kpad / 32, (unsigned)(M / 32)), dim3(32, 8), 0, s>>>(Ly.A, (int)M, Ly.kpad, u->at);
     transpose_kernel<<<dim3(Ly.cout / 32, (unsigned)(M / 32)), dim3(32, 8), 0, s>>>(u->dz, (int)M, Ly.cout, u->dzt);
@@ -337,14 +401,19 @@ int conv_backward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
     ew.err = ctx().dev_error;
     RN_TRY(tc_gemm(u->at, (int)M, u->dzt, (int)M, Ly.kpad, Ly.cout, (int)M, splits, ew, s, st));
     if (l == 0) return RN_OK;                          // the input needs no gradient
-    // dgrad: dX [M][cin_pad] = im2col(dZ) [M][kpad_t] * W'^T
-    Im2col a{u->dz, Ly.cout, 0, nullptr, 0, 0, u->B, H, W, Ly.kpad_t, u->bcol};
-    im2col_kernel<<<grid_for(M * (Ly.kpad_t / 8)), 256, 0, s>>>(a);
+    // dgrad: dX [M][cin_pad] = conv(dZ, W') with W'[ci][tap'][co] = W[co][8 - tap'][ci]
     tc::Epilogue ed{};
     ed.ldc = Ly.cin_pad;
     ed.c32 = u->dx;
     ed.err = ctx().dev_error;
-    RN_TRY(tc_gemm(u->bcol, Ly.kpad_t, Ly.wt, Ly.kpad_t, (int)M, Ly.cin_pad, Ly.kpad_t, 1, ed, s, st));
+    if (u->implicit) {
+        const tc::ConvSrc src{u->dz, Ly.cout};
+        RN_TRY(tc_conv3x3(&src, 1, u->B, H, W, Ly.wt, Ly.kpad_t, Ly.cin_pad, ed, nullptr, s, st));
+    } else {
+        Im2col a{u->dz, Ly.cout, 0, nullptr, 0, 0, u->B, H, W, Ly.kpad_t, u->bcol};
+        im2col_kernel<<<grid_for(M * (Ly.kpad_t / 8)), 256, 0, s>>>(a);
+        RN_TRY(tc_gemm(u->bcol, Ly.kpad_t, Ly.wt, Ly.kpad_t, (int)M, Ly.cin_pad, Ly.kpad_t, 1, ed, s, st));
+    }
     const int c0 = u->TC[sp.s0.tensor];
     route_kernel<<<grid_for(M * c0), 256, 0, s>>>(u->dx, Ly.cin_pad, 0, c0, sp.s0.up, u->B, H, W, u->dT[sp.s0.tensor]);
     if (sp.nsrc == 2)
@@ -384,11 +453,24 @@ void for_params(rn_unet* u, F f) {
     f(u->bh, 1);
 }
 
+// Adam's moments in the parameters' order: which 0 = first moment, 1 = second.
+template <typename F>
+void for_moments(rn_unet* u, int which, F f) {
+    for (int l = 0; l < kLayers; ++l) {
+        auto& Ly = u->L[l];
+        float* m = which ? Ly.v : Ly.m;
+        for (int co = 0; co < Ly.cout; ++co) f(m + (size_t)co * Ly.kpad, (size_t)9 * Ly.cin);
+        f(which ? Ly.bv : Ly.bm, (size_t)Ly.cout);
+    }
+    f(which ? u->vh : u->mh, 32);
+    f(which ? u->vbh : u->mbh, 1);
+}
+
 }  // namespace
 
 extern "C" {
 
-int rn_unet_create(int batch, int height, int width, uint64_t seed, rn_unet** out, rn_status* st) {
+int rn_unet_create(int batch, int height, int width, uint64_t seed, uint32_t flags, rn_unet** out, rn_status* st) {
     if (!out) return fail(st, RN_ERR_INVALID, "null output");
     *out = nullptr;
     if (batch <= 0 || height <= 0 || width <= 0 || height % 16 || width % 16)
@@ -398,6 +480,9 @@ int rn_unet_create(int batch, int height, int width, uint64_t seed, rn_unet** ou
     RN_TRY(ensure_ctx(st));
     rn_unet* u = new rn_unet();
     u->B = batch; u->H = height; u->W = width;
+    u->inference = (flags & RN_UNET_INFERENCE) != 0;
+    u->implicit = !(flags & RN_UNET_EXPLICIT);
+    for (int lv = 0; lv < 4; ++lv) u->implicit = u->implicit && tc::conv_tiling(height >> lv, width >> lv).ok;
     auto bail = [&](int rc) { rn_unet_free(u); return rc; };
     std::mt19937_64 rng(seed);
     std::normal_distribution<float> nd(0.0f, 1.0f);
@@ -416,7 +501,7 @@ int rn_unet_create(int batch, int height, int width, uint64_t seed, rn_unet** ou
         if (rc == RN_OK) rc = ualloc(u, (void**)&Ly.gw, (size_t)Ly.kpad * Ly.cout * 4, st);
         if (rc == RN_OK) rc = ualloc(u, (void**)&Ly.wq, nw * 2, st);
         if (rc == RN_OK) rc = ualloc(u, (void**)&Ly.wt, (size_t)Ly.cin_pad * Ly.kpad_t * 2, st);
-        if (rc == RN_OK) rc = ualloc(u, (void**)&Ly.A, M * Ly.kpad * 2, st);
+        if (rc == RN_OK && !u->inference && !u->implicit) rc = ualloc(u, (void**)&Ly.A, M * Ly.kpad * 2, st);
         if (rc != RN_OK) return bail(rc);
         // He initialization of the real taps; padded columns stay zero
         std::vector<float> w(nw, 0.0f);
@@ -432,6 +517,13 @@ int rn_unet_create(int batch, int height, int width, uint64_t seed, rn_unet** ou
         max_dx = std::max(max_dx, M * Ly.cin_pad);
     }
     max_at = max_a;
+    if (u->inference || u->implicit) {   // the layers run in order: one im2col buffer serves all
+        // (implicit inference forms im2col rows for the first layer only)
+        const size_t need = (u->implicit && u->inference) ? pixels(u, 0) * u->L[0].kpad : max_a;
+        bf16* shared = nullptr;
+        if (ualloc(u, (void**)&shared, need * 2, st)) return bail(RN_ERR_NO_MEMORY);
+        for (auto& Ly : u->L) Ly.A = shared;
+    }
     for (float** p : {&u->wh, &u->mh, &u->vh, &u->gwh}) if (ualloc(u, (void**)p, 32 * 4, st)) return bail(RN_ERR_CUDA);
     for (float** p : {&u->bh, &u->mbh, &u->vbh, &u->gbh, &u->loss}) if (ualloc(u, (void**)p, 4, st)) return bail(RN_ERR_CUDA);
     {
@@ -447,14 +539,35 @@ int rn_unet_create(int batch, int height, int width, uint64_t seed, rn_unet** ou
         u->Tlevel[t] = tlevel[t];
         u->TC[t] = tch[t];
         u->Tn[t] = pixels(u, tlevel[t]) * tch[t];
-        if (ualloc(u, (void**)&u->T[t], u->Tn[t] * 2, st) || ualloc(u, (void**)&u->dT[t], u->Tn[t] * 4, st))
+        if (ualloc(u, (void**)&u->T[t], u->Tn[t] * 2, st) ||
+            (!u->inference && ualloc(u, (void**)&u->dT[t], u->Tn[t] * 4, st)))
             return bail(RN_ERR_NO_MEMORY);
     }
-    if (ualloc(u, (void**)&u->at, max_at * 2, st) || ualloc(u, (void**)&u->dzt, max_dz * 2, st) ||
-        ualloc(u, (void**)&u->dz, max_dz * 2, st) || ualloc(u, (void**)&u->bcol, max_bcol * 2, st) ||
-        ualloc(u, (void**)&u->dx, max_dx * 4, st))
+    if (u->implicit)
+        for (int t : {8, 10, 12})            // b3, d2, d1: read upsampled by d2a, d1a, d0a
+            if (ualloc(u, (void**)&u->UT[t], pixels(u, u->Tlevel[t] - 1) * u->TC[t] * 2, st))
+                return bail(RN_ERR_NO_MEMORY);
+    if (!u->inference &&
+        (ualloc(u, (void**)&u->at, max_at * 2, st) || ualloc(u, (void**)&u->dzt, max_dz * 2, st) ||
+         ualloc(u, (void**)&u->dz, max_dz * 2, st) || ualloc(u, (void**)&u->bcol, (u->implicit ? 8 : max_bcol) * 2, st) ||
+         ualloc(u, (void**)&u->dx, max_dx * 4, st)))
         return bail(RN_ERR_NO_MEMORY);
-    if (cudaMallocHost((void**)&u->host_loss, 4) != cudaSuccess) return bail(fail(st, RN_ERR_NO_MEMORY, "pinned loss"));
+    if (cudaMallocHost((void**)&u->host_loss, 16) != cudaSuccess) return bail(fail(st, RN_ERR_NO_MEMORY, "pinned loss"));
+    std::memset(u->host_loss, 0, 16);
+    if (ualloc(u, (void**)&u->gstats, 16, st)) return bail(RN_ERR_NO_MEMORY);
+    {
+        std::vector<GradSeg> segs;
+        for (auto& Ly : u->L) {
+            segs.push_back({Ly.gw, (unsigned)((size_t)Ly.kpad * Ly.cout)});
+            segs.push_back({Ly.gb, (unsigned)Ly.cout});
+        }
+        segs.push_back({u->gwh, 32});
+        segs.push_back({u->gbh, 1});
+        u->nsegs = (int)segs.size();
+        if (ualloc(u, (void**)&u->segs, segs.size() * sizeof(GradSeg), st)) return bail(RN_ERR_NO_MEMORY);
+        if (cudaMemcpy(u->segs, segs.data(), segs.size() * sizeof(GradSeg), cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(st, RN_ERR_CUDA, "gradient table upload"));
+    }
     refresh_weights(u, nullptr, ctx().stream);
     if (cudaStreamSynchronize(ctx().stream) != cudaSuccess) return bail(cuda_fail(st, cudaGetLastError(), "unet init"));
     *out = u;
@@ -491,6 +604,7 @@ int rn_unet_forward(rn_unet* u, const float* input, int batch, float* output, rn
 int rn_unet_train_step(rn_unet* u, const float* input, const float* target, int batch, float lr, float* loss,
                        rn_status* st) {
     if (!u || !input || !target) return fail(st, RN_ERR_INVALID, "null argument");
+    if (u->inference) return fail(st, RN_ERR_INVALID, "network created for inference only");
     RN_TRY(check_shape(u, batch, st));
     cudaStream_t s = ctx().stream;
     const size_t M = pixels(u, 0);
@@ -514,13 +628,18 @@ int rn_unet_train_step(rn_unet* u, const float* input, const float* target, int 
         if (l == 4) pool_back_kernel<<<grid_for(u->Tn[4]), 256, 0, s>>>(u->dT[T_P1], u->B, u->H >> 1, u->W >> 1, 64, u->dT[4]);
         if (l == 2) pool_back_kernel<<<grid_for(u->Tn[2]), 256, 0, s>>>(u->dT[T_P0], u->B, u->H, u->W, 32, u->dT[2]);
     }
-    ++u->step;
+    // global gradient norm and the clip factor Adam applies
+    RN_CUDA(cudaMemsetAsync(u->gstats, 0, 4, s), st);
+    grad_sumsq_kernel<<<dim3(64, u->nsegs), 256, 0, s>>>(u->segs, u->gstats);
+    clip_kernel<<<1, 1, 0, s>>>(u->gstats, u->clip_ratio);
     if (lr > 0.0f) {
+        ++u->step;
         const AdamArgs a{lr, 0.9f, 0.999f, 1e-8f, 1.0f / (1.0f - std::pow(0.9f, (float)u->step)),
-                         1.0f / (1.0f - std::pow(0.999f, (float)u->step))};
+                         1.0f / (1.0f - std::pow(0.999f, (float)u->step)), u->gstats + 2};
         refresh_weights(u, &a, s);
     }
     RN_CUDA(cudaMemcpyAsync(u->host_loss, u->loss, 4, cudaMemcpyDeviceToHost, s), st);
+    RN_CUDA(cudaMemcpyAsync(u->host_loss + 1, u->gstats + 1, 8, cudaMemcpyDeviceToHost, s), st);
     RN_CUDA(cudaStreamSynchronize(s), st);
     RN_TRY(check_device_error(st, "rn_unet_train_step"));
     if (loss) *loss = *u->host_loss / (float)M;
@@ -544,6 +663,49 @@ int rn_unet_set_params(rn_unet* u, const float* host, rn_status* st) {
     RN_CUDA(cudaStreamSynchronize(ctx().stream), st);
     return ok(st);
 }
+// Adaptive gradient clipping for the following train steps: the global gradient norm is
+// limited to `ratio` x a running mean of past (clipped) norms; 0 turns clipping off.
+int rn_unet_set_clip(rn_unet* u, float ratio, rn_status* st) {
+    if (!u || !(ratio >= 0.0f)) return fail(st, RN_ERR_INVALID, "clip ratio must be >= 0");
+    u->clip_ratio = ratio;
+    return ok(st);
+}
+// The last train step's global gradient norm (before clipping) and the factor applied.
+int rn_unet_last_grad_norm(const rn_unet* u, float* norm, float* scale, rn_status* st) {
+    if (!u) return fail(st, RN_ERR_INVALID, "null argument");
+    if (norm) *norm = u->host_loss[1];
+    if (scale) *scale = u->host_loss[2];
+    return ok(st);
+}
+
+// Training state: master weights, then Adam's first and second moments (each in the params'
+// order and layout), and the step count.
+int rn_unet_get_state(rn_unet* u, float* host, uint64_t* step, rn_status* st) {
+    if (!u || !host || !step) return fail(st, RN_ERR_INVALID, "null argument");
+    RN_CUDA(cudaDeviceSynchronize(), st);
+    size_t o = 0;
+    auto get = [&](float* d, size_t n) { cudaMemcpy(host + o, d, n * 4, cudaMemcpyDeviceToHost); o += n; };
+    for_params(u, get);
+    for_moments(u, 0, get);
+    for_moments(u, 1, get);
+    *step = (uint64_t)u->step;
+    RN_CUDA(cudaGetLastError(), st);
+    return ok(st);
+}
+int rn_unet_set_state(rn_unet* u, const float* host, uint64_t step, rn_status* st) {
+    if (!u || !host) return fail(st, RN_ERR_INVALID, "null argument");
+    RN_CUDA(cudaDeviceSynchronize(), st);
+    size_t o = 0;
+    auto put = [&](float* d, size_t n) { cudaMemcpy(d, host + o, n * 4, cudaMemcpyHostToDevice); o += n; };
+    for_params(u, put);
+    for_moments(u, 0, put);
+    for_moments(u, 1, put);
+    u->step = (int)step;
+    refresh_weights(u, nullptr, ctx().stream);
+    RN_CUDA(cudaStreamSynchronize(ctx().stream), st);
+    return ok(st);
+}
+
 // Gradients of the last train step (lr 0 keeps them), same order and layout as the params.
 int rn_unet_get_grads(rn_unet* u, float* host, rn_status* st) {
     if (!u || !host) return fail(st, RN_ERR_INVALID, "null argument");

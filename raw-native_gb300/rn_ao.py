@@ -32,7 +32,9 @@ EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_ac
            "rn_occluded", "rn_raster_gbuffer", "rn_ao_trace_stats", "rn_reconcile_noalloc", "rn_batch_create",
            "rn_batch_run", "rn_batch_info", "rn_batch_free", "rn_ao_batch", "rn_tc_gemm", "rn_unet_create",
            "rn_unet_free", "rn_unet_param_count", "rn_unet_forward", "rn_unet_train_step", "rn_unet_get_params",
-           "rn_unet_set_params", "rn_unet_get_grads")
+           "rn_unet_set_params", "rn_unet_get_grads", "rn_unet_get_state", "rn_unet_set_state",
+           "rn_unet_set_clip", "rn_unet_last_grad_norm",
+           "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3")
 
 
 class RnError(RuntimeError):
@@ -102,7 +104,16 @@ def lib() -> C.CDLL:
                                   C.POINTER(ReconcileOut), st]
         L.rn_tc_gemm.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, vp, vp, C.c_int, vp,
                                  C.c_int, st]
-        L.rn_unet_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(vp), st]
+        L.rn_unet_create.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_uint32, C.POINTER(vp), st]
+        L.rn_unet_get_state.argtypes = [vp, vp, C.POINTER(C.c_uint64), st]
+        L.rn_unet_set_state.argtypes = [vp, vp, C.c_uint64, st]
+        L.rn_unet_set_clip.argtypes = [vp, C.c_float, st]
+        L.rn_tune_set.argtypes = [C.c_char_p, C.c_int, st]
+        L.rn_tc_conv3x3.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, vp,
+                                    vp, vp, C.c_int, st]
+        L.rn_tune_get.argtypes = [C.c_char_p, C.POINTER(C.c_int), st]
+        L.rn_tune_load.argtypes = [C.c_char_p, st]
+        L.rn_unet_last_grad_norm.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float), st]
         L.rn_unet_free.argtypes = [vp]
         L.rn_unet_free.restype = None
         L.rn_unet_param_count.argtypes = [vp, C.POINTER(C.c_uint64), st]
@@ -121,9 +132,44 @@ def _check(rc: int, st: Status) -> None:
         raise RnError(rc, st.message.decode(errors="replace"))
 
 
-def init() -> None:
+# ---------------------------------------------------------------- launch-shape tuning
+TUNE_KEYS = {"trace_min_blocks": (2, 3, 4), "trace_frontier": (0, 1), "trace_packet": (4, 8, 16),
+             "trace_stack": (48, 96), "ssao_tile_h": (4, 8, 16), "conv_bn_max": (64, 128, 256)}
+
+
+def tune_set(key: str, value: int) -> None:
+    st = Status()
+    _check(lib().rn_tune_set(key.encode(), int(value), C.byref(st)), st)
+
+
+def tune_get(key: str) -> int:
+    v = C.c_int()
+    st = Status()
+    _check(lib().rn_tune_get(key.encode(), C.byref(v), C.byref(st)), st)
+    return v.value
+
+
+def tune_all() -> dict:
+    return {k: tune_get(k) for k in TUNE_KEYS}
+
+
+def tune_load(path: str) -> None:
+    st = Status()
+    _check(lib().rn_tune_load(os.fsencode(path), C.byref(st)), st)
+
+
+TUNE_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tune_sm103.txt")
+
+
+def init(load_tune: bool = True) -> None:
+    """rn_init; then the autotuner's launch shapes: the file named by RN_TUNE_FILE, else the
+    package's tune_sm103.txt when present."""
     st = Status()
     _check(lib().rn_init(C.byref(st)), st)
+    if load_tune:
+        path = os.environ.get("RN_TUNE_FILE") or (TUNE_FILE if os.path.exists(TUNE_FILE) else None)
+        if path:
+            tune_load(path)
 
 
 def synchronize() -> None:
@@ -449,14 +495,38 @@ def tc_gemm(P, Q, out_dtype=None, bias=None, relu=False, splits=1):
     return c16 if c16 is not None else c32
 
 
+def tc_conv3x3(x0, w, x1=None, bias=None, relu=False, out_dtype=None, upsampled=False):
+    """Implicit-GEMM 3x3 convolution (stride 1, zero padding 1) on the tensor cores. x0, x1:
+    CUDA bf16 NHWC [B, H, W, C] (channels concatenated); w: bf16 [N, ldw] with column
+    tap * Cin + ci, tap = 3 (dy + 1) + (dx + 1). Returns the FP32 (or bf16) output
+    [B, H, W, N], and with upsampled=True also its 2x nearest-upsampled bf16 copy."""
+    import torch
+    B, H, W, c0 = x0.shape
+    c1 = x1.shape[3] if x1 is not None else 0
+    N = w.shape[0]
+    _use_torch_stream()
+    bf = out_dtype == torch.bfloat16 or upsampled
+    c32 = None if bf else torch.empty(B, H, W, N, device=x0.device)
+    c16 = torch.empty(B, H, W, N, device=x0.device, dtype=torch.bfloat16) if bf else None
+    up = torch.empty(B, 2 * H, 2 * W, N, device=x0.device, dtype=torch.bfloat16) if upsampled else None
+    ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+    st = Status()
+    _check(lib().rn_tc_conv3x3(ptr(x0), c0, ptr(x1), c1, B, H, W, ptr(w), w.stride(0), N, ptr(c32), ptr(c16), ptr(up),
+                               ptr(bias), int(relu), C.byref(st)), st)
+    out = c16 if bf else c32
+    return (out, up) if upsampled else out
+
+
 class UNet:
     """The learned AO surrogate network for one input shape (see rn_unet_create). Inputs,
     targets and outputs are CUDA float32 tensors: x [B, H, W, 5], y [B, H, W]."""
 
-    def __init__(self, batch: int, height: int, width: int, seed: int = 0):
+    def __init__(self, batch: int, height: int, width: int, seed: int = 0, inference: bool = False,
+                 explicit: bool = False):
         self._h = C.c_void_p()
         st = Status()
-        _check(lib().rn_unet_create(batch, height, width, seed, C.byref(self._h), C.byref(st)), st)
+        flags = (1 if inference else 0) | (2 if explicit else 0)
+        _check(lib().rn_unet_create(batch, height, width, seed, flags, C.byref(self._h), C.byref(st)), st)
         self.shape = (batch, height, width)
         n = C.c_uint64()
         _check(lib().rn_unet_param_count(self._h, C.byref(n), C.byref(st)), st)
@@ -481,6 +551,8 @@ class UNet:
 
     def _io(self, fn, arr=None):
         out = np.empty(self.param_count, np.float32) if arr is None else np.ascontiguousarray(arr, np.float32)
+        if out.size != self.param_count:
+            raise ValueError("%d values, expected %d" % (out.size, self.param_count))
         st = Status()
         _check(fn(self._h, C.c_void_p(out.ctypes.data), C.byref(st)), st)
         return out
@@ -493,6 +565,33 @@ class UNet:
 
     def get_grads(self):
         return self._io(lib().rn_unet_get_grads)
+
+    def set_clip(self, ratio: float):
+        """Adaptive gradient clipping at `ratio` x the running mean norm (0: off)."""
+        st = Status()
+        _check(lib().rn_unet_set_clip(self._h, float(ratio), C.byref(st)), st)
+
+    def last_grad_norm(self):
+        """(global gradient norm of the last train step, clip factor applied)."""
+        n, s = C.c_float(), C.c_float()
+        st = Status()
+        _check(lib().rn_unet_last_grad_norm(self._h, C.byref(n), C.byref(s), C.byref(st)), st)
+        return n.value, s.value
+
+    def get_state(self):
+        """(weights, first moments, second moments) as one FP32 array, and the step count."""
+        out = np.empty(3 * self.param_count, np.float32)
+        step = C.c_uint64()
+        st = Status()
+        _check(lib().rn_unet_get_state(self._h, C.c_void_p(out.ctypes.data), C.byref(step), C.byref(st)), st)
+        return out, step.value
+
+    def set_state(self, state, step: int):
+        arr = np.ascontiguousarray(state, np.float32)
+        if arr.size != 3 * self.param_count:
+            raise ValueError("state holds %d values, expected %d" % (arr.size, 3 * self.param_count))
+        st = Status()
+        _check(lib().rn_unet_set_state(self._h, C.c_void_p(arr.ctypes.data), int(step), C.byref(st)), st)
 
     def close(self):
         if self._h:

@@ -81,3 +81,47 @@ def test_host_and_device_arrays_do_not_mix():
         is_cuda = True
     with pytest.raises(rn_ao.RnError):
         rn_ao._Args(np.zeros(3, np.float32), FakeCuda())
+
+
+def test_tuning_keys_without_a_device(lib, tmp_path, monkeypatch):
+    """The launch-shape keys are host state: set, read back, loaded from a file (all or
+    nothing), and refused with RN_ERR_INVALID for an unknown key or value."""
+    import rn_ao
+    saved = rn_ao.tune_all()
+    try:
+        assert set(saved) == set(rn_ao.TUNE_KEYS)
+        for k, values in rn_ao.TUNE_KEYS.items():
+            for v in values:
+                rn_ao.tune_set(k, v)
+                assert rn_ao.tune_get(k) == v
+        with pytest.raises(rn_ao.RnError) as e:
+            rn_ao.tune_set("trace_packet", 5)
+        assert e.value.code == 1
+        with pytest.raises(rn_ao.RnError):
+            rn_ao.tune_set("no_such_key", 1)
+        rn_ao.tune_set("trace_packet", 8)
+        good = tmp_path / "good.txt"
+        good.write_text("# picked\ntrace_packet = 16\n\nssao_tile_h=4   # comment\n")
+        rn_ao.tune_load(str(good))
+        assert rn_ao.tune_get("trace_packet") == 16 and rn_ao.tune_get("ssao_tile_h") == 4
+        bad = tmp_path / "bad.txt"
+        bad.write_text("trace_packet = 4\nconv_bn_max = 7\n")
+        with pytest.raises(rn_ao.RnError):
+            rn_ao.tune_load(str(bad))
+        assert rn_ao.tune_get("trace_packet") == 16          # nothing of the bad file applied
+        unknown = tmp_path / "unknown.txt"
+        unknown.write_text("trace_packet = 4\nwarp_size = 64\n")
+        with pytest.raises(rn_ao.RnError) as e:
+            rn_ao.tune_load(str(unknown))
+        assert "warp_size" in str(e.value)
+        assert rn_ao.tune_get("trace_packet") == 16
+        with pytest.raises(rn_ao.RnError):
+            rn_ao.tune_load(str(tmp_path / "missing.txt"))
+        # an environment variable keeps its key out of the file's reach
+        monkeypatch.setenv("RN_TUNE_SSAO_TILE_H", "16")
+        rn_ao.tune_set("ssao_tile_h", 8)
+        rn_ao.tune_load(str(good))
+        assert rn_ao.tune_get("ssao_tile_h") == 8 and rn_ao.tune_get("trace_packet") == 16
+    finally:
+        for k, v in saved.items():
+            rn_ao.tune_set(k, v)

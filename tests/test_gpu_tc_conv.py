@@ -1,0 +1,75 @@
+"""The implicit-GEMM 3x3 convolution against PyTorch's FP32 conv2d on the same BF16-rounded
+operands (test harness only): FP32 accumulation of BF16 products, so the results agree to
+FP32 rounding of the sums (relative 1e-3 of the output scale)."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# (B, H, W, c0, c1, N): single and concatenated sources, 32- and 64-channel blocks, every
+# tile shape (W = 128, 64, 32, 16, and a wide frame), N from 32 to 384
+CASES = [
+    (2, 16, 128, 32, 0, 32),
+    (1, 32, 64, 64, 0, 64),
+    (3, 16, 32, 128, 0, 128),
+    (4, 16, 16, 256, 0, 256),
+    (1, 8, 1920, 32, 64, 32),
+    (2, 32, 32, 64, 128, 64),
+    (1, 16, 16, 128, 256, 128),
+    (1, 16, 64, 64, 0, 384),
+    (2, 24, 48, 96, 0, 64),
+]
+
+
+def _ref(x0, x1, w, bias, relu):
+    import torch
+    import torch.nn.functional as F
+    x = x0 if x1 is None else torch.cat([x0, x1], 3)
+    B, H, W, Cin = x.shape
+    N = w.shape[0]
+    k = w[:, :9 * Cin].float().view(N, 3, 3, Cin).permute(0, 3, 1, 2)
+    y = F.conv2d(x.float().permute(0, 3, 1, 2), k, bias, padding=1).permute(0, 2, 3, 1)
+    return F.relu(y) if relu else y
+
+
+@pytest.mark.parametrize("B,H,W,c0,c1,N", CASES)
+def test_conv_matches_torch(rn, B, H, W, c0, c1, N):
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(B * 1000 + H + W + c0 + c1 + N)
+    x0 = torch.randn(B, H, W, c0, device="cuda", generator=g).to(torch.bfloat16)
+    x1 = torch.randn(B, H, W, c1, device="cuda", generator=g).to(torch.bfloat16) if c1 else None
+    cin = c0 + c1
+    ldw = (9 * cin + 127) // 128 * 128
+    w = torch.zeros(N, ldw, device="cuda", dtype=torch.bfloat16)
+    w[:, :9 * cin] = (torch.randn(N, 9 * cin, device="cuda", generator=g) / (9 * cin) ** 0.5).to(torch.bfloat16)
+    bias = torch.randn(N, device="cuda", generator=g)
+    out = rn.tc_conv3x3(x0, w, x1, bias=bias, relu=True)
+    torch.cuda.synchronize()
+    ref = _ref(x0, x1, w, bias, True)
+    scale = ref.abs().max().item()
+    err = (out - ref).abs().max().item()
+    assert err <= 1e-3 * scale, (err, scale)
+
+
+def test_conv_bf16_output_and_upsampled_copy(rn):
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(9)
+    x0 = torch.randn(2, 16, 32, 64, device="cuda", generator=g).to(torch.bfloat16)
+    w = (torch.randn(128, 640, device="cuda", generator=g) / 24).to(torch.bfloat16)
+    w[:, 576:] = 0
+    out, up = rn.tc_conv3x3(x0, w, upsampled=True)
+    torch.cuda.synchronize()
+    ref = _ref(x0, None, w, None, False).to(torch.bfloat16)
+    assert (out.float() - ref.float()).abs().max().item() <= 0.02 * ref.float().abs().max().item()
+    want = out.repeat_interleave(2, 1).repeat_interleave(2, 2)
+    assert torch.equal(up, want)
+
+
+def test_conv_rejects_untileable_and_bad_channels(rn):
+    import torch
+    x = torch.zeros(1, 10, 24, 32, device="cuda", dtype=torch.bfloat16)      # W 24: TW 8, 16 rows > 10
+    w = torch.zeros(32, 384, device="cuda", dtype=torch.bfloat16)
+    with pytest.raises(rn.RnError):
+        rn.tc_conv3x3(x, w)
+    y = torch.zeros(1, 16, 16, 40, device="cuda", dtype=torch.bfloat16)       # 40 channels
+    with pytest.raises(rn.RnError):
+        rn.tc_conv3x3(y, torch.zeros(32, 384, device="cuda", dtype=torch.bfloat16))

@@ -1,0 +1,64 @@
+"""Launch-shape tuning never changes a result: every value of every key reproduces the
+default configuration's traced AO/sky/sun, SSAO and surrogate output bit for bit."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def restore_tune(rn):
+    saved = rn.tune_all()
+    yield
+    for k, v in saved.items():
+        rn.tune_set(k, v)
+
+
+def _scene(rn, w, h, n_boxes=300, n_spheres=60):
+    import torch
+    import scene as scenes
+    sc = scenes.build_synthetic_scene(11, n_boxes, n_spheres)
+    tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+    g = rn.rasterize(tris, nrms, scenes.orbit_views(11, 8)[3][3], w, h)
+    return g, rn.LinearAccel(tris), sc.to_light
+
+
+def test_trace_keys_keep_every_bit(rn, restore_tune):
+    g, acc, tl = _scene(rn, 333, 197)
+    for k, v in (("trace_min_blocks", 3), ("trace_packet", 8), ("trace_stack", 96), ("trace_frontier", 1)):
+        rn.tune_set(k, v)
+    ref_ao = rn.compute_rtao(g, acc, 16, 1.0).clone()
+    ref_vis = [t.clone() for t in rn.compute_rt_visibility(g, acc, 16, 1.0, tl)]
+    for k in ("trace_min_blocks", "trace_packet", "trace_stack", "trace_frontier"):
+        for v in rn.TUNE_KEYS[k]:
+            rn.tune_set(k, v)
+            assert bool((rn.compute_rtao(g, acc, 16, 1.0) == ref_ao).all()), (k, v)
+            vis = rn.compute_rt_visibility(g, acc, 16, 1.0, tl)
+            assert all(bool((a == b).all()) for a, b in zip(vis, ref_vis)), (k, v)
+        rn.tune_set(k, {"trace_min_blocks": 3, "trace_packet": 8, "trace_stack": 96, "trace_frontier": 1}[k])
+
+
+def test_ssao_tile_keeps_every_bit(rn, restore_tune):
+    import torch
+    g, acc, _ = _scene(rn, 333, 197)
+    rn.tune_set("ssao_tile_h", 8)
+    ref = rn.compute_ssao(g).clone()
+    truth = rn.compute_rtao(g, acc, 16, 1.0)
+    ref_rec = rn.reconcile(ref, truth, g.mask)
+    for v in rn.TUNE_KEYS["ssao_tile_h"]:
+        rn.tune_set("ssao_tile_h", v)
+        assert bool((rn.compute_ssao(g) == ref).all()), v
+        out = rn.ao_frame(g, acc, 16, 1.0, 24, 0.12)
+        assert bool((out["ss"] == ref).all()), v
+        assert out["rec"].pixels == ref_rec.pixels and out["rec"].max_error == ref_rec.max_error
+        assert abs(out["rec"].sum_sq - ref_rec.sum_sq) <= 1e-10 * ref_rec.sum_sq
+
+
+def test_conv_tile_keeps_every_bit(rn, restore_tune):
+    import torch
+    net = rn.UNet(2, 64, 64, seed=4, inference=True)
+    x = torch.rand(2, 64, 64, 5, device="cuda", generator=torch.Generator(device="cuda").manual_seed(1))
+    rn.tune_set("conv_bn_max", 256)
+    ref = net.forward(x).clone()
+    for v in rn.TUNE_KEYS["conv_bn_max"]:
+        rn.tune_set("conv_bn_max", v)
+        assert bool((net.forward(x) == ref).all()), v

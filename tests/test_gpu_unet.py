@@ -46,10 +46,12 @@ def _batch(B, H, W, seed):
     return x.contiguous(), y.contiguous()
 
 
-def test_unet_gradients_match_torch(rn):
+@pytest.mark.parametrize("B,H,W,explicit", [(8, 32, 32, True), (2, 128, 128, False)])
+def test_unet_gradients_match_torch(rn, B, H, W, explicit):
+    """32 x 32 runs on explicit im2col GEMMs (its deepest level cannot be tiled for the
+    implicit convolution); 128 x 128 on the implicit-GEMM convolutions."""
     import torch
-    B, H, W = 8, 32, 32
-    net = rn.UNet(B, H, W, seed=3)
+    net = rn.UNet(B, H, W, seed=3, explicit=explicit)
     x, y = _batch(B, H, W, 1)
     loss = net.train_step(x, y, lr=0.0)          # gradients only
     g_ours = torch.from_numpy(net.get_grads())
@@ -60,6 +62,8 @@ def test_unet_gradients_match_torch(rn):
     ref_loss = ((out - y.cpu()) ** 2).mean()
     ref_loss.backward()
     assert abs(loss - ref_loss.item()) <= 0.02 * ref_loss.item()
+    norm, scale = net.last_grad_norm()                 # the library's global norm, unclipped
+    assert abs(norm / p.grad.norm().item() - 1) < 0.05 and scale == 1.0
     import rn_ao
     o = 0
     for cin, cout in rn_ao.UNET_CONVS + [(32, 1)]:
@@ -85,6 +89,49 @@ def test_unet_training_lowers_loss(rn):
     assert float(((out - y) ** 2).mean()) < first
 
 
+def test_unet_clipping_bounds_the_update(rn):
+    """Clipping at ratio r limits the norm to r x the running mean of past clipped norms; the
+    mean starts at the first norm, so the first step is scaled by r and the second (same
+    batch, nearly the same weights) by r (0.99 + 0.01 r) n0 / n1."""
+    B, H, W = 8, 32, 32
+    net = rn.UNet(B, H, W, seed=7)
+    x, y = _batch(B, H, W, 3)
+    net.set_clip(0.5)
+    net.train_step(x, y, lr=1e-7)
+    n0, s0 = net.last_grad_norm()
+    assert n0 > 0 and abs(s0 - 0.5) < 1e-6
+    net.train_step(x, y, lr=1e-7)
+    n1, s1 = net.last_grad_norm()
+    assert abs(s1 - 0.5 * 0.995 * n0 / n1) < 1e-5
+    net.set_clip(0.0)
+    net.train_step(x, y, lr=1e-7)
+    assert net.last_grad_norm()[1] == 1.0
+    with pytest.raises(rn.RnError):
+        net.set_clip(-1.0)
+
+
+def test_unet_state_roundtrip_and_inference_mode(rn):
+    import torch
+    B, H, W = 8, 32, 32
+    net = rn.UNet(B, H, W, seed=2)
+    x, y = _batch(B, H, W, 4)
+    for _ in range(3):
+        net.train_step(x, y, lr=1e-3)
+    state, step = net.get_state()
+    assert step == 3 and state.size == 3 * net.param_count
+    twin = rn.UNet(B, H, W, seed=99)
+    twin.set_state(state, step)
+    a, b = net.train_step(x, y, lr=1e-3), twin.train_step(x, y, lr=1e-3)
+    # equal up to the order of floating-point atomics in the loss and head reductions
+    assert abs(a - b) <= 1e-6 * abs(a)
+    assert np.allclose(net.get_params(), twin.get_params(), rtol=1e-4, atol=1e-6)
+    inf = rn.UNet(B, H, W, inference=True)
+    inf.set_params(net.get_params())
+    torch.testing.assert_close(inf.forward(x), net.forward(x), rtol=0, atol=0)
+    with pytest.raises(rn.RnError):
+        inf.train_step(x, y, lr=1e-3)
+
+
 def test_unet_param_roundtrip_and_shapes(rn):
     net = rn.UNet(2, 64, 64, seed=1)
     p = net.get_params()
@@ -93,3 +140,22 @@ def test_unet_param_roundtrip_and_shapes(rn):
     assert np.allclose(net.get_params(), p * 0.5)
     with pytest.raises(rn.RnError):
         rn.UNet(1, 24, 32)                       # not a multiple of 16
+
+
+def test_unet_implicit_and_explicit_convolutions_agree(rn):
+    """The implicit-GEMM convolutions accumulate the same products in the same K order as the
+    explicit im2col GEMMs: the forward is bit-identical, the gradients equal up to the order
+    of the weight gradient's split-K atomics."""
+    import torch
+    B, H, W = 2, 128, 128
+    imp = rn.UNet(B, H, W, seed=6)
+    exp = rn.UNet(B, H, W, seed=6, explicit=True)
+    x, y = _batch(B, H, W, 8)
+    assert torch.equal(imp.forward(x), exp.forward(x))
+    la, lb = imp.train_step(x, y, lr=0.0), exp.train_step(x, y, lr=0.0)
+    assert abs(la - lb) <= 1e-6 * abs(la)
+    ga, gb = imp.get_grads(), exp.get_grads()
+    assert np.allclose(ga, gb, rtol=1e-3, atol=1e-6 * np.abs(gb).max())
+    inf = rn.UNet(B, H, W, inference=True)
+    inf.set_params(imp.get_params())
+    assert torch.equal(inf.forward(x), imp.forward(x))
