@@ -98,23 +98,39 @@ def _icosphere(subdiv: int):
     return np.array(verts, np.float64), f
 
 
-def _box_tris(c, s, yaw):
-    """12 triangles of a box with footprint centre c=(x, z), sides s=(sx, sy, sz), resting on
-    y = 0, rotated by `yaw` about the vertical axis; face normals."""
-    hx, hz = s[0] / 2.0, s[2] / 2.0
-    corners = np.array([[x, y, z] for y in (0.0, s[1]) for z in (-hz, hz) for x in (-hx, hx)])
-    cy, sy = np.cos(yaw), np.sin(yaw)
-    rot = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
-    p = corners @ rot.T + np.array([c[0], 0.0, c[1]])
-    faces = [((0, 1, 3, 2), (0, -1, 0)), ((4, 6, 7, 5), (0, 1, 0)), ((0, 4, 5, 1), (0, 0, -1)),
-             ((2, 3, 7, 6), (0, 0, 1)), ((0, 2, 6, 4), (-1, 0, 0)), ((1, 5, 7, 3), (1, 0, 0))]
-    tris, nrms = [], []
-    for (a, b, cc, d), n in faces:
-        nr = rot @ np.array(n, np.float64)
+_FACES = [((0, 1, 3, 2), (0, -1, 0)), ((4, 6, 7, 5), (0, 1, 0)), ((0, 4, 5, 1), (0, 0, -1)),
+          ((2, 3, 7, 6), (0, 0, 1)), ((0, 2, 6, 4), (-1, 0, 0)), ((1, 5, 7, 3), (1, 0, 0))]
+
+
+def _boxes_tris(centres, sides, yaws):
+    """12 triangles per box (positions and face normals, (12 n, 9) each): footprint centres
+    (x, z), sides (sx, sy, sz), boxes resting on y = 0 and rotated by their yaw about the
+    vertical axis."""
+    n = len(centres)
+    hx, hz, h = sides[:, 0] / 2.0, sides[:, 2] / 2.0, sides[:, 1]
+    corners = np.empty((n, 8, 3))
+    q = 0
+    for yv in (0, 1):
+        for zs in (-1, 1):
+            for xs in (-1, 1):
+                corners[:, q, 0] = hx if xs > 0 else -hx
+                corners[:, q, 1] = h if yv else 0.0
+                corners[:, q, 2] = hz if zs > 0 else -hz
+                q += 1
+    cy, sy = np.cos(yaws), np.sin(yaws)
+    rot = np.zeros((n, 3, 3))
+    rot[:, 0, 0], rot[:, 0, 2], rot[:, 1, 1], rot[:, 2, 0], rot[:, 2, 2] = cy, sy, 1.0, -sy, cy
+    p = np.matmul(corners, rot.transpose(0, 2, 1)) + np.stack([centres[:, 0], np.zeros(n), centres[:, 1]], 1)[:, None, :]
+    tris = np.empty((n, 12, 9))
+    nrms = np.empty((n, 12, 9))
+    t = 0
+    for (a, b, cc, d), nv in _FACES:
+        nr = np.matmul(rot, np.array(nv, np.float64))
         for t3 in ((a, b, cc), (a, cc, d)):
-            tris.append(np.concatenate([p[t3[0]], p[t3[1]], p[t3[2]]]))
-            nrms.append(np.concatenate([nr, nr, nr]))
-    return np.array(tris), np.array(nrms)
+            tris[:, t] = np.concatenate([p[:, t3[0]], p[:, t3[1]], p[:, t3[2]]], 1)
+            nrms[:, t] = np.concatenate([nr, nr, nr], 1)
+            t += 1
+    return tris.reshape(-1, 9), nrms.reshape(-1, 9)
 
 
 def build_synthetic_scene(seed: int, n_boxes: int, n_spheres: int, grid: int = 200, half: float = 50.0,
@@ -128,27 +144,38 @@ def build_synthetic_scene(seed: int, n_boxes: int, n_spheres: int, grid: int = 2
     a = np.stack([x0, zero, z0], 1); b = np.stack([x1, zero, z0], 1)
     c = np.stack([x1, zero, z1], 1); d = np.stack([x0, zero, z1], 1)
     ground = np.stack([np.concatenate([a, b, c], 1), np.concatenate([a, c, d], 1)], 1).reshape(-1, 9)
-    gnrm = np.tile(np.array([0, 1, 0] * 3, np.float64), (len(ground), 1))
-    parts, nparts = [ground], [gnrm]
     # boxes
     centres = rng.uniform(-half, half, (n_boxes, 2))
     sides = rng.uniform(0.2, 3.0, (n_boxes, 3))
     yaws = rng.uniform(0.0, 2.0 * np.pi, n_boxes)
-    for k in range(n_boxes):
-        t, n = _box_tris(centres[k], sides[k], yaws[k])
-        parts.append(t); nparts.append(n)
-    # icospheres resting on the ground
     if n_spheres:
         v, f = _icosphere(subdiv)
         unit = v[f].reshape(-1, 9)                    # (faces, 9) corner positions on the unit sphere
         sc = rng.uniform(-half, half, (n_spheres, 2))
         r = np.clip(rng.lognormal(0.0, 0.5, n_spheres), 0.2, 4.0)
-        off = np.stack([sc[:, 0], r, sc[:, 1]], 1)    # centres at height r
-        sph = unit[None, :, :] * r[:, None, None] + np.tile(off, 3)[:, None, :]
-        parts.append(sph.reshape(-1, 9))
-        nparts.append(np.tile(unit, (n_spheres, 1)))
-    tris = np.ascontiguousarray(np.concatenate(parts).astype(np.float32))
-    nrms = np.ascontiguousarray(np.concatenate(nparts).astype(np.float32))
+    # the output arrays are filled in place: positions computed in FP64, stored as FP32
+    nsph = len(unit) * n_spheres if n_spheres else 0
+    total = len(ground) + 12 * n_boxes + nsph
+    tris = np.empty((total, 9), np.float32)
+    nrms = np.empty((total, 9), np.float32)
+    tris[:len(ground)] = ground
+    nrms[:len(ground)] = np.array([0, 1, 0] * 3, np.float32)
+    o = len(ground)
+    if n_boxes:
+        t, n = _boxes_tris(centres, sides, yaws)
+        tris[o:o + 12 * n_boxes] = t
+        nrms[o:o + 12 * n_boxes] = n
+        o += 12 * n_boxes
+    # icospheres resting on the ground, centres at height r
+    if n_spheres:
+        off = np.tile(np.stack([sc[:, 0], r, sc[:, 1]], 1), 3)
+        nf = len(unit)
+        step = max(1, (1 << 20) // nf)
+        for k0 in range(0, n_spheres, step):
+            k1 = min(n_spheres, k0 + step)
+            sph = unit[None, :, :] * r[k0:k1, None, None] + off[k0:k1, None, :]
+            tris[o + k0 * nf:o + k1 * nf] = sph.reshape(-1, 9)
+        nrms[o:o + nsph].reshape(n_spheres, nf, 9)[:] = unit.astype(np.float32)[None]
     return Scene(tris, nrms, _normalize((-0.4, -1.0, -0.3)), (40.0, 12.0, 0.0, 0.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.9))
 
 

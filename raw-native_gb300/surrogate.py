@@ -69,18 +69,45 @@ def masked_trace(g, acc, spp: int, pixel_mask, radius: float = RADIUS):
     return rn.compute_rtao(sub, acc, spp, radius)
 
 
-class SceneSource:
-    """Seeded scenes built on host threads ahead of their use."""
+def scene_counts(seed: int, density: str):
+    """(boxes, spheres) of a training or evaluation scene. "fixed": 200 and 50 (146,400
+    triangles). "mixed": each drawn log-uniformly per seed, boxes in [200, 10000] and spheres
+    in [50, 6000], from the sparse scenes up to the density of the 7.88M-triangle scene."""
+    if density == "fixed":
+        return SCENE_BOXES, SCENE_SPHERES
+    if density != "mixed":
+        raise ValueError("density %r" % density)
+    rng = np.random.Generator(np.random.PCG64(seed ^ 0xD3))
+    b = int(round(np.exp(rng.uniform(np.log(200.0), np.log(10000.0)))))
+    s = int(round(np.exp(rng.uniform(np.log(50.0), np.log(6000.0)))))
+    return b, s
 
-    def __init__(self, seeds, boxes=SCENE_BOXES, spheres=SCENE_SPHERES, workers: int = 6):
-        self.seeds = list(seeds)
-        self.pool = cf.ThreadPoolExecutor(workers)
-        self.futs = [self.pool.submit(scenes.build_synthetic_scene, s, boxes, spheres) for s in self.seeds]
+
+class SceneSource:
+    """Seeded scenes built on host threads, at most `ahead` of them ahead of their use."""
+
+    def __init__(self, seeds, density: str = "fixed", workers: int = 8, ahead: int = 16):
+        self.seeds, self.density, self.workers, self.ahead = list(seeds), density, workers, ahead
+
+    def _build(self, seed):
+        b, s = scene_counts(seed, self.density)
+        return scenes.build_synthetic_scene(seed, b, s)
 
     def __iter__(self):
-        for s, f in zip(self.seeds, self.futs):
-            yield s, f.result()
-        self.pool.shutdown()
+        import collections
+        with cf.ThreadPoolExecutor(self.workers) as pool:
+            pending = collections.deque()
+            it = iter(self.seeds)
+            for sd in it:
+                pending.append((sd, pool.submit(self._build, sd)))
+                if len(pending) >= self.ahead:
+                    break
+            while pending:
+                sd, f = pending.popleft()
+                nxt = next(it, None)
+                if nxt is not None:
+                    pending.append((nxt, pool.submit(self._build, nxt)))
+                yield sd, f.result()
 
 
 @dataclasses.dataclass
@@ -94,7 +121,7 @@ class Dataset:
         return hashlib.sha256(json.dumps(self.manifest, sort_keys=True).encode()).hexdigest()[:16]
 
 
-def generate_dataset(n_seeds: int, n_crops: int, seed0: int = TRAIN_SEED0, log=print) -> Dataset:
+def generate_dataset(n_seeds: int, n_crops: int, seed0: int = TRAIN_SEED0, log=print, density: str = "fixed") -> Dataset:
     """n_crops random CROP x CROP crops, spread evenly over n_seeds scenes (one 1920 x 1080
     orbit view each): features from the 4-spp trace, target from the 1024-spp trace, both
     traced only inside the crops."""
@@ -104,7 +131,7 @@ def generate_dataset(n_seeds: int, n_crops: int, seed0: int = TRAIN_SEED0, log=p
     ys = torch.empty(n_seeds * per, CROP, CROP, device="cuda")
     k = 0
     t0 = time.time()
-    for i, (sd, sc) in enumerate(SceneSource(range(seed0, seed0 + n_seeds))):
+    for i, (sd, sc) in enumerate(SceneSource(range(seed0, seed0 + n_seeds), density)):
         tris = torch.from_numpy(sc.tris).cuda()
         nrms = torch.from_numpy(sc.normals).cuda()
         acc = rn.LinearAccel(tris)
@@ -125,8 +152,9 @@ def generate_dataset(n_seeds: int, n_crops: int, seed0: int = TRAIN_SEED0, log=p
         acc.close()
         if log and (i + 1) % max(1, n_seeds // 10) == 0:
             log("data: %d/%d scenes, %d crops, %.1f s" % (i + 1, n_seeds, k, time.time() - t0))
-    man = dict(seeds=[seed0, seed0 + n_seeds], view=[VIEW_W, VIEW_H], crop=CROP, crops=k, boxes=SCENE_BOXES,
-               spheres=SCENE_SPHERES, spp_in=SPP_IN, spp_target=SPP_TARGET, radius=RADIUS, crop_rng="PCG64(seed^0xC409)")
+    man = dict(seeds=[seed0, seed0 + n_seeds], view=[VIEW_W, VIEW_H], crop=CROP, crops=k, density=density,
+               boxes=SCENE_BOXES if density == "fixed" else [200, 10000],
+               spheres=SCENE_SPHERES if density == "fixed" else [50, 6000], spp_in=SPP_IN, spp_target=SPP_TARGET, radius=RADIUS, crop_rng="PCG64(seed^0xC409)")
     return Dataset(xs[:k], ys[:k], man)
 
 
@@ -299,9 +327,10 @@ def eval_frame(net, sc, cam, w: int, h: int, spps=(16, 32, 64, 128, 256), k: flo
     return r
 
 
-def evaluate(net, n_seeds: int, seed0: int = EVAL_SEED0, w: int = VIEW_W, h: int = VIEW_H, log=print, **kw):
+def evaluate(net, n_seeds: int, seed0: int = EVAL_SEED0, w: int = VIEW_W, h: int = VIEW_H, log=print,
+             density: str = "fixed", **kw):
     rows = []
-    for sd, sc in SceneSource(range(seed0, seed0 + n_seeds)):
+    for sd, sc in SceneSource(range(seed0, seed0 + n_seeds), density):
         rows.append(dict(seed=sd, **eval_frame(net, sc, camera_for(sd), w, h, **kw)))
         if log and len(rows) % max(1, n_seeds // 10) == 0:
             log("eval: %d/%d  net %.4f  surrogate %.4f  fallback %.3f" % (
@@ -328,10 +357,13 @@ def main(argv=None):
     t.add_argument("--clip", type=float, default=2.0)
     t.add_argument("--ckpt-every", type=int, default=5000)
     t.add_argument("--eval-seeds", type=int, default=0)
+    t.add_argument("--density", choices=["fixed", "mixed"], default="fixed",
+                   help="training scenes: 200 boxes + 50 spheres, or counts drawn per seed up to the large scene's")
     e = sub.add_parser("eval")
     e.add_argument("--ckpt", required=True)
     e.add_argument("--seeds", type=int, default=200)
     e.add_argument("--out", default=None)
+    e.add_argument("--density", choices=["fixed", "mixed"], default="fixed")
     a = ap.parse_args(argv)
     import torch
     rn.init()
@@ -344,7 +376,7 @@ def main(argv=None):
             log_f.write(msg + "\n")
             log_f.flush()
         t0 = time.time()
-        data = generate_dataset(a.seeds, a.crops, log=log)
+        data = generate_dataset(a.seeds, a.crops, log=log, density=a.density)
         torch.cuda.synchronize()
         log("data: %d crops in %.1f s, digest %s" % (data.x.shape[0], time.time() - t0, data.digest))
         net = rn.UNet(a.batch, CROP, CROP, seed=a.init_seed)
@@ -372,7 +404,7 @@ def main(argv=None):
     else:
         inf = rn.UNet(1, *padded_shape(VIEW_H, VIEW_W), inference=True)
         meta = load_weights(inf, a.ckpt)
-        summary, rows = evaluate(inf, a.seeds)
+        summary, rows = evaluate(inf, a.seeds, density=a.density)
         print(json.dumps(summary))
         if a.out:
             json.dump(dict(summary=summary, rows=rows, meta=meta), open(a.out, "w"), indent=1)

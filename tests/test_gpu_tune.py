@@ -41,12 +41,12 @@ def test_ssao_tile_keeps_every_bit(rn, restore_tune):
     import torch
     g, acc, _ = _scene(rn, 333, 197)
     rn.tune_set("ssao_tile_h", 8)
-    ref = rn.compute_ssao(g).clone()
+    ref = rn.compute_ssao(g, 24, 1.0).clone()
     truth = rn.compute_rtao(g, acc, 16, 1.0)
     ref_rec = rn.reconcile(ref, truth, g.mask)
     for v in rn.TUNE_KEYS["ssao_tile_h"]:
         rn.tune_set("ssao_tile_h", v)
-        assert bool((rn.compute_ssao(g) == ref).all()), v
+        assert bool((rn.compute_ssao(g, 24, 1.0) == ref).all()), v
         out = rn.ao_frame(g, acc, 16, 1.0, 24, 0.12)
         assert bool((out["ss"] == ref).all()), v
         assert out["rec"].pixels == ref_rec.pixels and out["rec"].max_error == ref_rec.max_error
