@@ -51,7 +51,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-row-stride", type=int, default=4, help="rows of the CPU sample: every n-th")
-    p.add_argument("--profile", choices=["frame", "trace", "ssao", "reconcile", "build"],
+    p.add_argument("--profile", choices=["frame", "trace", "ssao", "reconcile", "build", "unet", "surrogate"],
                    help="run only this pass `--steps` times after `--warmup` (for ncu), print nothing")
     p.add_argument("--spp", type=int, default=SPP, help="samples per pixel (the benchmark uses 256)")
     p.add_argument("--tris", type=int, default=1000000, help="--profile build: soup triangles")
@@ -315,16 +315,43 @@ def run_ours(args):
     }
     if cpu:
         out["cpu_baseline"] = cpu
+    if world == 1 and os.path.exists(SURROGATE_WEIGHTS) and not os.environ.get("RN_BENCH_NO_SURROGATE"):
+        # the metric's other half: surrogate vs plain GPU RT at 4K on the 7.88M-triangle scene
+        out["surrogate_4k"] = surrogate_headtohead(max(2, args.steps // 4), max(1, args.warmup // 3))
     print(json.dumps(out), flush=True)
 
 
 def run_profile(args):
-    """One pass, repeated, for a profiler: the 4K G-buffer and accelerator are built first."""
+    """One pass, repeated, for a profiler: the 4K G-buffer and accelerator are built first.
+    unet: the surrogate network's forward on a 3840 x 2160 frame (padded to 2176 x 3840);
+    surrogate: one rn_surrogate_ao frame of the 7.88M-triangle scene at 4K (256-spp fallback)."""
     import torch
     import rn_ao as rn
     import scene as scenes
     torch.cuda.set_device(0)
     rn.init()
+    if args.profile == "unet":
+        import surrogate as S
+        net = rn.UNet(1, *S.padded_shape(2160, 3840), inference=True)
+        S.load_weights(net, SURROGATE_WEIGHTS)
+        x = torch.rand(1, *net.shape[1:], 5, device="cuda")
+        for _ in range(args.warmup + args.steps):
+            net.forward(x)
+        torch.cuda.synchronize()
+        return
+    if args.profile == "surrogate":
+        import surrogate as S
+        sc = scenes.build_synthetic_scene(5, 10000, 6000)
+        tris = torch.from_numpy(sc.tris).cuda()
+        g, depth = rn.rasterize(tris, torch.from_numpy(sc.normals).cuda(), scenes.orbit_views(5, 16)[5][3], 3840, 2160,
+                                want_depth=True)
+        acc = rn.LinearAccel(tris)
+        net = rn.UNet(1, *S.padded_shape(2160, 3840), inference=True)
+        S.load_weights(net, SURROGATE_WEIGHTS)
+        for _ in range(args.warmup + args.steps):
+            rn.surrogate_ao(net, g, depth, acc, 256, 1.0, 3.0)
+        torch.cuda.synchronize()
+        return
     radius = RADIUS
     if args.workload == "4k":
         sc = scenes.build_test_scene()
@@ -415,29 +442,29 @@ def run_views(args):
     print(json.dumps(out), flush=True)
 
 
-SURROGATE_WEIGHTS = os.path.join(PKG, "weights", "surrogate_bf16.npz")
+# the network trained on mixed-density scenes (the 200-box recipe's network is
+# weights/surrogate_bf16.npz; RN_SURROGATE_WEIGHTS selects another file)
+SURROGATE_WEIGHTS = os.path.join(PKG, "weights", "surrogate_mixed_bf16.npz")
 
 
-def run_surrogate(args):
-    """The 4K head-to-head: 16 orbit views at 3840 x 2160 of the seeded 7.88M-triangle scene,
-    AO radius 1. Truth: the 1024-spp trace of each view. Plain GPU RT runs at the smallest
-    spp of {16, 32, 64, 128, 256} whose RMSE against the truth is <= 0.02 on every view; the
-    surrogate (4-spp trace + U-Net + fallback tiles traced at that same spp) is timed on the
-    same views. Both are timed per frame with CUDA events, G-buffers resident."""
+def surrogate_headtohead(steps: int, warmup: int, n_views: int = 16, weights: str = None):
+    """The 4K head-to-head: orbit views at 3840 x 2160 of the seeded 7.88M-triangle scene, AO
+    radius 1. Truth: the 1024-spp trace of each view. Plain GPU RT runs at the smallest spp
+    of {16, 32, 64, 128, 256} whose RMSE against the truth is <= 0.02 on every view; the
+    surrogate (rn_surrogate_ao: 4-spp trace + U-Net + fallback tiles traced at that same spp)
+    runs on the same views. Both are timed per frame with CUDA events, G-buffers resident."""
     import numpy as np
     import torch
     import rn_ao as rn
     import scene as scenes
     import surrogate as S
-    torch.cuda.set_device(0)
-    rn.init()
-    n_views = args.views or 16
+    weights = weights or os.environ.get("RN_SURROGATE_WEIGHTS") or SURROGATE_WEIGHTS
     sc = scenes.build_synthetic_scene(5, 10000, 6000)
     tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
     acc = rn.LinearAccel(tris)
     W, H, R = 3840, 2160, 1.0
     net = rn.UNet(1, *S.padded_shape(H, W), inference=True)
-    meta = S.load_weights(net, SURROGATE_WEIGHTS)
+    meta = S.load_weights(net, weights)
     frames = []
     spps = (16, 32, 64, 128, 256)
     for (_, _, _, cam) in scenes.orbit_views(5, n_views):
@@ -450,7 +477,7 @@ def run_surrogate(args):
     stream = torch.cuda.current_stream()
 
     def timed(fn, reps):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -461,34 +488,48 @@ def run_surrogate(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps, out
 
-    rt_ms, sur_ms, sur_rmse, fb = [], [], [], []
+    rt_ms, sur_ms, sur_rmse, fb, t4_ms, net_ms = [], [], [], [], [], []
+    x = torch.zeros(1, *net.shape[1:], 5, device="cuda")
     with Clocks(0) as clk:
         for f in frames:
-            ms, _ = timed(lambda: rn.compute_rtao(f["g"], acc, spp_rt, R), args.steps)
+            ms, _ = timed(lambda: rn.compute_rtao(f["g"], acc, spp_rt, R), steps)
             rt_ms.append(ms)
-            ms, (ao, frac) = timed(lambda: S.surrogate_ao(net, f["g"], f["depth"], acc, spp_rt, R), args.steps)
+            ms, (ao, st) = timed(lambda: rn.surrogate_ao(net, f["g"], f["depth"], acc, spp_rt, R, 3.0), steps)
             sur_ms.append(ms)
             sur_rmse.append(S.rmse(ao, f["truth"], f["g"].mask))
-            fb.append(frac)
+            fb.append(st["fallback_fraction"])
+            t4_ms.append(timed(lambda: rn.compute_rtao(f["g"], acc, S.SPP_IN, R), steps)[0])
+        net_ms.append(timed(lambda: net.forward(x), steps)[0])
     rays_rt = sum(f["covered"] for f in frames) * spp_rt
-    out = {
-        "metric": METRIC, "value": float(np.mean(sur_ms)), "unit": "ms/frame (surrogate)", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(sur_ms)), "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, f32 trace", "data": "synthetic",
-        "config": {"workload": "surrogate vs plain GPU RT: seeded 7.88M-triangle scene, %d orbit views at 3840x2160, "
-                               "radius 1, truth 1024 spp" % n_views, "triangles": int(len(sc.tris)),
-                   "views": n_views, "weights": os.path.relpath(SURROGATE_WEIGHTS, ROOT),
-                   "trained": {k: meta.get(k) for k in ("steps", "batch", "lr", "data_digest")}},
+    return {
+        "workload": "surrogate vs plain GPU RT: seeded 7.88M-triangle scene, %d orbit views at 3840x2160, radius 1, "
+                    "truth 1024 spp" % n_views,
+        "triangles": int(len(sc.tris)), "views": n_views, "weights": os.path.relpath(weights, ROOT),
+        "trained": {k: meta.get(k) for k in ("steps", "batch", "lr", "data_digest")},
+        "training_scenes": (meta.get("data") or {}).get("density", "fixed"),
         "plain_rt": {"spp": spp_rt, "ms_per_frame": float(np.mean(rt_ms)),
                      "grays_per_s": rays_rt / (sum(rt_ms) * 1e-3) / 1e9,
                      "rmse_by_spp_max_over_views": {s: max(f["rmse_rt"][s] for f in frames) for s in spps}},
         "surrogate": {"ms_per_frame": float(np.mean(sur_ms)), "rmse_max_over_views": max(sur_rmse),
                       "rmse_mean": float(np.mean(sur_rmse)), "fallback_fraction_mean": float(np.mean(fb)),
-                      "spp_input": S.SPP_IN, "fallback_spp": spp_rt},
+                      "spp_input": S.SPP_IN, "fallback_spp": spp_rt, "trace4_ms": float(np.mean(t4_ms)),
+                      "network_ms": float(np.mean(net_ms))},
         "speedup_vs_plain_rt": float(np.mean(rt_ms) / np.mean(sur_ms)),
         "surrogate_meets_rmse": bool(max(sur_rmse) <= 0.02),
         "clocks": clk.summary(),
     }
+
+
+def run_surrogate(args):
+    import torch
+    import rn_ao as rn
+    torch.cuda.set_device(0)
+    rn.init()
+    r = surrogate_headtohead(args.steps, args.warmup, args.views or 16)
+    out = {"metric": METRIC, "value": r["surrogate"]["ms_per_frame"], "unit": "ms/frame (surrogate)", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["surrogate"]["ms_per_frame"],
+           "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network, f32 trace",
+           "data": "synthetic", "config": {"workload": r.pop("workload"), "views": r["views"]}, **r}
     print(json.dumps(out), flush=True)
 
 

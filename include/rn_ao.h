@@ -311,6 +311,25 @@ int rn_unet_last_grad_norm(const rn_unet* net, float* norm, float* scale, rn_sta
 int rn_unet_get_state(rn_unet* net, float* host, uint64_t* step, rn_status* st);
 int rn_unet_set_state(rn_unet* net, const float* host, uint64_t step, rn_status* st);
 
+/* One AO frame by the surrogate (no counterpart in the reference): the 4-spp trace of the
+ * G-buffer, the network on (depth over radius relative to the covered pixels' mean depth,
+ * normal, 4-spp AO), then per 16 x 16 tile the confidence-band test: a tile whose predicted
+ * mean leaves mean(ao4) +- k sigma (sigma = max(sqrt(sum p (1 - p) / 4) / n, 0.5 / sqrt(4 n))
+ * over its n covered pixels) is traced at spp_full and its traced values replace the
+ * prediction. ao receives the frame (1 off the coverage). Optional outputs: ao4 (the 4-spp
+ * trace), pred (the network alone), tile_flags (ceil(h/16) x ceil(w/16), 1 = traced).
+ * DEVICE pointers only (G-buffer planes, depth, outputs); `net` was created with batch 1 for
+ * a shape covering w x h. Synchronizes the library's stream to return the stats. */
+typedef struct rn_surrogate_stats {
+    uint32_t tiles_covered;   /* tiles with a covered pixel */
+    uint32_t tiles_fallback;  /* of those, traced at spp_full */
+    float mean_depth;         /* the covered pixels' mean depth the features used */
+    float reserved;
+} rn_surrogate_stats;
+int rn_surrogate_ao(rn_unet* net, const rn_gbuf* g, const float* depth, const rn_accel* accel, int spp_full,
+                    float radius, float k, float* ao, float* ao4, float* pred, uint8_t* tile_flags,
+                    rn_surrogate_stats* stats, rn_status* st);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

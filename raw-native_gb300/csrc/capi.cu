@@ -152,6 +152,25 @@ int packet_log2(int packet) { return packet == 4 ? 2 : packet == 16 ? 4 : 3; }
 
 }  // namespace
 
+int trace_ao_device(const float* pos, const float* nrm, const uint8_t* mask, int w, int h, const rn_accel* accel,
+                    int spp, float radius, float* ao, rn_status* st) {
+    Context& c = ctx();
+    TraceParams p{};
+    p.w = w; p.h = h;
+    p.pos = pos; p.nrm = nrm; p.mask = mask;
+    p.nodes = accel->d_nodes; p.tris = accel->d_tris;
+    p.has_geometry = accel->ntri > 0;
+    p.spp = spp; p.radius = radius;
+    p.want_sky = 0; p.sun_forced = 0;
+    p.lx = 0.0f; p.ly = 1.0f; p.lz = 0.0f;
+    p.corr = c.trig_corr;
+    p.ao = ao; p.sky = nullptr; p.sun = nullptr;
+    p.err_word = c.dev_error;
+    apply_tune(p, accel);
+    if (launch_trace(p, c.sm_count, c.stream) != RN_OK) return cuda_fail(st, cudaGetLastError(), "trace_kernel");
+    return RN_OK;
+}
+
 void apply_tune(TraceParams& p, const rn_accel* accel) {
     const Tune& t = ctx().tune;
     p.frontier = t.trace_frontier;

@@ -31,6 +31,7 @@ enum Slot {
     WS_POS, WS_NRM, WS_MASK, WS_AO, WS_SKY, WS_SUN, WS_SS, WS_ERR, WS_TRUTH, WS_APPROX,
     WS_PARTIALS, WS_WORKLIST, WS_COUNTERS, WS_RAYS, WS_TMAX, WS_HITS, WS_TRIS_IN,
     WS_NRM_IN, WS_RASTER, WS_DEPTH, WS_STATS,
+    WS_SUR_AO4, WS_SUR_PRED, WS_SUR_FB, WS_SUR_AOFB, WS_SUR_STATS,
     WS_COUNT
 };
 
@@ -178,6 +179,10 @@ struct TraceParams {
     int packet_log2;      // log2 of the packet width (pixels per warp row): 2, 3 or 4
     int stack_need;       // entries the walk can push on this tree: 16 + 3 x wide depth
 };
+// Traced AO (AO only, the library's sampler and tuning) of a device G-buffer into a device
+// image, on the library's stream.
+int trace_ao_device(const float* pos, const float* nrm, const uint8_t* mask, int w, int h, const rn_accel* accel,
+                    int spp, float radius, float* ao, rn_status* st);
 // The tuned trace fields of p (frontier, packet, stack bound for this tree).
 void apply_tune(TraceParams& p, const rn_accel* accel);
 int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned long long* counts = nullptr,

@@ -284,6 +284,131 @@ __global__ void clip_kernel(float* __restrict__ stats, float ratio) {
     stats[3] = ema;
 }
 
+
+// ------------------------------------------------------------------ the surrogate's frame
+constexpr int kSppIn = 4;                 // samples of the traced input
+constexpr int kTile = 16;                 // fallback tiles: 16 x 16 pixels
+constexpr int kDepthBlocks = 512;
+
+// Per-block sums of the covered pixels' depth (FP64) and count, in a fixed order.
+__global__ void depth_partial_kernel(const float* __restrict__ depth, const uint8_t* __restrict__ mask, size_t n,
+                                     double* __restrict__ part_sum, unsigned* __restrict__ part_cnt) {
+    double s = 0.0;
+    unsigned c = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        if (mask[i]) { s += (double)depth[i]; ++c; }
+    for (int o = 16; o; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    __shared__ double ss[8];
+    __shared__ unsigned sc[8];
+    if ((threadIdx.x & 31) == 0) { ss[threadIdx.x >> 5] = s; sc[threadIdx.x >> 5] = c; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        unsigned tc = 0;
+        for (int k = 0; k < 8; ++k) { t += ss[k]; tc += sc[k]; }
+        part_sum[blockIdx.x] = t;
+        part_cnt[blockIdx.x] = tc;
+    }
+}
+// mean = (float)(sum / count) over the partials in block order (0 without covered pixels).
+__global__ void depth_mean_kernel(const double* __restrict__ part_sum, const unsigned* __restrict__ part_cnt, int nb,
+                                  float* __restrict__ mean) {
+    if (threadIdx.x != 0) return;
+    double t = 0.0;
+    unsigned long long c = 0;
+    for (int k = 0; k < nb; ++k) { t += part_sum[k]; c += part_cnt[k]; }
+    *mean = c ? (float)(t / (double)c) : 0.0f;
+}
+
+// The network's BF16 input for a w x h frame inside its H x W shape: clamp((depth - mean) /
+// radius, -32, 32) / 8, the world normal and the 4-spp AO on covered pixels; 0, 0 and AO 1 on
+// uncovered and padding pixels (channels 5..7 zero).
+__global__ void features_kernel(const float* __restrict__ depth, const float* __restrict__ nrm,
+                                const uint8_t* __restrict__ mask, const float* __restrict__ ao4, int w, int h, int W,
+                                int H, const float* __restrict__ mean, float radius, bf16* __restrict__ out) {
+    const size_t total = (size_t)W * H;
+    const float mu = *mean;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % W), y = (int)(i / W);
+        float f[5] = {0.0f, 0.0f, 0.0f, 0.0f, 1.0f};
+        if (x < w && y < h) {
+            const size_t p = (size_t)y * w + x;
+            if (mask[p]) {
+                f[0] = fminf(fmaxf((depth[p] - mu) / radius, -32.0f), 32.0f) * 0.125f;
+                f[1] = nrm[3 * p];
+                f[2] = nrm[3 * p + 1];
+                f[3] = nrm[3 * p + 2];
+                f[4] = ao4[p];
+            }
+        }
+        uint4 v = make_uint4(0, 0, 0, 0);
+        bf16* hb = reinterpret_cast<bf16*>(&v);
+#pragma unroll
+        for (int c = 0; c < 5; ++c) hb[c] = __float2bfloat16_rn(f[c]);
+        *reinterpret_cast<uint4*>(out + i * 8) = v;
+    }
+}
+
+// One 16 x 16 tile per block: the confidence band test of the prediction's tile mean against
+// the 4-spp tile mean (sigma = max(sqrt(sum p (1 - p) / 4) / n, 0.5 / sqrt(4 n)) over the n
+// covered pixels), the tile's flag, and the fallback mask of its pixels.
+__global__ void __launch_bounds__(kTile * kTile) band_kernel(const float* __restrict__ pred, int W,
+                                                              const float* __restrict__ ao4,
+                                                              const uint8_t* __restrict__ mask, int w, int h, float k,
+                                                              uint8_t* __restrict__ tile_flag,
+                                                              uint8_t* __restrict__ fb_mask,
+                                                              unsigned* __restrict__ counts) {
+    const int x = blockIdx.x * kTile + (threadIdx.x % kTile), y = blockIdx.y * kTile + (threadIdx.x / kTile);
+    const bool in = x < w && y < h;
+    const size_t p = (size_t)y * w + x;
+    const bool cov = in && mask[p];
+    float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (cov) {
+        const float a = ao4[p];
+        v[0] = 1.0f;
+        v[1] = pred[(size_t)y * W + x];
+        v[2] = a;
+        v[3] = a * (1.0f - a);
+    }
+    __shared__ float red[4][kTile * kTile / 32];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        float t = v[q];
+        for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = t;
+    }
+    __syncthreads();
+    __shared__ int s_flag;
+    if (threadIdx.x == 0) {
+        float t[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        for (int q = 0; q < 4; ++q)
+            for (int j = 0; j < kTile * kTile / 32; ++j) t[q] += red[q][j];
+        const float n = fmaxf(t[0], 1.0f);
+        const float sigma = fmaxf(sqrtf(fmaxf(t[3], 0.0f) / (float)kSppIn) / n, 0.5f / sqrtf((float)kSppIn * n));
+        const int flag = t[0] > 0.0f && fabsf(t[1] / n - t[2] / n) > k * sigma;
+        tile_flag[blockIdx.y * gridDim.x + blockIdx.x] = (uint8_t)flag;
+        if (t[0] > 0.0f) atomicAdd(counts, 1u);
+        if (flag) atomicAdd(counts + 1, 1u);
+        s_flag = flag;
+    }
+    __syncthreads();
+    if (in) fb_mask[p] = (uint8_t)(cov && s_flag);
+}
+
+// ao = 1 off the coverage, the traced value on fallback pixels, the prediction elsewhere.
+__global__ void composite_kernel(const float* __restrict__ pred, int W, const float* __restrict__ traced,
+                                 const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fb, int w, int h,
+                                 float* __restrict__ ao) {
+    const size_t total = (size_t)w * h;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(i % w), y = (int)(i / w);
+        ao[i] = !mask[i] ? 1.0f : fb[i] ? traced[i] : pred[(size_t)y * W + x];
+    }
+}
+
 inline unsigned grid_for(size_t n, int block = 256) {
     size_t g = (n + block - 1) / block;
     return (unsigned)(g > 65535 * 8 ? 65535 * 8 : (g ? g : 1));
@@ -675,6 +800,70 @@ int rn_unet_last_grad_norm(const rn_unet* u, float* norm, float* scale, rn_statu
     if (!u) return fail(st, RN_ERR_INVALID, "null argument");
     if (norm) *norm = u->host_loss[1];
     if (scale) *scale = u->host_loss[2];
+    return ok(st);
+}
+
+
+// One AO frame by the surrogate: the 4-spp trace, the network, the confidence-band test per
+// 16 x 16 tile and the fallback tiles traced at spp_full. Device pointers; batch-1 network
+// whose shape covers the frame.
+int rn_surrogate_ao(rn_unet* u, const rn_gbuf* g, const float* depth, const rn_accel* accel, int spp_full, float radius,
+                    float k, float* ao, float* ao4_out, float* pred_out, uint8_t* tile_flags,
+                    rn_surrogate_stats* stats, rn_status* st) {
+    if (!u || !g || !depth || !accel || !ao) return fail(st, RN_ERR_INVALID, "null argument");
+    if (!g->position || !g->normal || !g->mask) return fail(st, RN_ERR_INVALID, "null G-buffer plane");
+    if (u->B != 1) return fail(st, RN_ERR_INVALID, "the surrogate frame needs a batch-1 network (batch %d)", u->B);
+    const int w = g->w, h = g->h;
+    if (w <= 0 || h <= 0 || w > u->W || h > u->H)
+        return fail(st, RN_ERR_INVALID, "frame %dx%d does not fit the network's %dx%d", w, h, u->W, u->H);
+    if (spp_full <= 0 || !(radius > 0.0f) || !(k >= 0.0f)) return fail(st, RN_ERR_INVALID, "spp %d radius %g k %g", spp_full, radius, k);
+    if (accel->device != ctx().device) return fail(st, RN_ERR_STATE, "accelerator built on another device");
+    cudaStream_t s = ctx().stream;
+    const size_t np = (size_t)w * h, npad = (size_t)u->W * u->H;
+    const int tx = (w + kTile - 1) / kTile, ty = (h + kTile - 1) / kTile;
+    void *p_ao4, *p_pred, *p_fb, *p_aofb, *p_st;
+    RN_TRY(ws_get(WS_SUR_AO4, np * 4, &p_ao4, st));
+    RN_TRY(ws_get(WS_SUR_PRED, npad * 4, &p_pred, st));
+    RN_TRY(ws_get(WS_SUR_FB, np + (size_t)tx * ty, &p_fb, st));
+    RN_TRY(ws_get(WS_SUR_AOFB, np * 4, &p_aofb, st));
+    RN_TRY(ws_get(WS_SUR_STATS, 16 + kDepthBlocks * 12, &p_st, st));
+    float* a4 = ao4_out ? ao4_out : (float*)p_ao4;
+    float* pr = (float*)p_pred;
+    uint8_t* fbm = (uint8_t*)p_fb;
+    uint8_t* tf = tile_flags ? tile_flags : fbm + np;
+    unsigned* counts = (unsigned*)p_st;
+    float* mean = (float*)p_st + 2;
+    double* psum = (double*)((char*)p_st + 16);
+    unsigned* pcnt = (unsigned*)(psum + kDepthBlocks);
+    RN_CUDA(cudaMemsetAsync(counts, 0, 8, s), st);
+    // 1. the 4-spp trace
+    RN_TRY(trace_ao_device(g->position, g->normal, g->mask, w, h, accel, kSppIn, radius, a4, st));
+    // 2. features straight into the network's input, 3. the network
+    depth_partial_kernel<<<kDepthBlocks, 256, 0, s>>>(depth, g->mask, np, psum, pcnt);
+    depth_mean_kernel<<<1, 32, 0, s>>>(psum, pcnt, kDepthBlocks, mean);
+    features_kernel<<<grid_for(npad), 256, 0, s>>>(depth, g->normal, g->mask, a4, w, h, u->W, u->H, mean, radius,
+                                                    u->T[T_IN]);
+    RN_TRY(forward_all(u, s, st));
+    head_kernel<<<(unsigned)((npad + 255) / 256), 256, 0, s>>>(u->T[14], u->wh, u->bh, npad, pr, nullptr, 0.0f, nullptr,
+                                                              nullptr, nullptr, nullptr);
+    // 4. the band test, 5. the fallback trace, 6. the composite
+    band_kernel<<<dim3(tx, ty), kTile * kTile, 0, s>>>(pr, u->W, a4, g->mask, w, h, k, tf, fbm, counts);
+    RN_TRY(trace_ao_device(g->position, g->normal, fbm, w, h, accel, spp_full, radius, (float*)p_aofb, st));
+    composite_kernel<<<grid_for(np), 256, 0, s>>>(pr, u->W, (const float*)p_aofb, g->mask, fbm, w, h, ao);
+    if (pred_out) RN_CUDA(cudaMemcpy2DAsync(pred_out, (size_t)w * 4, pr, (size_t)u->W * 4, (size_t)w * 4, h,
+                                            cudaMemcpyDeviceToDevice, s), st);
+    RN_CUDA(cudaGetLastError(), st);
+    unsigned hc[2] = {0, 0};
+    float hm = 0.0f;
+    RN_CUDA(cudaMemcpyAsync(hc, counts, 8, cudaMemcpyDeviceToHost, s), st);
+    RN_CUDA(cudaMemcpyAsync(&hm, mean, 4, cudaMemcpyDeviceToHost, s), st);
+    RN_TRY(check_device_error(st, "rn_surrogate_ao"));
+    if (stats) {
+        stats->tiles_covered = hc[0];
+        stats->tiles_fallback = hc[1];
+        stats->mean_depth = hm;
+        stats->reserved = 0.0f;
+    }
     return ok(st);
 }
 

@@ -34,7 +34,7 @@ EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_ac
            "rn_unet_free", "rn_unet_param_count", "rn_unet_forward", "rn_unet_train_step", "rn_unet_get_params",
            "rn_unet_set_params", "rn_unet_get_grads", "rn_unet_get_state", "rn_unet_set_state",
            "rn_unet_set_clip", "rn_unet_last_grad_norm",
-           "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3")
+           "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3", "rn_surrogate_ao")
 
 
 class RnError(RuntimeError):
@@ -51,6 +51,11 @@ class Status(C.Structure):
 class GBuf(C.Structure):
     _fields_ = [("w", C.c_int), ("h", C.c_int), ("position", C.c_void_p), ("normal", C.c_void_p),
                 ("mask", C.c_void_p)]
+
+
+class SurrogateStats(C.Structure):
+    _fields_ = [("tiles_covered", C.c_uint32), ("tiles_fallback", C.c_uint32), ("mean_depth", C.c_float),
+                ("reserved", C.c_float)]
 
 
 class View(C.Structure):
@@ -109,6 +114,8 @@ def lib() -> C.CDLL:
         L.rn_unet_set_state.argtypes = [vp, vp, C.c_uint64, st]
         L.rn_unet_set_clip.argtypes = [vp, C.c_float, st]
         L.rn_tune_set.argtypes = [C.c_char_p, C.c_int, st]
+        L.rn_surrogate_ao.argtypes = [vp, C.POINTER(GBuf), vp, vp, C.c_int, C.c_float, C.c_float, vp, vp, vp, vp,
+                                      C.POINTER(SurrogateStats), st]
         L.rn_tc_conv3x3.argtypes = [vp, C.c_int, vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int, C.c_int, vp, vp,
                                     vp, vp, C.c_int, st]
         L.rn_tune_get.argtypes = [C.c_char_p, C.POINTER(C.c_int), st]
@@ -603,6 +610,30 @@ class UNet:
             self.close()
         except Exception:
             pass
+
+
+def surrogate_ao(net: "UNet", g: GBuffer, depth, accel: LinearAccel, spp_full: int, radius: float = 1.0,
+                 k: float = 3.0, want_parts: bool = False):
+    """One AO frame by the surrogate (rn_surrogate_ao): returns (ao, stats dict) and, with
+    want_parts, also dict(ao4, pred, tile_flags). CUDA tensors; `net` has batch 1."""
+    import torch
+    h, w = g.shape
+    dev = g.mask.device
+    ao = torch.empty(h, w, device=dev)
+    parts = dict(ao4=torch.empty(h, w, device=dev), pred=torch.empty(h, w, device=dev),
+                 tile_flags=torch.empty((h + 15) // 16, (w + 15) // 16, device=dev, dtype=torch.uint8)) if want_parts else {}
+    args = _Args(g.position, g.normal, g.mask)
+    gb = _gbuf(g, args)
+    _use_torch_stream()
+    ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+    stt = SurrogateStats()
+    st = Status()
+    _check(lib().rn_surrogate_ao(net._h, C.byref(gb), ptr(depth), accel.handle, int(spp_full), float(radius), float(k),
+                                 ptr(ao), ptr(parts.get("ao4")), ptr(parts.get("pred")), ptr(parts.get("tile_flags")),
+                                 C.byref(stt), C.byref(st)), st)
+    stats = dict(tiles_covered=stt.tiles_covered, tiles_fallback=stt.tiles_fallback, mean_depth=stt.mean_depth,
+                 fallback_fraction=stt.tiles_fallback / max(1, stt.tiles_covered))
+    return (ao, stats, parts) if want_parts else (ao, stats)
 
 
 # The surrogate's layer table, for code that restates the network (tests): (cin, cout) of

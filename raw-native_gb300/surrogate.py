@@ -53,7 +53,8 @@ def features(g, depth, ao4, radius: float = RADIUS):
     """(H, W, 5) float32 CUDA features of a G-buffer, its depth and a 4-spp AO image."""
     import torch
     m = g.mask.bool()
-    mean = depth[m].mean() if bool(m.any()) else torch.zeros((), device=depth.device)
+    # the covered pixels' mean depth, summed in FP64 and rounded to FP32 (as rn_surrogate_ao)
+    mean = (depth[m].double().sum() / m.sum()).float() if bool(m.any()) else torch.zeros((), device=depth.device)
     f = torch.zeros(*g.mask.shape, 5, device=g.mask.device)
     f[..., 0] = torch.where(m, ((depth - mean) / radius).clamp(-32, 32) * 0.125, torch.zeros_like(depth))
     f[..., 1:4] = torch.where(m[..., None], g.normal, torch.zeros_like(g.normal))
