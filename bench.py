@@ -59,6 +59,7 @@ def parse():
                    help="4k: the benchmark (built-in scene, 3840x2160, 256 spp); batch: 64 orbit views of the "
                         "seeded 744k-triangle scene in one batch; large: 16 4K views of the 7.88M-triangle scene")
     p.add_argument("--views", type=int, default=0, help="batch/large: number of views (default 64 / 16)")
+    p.add_argument("--res", default="3840x2160", help="--profile unet: frame size WxH")
     return p.parse_args()
 
 
@@ -332,7 +333,8 @@ def run_profile(args):
     rn.init()
     if args.profile == "unet":
         import surrogate as S
-        net = rn.UNet(1, *S.padded_shape(2160, 3840), inference=True)
+        fw, fh = (int(v) for v in args.res.split("x"))
+        net = rn.UNet(1, *S.padded_shape(fh, fw), inference=True)
         S.load_weights(net, SURROGATE_WEIGHTS)
         x = torch.rand(1, *net.shape[1:], 5, device="cuda")
         for _ in range(args.warmup + args.steps):

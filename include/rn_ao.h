@@ -242,6 +242,7 @@ int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t*
  * Keys and values:
  *   trace_min_blocks  2 | 3 | 4      resident traversal blocks per SM (register budget)
  *   trace_frontier    0 | 1          per-warp frontier for AO-only walks
+ *   trace_frontier_min_spp 1|8|16|32 ... built only at this spp or more
  *   trace_packet      4 | 8 | 16     a warp's pixel packet: packet x (32 / packet)
  *   trace_stack       48 | 96        traversal stack entries (48 only where the tree allows)
  *   ssao_tile_h       4 | 8 | 16     SSAO tile 32 x h (the fused FP64 sum follows the tiling)

@@ -17,7 +17,8 @@ Workloads:
   ssao           the built-in scene at 4K: SSAO, 24 taps
   conv           the surrogate U-Net: a forward at 1088 x 1920 and a training step on
                  64 crops of 128 x 128
-The traversal keys are searched jointly (every combination); the SSAO and GEMM keys alone.
+  trace/low-spp  the synthetic scene's view at 4, 8, 16 and 32 spp (trace_frontier_min_spp)
+The traversal keys are searched jointly (every combination); the others one at a time.
 """
 from __future__ import annotations
 
@@ -97,6 +98,25 @@ def tune_trace(quick: bool, reps: int, log):
     return best["cfg"], rows
 
 
+def tune_frontier_min_spp(quick: bool, reps: int, log):
+    """The spp from which the per-warp frontier pays for its build: AO-only traces of the
+    synthetic scene at 4, 8, 16 and 32 spp; the candidate with the least total time."""
+    import torch
+    big = scenes.build_synthetic_scene(7, 500 if quick else 2000, 100 if quick else 500)
+    bt, bn = torch.from_numpy(big.tris).cuda(), torch.from_numpy(big.normals).cuda()
+    g = rn.rasterize(bt, bn, scenes.orbit_views(7, 8)[0][3], 1920, 1080)
+    acc = rn.LinearAccel(bt)
+    rows = []
+    for v in rn.TUNE_KEYS["trace_frontier_min_spp"]:
+        rn.tune_set("trace_frontier_min_spp", v)
+        ms = {"spp%d" % spp: _time(lambda: rn.compute_rtao(g, acc, spp, 1.0), reps) for spp in (4, 8, 16, 32)}
+        rows.append(dict(cfg={"trace_frontier_min_spp": v}, ms=ms, total=sum(ms.values())))
+        log("trace_frontier_min_spp %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    best = min(rows, key=lambda r: r["total"])
+    rn.tune_set("trace_frontier_min_spp", best["cfg"]["trace_frontier_min_spp"])
+    return best["cfg"], rows
+
+
 def tune_ssao(quick: bool, reps: int, log):
     import torch
     sc = scenes.build_test_scene()
@@ -173,6 +193,8 @@ def main(argv=None):
     log = lambda m: print(m, flush=True)
     cfg, report = {}, {}
     c, report["trace"] = tune_trace(a.quick, a.reps, log)
+    cfg.update(c)
+    c, report["frontier_min_spp"] = tune_frontier_min_spp(a.quick, a.reps, log)
     cfg.update(c)
     c, report["ssao"] = tune_ssao(a.quick, a.reps, log)
     cfg.update(c)

@@ -113,6 +113,7 @@ struct TuneKey {
 const TuneKey kTuneKeys[] = {
     {"trace_min_blocks", "RN_TUNE_TRACE_MIN_BLOCKS", &Tune::trace_min_blocks, {2, 3, 4}, 3},
     {"trace_frontier", "RN_TUNE_TRACE_FRONTIER", &Tune::trace_frontier, {0, 1}, 2},
+    {"trace_frontier_min_spp", "RN_TUNE_TRACE_FRONTIER_MIN_SPP", &Tune::trace_frontier_min_spp, {1, 8, 16, 32}, 4},
     {"trace_packet", "RN_TUNE_TRACE_PACKET", &Tune::trace_packet, {4, 8, 16}, 3},
     {"trace_stack", "RN_TUNE_TRACE_STACK", &Tune::trace_stack, {48, 96}, 2},
     {"ssao_tile_h", "RN_TUNE_SSAO_TILE_H", &Tune::ssao_tile_h, {4, 8, 16}, 3},
@@ -152,6 +153,22 @@ int packet_log2(int packet) { return packet == 4 ? 2 : packet == 16 ? 4 : 3; }
 
 }  // namespace
 
+TraceParams ao_trace_params(const float* pos, const float* nrm, const uint8_t* mask, int w, int h,
+                            const rn_accel* accel, int spp, float radius) {
+    Context& c = ctx();
+    TraceParams p{};
+    p.w = w; p.h = h;
+    p.pos = pos; p.nrm = nrm; p.mask = mask;
+    p.nodes = accel->d_nodes; p.tris = accel->d_tris;
+    p.has_geometry = accel->ntri > 0;
+    p.spp = spp; p.radius = radius;
+    p.lx = 0.0f; p.ly = 1.0f; p.lz = 0.0f;
+    p.corr = c.trig_corr;
+    p.err_word = c.dev_error;
+    apply_tune(p, accel);
+    return p;
+}
+
 int trace_ao_device(const float* pos, const float* nrm, const uint8_t* mask, int w, int h, const rn_accel* accel,
                     int spp, float radius, float* ao, rn_status* st) {
     Context& c = ctx();
@@ -173,7 +190,7 @@ int trace_ao_device(const float* pos, const float* nrm, const uint8_t* mask, int
 
 void apply_tune(TraceParams& p, const rn_accel* accel) {
     const Tune& t = ctx().tune;
-    p.frontier = t.trace_frontier;
+    p.frontier = t.trace_frontier && p.spp >= t.trace_frontier_min_spp;
     p.packet_log2 = packet_log2(t.trace_packet);
     p.stack_need = 16 + 3 * (int)(accel ? accel->depth : 0);
 }

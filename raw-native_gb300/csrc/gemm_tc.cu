@@ -18,6 +18,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <algorithm>
 #include <mutex>
 
 namespace rn {
@@ -229,47 +230,75 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
 
 
 // ------------------------------------------------------------------ implicit 3x3 convolution
-// Same roles as tc_gemm_kernel. CB is the channel block of one K step (64: 128-byte rows and
-// swizzle; 32: 64-byte rows and swizzle); a K step is (tap, source, channel block), taps
-// outermost, matching the weights' column order tap * Cin + ci.
+// A persistent kernel: each CTA walks work items (128-pixel tile, BN-column slice) with a
+// stride of the grid, keeping its barriers and TMEM across items. CB is the channel block of
+// one K step (64: 128-byte rows and swizzle; 32: 64-byte rows and swizzle); a K step is
+// (tap, source, channel block), taps outermost, matching the weights' column order
+// tap * Cin + ci. Roles (6 warps):
+//   - warp 0, lane 0: TMA producer over all items' K steps, through a ring of kSt stages;
+//   - warp 1, lane 0: MMA issuer; item i accumulates into TMEM buffer i & 1 (2 x BN columns),
+//     so the MMAs of item i + 1 run while the epilogue drains item i;
+//   - warps 2..5: epilogue; warp w reads TMEM lanes 32 (w % 4) .. +31 (its row quarter),
+//     then releases the buffer.
+// Every wait is bounded and also gives up when another role has aborted.
+constexpr int kConvThreads = 192;
+
 struct ConvArgs {
     int nsrc;
     int C0, C1;                 // channels of the sources
     int B, H, W, tw_log2;       // output (= input) geometry and tiling
     int tiles_x, tiles_y;       // tiles per image row / column
     int cin;                    // C0 + C1
+    int n_slices;               // N / BN
+    int items;                  // tiles x slices
     __nv_bfloat16* up16;        // optional 2x nearest-upsampled copy of the BF16 output
 };
 
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+    for (uint32_t i = 0; i < kSpin; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if ((i & 255u) == 255u && *abort_flag) return false;
+    }
+    return false;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 template <int BN, int CB>
-__global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const __grid_constant__ CUtensorMap map0,
-                                                              const __grid_constant__ CUtensorMap map1,
-                                                              const __grid_constant__ CUtensorMap mapW,
-                                                              const ConvArgs a, const Epilogue e) {
+__global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_constant__ CUtensorMap map0,
+                                                                  const __grid_constant__ CUtensorMap map1,
+                                                                  const __grid_constant__ CUtensorMap mapW,
+                                                                  const ConvArgs a, const Epilogue e) {
     constexpr int kSt = CB == 32 ? 8 : 4;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr uint32_t kABytes = kBM * CB * 2, kBBytes = BN * CB * 2;
-    constexpr uint32_t kCols = BN < 32 ? 32 : BN;
+    constexpr uint32_t kCols = 2 * BN;                       // two accumulator buffers
     uint8_t* sA = smem;
     uint8_t* sB = smem + kSt * kABytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kSt * kBBytes);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 1);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 4);
     __shared__ int s_abort;
+    volatile int* abort_flag = &s_abort;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tw = 1 << a.tw_log2, th = kBM >> a.tw_log2;
-    const int tile = blockIdx.x;
-    const int tx = tile % a.tiles_x, ty = (tile / a.tiles_x) % a.tiles_y, b = tile / (a.tiles_x * a.tiles_y);
-    const int x0 = tx * tw, y0 = ty * th, n0 = blockIdx.y * BN;
     const int nb0 = a.C0 / CB, nb1 = a.nsrc > 1 ? a.C1 / CB : 0, per_tap = nb0 + nb1;
     const int nkb = 9 * per_tap;
     auto full = [&](int s) { return smem_u32(&bars[s]); };
     auto empty = [&](int s) { return smem_u32(&bars[kSt + s]); };
-    const uint32_t done = smem_u32(&bars[2 * kSt]);
+    auto acc_full = [&](int b) { return smem_u32(&bars[2 * kSt + b]); };
+    auto acc_empty = [&](int b) { return smem_u32(&bars[2 * kSt + 2 + b]); };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kSt; ++s) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
-        mbar_init(done, 1);
+        for (int b = 0; b < 2; ++b) { mbar_init(acc_full(b), 1); mbar_init(acc_empty(b), 4); }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
@@ -284,89 +313,132 @@ __global__ void __launch_bounds__(kThreads, 1) tc_conv_kernel(const __grid_const
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    if (warp == 0 && lane == 0) {
-        int issued = 0;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % kSt;
-            const uint32_t ph = (uint32_t)(kb / kSt) & 1u;
-            if (!mbar_wait(empty(s), ph ^ 1u)) { atomicOr(e.err, DEV_GUARD); s_abort = 1; break; }
-            const int tap = kb / per_tap, r = kb % per_tap;
-            const bool second = r >= nb0;
-            const int cb = second ? r - nb0 : r;
-            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-            mbar_expect_tx(full(s), kABytes + kBBytes);
-            tma_load_4d(smem_u32(sA + s * kABytes), second ? &map1 : &map0, cb * CB, x0 + dx, y0 + dy, b, full(s));
-            tma_load_2d(smem_u32(sB + s * kBBytes), &mapW, tap * a.cin + (second ? a.C0 : 0) + cb * CB, n0, full(s));
-            ++issued;
+    if (warp == 0) {
+        // lane s < kSt owns stage s: it issues K steps kc = s, s + kSt, ... of this CTA's
+        // sequence (items blockIdx.x, + gridDim.x, ...; nkb steps each), waiting for each
+        // previous use of its stage in order, so the stages fill in parallel
+        if (lane < kSt) {
+            const int my_items = a.items > (int)blockIdx.x ? (a.items - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+            const uint32_t total = (uint32_t)my_items * (uint32_t)nkb;
+            uint32_t last = 0xFFFFFFFFu;
+            for (uint32_t kc = lane; kc < total; kc += kSt) {
+                const uint32_t ph = (kc / kSt) & 1u;
+                if (!mbar_wait_or_abort(empty(lane), ph ^ 1u, abort_flag)) {
+                    atomicOr(e.err, DEV_GUARD);
+                    s_abort = 1;
+                    break;
+                }
+                const int item = (int)blockIdx.x + (int)(kc / nkb) * (int)gridDim.x, kb = (int)(kc % nkb);
+                const int tile = item / a.n_slices, n0 = (item % a.n_slices) * BN;
+                const int tx = tile % a.tiles_x, ty = (tile / a.tiles_x) % a.tiles_y, b = tile / (a.tiles_x * a.tiles_y);
+                const int tap = kb / per_tap, r = kb % per_tap;
+                const bool second = r >= nb0;
+                const int cb = second ? r - nb0 : r;
+                mbar_expect_tx(full(lane), kABytes + kBBytes);
+                tma_load_4d(smem_u32(sA + lane * kABytes), second ? &map1 : &map0, cb * CB, tx * tw + tap % 3 - 1,
+                            ty * th + tap / 3 - 1, b, full(lane));
+                tma_load_2d(smem_u32(sB + lane * kBBytes), &mapW, tap * a.cin + (second ? a.C0 : 0) + cb * CB, n0,
+                            full(lane));
+                last = kc;
+            }
+            // the copies this lane issued must land before the CTA can leave
+            if (last != 0xFFFFFFFFu) mbar_wait(full(lane), (last / kSt) & 1u);
         }
-        for (int kb = issued > kSt ? issued - kSt : 0; kb < issued; ++kb)
-            mbar_wait(full(kb % kSt), (uint32_t)(kb / kSt) & 1u);
-    } else if (warp == 1 && lane == 0) {
-        const uint32_t idesc = instr_desc(BN);
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % kSt;
-            const uint32_t ph = (uint32_t)(kb / kSt) & 1u;
-            if (!mbar_wait(full(s), ph)) { atomicOr(e.err, DEV_GUARD); s_abort = 1; break; }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = instr_desc(BN);
+            uint32_t kc = 0, i = 0;
+            for (int item = blockIdx.x; item < a.items && !*abort_flag; item += gridDim.x, ++i) {
+                const uint32_t buf = i & 1u, use = i >> 1;
+                if (!mbar_wait_or_abort(acc_empty(buf), (use & 1u) ^ 1u, abort_flag)) {
+                    atomicOr(e.err, DEV_GUARD);
+                    s_abort = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t acc = tmem + buf * BN;
+                bool ok = true;
+                for (int kb = 0; kb < nkb; ++kb, ++kc) {
+                    const int s = kc % kSt;
+                    const uint32_t ph = (kc / kSt) & 1u;
+                    if (!mbar_wait_or_abort(full(s), ph, abort_flag)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t a0 = smem_u32(sA + s * kABytes), b0 = smem_u32(sB + s * kBBytes);
+#pragma unroll
+                    for (int k = 0; k < CB / 16; ++k) {
+                        const uint64_t da = CB == 64 ? smem_desc(a0 + k * 32) : smem_desc64(a0 + k * 32);
+                        const uint64_t db = CB == 64 ? smem_desc(b0 + k * 32) : smem_desc64(b0 + k * 32);
+                        tc_mma(acc, da, db, idesc, (kb | k) != 0 ? 1u : 0u);
+                    }
+                    tc_commit(empty(s));
+                }
+                if (!ok) {
+                    atomicOr(e.err, DEV_GUARD);
+                    s_abort = 1;
+                    break;
+                }
+                tc_commit(acc_full(buf));
+            }
+        }
+    } else {
+        // epilogue warps 2..5: TMEM lane quarter q = warp % 4 holds rows 32 q .. 32 q + 31
+        const int q = warp & 3;
+        const int r = q * 32 + lane;
+        uint32_t i = 0;
+        for (int item = blockIdx.x; item < a.items; item += gridDim.x, ++i) {
+            const uint32_t buf = i & 1u, use = i >> 1;
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_or_abort(acc_full(buf), use & 1u, abort_flag));
+            if (!ok) {
+                if (lane == 0) { atomicOr(e.err, DEV_GUARD); s_abort = 1; }
+                break;
+            }
             tc_fence_after();
-            const uint32_t a0 = smem_u32(sA + s * kABytes), b0 = smem_u32(sB + s * kBBytes);
-#pragma unroll
-            for (int k = 0; k < CB / 16; ++k) {
-                const uint64_t da = CB == 64 ? smem_desc(a0 + k * 32) : smem_desc64(a0 + k * 32);
-                const uint64_t db = CB == 64 ? smem_desc(b0 + k * 32) : smem_desc64(b0 + k * 32);
-                tc_mma(tmem, da, db, idesc, (kb | k) != 0 ? 1u : 0u);
-            }
-            tc_commit(empty(s));
-        }
-        tc_commit(done);
-    }
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));
-    tc_fence_after();
-    if (!ok && lane == 0) atomicOr(e.err, DEV_GUARD);
-    const int abort_warp = __shfl_sync(0xffffffffu, *(volatile int*)&s_abort, 0);
-    if (ok && !abort_warp) {
-        const int r = warp * 32 + lane;
-        const int y = y0 + (r >> a.tw_log2), x = x0 + (r & (tw - 1));
-        const size_t pix = ((size_t)b * a.H + y) * a.W + x;
-        const uint32_t tbase = tmem + ((uint32_t)(warp * 32) << 16);
+            const int tile = item / a.n_slices, n0 = (item % a.n_slices) * BN;
+            const int tx = tile % a.tiles_x, ty = (tile / a.tiles_x) % a.tiles_y, b = tile / (a.tiles_x * a.tiles_y);
+            const int y = ty * th + (r >> a.tw_log2), x = tx * tw + (r & (tw - 1));
+            const size_t pix = ((size_t)b * a.H + y) * a.W + x;
+            const uint32_t tbase = tmem + buf * BN + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 16) {
-            uint32_t v[16];
-            tmem_ld16(tbase + (uint32_t)c0, v);
-            float f[16];
-            const int col = n0 + c0;
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                uint32_t v[16];
+                tmem_ld16(tbase + (uint32_t)c0, v);
+                float f[16];
+                const int col = n0 + c0;
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                float q = __uint_as_float(v[j]);
-                if (e.bias) q += e.bias[col + j];
-                if (e.relu) q = fmaxf(q, 0.0f);
-                f[j] = q;
-            }
-            const size_t o = pix * e.ldc + col;
-            if (e.c16 || a.up16) {
-                uint4 out[2];
-                __nv_bfloat16* ob = reinterpret_cast<__nv_bfloat16*>(out);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) ob[j] = __float2bfloat16_rn(f[j]);
+                for (int j = 0; j < 16; ++j) {
+                    float t = __uint_as_float(v[j]);
+                    if (e.bias) t += e.bias[col + j];
+                    if (e.relu) t = fmaxf(t, 0.0f);
+                    f[j] = t;
+                }
+                const size_t o = pix * e.ldc + col;
                 if (e.c16) {
+                    uint4 out[2];
+                    __nv_bfloat16* ob = reinterpret_cast<__nv_bfloat16*>(out);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) ob[j] = __float2bfloat16_rn(f[j]);
                     uint4* d4 = reinterpret_cast<uint4*>(e.c16 + o);
                     d4[0] = out[0];
                     d4[1] = out[1];
-                }
-                if (a.up16) {
+                    if (a.up16) {
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const size_t up = ((size_t)b * 2 * a.H + 2 * y + (q >> 1)) * (2 * a.W) + 2 * x + (q & 1);
-                        uint4* d4 = reinterpret_cast<uint4*>(a.up16 + up * e.ldc + col);
-                        d4[0] = out[0];
-                        d4[1] = out[1];
+                        for (int u = 0; u < 4; ++u) {
+                            const size_t up = ((size_t)b * 2 * a.H + 2 * y + (u >> 1)) * (2 * a.W) + 2 * x + (u & 1);
+                            uint4* d = reinterpret_cast<uint4*>(a.up16 + up * e.ldc + col);
+                            d[0] = out[0];
+                            d[1] = out[1];
+                        }
                     }
                 }
-            }
-            if (e.c32) {
-                float4* d4 = reinterpret_cast<float4*>(e.c32 + o);
+                if (e.c32) {
+                    float4* d4 = reinterpret_cast<float4*>(e.c32 + o);
 #pragma unroll
-                for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
+                    for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
+                }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty(buf));
         }
     }
     tc_fence_before();
@@ -433,18 +505,25 @@ bool make_map_nhwc(CUtensorMap* m, const void* base, int B, int H, int W, int C,
 
 template <int BN, int CB>
 int launch_conv(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap& mw, const ConvArgs& a,
-                const Epilogue& e, int N, cudaStream_t s) {
+                const Epilogue& e, cudaStream_t s) {
     constexpr int kSt = CB == 32 ? 8 : 4;
-    const size_t smem = 1024 + kSt * (kBM * CB * 2 + BN * CB * 2) + (2 * kSt + 1) * 8 + 16;
-    static bool attr = false;
-    if (!attr) {
+    const size_t smem = 1024 + kSt * (kBM * CB * 2 + BN * CB * 2) + (2 * kSt + 4) * 8 + 16;
+    static int per_sm = 0;
+    if (!per_sm) {
         if (cudaFuncSetAttribute(tc_conv_kernel<BN, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
+                cudaSuccess ||
+            cudaFuncSetAttribute(tc_conv_kernel<BN, CB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return RN_ERR_CUDA;
-        attr = true;
+        // residency: shared memory (228 KB per SM, 1 KB reserved per CTA), TMEM (512 columns per
+        // SM, 2 x BN per CTA) and at most 3 CTAs of 192 threads and 88 registers
+        int smem_sm = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx().device);
+        const int by_smem = smem_sm / (int)(smem + 1024);
+        per_sm = std::max(1, std::min(std::min(by_smem, 512 / (2 * BN)), 3));
     }
-    const dim3 grid((unsigned)(a.tiles_x * a.tiles_y * a.B), (unsigned)(N / BN));
-    tc_conv_kernel<BN, CB><<<grid, kThreads, smem, s>>>(m0, m1, mw, a, e);
+    const int ctas = std::min(a.items, per_sm * ctx().sm_count);
+    tc_conv_kernel<BN, CB><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 
@@ -542,12 +621,14 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     a.B = B; a.H = H; a.W = W; a.tw_log2 = t.tw_log2;
     a.tiles_x = W / tw; a.tiles_y = H / th;
     a.cin = cin;
+    a.n_slices = N / bn;
+    a.items = a.tiles_x * a.tiles_y * B * a.n_slices;
     a.up16 = up16;
     int rc;
 #define RN_CONV_CASE(BNV)                                                                             \
     case BNV:                                                                                         \
-        rc = cb == 64 ? tc::launch_conv<BNV, 64>(m[0], m[1], mw, a, epi, N, s)                        \
-                      : tc::launch_conv<BNV, 32>(m[0], m[1], mw, a, epi, N, s);                       \
+        rc = cb == 64 ? tc::launch_conv<BNV, 64>(m[0], m[1], mw, a, epi, s)                           \
+                      : tc::launch_conv<BNV, 32>(m[0], m[1], mw, a, epi, s);                          \
         break;
     switch (bn) {
         RN_CONV_CASE(32)

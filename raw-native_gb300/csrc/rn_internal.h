@@ -40,6 +40,7 @@ enum Slot {
 struct Tune {
     int trace_min_blocks = 3;   // resident 256-thread traversal blocks per SM: 2, 3 or 4
     int trace_frontier = 1;     // per-warp frontier for AO-only walks
+    int trace_frontier_min_spp = 16;  // ... built only when spp reaches this (its cost is per packet)
     int trace_packet = 8;       // a warp's pixel packet: trace_packet x (32 / trace_packet); 4, 8 or 16
     int trace_stack = 96;       // traversal stack entries: 48 or 96 (48 only where the tree's depth allows)
     int ssao_tile_h = 8;        // SSAO tile: 32 x ssao_tile_h pixels, one thread each; 4, 8 or 16
@@ -183,6 +184,13 @@ struct TraceParams {
 // image, on the library's stream.
 int trace_ao_device(const float* pos, const float* nrm, const uint8_t* mask, int w, int h, const rn_accel* accel,
                     int spp, float radius, float* ao, rn_status* st);
+// AO-only sample-parallel trace of the pixels list[0 .. *count) (indices into the frame,
+// count on the device): open[px] += open rays of pixel px (the caller zeroes `open`).
+int launch_ao_samples(const TraceParams& p, const uint32_t* list, const uint32_t* count, uint32_t* open,
+                      int sm_count, cudaStream_t s);
+// TraceParams for an AO-only trace of a device G-buffer with the library's sampler and tuning.
+TraceParams ao_trace_params(const float* pos, const float* nrm, const uint8_t* mask, int w, int h,
+                            const rn_accel* accel, int spp, float radius);
 // The tuned trace fields of p (frontier, packet, stack bound for this tree).
 void apply_tune(TraceParams& p, const rn_accel* accel);
 int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned long long* counts = nullptr,

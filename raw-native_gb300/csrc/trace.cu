@@ -75,7 +75,49 @@ __global__ void occluded_kernel(const Node4* __restrict__ nodes, const LeafTri* 
     hit[i] = (has_geometry && walk<false>(nodes, tris, o, d, tm, tm, err, cn) != 0) ? 1 : 0;
 }
 
+// AO of listed pixels with one thread per (pixel, sample): the same rays and hit rule as
+// trace_pixel (AO only), for pixel sets too small or too uneven to keep packets of pixels
+// busy (the surrogate's fallback tiles). open[list[i]] receives pixel list[i]'s open rays,
+// added by one atomic per warp and pixel.
+__global__ void __launch_bounds__(256) ao_samples_kernel(const __grid_constant__ TraceParams p,
+                                                         const uint32_t* __restrict__ list,
+                                                         const uint32_t* __restrict__ count,
+                                                         uint32_t* __restrict__ open) {
+    const uint64_t total = (uint64_t)(*count) * (uint32_t)p.spp;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t base = (uint64_t)blockIdx.x * blockDim.x;
+    Counts cn;
+    // whole warps step together, so the per-warp vote below sees every lane
+    for (uint64_t w0 = base; w0 < total; w0 += stride) {
+        const uint64_t w = w0 + threadIdx.x;
+        const bool valid = w < total;
+        uint32_t px = 0xFFFFFFFFu;
+        int o = 0;
+        if (valid) {
+            px = list[w / (uint32_t)p.spp];
+            const uint32_t s = (uint32_t)(w % (uint32_t)p.spp);
+            const uint32_t x = px % (uint32_t)p.w, y = px / (uint32_t)p.w;
+            const v3 P = load3(p.pos + 3 * (size_t)px), n = load3(p.nrm + 3 * (size_t)px);
+            const v3 a = fabsf(n.x) > 0.9f ? mk(0.0f, 1.0f, 0.0f) : mk(1.0f, 0.0f, 0.0f);
+            const v3 t = normalize(cross(a, n)), b = cross(n, t);
+            const v3 origin = add(P, scale(n, 1e-3f));
+            const v3 dir = sample_direction(t, b, n, x, y, s, p.corr);
+            const int h = p.has_geometry ? walk<false>(p.nodes, p.tris, origin, dir, p.radius, p.radius, p.err_word, cn) : 0;
+            o = (h & HIT_NEAR) ? 0 : 1;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, px);
+        const int sum = __popc(__ballot_sync(0xffffffffu, o) & peers);
+        if (valid && (__ffs(peers) - 1) == (int)(threadIdx.x & 31u) && sum) atomicAdd(open + px, (uint32_t)sum);
+    }
+}
+
 }  // namespace
+
+int launch_ao_samples(const TraceParams& p, const uint32_t* list, const uint32_t* count, uint32_t* open,
+                      int sm_count, cudaStream_t s) {
+    ao_samples_kernel<<<sm_count * 8, 256, 0, s>>>(p, list, count, open);
+    return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
+}
 
 // Residency variants: the register budget decides how many 256-thread blocks share an SM
 // (2: up to 128 registers, 3: 80, 4: 64, with spills to L1). The launch uses enough

@@ -229,6 +229,22 @@ __device__ __forceinline__ int tile_frontier(const TraceParams& p, int x, int y,
     return n;
 }
 
+// Hemisphere direction of sample s of pixel (ux, uy) with frame (t, b, n): the arithmetic of
+// trace_pixel's loop below (src/renderer/ray_ao.cpp:30-37), for callers that trace one
+// sample per thread.
+__device__ __forceinline__ v3 sample_direction(const v3& t, const v3& b, const v3& n, uint32_t ux, uint32_t uy,
+                                               uint32_t s, const uint8_t* __restrict__ corr) {
+    const uint32_t k2 = hash24(ux, uy, 2u * s + 1u);
+    const float u1 = unit24(hash24(ux, uy, 2u * s));
+    float c, sn;
+    angle_sincos(sample_angle(k2), sn, c);
+    if (corr) apply_corr(__ldg(corr + k2), c, sn);
+    const float r = fsqrt(u1);
+    const float lx = fmul(r, c), ly = fmul(r, sn);
+    const float lz = fsqrt(smax(0.0f, fsub(1.0f, u1)));
+    return normalize(add(add(scale(t, lx), scale(b, ly)), scale(n, lz)));
+}
+
 // One pixel: its spp cosine-weighted rays (AO and, when asked, the sky), then the sun ray.
 template <bool kCount, int kStackN = kStack>
 __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, const v3& toLight, Counts& cn,

@@ -360,7 +360,8 @@ __global__ void __launch_bounds__(kTile * kTile) band_kernel(const float* __rest
                                                               const uint8_t* __restrict__ mask, int w, int h, float k,
                                                               uint8_t* __restrict__ tile_flag,
                                                               uint8_t* __restrict__ fb_mask,
-                                                              unsigned* __restrict__ counts) {
+                                                              unsigned* __restrict__ counts,
+                                                              uint32_t* __restrict__ fb_list) {
     const int x = blockIdx.x * kTile + (threadIdx.x % kTile), y = blockIdx.y * kTile + (threadIdx.x / kTile);
     const bool in = x < w && y < h;
     const size_t p = (size_t)y * w + x;
@@ -396,16 +397,18 @@ __global__ void __launch_bounds__(kTile * kTile) band_kernel(const float* __rest
     }
     __syncthreads();
     if (in) fb_mask[p] = (uint8_t)(cov && s_flag);
+    if (cov && s_flag) fb_list[atomicAdd(counts + 2, 1u)] = (uint32_t)p;
 }
 
-// ao = 1 off the coverage, the traced value on fallback pixels, the prediction elsewhere.
-__global__ void composite_kernel(const float* __restrict__ pred, int W, const float* __restrict__ traced,
+// ao = 1 off the coverage, the traced AO (open rays / spp, as the trace divides) on fallback
+// pixels, the prediction elsewhere.
+__global__ void composite_kernel(const float* __restrict__ pred, int W, const uint32_t* __restrict__ open, int spp,
                                  const uint8_t* __restrict__ mask, const uint8_t* __restrict__ fb, int w, int h,
                                  float* __restrict__ ao) {
     const size_t total = (size_t)w * h;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % w), y = (int)(i / w);
-        ao[i] = !mask[i] ? 1.0f : fb[i] ? traced[i] : pred[(size_t)y * W + x];
+        ao[i] = !mask[i] ? 1.0f : fb[i] ? __fdiv_rn((float)open[i], (float)spp) : pred[(size_t)y * W + x];
     }
 }
 
@@ -825,17 +828,20 @@ int rn_surrogate_ao(rn_unet* u, const rn_gbuf* g, const float* depth, const rn_a
     RN_TRY(ws_get(WS_SUR_AO4, np * 4, &p_ao4, st));
     RN_TRY(ws_get(WS_SUR_PRED, npad * 4, &p_pred, st));
     RN_TRY(ws_get(WS_SUR_FB, np + (size_t)tx * ty, &p_fb, st));
-    RN_TRY(ws_get(WS_SUR_AOFB, np * 4, &p_aofb, st));
+    RN_TRY(ws_get(WS_SUR_AOFB, np * 8, &p_aofb, st));          // open-ray counts, then the pixel list
     RN_TRY(ws_get(WS_SUR_STATS, 16 + kDepthBlocks * 12, &p_st, st));
     float* a4 = ao4_out ? ao4_out : (float*)p_ao4;
     float* pr = (float*)p_pred;
     uint8_t* fbm = (uint8_t*)p_fb;
     uint8_t* tf = tile_flags ? tile_flags : fbm + np;
-    unsigned* counts = (unsigned*)p_st;
-    float* mean = (float*)p_st + 2;
+    unsigned* counts = (unsigned*)p_st;          // covered tiles, fallback tiles, fallback pixels
+    float* mean = (float*)p_st + 3;
     double* psum = (double*)((char*)p_st + 16);
+    uint32_t* open = (uint32_t*)p_aofb;
+    uint32_t* fb_list = open + np;
     unsigned* pcnt = (unsigned*)(psum + kDepthBlocks);
-    RN_CUDA(cudaMemsetAsync(counts, 0, 8, s), st);
+    RN_CUDA(cudaMemsetAsync(counts, 0, 12, s), st);
+    RN_CUDA(cudaMemsetAsync(open, 0, np * 4, s), st);
     // 1. the 4-spp trace
     RN_TRY(trace_ao_device(g->position, g->normal, g->mask, w, h, accel, kSppIn, radius, a4, st));
     // 2. features straight into the network's input, 3. the network
@@ -847,15 +853,19 @@ int rn_surrogate_ao(rn_unet* u, const rn_gbuf* g, const float* depth, const rn_a
     head_kernel<<<(unsigned)((npad + 255) / 256), 256, 0, s>>>(u->T[14], u->wh, u->bh, npad, pr, nullptr, 0.0f, nullptr,
                                                               nullptr, nullptr, nullptr);
     // 4. the band test, 5. the fallback trace, 6. the composite
-    band_kernel<<<dim3(tx, ty), kTile * kTile, 0, s>>>(pr, u->W, a4, g->mask, w, h, k, tf, fbm, counts);
-    RN_TRY(trace_ao_device(g->position, g->normal, fbm, w, h, accel, spp_full, radius, (float*)p_aofb, st));
-    composite_kernel<<<grid_for(np), 256, 0, s>>>(pr, u->W, (const float*)p_aofb, g->mask, fbm, w, h, ao);
+    band_kernel<<<dim3(tx, ty), kTile * kTile, 0, s>>>(pr, u->W, a4, g->mask, w, h, k, tf, fbm, counts, fb_list);
+    // the fallback pixels' rays, one thread per (pixel, sample): a few tiles' worth of work
+    // spreads over the whole GPU instead of a few warps
+    const TraceParams tp = ao_trace_params(g->position, g->normal, fbm, w, h, accel, spp_full, radius);
+    if (launch_ao_samples(tp, fb_list, counts + 2, open, ctx().sm_count, s) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "ao_samples_kernel");
+    composite_kernel<<<grid_for(np), 256, 0, s>>>(pr, u->W, open, spp_full, g->mask, fbm, w, h, ao);
     if (pred_out) RN_CUDA(cudaMemcpy2DAsync(pred_out, (size_t)w * 4, pr, (size_t)u->W * 4, (size_t)w * 4, h,
                                             cudaMemcpyDeviceToDevice, s), st);
     RN_CUDA(cudaGetLastError(), st);
-    unsigned hc[2] = {0, 0};
+    unsigned hc[3] = {0, 0, 0};
     float hm = 0.0f;
-    RN_CUDA(cudaMemcpyAsync(hc, counts, 8, cudaMemcpyDeviceToHost, s), st);
+    RN_CUDA(cudaMemcpyAsync(hc, counts, 12, cudaMemcpyDeviceToHost, s), st);
     RN_CUDA(cudaMemcpyAsync(&hm, mean, 4, cudaMemcpyDeviceToHost, s), st);
     RN_TRY(check_device_error(st, "rn_surrogate_ao"));
     if (stats) {
