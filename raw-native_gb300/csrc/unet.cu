@@ -56,6 +56,7 @@ struct Im2col {
     const bf16* s1; int c1; int up1;
     int B, H, W, kpad;
     bf16* out;
+    int ld0;                    // channels stored per pixel of s0 (0: c0)
 };
 // One thread per (row, 8 consecutive columns): a group never straddles a tap or a source
 // because every channel count is a multiple of 8.
@@ -74,7 +75,8 @@ __global__ void im2col_kernel(const Im2col a) {
             if (yy >= 0 && yy < a.H && xx >= 0 && xx < a.W) {
                 const bool first = ci < a.c0;
                 const bf16* s = first ? a.s0 : a.s1;
-                const int C = first ? a.c0 : a.c1, c = first ? ci : ci - a.c0, up = first ? a.up0 : a.up1;
+                const int C = first ? (a.ld0 ? a.ld0 : a.c0) : a.c1, c = first ? ci : ci - a.c0,
+                          up = first ? a.up0 : a.up1;
                 const int h = up ? a.H / 2 : a.H, w = up ? a.W / 2 : a.W;
                 const int sy = up ? yy >> 1 : yy, sx = up ? xx >> 1 : xx;
                 v = *reinterpret_cast<const uint4*>(s + (((size_t)b * h + sy) * w + sx) * C + c);
@@ -93,17 +95,30 @@ __global__ void transpose_kernel(const bf16* __restrict__ in, int R, int Cc, bf1
     for (int j = threadIdx.y; j < 32; j += 8) out[(size_t)(c0 + j) * R + r0 + threadIdx.x] = tile[threadIdx.x][j];
 }
 
+// 2x2 average pool, 8 channels (16 bytes) per thread; the sum order (top-left, top-right,
+// bottom-left, bottom-right) is fixed.
 __global__ void pool_kernel(const bf16* __restrict__ in, int B, int H, int W, int C, bf16* __restrict__ out) {
-    const int h = H / 2, w = W / 2;
-    const size_t total = (size_t)B * h * w * C;
+    const int h = H / 2, w = W / 2, G = C / 8;
+    const size_t total = (size_t)B * h * w * G;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const size_t p = i / C;
+        const int c = (int)(i % G) * 8;
+        const size_t p = i / G;
         const int x = (int)(p % w), y = (int)((p / w) % h), b = (int)(p / ((size_t)w * h));
         const size_t base = (((size_t)b * H + 2 * y) * W + 2 * x) * C + c;
-        const float s = __bfloat162float(in[base]) + __bfloat162float(in[base + C]) +
-                        __bfloat162float(in[base + (size_t)W * C]) + __bfloat162float(in[base + (size_t)W * C + C]);
-        out[i] = __float2bfloat16_rn(0.25f * s);
+        uint4 q[4] = {*reinterpret_cast<const uint4*>(in + base), *reinterpret_cast<const uint4*>(in + base + C),
+                      *reinterpret_cast<const uint4*>(in + base + (size_t)W * C),
+                      *reinterpret_cast<const uint4*>(in + base + (size_t)W * C + C)};
+        uint4 o;
+        bf16* ob = reinterpret_cast<bf16*>(&o);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float s = __bfloat162float(reinterpret_cast<const bf16*>(&q[0])[j]) +
+                            __bfloat162float(reinterpret_cast<const bf16*>(&q[1])[j]) +
+                            __bfloat162float(reinterpret_cast<const bf16*>(&q[2])[j]) +
+                            __bfloat162float(reinterpret_cast<const bf16*>(&q[3])[j]);
+            ob[j] = __float2bfloat16_rn(0.25f * s);
+        }
+        *reinterpret_cast<uint4*>(out + p * C + c) = o;
     }
 }
 
@@ -200,14 +215,25 @@ __global__ void head_kernel(const bf16* __restrict__ d0, const float* __restrict
     }
 }
 
-// fp32 features [M][5] -> bf16 [M][8] (zero-padded channels)
-__global__ void input_kernel(const float* __restrict__ in, size_t M, bf16* __restrict__ out) {
+// fp32 features [M][5] -> bf16 [M][C] (C = 8 or 32; channels 5.. zero)
+__global__ void input_kernel(const float* __restrict__ in, size_t M, int C, bf16* __restrict__ out) {
     for (size_t m = (size_t)blockIdx.x * blockDim.x + threadIdx.x; m < M; m += (size_t)gridDim.x * blockDim.x) {
         uint4 v;
         bf16* h = reinterpret_cast<bf16*>(&v);
         for (int c = 0; c < 8; ++c) h[c] = __float2bfloat16_rn(c < 5 ? in[m * 5 + c] : 0.0f);
-        *reinterpret_cast<uint4*>(out + m * 8) = v;
+        uint4* o = reinterpret_cast<uint4*>(out + m * C);
+        o[0] = v;
+        for (int q = 1; q < C / 8; ++q) o[q] = make_uint4(0, 0, 0, 0);
     }
+}
+
+// The first convolution's weights in the 32-channel input layout of the implicit path:
+// w0[co][tap * 32 + ci] = wq[co][tap * 8 + ci] (ci < 8; the other columns stay zero).
+__global__ void expand_w0_kernel(const bf16* __restrict__ wq, int kpad, bf16* __restrict__ w0, int kpad0, int cout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cout * 72) return;
+    const int co = i / 72, k = i % 72, tap = k / 8, ci = k % 8;
+    w0[(size_t)co * kpad0 + tap * 32 + ci] = wq[(size_t)co * kpad + k];
 }
 
 struct AdamArgs { float lr, b1, b2, eps, c1, c2; const float* scale; };
@@ -328,7 +354,7 @@ __global__ void depth_mean_kernel(const double* __restrict__ part_sum, const uns
 // uncovered and padding pixels (channels 5..7 zero).
 __global__ void features_kernel(const float* __restrict__ depth, const float* __restrict__ nrm,
                                 const uint8_t* __restrict__ mask, const float* __restrict__ ao4, int w, int h, int W,
-                                int H, const float* __restrict__ mean, float radius, bf16* __restrict__ out) {
+                                int H, const float* __restrict__ mean, float radius, int C, bf16* __restrict__ out) {
     const size_t total = (size_t)W * H;
     const float mu = *mean;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
@@ -348,7 +374,9 @@ __global__ void features_kernel(const float* __restrict__ depth, const float* __
         bf16* hb = reinterpret_cast<bf16*>(&v);
 #pragma unroll
         for (int c = 0; c < 5; ++c) hb[c] = __float2bfloat16_rn(f[c]);
-        *reinterpret_cast<uint4*>(out + i * 8) = v;
+        uint4* o = reinterpret_cast<uint4*>(out + i * C);
+        o[0] = v;
+        for (int q = 1; q < C / 8; ++q) o[q] = make_uint4(0, 0, 0, 0);
     }
 }
 
@@ -428,6 +456,8 @@ struct rn_unet {
     bool inference = false;       // forward only: one shared im2col buffer, no gradient storage
     bool implicit = false;        // 3x3 convolutions of >= 32 input channels on the implicit GEMM
     bf16* UT[T_COUNT] = {};       // implicit: 2x upsampled copies of the tensors read upsampled
+    bf16* wq0 = nullptr;          // implicit: the first convolution's weights for a 32-channel input
+    int kpad0 = 0;
     // per layer
     struct Layer {
         int level, cin, cout, kpad, kpad_t, cin_pad;
@@ -470,7 +500,17 @@ int conv_forward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
     const LayerSpec& sp = kSpec[l];
     const int H = u->H >> Ly.level, W = u->W >> Ly.level;
     const size_t M = pixels(u, Ly.level);
-    if (u->implicit && l > 0) {
+    if (u->implicit && l == 0) {          // the input is stored with 32 channels (5 used)
+        const tc::ConvSrc src{u->T[T_IN], u->TC[T_IN]};
+        tc::Epilogue e{};
+        e.ldc = Ly.cout;
+        e.c16 = u->T[1];
+        e.bias = Ly.b;
+        e.relu = 1;
+        e.err = ctx().dev_error;
+        return tc_conv3x3(&src, 1, u->B, H, W, u->wq0, u->kpad0, Ly.cout, e, nullptr, s, st);
+    }
+    if (u->implicit) {
         tc::ConvSrc src[2] = {{u->T[sp.s0.tensor], u->TC[sp.s0.tensor]}, {nullptr, 0}};
         if (sp.nsrc == 2) src[1] = {sp.s1.up ? u->UT[sp.s1.tensor] : u->T[sp.s1.tensor], u->TC[sp.s1.tensor]};
         tc::Epilogue e{};
@@ -495,9 +535,9 @@ int conv_forward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
 
 int forward_all(rn_unet* u, cudaStream_t s, rn_status* st) {
     for (int l = 0; l < kLayers; ++l) {
-        if (l == 2) pool_kernel<<<grid_for(pixels(u, 1) * 32), 256, 0, s>>>(u->T[2], u->B, u->H, u->W, 32, u->T[T_P0]);
-        if (l == 4) pool_kernel<<<grid_for(pixels(u, 2) * 64), 256, 0, s>>>(u->T[4], u->B, u->H >> 1, u->W >> 1, 64, u->T[T_P1]);
-        if (l == 6) pool_kernel<<<grid_for(pixels(u, 3) * 128), 256, 0, s>>>(u->T[6], u->B, u->H >> 2, u->W >> 2, 128, u->T[T_P2]);
+        if (l == 2) pool_kernel<<<grid_for(pixels(u, 1) * 4), 256, 0, s>>>(u->T[2], u->B, u->H, u->W, 32, u->T[T_P0]);
+        if (l == 4) pool_kernel<<<grid_for(pixels(u, 2) * 8), 256, 0, s>>>(u->T[4], u->B, u->H >> 1, u->W >> 1, 64, u->T[T_P1]);
+        if (l == 6) pool_kernel<<<grid_for(pixels(u, 3) * 16), 256, 0, s>>>(u->T[6], u->B, u->H >> 2, u->W >> 2, 128, u->T[T_P2]);
         RN_TRY(conv_forward(u, l, s, st));
     }
     return RN_OK;
@@ -515,6 +555,7 @@ int conv_backward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
         // the forward left no im2col rows: form this layer's now (one shared buffer)
         Im2col a{u->T[sp.s0.tensor], u->TC[sp.s0.tensor], sp.s0.up, nullptr, 0, 0, u->B, H, W, Ly.kpad, Ly.A};
         if (sp.nsrc == 2) { a.s1 = u->T[sp.s1.tensor]; a.c1 = u->TC[sp.s1.tensor]; a.up1 = sp.s1.up; }
+        if (l == 0) { a.c0 = kInC; a.ld0 = u->TC[T_IN]; }
         im2col_kernel<<<grid_for(M * (Ly.kpad / 8)), 256, 0, s>>>(a);
     }
     // wgrad: dW^T [kpad][cout] = A^T (kpad x M) * (dZ^T (cout x M))^T
@@ -558,6 +599,9 @@ void refresh_weights(rn_unet* u, const AdamArgs* a, cudaStream_t s) {
                                                         Ly.kpad, Ly.kpad_t, a ? *a : AdamArgs{}, Ly.wq, Ly.wt);
         if (a) adam_vec_kernel<<<(Ly.cout + 255) / 256, 256, 0, s>>>(Ly.b, Ly.bm, Ly.bv, Ly.gb, Ly.cout, *a);
     }
+    if (u->wq0)
+        expand_w0_kernel<<<(u->L[0].cout * 72 + 255) / 256, 256, 0, s>>>(u->L[0].wq, u->L[0].kpad, u->wq0, u->kpad0,
+                                                                          u->L[0].cout);
     if (a) {
         adam_vec_kernel<<<1, 32, 0, s>>>(u->wh, u->mh, u->vh, u->gwh, 32, *a);
         adam_vec_kernel<<<1, 32, 0, s>>>(u->bh, u->mbh, u->vbh, u->gbh, 1, *a);
@@ -646,8 +690,8 @@ int rn_unet_create(int batch, int height, int width, uint64_t seed, uint32_t fla
     }
     max_at = max_a;
     if (u->inference || u->implicit) {   // the layers run in order: one im2col buffer serves all
-        // (implicit inference forms im2col rows for the first layer only)
-        const size_t need = (u->implicit && u->inference) ? pixels(u, 0) * u->L[0].kpad : max_a;
+        // (implicit inference forms no im2col rows at all)
+        const size_t need = (u->implicit && u->inference) ? 8 : max_a;
         bf16* shared = nullptr;
         if (ualloc(u, (void**)&shared, need * 2, st)) return bail(RN_ERR_NO_MEMORY);
         for (auto& Ly : u->L) Ly.A = shared;
@@ -665,11 +709,15 @@ int rn_unet_create(int batch, int height, int width, uint64_t seed, uint32_t fla
     const int tch[T_COUNT] = {kInC, 32, 32, 64, 64, 128, 128, 256, 256, 128, 128, 64, 64, 32, 32, 32, 64, 128};
     for (int t = 0; t < T_COUNT; ++t) {
         u->Tlevel[t] = tlevel[t];
-        u->TC[t] = tch[t];
-        u->Tn[t] = pixels(u, tlevel[t]) * tch[t];
+        u->TC[t] = (t == T_IN && u->implicit) ? 32 : tch[t];
+        u->Tn[t] = pixels(u, tlevel[t]) * u->TC[t];
         if (ualloc(u, (void**)&u->T[t], u->Tn[t] * 2, st) ||
             (!u->inference && ualloc(u, (void**)&u->dT[t], u->Tn[t] * 4, st)))
             return bail(RN_ERR_NO_MEMORY);
+    }
+    if (u->implicit) {
+        u->kpad0 = round_up(9 * 32, 128);
+        if (ualloc(u, (void**)&u->wq0, (size_t)u->L[0].cout * u->kpad0 * 2, st)) return bail(RN_ERR_NO_MEMORY);
     }
     if (u->implicit)
         for (int t : {8, 10, 12})            // b3, d2, d1: read upsampled by d2a, d1a, d0a
@@ -721,7 +769,7 @@ int rn_unet_forward(rn_unet* u, const float* input, int batch, float* output, rn
     RN_TRY(check_shape(u, batch, st));
     cudaStream_t s = ctx().stream;
     const size_t M = pixels(u, 0);
-    input_kernel<<<grid_for(M), 256, 0, s>>>(input, M, u->T[T_IN]);
+    input_kernel<<<grid_for(M), 256, 0, s>>>(input, M, u->TC[T_IN], u->T[T_IN]);
     RN_TRY(forward_all(u, s, st));
     head_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(u->T[14], u->wh, u->bh, M, output, nullptr, 0.0f, nullptr,
                                                            nullptr, nullptr, nullptr);
@@ -736,7 +784,7 @@ int rn_unet_train_step(rn_unet* u, const float* input, const float* target, int 
     RN_TRY(check_shape(u, batch, st));
     cudaStream_t s = ctx().stream;
     const size_t M = pixels(u, 0);
-    input_kernel<<<grid_for(M), 256, 0, s>>>(input, M, u->T[T_IN]);
+    input_kernel<<<grid_for(M), 256, 0, s>>>(input, M, u->TC[T_IN], u->T[T_IN]);
     RN_TRY(forward_all(u, s, st));
     // zero the gradient accumulators
     for (int t = 0; t < T_COUNT; ++t) RN_CUDA(cudaMemsetAsync(u->dT[t], 0, u->Tn[t] * 4, s), st);
@@ -848,7 +896,7 @@ int rn_surrogate_ao(rn_unet* u, const rn_gbuf* g, const float* depth, const rn_a
     depth_partial_kernel<<<kDepthBlocks, 256, 0, s>>>(depth, g->mask, np, psum, pcnt);
     depth_mean_kernel<<<1, 32, 0, s>>>(psum, pcnt, kDepthBlocks, mean);
     features_kernel<<<grid_for(npad), 256, 0, s>>>(depth, g->normal, g->mask, a4, w, h, u->W, u->H, mean, radius,
-                                                    u->T[T_IN]);
+                                                    u->TC[T_IN], u->T[T_IN]);
     RN_TRY(forward_all(u, s, st));
     head_kernel<<<(unsigned)((npad + 255) / 256), 256, 0, s>>>(u->T[14], u->wh, u->bh, npad, pr, nullptr, 0.0f, nullptr,
                                                               nullptr, nullptr, nullptr);
