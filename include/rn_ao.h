@@ -238,6 +238,16 @@ int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t*
                          float tolerance, void* stream, float* err, rn_reconcile_result* out,
                          rn_status* st);
 
+/* GTAO (ground-truth-based ambient occlusion, Jimenez et al. 2016): raw::post::gtao over
+ * raw::post::viewGBuffer (raw/renderer/post.hpp:23-30; src/renderer/post_gtao.cpp:36-135),
+ * the screen-space approximation judged, like SSAO, by the traced AO through rn_reconcile.
+ * camera: eye(3), target(3), up(3), fovy (aspect w / h). radius in world units (the
+ * reference's default 0.5), slices and steps per side (16, 16). ao receives 1 off the
+ * coverage. FP32 on the GPU against the reference's FP64: |gpu - cpu| <= 1e-3 on all but
+ * 0.1 % of pixels, the reference's own bound for its GPU pass (raw/renderer/post_parity.hpp:15-19). */
+int rn_gtao(const rn_gbuf* g, const float* camera, float radius, int slices, int steps, int flags, float* ao,
+            rn_status* st);
+
 /* Launch-shape tuning (no counterpart in the reference; no key changes a per-pixel result).
  * Keys and values:
  *   trace_min_blocks  2 | 3 | 4      resident traversal blocks per SM (register budget)

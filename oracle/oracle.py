@@ -30,6 +30,7 @@ _F = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _U8 = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 _I32 = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 _U64 = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
+_D = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 
 
 def build(with_ref: bool | None = None) -> None:
@@ -72,6 +73,8 @@ def lib() -> C.CDLL:
         L.rno_test_scene.restype = C.c_int
         L.rno_test_scene.argtypes = [_F, _F, _F]
         L.rno_rasterize.argtypes = [_F, _F, C.c_int, _F, C.c_int, C.c_int, _F, _F, _F, _U8]
+        L.rno_view_gbuffer.argtypes = [C.c_int, C.c_int, _F, _F, _U8, _F, _F, _F, _F]
+        L.rno_gtao.argtypes = [C.c_int, C.c_int, _F, _F, _F, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _D]
         L.rno_morton_keys.argtypes = [_F, C.c_int, _U64]
         L.rno_ploc_build.restype = C.c_int
         L.rno_ploc_build.argtypes = [_F, C.c_int, C.c_int, _I32, C.POINTER(C.c_uint32)]
@@ -98,6 +101,9 @@ def ref() -> C.CDLL:
         R.ref_reconcile.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_float, _F, _F]
         R.ref_ploc.restype = C.c_int
         R.ref_ploc.argtypes = [_F, C.c_int, C.c_int, _I32, C.POINTER(C.c_uint32)]
+        R.ref_view_gbuffer.argtypes = [C.c_int, C.c_int, _F, _F, _U8, _F, _F, _F, _F]
+        R.ref_gtao.argtypes = [C.c_int, C.c_int, _F, _F, _F, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
+                               _D]
         _ref = R
     return _ref
 
@@ -235,6 +241,30 @@ def pgm_bytes(buf) -> bytes:
 
 def sha256(b: bytes) -> str:
     return hashlib.sha256(b).hexdigest()
+
+
+# ---------------------------------------------------------------- GTAO (raw::post)
+def view_gbuffer(pos, nrm, mask, cam, use_ref=False):
+    """raw::post::viewGBuffer: (view positions (h,w,3), view normals, view depth (-1 empty))."""
+    mask = np.ascontiguousarray(mask, np.uint8)
+    h, w = mask.shape
+    vp = np.zeros((h, w, 3), np.float32)
+    vn = np.zeros((h, w, 3), np.float32)
+    vd = np.zeros((h, w), np.float32)
+    cam10 = np.ascontiguousarray(cam, np.float32)
+    (ref().ref_view_gbuffer if use_ref else lib().rno_view_gbuffer)(w, h, _f32(pos), _f32(nrm), mask, cam10, vp, vn, vd)
+    return vp, vn, vd
+
+
+def gtao(vpos, vnrm, vdepth, fovy, radius=0.5, slices=16, steps=16, use_ref=False):
+    """raw::post::gtao (FP64) on a view-space G-buffer; aspect = w / h as a float."""
+    h, w = vdepth.shape
+    out = np.zeros((h, w), np.float64)
+    tan_half = float(np.tan(0.5 * np.float64(np.float32(fovy))))
+    aspect = float(np.float32(w) / np.float32(h))
+    (ref().ref_gtao if use_ref else lib().rno_gtao)(w, h, _f32(vpos), _f32(vnrm), _f32(vdepth), tan_half, aspect,
+                                                   float(radius), int(slices), int(steps), out)
+    return out
 
 
 def render_default(w, h, cam=DEFAULT_CAMERA, spp=RT_SAMPLES, radius=AO_RADIUS, ss_samples=SS_SAMPLES,

@@ -14,6 +14,7 @@
 #include "raw/renderer/rt_bvh.hpp"
 #include "raw/cert/reconcile.hpp"
 #include "raw/scene/scene.hpp"
+#include "raw/renderer/post.hpp"
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -137,3 +138,37 @@ int ref_ploc(const float* tris9, int n, int radius, int32_t* out9, uint32_t* rou
 }
 
 }  // extern "C"
+
+
+// raw::post::viewGBuffer (src/renderer/post_gtao.cpp:36-53) of a G-buffer and a camera
+// (cam10: eye, center, up, fovy; aspect w / h; nearZ 0.1).
+extern "C" void ref_view_gbuffer(int w, int h, const float* pos, const float* nrm, const uint8_t* mask,
+                                 const float* cam10, float* vpos, float* vnrm, float* vdepth) {
+    GBuffer g = gbufferFrom(w, h, pos, nrm, mask);
+    g.depth.resize(w, h);
+    Camera cam;
+    cam.eye = Vec3{cam10[0], cam10[1], cam10[2]};
+    cam.center = Vec3{cam10[3], cam10[4], cam10[5]};
+    cam.up = Vec3{cam10[6], cam10[7], cam10[8]};
+    cam.fovy = cam10[9];
+    cam.aspect = (float)w / (float)h;
+    const post::ViewGBuffer v = post::viewGBuffer(g, cam);
+    std::memcpy(vpos, v.pos.data(), v.pos.size() * sizeof(float));
+    std::memcpy(vnrm, v.nrm.data(), v.nrm.size() * sizeof(float));
+    std::memcpy(vdepth, v.depth.data(), v.depth.size() * sizeof(float));
+}
+
+// raw::post::gtao (src/renderer/post_gtao.cpp:64-135) on a view-space G-buffer.
+extern "C" void ref_gtao(int w, int h, const float* vpos, const float* vnrm, const float* vdepth, double tanHalf,
+                         double aspect, double radius, int slices, int steps, double* out) {
+    post::ViewGBuffer v;
+    v.w = w; v.h = h; v.tanHalf = tanHalf; v.aspect = aspect;
+    const std::size_t n = (std::size_t)w * h;
+    v.pos.assign(vpos, vpos + 3 * n);
+    v.nrm.assign(vnrm, vnrm + 3 * n);
+    v.depth.assign(vdepth, vdepth + n);
+    post::GtaoParams p;
+    p.radius = radius; p.slices = slices; p.steps = steps;
+    const std::vector<double> r = post::gtao(v, p);
+    std::memcpy(out, r.data(), n * sizeof(double));
+}

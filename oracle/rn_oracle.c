@@ -726,3 +726,134 @@ RNO_API void rno_occluded_scan_batch(const float* tris9, int ntri, const float* 
     scan_ctx c = {(const tri_t*)tris9, ntri, rays6, tmax, hit, n};
     parallel_rows(n, threads, scan_row, &c);
 }
+
+/* ------------------------------------------------------------------ GTAO (raw::post)
+ * The view-space G-buffer (src/renderer/post_gtao.cpp:36-53, in float as there), the screen
+ * projection (:55-61), the depth sample between pixel centres (:14-33) and GTAO itself
+ * (:64-135: Jimenez et al. 2016, per slice the two horizon angles clamped to the projected
+ * normal's hemisphere, integrated against the cosine), all in double as the reference. The
+ * view depth is negative where nothing was drawn. cam10 as rno_rasterize. */
+RNO_API void rno_view_gbuffer(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, const float* cam10,
+                              float* vpos, float* vnrm, float* vdepth) {
+    const v3 eye = v3m(cam10[0], cam10[1], cam10[2]), ctr = v3m(cam10[3], cam10[4], cam10[5]);
+    const v3 up = v3m(cam10[6], cam10[7], cam10[8]);
+    const mat4 view = look_at(eye, ctr, up);
+    const size_t n = (size_t)w * h;
+    for (size_t i = 0; i < n; ++i) {
+        vpos[3 * i] = vpos[3 * i + 1] = vpos[3 * i + 2] = 0.0f;
+        vnrm[3 * i] = vnrm[3 * i + 1] = vnrm[3 * i + 2] = 0.0f;
+        vdepth[i] = -1.0f;
+        if (!mask[i]) continue;
+        const float p4[4] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 1.0f};
+        const float n4[4] = {nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2], 0.0f};
+        float pv[4], nv[4];
+        mat_vec(&view, p4, pv);
+        mat_vec(&view, n4, nv);
+        const v3 nn = norm3(v3m(nv[0], nv[1], nv[2]));
+        vpos[3 * i] = pv[0]; vpos[3 * i + 1] = pv[1]; vpos[3 * i + 2] = pv[2];
+        vnrm[3 * i] = nn.x; vnrm[3 * i + 1] = nn.y; vnrm[3 * i + 2] = nn.z;
+        vdepth[i] = -pv[2];
+    }
+}
+
+typedef struct { int w, h; double tanHalf, aspect; const float *pos, *nrm, *depth; } vgb;
+static int vgb_valid(const vgb* v, int x, int y) {
+    return x >= 0 && y >= 0 && x < v->w && y < v->h && v->depth[(size_t)y * v->w + x] >= 0.0f;
+}
+static double d3(const double a[3], const double b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static double gt_sample_depth(const vgb* v, double fx, double fy, int sx, int sy) {
+    const double nearest = v->depth[(size_t)sy * v->w + sx];
+    const int x0 = (int)floor(fx - 0.5), y0 = (int)floor(fy - 0.5);
+    const double ax = fx - 0.5 - x0, ay = fy - 0.5 - y0;
+    double k[4], lo = 1e30, hi = 0.0;
+    for (int q = 0; q < 4; ++q) {
+        const int qx = x0 + (q & 1), qy = y0 + (q >> 1);
+        if (!vgb_valid(v, qx, qy)) return nearest;
+        const double d = v->depth[(size_t)qy * v->w + qx];
+        lo = d < lo ? d : lo; hi = d > hi ? d : hi;
+        k[q] = 1.0 / d;
+    }
+    if (hi > 1.1 * lo) return nearest;
+    const double inv = (k[0] * (1 - ax) + k[1] * ax) * (1 - ay) + (k[2] * (1 - ax) + k[3] * ax) * ay;
+    return 1.0 / inv;
+}
+static int gt_project(const vgb* v, const double p[3], double* sx, double* sy) {
+    if (p[2] >= -1e-6) return 0;
+    const double w = -p[2];
+    *sx = (p[0] / (w * v->tanHalf * v->aspect) * 0.5 + 0.5) * v->w;
+    *sy = (1.0 - (p[1] / (w * v->tanHalf) * 0.5 + 0.5)) * v->h;
+    return 1;
+}
+static double clampd(double x, double lo, double hi) { return x < lo ? lo : x > hi ? hi : x; }
+
+/* tanHalf = tan(0.5 * (double)fovy), aspect = (double)(float)(w / h) as the Camera holds it. */
+RNO_API void rno_gtao(int w, int h, const float* vpos, const float* vnrm, const float* vdepth, double tanHalf,
+                      double aspect, double radius, int slices, int steps, double* out) {
+    const double kPi = 3.14159265358979323846;
+    const vgb V0 = {w, h, tanHalf, aspect, vpos, vnrm, vdepth};
+    const vgb* v = &V0;
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const size_t i = (size_t)y * w + x;
+            out[i] = 1.0;
+            if (vdepth[i] < 0.0f) continue;
+            const double P[3] = {vpos[3 * i], vpos[3 * i + 1], vpos[3 * i + 2]};
+            const double N[3] = {vnrm[3 * i], vnrm[3 * i + 1], vnrm[3 * i + 2]};
+            const double pl = sqrt(d3(P, P));
+            const double Vv[3] = {-P[0] / pl, -P[1] / pl, -P[2] / pl};
+            const double rpx = radius * h / (2.0 * tanHalf * vdepth[i]);
+            double T[3] = {1.0 - Vv[0] * Vv[0], -Vv[0] * Vv[1], -Vv[0] * Vv[2]};
+            const double tl = sqrt(d3(T, T));
+            T[0] /= tl; T[1] /= tl; T[2] /= tl;
+            const double B[3] = {Vv[1] * T[2] - Vv[2] * T[1], Vv[2] * T[0] - Vv[0] * T[2], Vv[0] * T[1] - Vv[1] * T[0]};
+            double sx0 = 0, sy0 = 0;
+            gt_project(v, P, &sx0, &sy0);
+            double sum = 0.0;
+            for (int s = 0; s < slices; ++s) {
+                const double phi = kPi * (s + 0.5) / slices, cp = cos(phi), sp = sin(phi);
+                const double dir[3] = {cp * T[0] + sp * B[0], cp * T[1] + sp * B[1], cp * T[2] + sp * B[2]};
+                const double e = 1e-3 * vdepth[i];
+                const double Q[3] = {P[0] + dir[0] * e, P[1] + dir[1] * e, P[2] + dir[2] * e};
+                double sx1 = 0, sy1 = 0;
+                gt_project(v, Q, &sx1, &sy1);
+                const double ddl = hypot(sx1 - sx0, sy1 - sy0);
+                if (ddl < 1e-12) continue;
+                const double c = (sx1 - sx0) / ddl, sn = (sy1 - sy0) / ddl;
+                const double dv = d3(dir, Vv);
+                const double od[3] = {dir[0] - dv * Vv[0], dir[1] - dv * Vv[1], dir[2] - dv * Vv[2]};
+                double ax[3] = {od[1] * Vv[2] - od[2] * Vv[1], od[2] * Vv[0] - od[0] * Vv[2], od[0] * Vv[1] - od[1] * Vv[0]};
+                const double al = sqrt(d3(ax, ax));
+                ax[0] /= al; ax[1] /= al; ax[2] /= al;
+                const double na = d3(N, ax);
+                const double pn[3] = {N[0] - ax[0] * na, N[1] - ax[1] * na, N[2] - ax[2] * na};
+                const double pnl = sqrt(d3(pn, pn));
+                if (pnl < 1e-9) continue;
+                const double sgn = d3(od, pn) >= 0.0 ? 1.0 : -1.0;
+                const double cn = clampd(d3(pn, Vv) / pnl, 0.0, 1.0), nang = sgn * acos(cn);
+                double hc[2] = {cos(nang + kPi / 2), cos(nang - kPi / 2)};
+                for (int side = 0; side < 2; ++side) {
+                    const double sd = side == 0 ? 1.0 : -1.0;
+                    for (int k = 1; k <= steps; ++k) {
+                        const double off = sd * rpx * k / steps;
+                        const double fx = x + 0.5 + off * c, fy = y + 0.5 + off * sn;
+                        const int sx = (int)floor(fx), sy = (int)floor(fy);
+                        if (!vgb_valid(v, sx, sy) || (sx == x && sy == y)) continue;
+                        const double D = gt_sample_depth(v, fx, fy, sx, sy);
+                        const double S[3] = {(fx / w * 2.0 - 1.0) * D * tanHalf * aspect, (1.0 - fy / h * 2.0) * D * tanHalf, -D};
+                        const double dd[3] = {S[0] - P[0], S[1] - P[1], S[2] - P[2]}, dl = sqrt(d3(dd, dd));
+                        if (dl < 1e-9 || dl > radius) continue;
+                        const double cosh_ = d3(dd, Vv) / dl;
+                        hc[side] = cosh_ > hc[side] ? cosh_ : hc[side];
+                    }
+                }
+                const double m1 = acos(clampd(hc[0], -1.0, 1.0)) - nang, m0 = -acos(clampd(hc[1], -1.0, 1.0)) - nang;
+                const double h1 = nang + (m1 < kPi / 2 ? m1 : kPi / 2);
+                const double h0 = nang + (m0 > -kPi / 2 ? m0 : -kPi / 2);
+                const double sn2 = sin(nang);
+                const double a0 = (cn + 2.0 * h0 * sn2 - cos(2.0 * h0 - nang)) / 4.0;
+                const double a1 = (cn + 2.0 * h1 * sn2 - cos(2.0 * h1 - nang)) / 4.0;
+                sum += pnl * (a0 + a1);
+            }
+            out[i] = sum / slices;
+        }
+}

@@ -363,7 +363,7 @@ void h_cross(const float a[3], const float b[3], float o[3]) {
     o[2] = a[0] * b[1] - a[1] * b[0];
 }
 float h_dot(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-M4 view_proj(const float* cam, int w, int h, float nearZ, float farZ) {
+M4 view_matrix(const float* cam) {
     const float eye[3] = {cam[0], cam[1], cam[2]}, ctr[3] = {cam[3], cam[4], cam[5]}, up[3] = {cam[6], cam[7], cam[8]};
     const float d[3] = {ctr[0] - eye[0], ctr[1] - eye[1], ctr[2] - eye[2]};
     float f[3], s0[3], sv[3], u[3];
@@ -376,6 +376,10 @@ M4 view_proj(const float* cam, int w, int h, float nearZ, float farZ) {
     view.m[0] = sv[0]; view.m[1] = sv[1]; view.m[2] = sv[2]; view.m[3] = -h_dot(sv, eye);
     view.m[4] = u[0]; view.m[5] = u[1]; view.m[6] = u[2]; view.m[7] = -h_dot(u, eye);
     view.m[8] = -f[0]; view.m[9] = -f[1]; view.m[10] = -f[2]; view.m[11] = h_dot(f, eye);
+    return view;
+}
+M4 view_proj(const float* cam, int w, int h, float nearZ, float farZ) {
+    const M4 view = view_matrix(cam);
     const float aspect = h > 0 ? (float)w / (float)h : 1.0f;
     const float t = 1.0f / ::tanf(cam[9] * 0.5f);
     M4 proj{};
@@ -552,6 +556,34 @@ int rn_ssao(const rn_gbuf* g, int samples, float radius, int flags, float* ao_ss
         return cuda_fail(st, cudaGetLastError(), "ssao_kernel");
     if (dev) return ok(st);
     RN_TRY(copy_back(ao_ss, d_ss, np, st));
+    RN_CUDA(cudaStreamSynchronize(c.stream), st);
+    return ok(st);
+}
+
+int rn_gtao(const rn_gbuf* g, const float* camera, float radius, int slices, int steps, int flags, float* ao,
+            rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    RN_TRY(check_gbuf(g, st));
+    if (!ao || !camera) return fail(st, RN_ERR_INVALID, "null argument");
+    if (!(radius > 0.0f) || slices <= 0 || steps <= 0 || slices > 1024 || steps > 1024)
+        return fail(st, RN_ERR_INVALID, "radius %g slices %d steps %d", radius, slices, steps);
+    Context& c = ctx();
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const size_t np = (size_t)g->w * g->h;
+    StagedGbuf sg;
+    RN_TRY(stage_gbuf(g, dev, &sg, st));
+    void *vp, *vn, *vd;
+    RN_TRY(ws_get(WS_VPOS, np * 12, &vp, st));
+    RN_TRY(ws_get(WS_VNRM, np * 12, &vn, st));
+    RN_TRY(ws_get(WS_VDEPTH, np * 4, &vd, st));
+    float* d_ao;
+    RN_TRY(stage_out(ao, np, dev, WS_GTAO, &d_ao, st));
+    const M4 view = view_matrix(camera);
+    if (launch_gtao(g->w, g->h, sg.pos, sg.nrm, sg.mask, view.m, camera[9], radius, slices, steps, (float*)vp,
+                    (float*)vn, (float*)vd, d_ao, c.stream) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "gtao_kernel");
+    if (dev) return ok(st);
+    RN_TRY(copy_back(ao, d_ao, np, st));
     RN_CUDA(cudaStreamSynchronize(c.stream), st);
     return ok(st);
 }

@@ -31,7 +31,7 @@ enum Slot {
     WS_POS, WS_NRM, WS_MASK, WS_AO, WS_SKY, WS_SUN, WS_SS, WS_ERR, WS_TRUTH, WS_APPROX,
     WS_PARTIALS, WS_WORKLIST, WS_COUNTERS, WS_RAYS, WS_TMAX, WS_HITS, WS_TRIS_IN,
     WS_NRM_IN, WS_RASTER, WS_DEPTH, WS_STATS,
-    WS_SUR_AO4, WS_SUR_PRED, WS_SUR_FB, WS_SUR_AOFB, WS_SUR_STATS,
+    WS_SUR_AO4, WS_SUR_PRED, WS_SUR_FB, WS_SUR_AOFB, WS_SUR_STATS, WS_VPOS, WS_VNRM, WS_VDEPTH, WS_GTAO,
     WS_COUNT
 };
 
@@ -195,6 +195,13 @@ TraceParams ao_trace_params(const float* pos, const float* nrm, const uint8_t* m
 void apply_tune(TraceParams& p, const rn_accel* accel);
 int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned long long* counts = nullptr,
                  uint32_t stride = 1);
+
+// ---------------------------------------------------------------- GTAO (gtao.cu)
+// The view-space G-buffer (view16: the camera's row-major view matrix) into vpos/vnrm/vdepth,
+// then GTAO (radius, slices, steps; fovy and aspect w / h of the camera) into out.
+int launch_gtao(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, const float* view16,
+                float fovy, float radius, int slices, int steps, float* vpos, float* vnrm, float* vdepth, float* out,
+                cudaStream_t s);
 
 // ---------------------------------------------------------------- G-buffer
 // Scratch bytes for ntri triangles, npx pixels and npairs (record, 8x8 bin) pairs.

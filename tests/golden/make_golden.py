@@ -7,6 +7,9 @@ raw-native tree; the committed JSON is what the tests read).
   - ploc.json: PLOC tree hashes and round counts: the soup scene from the reference's GPU
     evidence (evidence/rt-r2-bvh-gpu-d3d12-rtx4090.json) and the built-in test scene from
     the reference's rt::buildPloc.
+  - gtao.json: raw::post::gtao (FP64) of the built-in scene at 256 x 256 from the two test
+    cameras of evidence/m3-post-bounds.json, by the reference's own code: SHA-256 of the
+    float64 output, its mean over covered pixels and the covered count.
 
     python tests/golden/make_golden.py [/path/to/raw-native]
 """
@@ -23,6 +26,9 @@ sys.path.insert(0, ROOT)
 from oracle import oracle as O  # noqa: E402
 
 FILES = ("ao_rt.pfm", "ao_ss.pfm", "mask.pgm", "ao_error.pgm")
+# evidence/m3-post-bounds.json "scenes": the built-in scene from the CLI camera and from the
+# near camera (eye 1.8, 3.2, 2.4 toward 0.8, 0.2, 1.0)
+GTAO_CAMERAS = {"test_scene": tuple(O.DEFAULT_CAMERA), "near": (1.8, 3.2, 2.4, 0.8, 0.2, 1.0, 0.0, 1.0, 0.0, 0.9)}
 
 
 def camera_of(args):
@@ -89,7 +95,19 @@ def main(ref_dir):
                                test_scene=dict(triangles=n, rounds=rounds.value, root=root,
                                                tree_hash=O.tree_hash(out)))),
               open(os.path.join(HERE, "ploc.json"), "w"), indent=1, sort_keys=True)
-    print("wrote", os.path.join(HERE, "identity.json"), os.path.join(HERE, "ploc.json"))
+    gt = {}
+    tris, nrm9, _ = O.test_scene()
+    for name, cam in GTAO_CAMERAS.items():
+        _, pos, nrm, mask = O.rasterize(tris, nrm9, cam, 256, 256)
+        vp, vn, vd = O.view_gbuffer(pos, nrm, mask, cam, use_ref=True)
+        a = O.gtao(vp, vn, vd, cam[9], use_ref=True)
+        gt[name] = dict(camera=list(cam), width=256, height=256, radius=0.5, slices=16, steps=16,
+                        sha256=O.sha256(np.ascontiguousarray(a).tobytes()), covered=int(mask.sum()),
+                        mean_covered=float(a[mask > 0].mean()))
+    json.dump(dict(source="raw::post::gtao (src/renderer/post_gtao.cpp) built from the reference's sources",
+                   cases=gt), open(os.path.join(HERE, "gtao.json"), "w"), indent=1, sort_keys=True)
+    print("wrote", os.path.join(HERE, "identity.json"), os.path.join(HERE, "ploc.json"),
+          os.path.join(HERE, "gtao.json"))
 
 
 if __name__ == "__main__":

@@ -155,3 +155,18 @@ def test_synthetic_scenes_are_seeded_and_sized():
     v = scenes.orbit_views(1, 64)
     assert len(v) == 64 and {(w, h) for w, h, _, _ in v} <= set(scenes.RESOLUTIONS)
     assert {s for _, _, s, _ in v} <= set(scenes.SPPS)
+
+
+def test_gtao_restatement_matches_reference_golden(oracle):
+    """raw::post::gtao restated in C (FP64) reproduces the reference build's output bytes on
+    the built-in scene from both test cameras (tests/golden/gtao.json)."""
+    import json
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "gtao.json")))["cases"]
+    tris, nrm9, _ = oracle.test_scene()
+    for name, case in gold.items():
+        cam = case["camera"]
+        _, pos, nrm, mask = oracle.rasterize(tris, nrm9, cam, case["width"], case["height"])
+        vp, vn, vd = oracle.view_gbuffer(pos, nrm, mask, cam)
+        a = oracle.gtao(vp, vn, vd, cam[9], case["radius"], case["slices"], case["steps"])
+        assert int(mask.sum()) == case["covered"]
+        assert oracle.sha256(np.ascontiguousarray(a).tobytes()) == case["sha256"], name
