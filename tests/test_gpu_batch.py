@@ -42,7 +42,10 @@ def test_batch_equals_single_frames(rn):
         for key in ("ao", "sky", "sun", "ss", "err"):
             assert torch.equal(b.outputs[k][key], ref[key]), (k, key)
         assert res[k].pixels == ref["rec"].pixels and res[k].rmse == ref["rec"].rmse
-        assert res[k].sum_sq == ref["rec"].sum_sq and res[k].within_tolerance == ref["rec"].within_tolerance
+        # the FP64 sum's order follows the SSAO tiling (the batch's 32 x 8 tiles, the single
+        # frame's tuned tile height): equal to rounding
+        assert abs(res[k].sum_sq - ref["rec"].sum_sq) <= 1e-12 * ref["rec"].sum_sq
+        assert res[k].within_tolerance == ref["rec"].within_tolerance
     res2 = b.run()                                      # the graph replays to the same bits
     assert [r.sum_sq for r in res2] == [r.sum_sq for r in res]
     info = b.info()
@@ -91,7 +94,7 @@ def test_config3_batch_on_big_scene(rn, oracle, big_scene):
         ref = rn.ao_frame(v["g"], acc, v["spp"], 1.0, 24, 0.12)
         torch.cuda.synchronize()
         assert torch.equal(b.outputs[k]["ao"], ref["ao"]) and torch.equal(b.outputs[k]["ss"], ref["ss"])
-        assert res[k].sum_sq == ref["rec"].sum_sq
+        assert abs(res[k].sum_sq - ref["rec"].sum_sq) <= 1e-12 * ref["rec"].sum_sq
     v = views[0]
     g = v["g"]
     pos, nrm, mask = g.position.cpu().numpy(), g.normal.cpu().numpy(), g.mask.cpu().numpy()
