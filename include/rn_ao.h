@@ -257,6 +257,7 @@ int rn_gtao(const rn_gbuf* g, const float* camera, float radius, int slices, int
  *   trace_stack       48 | 96        traversal stack entries (48 only where the tree allows)
  *   ssao_tile_h       4 | 8 | 16     SSAO tile 32 x h (the fused FP64 sum follows the tiling)
  *   conv_bn_max       64 | 128 | 256 widest GEMM tile of the surrogate's convolutions
+ *   conv_halo         0 | 1          row tiles of 128 pixels from one halo box each (where they fit)
  * Process-wide; RN_TUNE_<KEY> environment variables apply before the first call.
  * rn_tune_load reads "key = value" lines ('#' comments), all or nothing. */
 int rn_tune_set(const char* key, int value, rn_status* st);

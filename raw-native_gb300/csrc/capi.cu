@@ -118,6 +118,7 @@ const TuneKey kTuneKeys[] = {
     {"trace_stack", "RN_TUNE_TRACE_STACK", &Tune::trace_stack, {48, 96}, 2},
     {"ssao_tile_h", "RN_TUNE_SSAO_TILE_H", &Tune::ssao_tile_h, {4, 8, 16}, 3},
     {"conv_bn_max", "RN_TUNE_CONV_BN_MAX", &Tune::conv_bn_max, {64, 128, 256}, 3},
+    {"conv_halo", "RN_TUNE_CONV_HALO", &Tune::conv_halo, {0, 1}, 2},
 };
 
 const TuneKey* find_tune_key(const char* name) {

@@ -447,6 +447,210 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
 }
 
+
+// ------------------------------------------------------------------ implicit 3x3, halo tiles
+// For 128-pixel tiles of one image row (W % 128 == 0) and a layer whose whole weight matrix
+// fits in shared memory: per tile ONE TMA box per source holds the 3 rows x 136 pixels
+// (x0 - 1 .. x0 + 134) of every input channel, and the 9 taps read it in place, each tap's
+// A operand starting 16 bytes (one pixel) further along a row or 136 pixels further down.
+// Layouts are the no-swizzle K-major canonical form: 8 rows x 16 bytes (8 channels) per
+// core matrix, core matrices 128 bytes apart along M (pixels) and one channel group apart
+// along K (3 x 136 x 16 bytes for A, N x 16 bytes for B). The weights are loaded once per
+// CTA. K order (tap outermost, then channel) and the K16 steps are the same as
+// tc_conv_kernel's, so the two kernels give identical results.
+constexpr int kHaloW = 136;                        // box width: 128 + 2 halo, rounded for alignment
+constexpr uint32_t kHaloGroup = 3 * kHaloW * 16;   // bytes of one 8-channel group of a box
+
+__device__ __forceinline__ uint64_t desc_plain(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;      // leading byte offset: next core matrix along K
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;      // stride byte offset: next 8 rows along M / N
+    d |= (uint64_t)1 << 46;                           // descriptor version; layout 0: no swizzle
+    return d;
+}
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+        : "memory");
+}
+
+struct HaloArgs {
+    int nsrc, C0, C1, cin;
+    int B, H, W;
+    int tiles;                  // (W / 128) x H x B
+    int stages;
+    uint32_t a_bytes, b_bytes;  // one stage of A (all sources), the resident weights
+    __nv_bfloat16* up16;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __grid_constant__ CUtensorMap map0,
+                                                                       const __grid_constant__ CUtensorMap map1,
+                                                                       const __grid_constant__ CUtensorMap mapW,
+                                                                       const HaloArgs a, const Epilogue e) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    constexpr uint32_t kCols = 2 * BN;
+    const int kSt = a.stages;
+    uint8_t* sB = smem;
+    uint8_t* sA = smem + ((a.b_bytes + 1023) & ~1023u);
+    const uint32_t a_stride = (a.a_bytes + 1023) & ~1023u;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sA + kSt * a_stride);     // full[kSt], empty[kSt], acc_full[2], acc_empty[2], w
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 5);
+    __shared__ int s_abort;
+    volatile int* abort_flag = &s_abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tiles_x = a.W >> 7;
+    auto full = [&](int s) { return smem_u32(&bars[s]); };
+    auto empty = [&](int s) { return smem_u32(&bars[kSt + s]); };
+    auto acc_full = [&](int b) { return smem_u32(&bars[2 * kSt + b]); };
+    auto acc_empty = [&](int b) { return smem_u32(&bars[2 * kSt + 2 + b]); };
+    const uint32_t wbar = smem_u32(&bars[2 * kSt + 4]);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kSt; ++s) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(acc_full(b), 1); mbar_init(acc_empty(b), 4); }
+        mbar_init(wbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_abort = 0;
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t src1_off = (uint32_t)(a.C0 / 8) * kHaloGroup;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            mbar_expect_tx(wbar, a.b_bytes);
+            tma_load_3d(smem_u32(sB), &mapW, 0, 0, 0, wbar);
+            uint32_t kc = 0;
+            for (int tile = blockIdx.x; tile < a.tiles && !*abort_flag; tile += gridDim.x, ++kc) {
+                const int s = kc % kSt;
+                const uint32_t ph = (kc / kSt) & 1u;
+                if (!mbar_wait_or_abort(empty(s), ph ^ 1u, abort_flag)) {
+                    atomicOr(e.err, DEV_GUARD);
+                    s_abort = 1;
+                    break;
+                }
+                const int tx = tile % tiles_x, y = (tile / tiles_x) % a.H, b = tile / (tiles_x * a.H);
+                mbar_expect_tx(full(s), a.a_bytes);
+                const uint32_t dst = smem_u32(sA + s * a_stride);
+                tma_load_5d(dst, &map0, 0, tx * 128 - 1, y - 1, b, 0, full(s));
+                if (a.nsrc > 1) tma_load_5d(dst + src1_off, &map1, 0, tx * 128 - 1, y - 1, b, 0, full(s));
+            }
+            for (uint32_t k = kc > (uint32_t)kSt ? kc - kSt : 0; k < kc; ++k) mbar_wait(full(k % kSt), (k / kSt) & 1u);
+            mbar_wait(wbar, 0);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = instr_desc(BN);
+            const uint32_t b0 = smem_u32(sB);
+            const int q16 = a.cin / 16, g_tap = a.cin / 8;
+            bool ok = mbar_wait_or_abort(wbar, 0, abort_flag);
+            uint32_t kc = 0, i = 0;
+            for (int tile = blockIdx.x; ok && tile < a.tiles && !*abort_flag; tile += gridDim.x, ++kc, ++i) {
+                const uint32_t buf = i & 1u, use = i >> 1;
+                if (!mbar_wait_or_abort(acc_empty(buf), (use & 1u) ^ 1u, abort_flag)) { ok = false; break; }
+                const int s = kc % kSt;
+                if (!mbar_wait_or_abort(full(s), (kc / kSt) & 1u, abort_flag)) { ok = false; break; }
+                tc_fence_after();
+                const uint32_t acc = tmem + buf * BN;
+                const uint32_t a0 = smem_u32(sA + s * a_stride);
+                for (int t = 0; t < 9; ++t) {
+                    const uint32_t a_tap = a0 + (uint32_t)((t / 3) * kHaloW + (t % 3)) * 16u;
+                    for (int q = 0; q < q16; ++q) {
+                        const uint64_t da = desc_plain(a_tap + (uint32_t)(2 * q) * kHaloGroup, kHaloGroup, 128);
+                        const uint64_t db = desc_plain(b0 + (uint32_t)(t * g_tap + 2 * q) * (BN * 16), BN * 16, 128);
+                        tc_mma(acc, da, db, idesc, (t | q) != 0 ? 1u : 0u);
+                    }
+                }
+                tc_commit(empty(s));
+                tc_commit(acc_full(buf));
+            }
+            if (!ok) {
+                atomicOr(e.err, DEV_GUARD);
+                s_abort = 1;
+            }
+        }
+    } else {
+        const int q = warp & 3;
+        const int r = q * 32 + lane;
+        uint32_t i = 0;
+        for (int tile = blockIdx.x; tile < a.tiles; tile += gridDim.x, ++i) {
+            const uint32_t buf = i & 1u, use = i >> 1;
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_or_abort(acc_full(buf), use & 1u, abort_flag));
+            if (!ok) {
+                if (lane == 0) { atomicOr(e.err, DEV_GUARD); s_abort = 1; }
+                break;
+            }
+            tc_fence_after();
+            const int tx = tile % tiles_x, y = (tile / tiles_x) % a.H, b = tile / (tiles_x * a.H);
+            const int x = tx * 128 + r;
+            const size_t pix = ((size_t)b * a.H + y) * a.W + x;
+            const uint32_t tbase = tmem + buf * BN + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                uint32_t v[16];
+                tmem_ld16(tbase + (uint32_t)c0, v);
+                float f[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float t = __uint_as_float(v[j]);
+                    if (e.bias) t += e.bias[c0 + j];
+                    if (e.relu) t = fmaxf(t, 0.0f);
+                    f[j] = t;
+                }
+                const size_t o = pix * e.ldc + c0;
+                if (e.c16) {
+                    uint4 out[2];
+                    __nv_bfloat16* ob = reinterpret_cast<__nv_bfloat16*>(out);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) ob[j] = __float2bfloat16_rn(f[j]);
+                    uint4* d4 = reinterpret_cast<uint4*>(e.c16 + o);
+                    d4[0] = out[0];
+                    d4[1] = out[1];
+                    if (a.up16) {
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            const size_t up = ((size_t)b * 2 * a.H + 2 * y + (u >> 1)) * (2 * a.W) + 2 * x + (u & 1);
+                            uint4* d = reinterpret_cast<uint4*>(a.up16 + up * e.ldc + c0);
+                            d[0] = out[0];
+                            d[1] = out[1];
+                        }
+                    }
+                }
+                if (e.c32) {
+                    float4* d4 = reinterpret_cast<float4*>(e.c32 + o);
+#pragma unroll
+                    for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty(buf));
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+}
+
 // ------------------------------------------------------------------ host side
 PFN_cuTensorMapEncodeTiled_v12000 encoder() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -524,6 +728,54 @@ int launch_conv(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap&
     }
     const int ctas = std::min(a.items, per_sm * ctx().sm_count);
     tc_conv_kernel<BN, CB><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
+    return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
+}
+
+
+// The halo box of one source: a 5-D view of the NHWC tensor, (8 channels, W, H, B, C / 8
+// groups), read in boxes of 8 x 136 x 3 x 1 x C/8 without swizzle (the channel groups
+// outermost in shared memory).
+bool make_map_halo(CUtensorMap* m, const void* base, int B, int H, int W, int C) {
+    auto fn = encoder();
+    if (!fn) return false;
+    const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B, (cuuint64_t)(C / 8)};
+    const cuuint64_t strides[4] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2, 16};
+    const cuuint32_t box[5] = {8, (cuuint32_t)kHaloW, 3, 1, (cuuint32_t)(C / 8)};
+    const cuuint32_t elem[5] = {1, 1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, elem,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+// The resident weights: (8 columns, N rows, K / 8 groups), one box of 8 x N x kgroups.
+bool make_map_wgroups(CUtensorMap* m, const void* base, int N, int ldw, int kgroups) {
+    auto fn = encoder();
+    if (!fn) return false;
+    const cuuint64_t dims[3] = {8, (cuuint64_t)N, (cuuint64_t)(ldw / 8)};
+    const cuuint64_t strides[2] = {(cuuint64_t)ldw * 2, 16};
+    const cuuint32_t box[3] = {8, (cuuint32_t)N, (cuuint32_t)kgroups};
+    const cuuint32_t elem[3] = {1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, elem,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+int launch_conv_halo(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap& mw, const HaloArgs& a,
+                     const Epilogue& e, size_t smem, cudaStream_t s) {
+    static size_t attr = 0;
+    if (attr < smem) {
+        if (cudaFuncSetAttribute(tc_conv_halo_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(tc_conv_halo_kernel<BN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+            return RN_ERR_CUDA;
+        attr = smem;
+    }
+    int smem_sm = 0;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx().device);
+    const int per_sm = std::max(1, std::min(std::min(smem_sm / (int)(smem + 1024), 512 / (2 * BN)), 3));
+    const int ctas = std::min(a.tiles, per_sm * ctx().sm_count);
+    tc_conv_halo_kernel<BN><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 
@@ -605,6 +857,34 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     if (N % bn) return fail(st, RN_ERR_INVALID, "tc_conv3x3 N %d", N);
     while (bn > ctx().tune.conv_bn_max && bn > 32) bn /= 2;
     if (up16 && !epi.c16) return fail(st, RN_ERR_INVALID, "tc_conv3x3: the upsampled copy needs a BF16 output");
+    // halo tiles: rows of 128 pixels, channels in groups of 16, N 32 or 64 in one slice, the
+    // weights and at least two stages of boxes in shared memory
+    if (ctx().tune.conv_halo && t.tw_log2 == 7 && (N == 32 || N == 64) && (9 * cin) / 8 <= 256 && cin % 16 == 0) {
+        const uint32_t b_bytes = (uint32_t)N * 9 * cin * 2;
+        const uint32_t a_bytes = (uint32_t)cin / 8 * tc::kHaloGroup;
+        const uint32_t a_stride = (a_bytes + 1023) & ~1023u, b_pad = (b_bytes + 1023) & ~1023u;
+        const size_t budget = 220 * 1024;
+        int stages = (int)std::min<size_t>(4, (budget - std::min<size_t>(budget, b_pad + 2048)) / a_stride);
+        CUtensorMap hm[2], hw;
+        bool maps = stages >= 2;
+        for (int i = 0; maps && i < nsrc; ++i) maps = tc::make_map_halo(&hm[i], src[i].ptr, B, H, W, src[i].C);
+        if (maps && nsrc == 1) hm[1] = hm[0];
+        maps = maps && tc::make_map_wgroups(&hw, w, N, ldw, 9 * cin / 8);
+        if (maps) {
+            tc::HaloArgs h{};
+            h.nsrc = nsrc; h.C0 = src[0].C; h.C1 = nsrc > 1 ? src[1].C : 0; h.cin = cin;
+            h.B = B; h.H = H; h.W = W;
+            h.tiles = (W / 128) * H * B;
+            h.stages = stages;
+            h.a_bytes = a_bytes; h.b_bytes = b_bytes;
+            h.up16 = up16;
+            const size_t smem = 1024 + b_pad + (size_t)stages * a_stride + (2 * stages + 5) * 8 + 16;
+            const int rc = N == 32 ? tc::launch_conv_halo<32>(hm[0], hm[1], hw, h, epi, smem, s)
+                                   : tc::launch_conv_halo<64>(hm[0], hm[1], hw, h, epi, smem, s);
+            if (rc != RN_OK) return cuda_fail(st, cudaGetLastError(), "tc_conv_halo_kernel");
+            return RN_OK;
+        }
+    }
     const int cb = all64 ? 64 : 32;
     const int tw = 1 << t.tw_log2, th = tc::kBM >> t.tw_log2;
     CUtensorMap m[2], mw;

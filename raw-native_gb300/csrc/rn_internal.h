@@ -45,6 +45,7 @@ struct Tune {
     int trace_stack = 96;       // traversal stack entries: 48 or 96 (48 only where the tree's depth allows)
     int ssao_tile_h = 8;        // SSAO tile: 32 x ssao_tile_h pixels, one thread each; 4, 8 or 16
     int conv_bn_max = 256;      // largest GEMM tile width (columns of C per CTA): 64, 128 or 256
+    int conv_halo = 1;          // 128-pixel row tiles from one halo box per tile (where they fit)
 };
 
 struct Context {

@@ -73,3 +73,35 @@ def test_conv_rejects_untileable_and_bad_channels(rn):
     y = torch.zeros(1, 16, 16, 40, device="cuda", dtype=torch.bfloat16)       # 40 channels
     with pytest.raises(rn.RnError):
         rn.tc_conv3x3(y, torch.zeros(32, 384, device="cuda", dtype=torch.bfloat16))
+
+
+@pytest.mark.parametrize("B,H,W,c0,c1,N", [(2, 8, 128, 32, 0, 32), (1, 6, 256, 32, 0, 64), (1, 4, 1920, 32, 0, 32),
+                                            (2, 8, 128, 32, 64, 32), (1, 5, 384, 64, 0, 64)])
+def test_conv_halo_tiles_match_the_general_kernel(rn, B, H, W, c0, c1, N):
+    """Row tiles from one halo box (conv_halo 1) accumulate the same K16 steps in the same
+    order as the per-tap boxes (conv_halo 0): identical outputs, bias, ReLU and the
+    upsampled copy included."""
+    import torch
+    saved = rn.tune_get("conv_halo")
+    try:
+        g = torch.Generator(device="cuda").manual_seed(B + H + W + c0 + c1 + N)
+        x0 = torch.randn(B, H, W, c0, device="cuda", generator=g).to(torch.bfloat16)
+        x1 = torch.randn(B, H, W, c1, device="cuda", generator=g).to(torch.bfloat16) if c1 else None
+        cin = c0 + c1
+        ldw = (9 * cin + 127) // 128 * 128
+        w = torch.zeros(N, ldw, device="cuda", dtype=torch.bfloat16)
+        w[:, :9 * cin] = (torch.randn(N, 9 * cin, device="cuda", generator=g) / (9 * cin) ** 0.5).to(torch.bfloat16)
+        bias = torch.randn(N, device="cuda", generator=g)
+        outs = []
+        for halo in (0, 1):
+            rn.tune_set("conv_halo", halo)
+            o, u = rn.tc_conv3x3(x0, w, x1, bias=bias, relu=True, upsampled=True)
+            f = rn.tc_conv3x3(x0, w, x1, bias=bias, relu=False)
+            torch.cuda.synchronize()
+            outs.append((o.clone(), u.clone(), f.clone()))
+        for a, b in zip(*outs):
+            assert torch.equal(a, b)
+        ref = _ref(x0, x1, w, bias, False)
+        assert (outs[1][2] - ref).abs().max().item() <= 1e-3 * ref.abs().max().item()
+    finally:
+        rn.tune_set("conv_halo", saved)
