@@ -248,6 +248,12 @@ int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t*
 int rn_gtao(const rn_gbuf* g, const float* camera, float radius, int slices, int steps, int flags, float* ao,
             rn_status* st);
 
+/* Self-test of the device-side wait budget (no counterpart in the reference): runs a small
+ * tensor-core GEMM with one stage's copies withheld, so that its bounded mbarrier wait runs
+ * out after spin_limit rounds (1 .. 2^24). Returns RN_ERR_BUDGET from the device error word,
+ * with the kernel having freed its TMEM and returned; the context stays usable. */
+int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
+
 /* Launch-shape tuning (no counterpart in the reference; no key changes a per-pixel result).
  * Keys and values:
  *   trace_min_blocks  2 | 3 | 4      resident traversal blocks per SM (register budget)

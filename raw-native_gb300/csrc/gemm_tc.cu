@@ -35,8 +35,8 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kSpin; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t limit = kSpin) {
+    for (uint32_t i = 0; i < limit; ++i) {
         uint32_t ok;
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
@@ -138,28 +138,30 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
+    const uint32_t spin = e.spin ? e.spin : kSpin;
     if (warp == 0 && lane == 0) {
         // producer
         int issued = 0;
         for (int kb = 0; kb < nkb; ++kb) {
             const int s = kb % kStages;
             const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
-            if (!mbar_wait(empty(s), ph ^ 1u)) { atomicOr(e.err, DEV_GUARD); s_abort = 1; break; }
+            if (!mbar_wait(empty(s), ph ^ 1u, spin)) { atomicOr(e.err, DEV_GUARD); s_abort = 1; break; }
             mbar_expect_tx(full(s), kABytes + kBBytes);
+            if (e.withhold && kb == 0) continue;      // the self-test's missing copy: its stage never fills
             tma_load_2d(smem_u32(sA + s * kABytes), &mapP, kbeg + kb * kBK, m0, full(s));
             tma_load_2d(smem_u32(sB + s * kBBytes), &mapQ, kbeg + kb * kBK, n0, full(s));
             ++issued;
         }
         // the copies this thread issued must land before the CTA can leave
         for (int kb = issued > kStages ? issued - kStages : 0; kb < issued; ++kb)
-            mbar_wait(full(kb % kStages), (uint32_t)(kb / kStages) & 1u);
+            mbar_wait(full(kb % kStages), (uint32_t)(kb / kStages) & 1u, spin);
     } else if (warp == 1 && lane == 0) {
         // MMA issuer
         const uint32_t idesc = instr_desc(BN);
         for (int kb = 0; kb < nkb; ++kb) {
             const int s = kb % kStages;
             const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
-            if (!mbar_wait(full(s), ph)) { atomicOr(e.err, DEV_GUARD); s_abort = 1; break; }
+            if (!mbar_wait(full(s), ph, spin)) { atomicOr(e.err, DEV_GUARD); s_abort = 1; break; }
             tc_fence_after();
             const uint32_t a0 = smem_u32(sA + s * kABytes), b0 = smem_u32(sB + s * kBBytes);
 #pragma unroll
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_const
         tc_commit(done);
     }
     // epilogue: thread t owns row m0 + t, TMEM lane t
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0));    // warp-uniform: the loads below are .sync.aligned
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0, spin));    // warp-uniform: the loads below are .sync.aligned
     tc_fence_after();
     if (!ok && lane == 0) atomicOr(e.err, DEV_GUARD);
     const int abort_warp = __shfl_sync(0xffffffffu, *(volatile int*)&s_abort, 0);
@@ -958,4 +960,32 @@ extern "C" int rn_tc_conv3x3(const void* src0, int c0, const void* src1, int c1,
     RN_TRY(tc_conv3x3(src, src1 ? 2 : 1, B, H, W, (const __nv_bfloat16*)w, ldw, N, e, (__nv_bfloat16*)up16,
                       ctx().stream, st));
     return ok(st);
+}
+
+// Self-test of the device-side wait budget (no counterpart in the reference): a 128 x 32 x 64
+// GEMM whose only K block's copies are withheld, so its stage never fills. The MMA thread's
+// bounded wait gives up after `spin_limit` rounds, sets the error word and the CTA frees its
+// TMEM and returns: the call must come back with RN_ERR_BUDGET and leave the context usable.
+extern "C" int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    if (spin_limit == 0 || spin_limit > (1u << 24)) return fail(st, RN_ERR_INVALID, "spin limit %u", spin_limit);
+    void *p = nullptr, *q = nullptr, *c = nullptr;
+    RN_CUDA(cudaMalloc(&p, 128 * 64 * 2), st);
+    RN_CUDA(cudaMalloc(&q, 32 * 64 * 2), st);
+    RN_CUDA(cudaMalloc(&c, 128 * 32 * 4), st);
+    cudaMemsetAsync(p, 0, 128 * 64 * 2, ctx().stream);
+    cudaMemsetAsync(q, 0, 32 * 64 * 2, ctx().stream);
+    tc::Epilogue e{};
+    e.ldc = 32;
+    e.c32 = (float*)c;
+    e.err = ctx().dev_error;
+    e.spin = spin_limit;
+    e.withhold = 1;
+    int rc = tc_gemm((const __nv_bfloat16*)p, 64, (const __nv_bfloat16*)q, 64, 128, 32, 64, 1, e, ctx().stream, st);
+    if (rc == RN_OK) rc = check_device_error(st, "rn_selftest_wait_budget");
+    cudaStreamSynchronize(ctx().stream);
+    cudaFree(p);
+    cudaFree(q);
+    cudaFree(c);
+    return rc;
 }

@@ -19,6 +19,8 @@ struct Epilogue {
     int atomic;
     int k_per_split;                 // K range of one grid.z slice (a multiple of 64)
     uint32_t* err;
+    uint32_t spin;                   // try_wait rounds before a wait gives up (0: the default)
+    int withhold;                    // self-test only: the first K block's copies are never issued
 };
 
 // One input of an implicit-GEMM 3x3 convolution: an NHWC BF16 tensor at the output's

@@ -34,7 +34,7 @@ EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_ac
            "rn_unet_free", "rn_unet_param_count", "rn_unet_forward", "rn_unet_train_step", "rn_unet_get_params",
            "rn_unet_set_params", "rn_unet_get_grads", "rn_unet_get_state", "rn_unet_set_state",
            "rn_unet_set_clip", "rn_unet_last_grad_norm",
-           "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3", "rn_surrogate_ao", "rn_gtao")
+           "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3", "rn_surrogate_ao", "rn_gtao", "rn_selftest_wait_budget")
 
 
 class RnError(RuntimeError):
@@ -114,6 +114,7 @@ def lib() -> C.CDLL:
         L.rn_unet_set_state.argtypes = [vp, vp, C.c_uint64, st]
         L.rn_unet_set_clip.argtypes = [vp, C.c_float, st]
         L.rn_tune_set.argtypes = [C.c_char_p, C.c_int, st]
+        L.rn_selftest_wait_budget.argtypes = [C.c_uint32, st]
         L.rn_gtao.argtypes = [C.POINTER(GBuf), vp, C.c_float, C.c_int, C.c_int, C.c_int, vp, st]
         L.rn_surrogate_ao.argtypes = [vp, C.POINTER(GBuf), vp, vp, C.c_int, C.c_float, C.c_float, vp, vp, vp, vp,
                                       C.POINTER(SurrogateStats), st]
@@ -328,6 +329,12 @@ def compute_ssao(g: GBuffer, samples: int = SS_SAMPLES, radius: float = AO_RADIU
     flags = args.flags | (RN_DEVICE_TRIG if device_trig else 0)
     _check(lib().rn_ssao(C.byref(gb), int(samples), float(radius), flags, args.ptr(out, np.float32), C.byref(st)), st)
     return out
+
+
+def selftest_wait_budget(spin_limit: int = 1 << 16) -> None:
+    """Runs the device-side wait-budget self-test; raises RnError (code RN_ERR_BUDGET)."""
+    st = Status()
+    _check(lib().rn_selftest_wait_budget(int(spin_limit), C.byref(st)), st)
 
 
 def gtao(g: GBuffer, camera, radius: float = 0.5, slices: int = 16, steps: int = 16):
