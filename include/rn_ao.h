@@ -238,6 +238,53 @@ int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t*
                          float tolerance, void* stream, float* err, rn_reconcile_result* out,
                          rn_status* st);
 
+/* The whole frame (raw::renderWithParams, raw/renderer/render.hpp:43-55; src/renderer/render.cpp:99-137)
+ * on the GPU: G-buffer with albedo, the AO passes, the shaded frame and its HDR view, motion.
+ * tris / normals: 9 floats per triangle; albedo: 3 floats per triangle (its mesh's material
+ * albedo); the light is scene.lights[0] (has_light 0: direction (0,-1,0), intensity 1).
+ * camera: eye(3), target(3), up(3), fovy (aspect w / h, near 0.1, far 100). prev_view_proj:
+ * the previous frame's view-projection (16 floats, row-major) for motion, or NULL (static
+ * frame: zero motion). options NULL: tolerance 0.12, rtao 1, lighting 2, spp 64, radius 2,
+ * ss_samples 24 (the CLI's). Any output plane may be NULL; host pointers by default, device
+ * pointers with RN_DEVICE_PTRS. Every plane equals the CPU path's bit for bit. */
+typedef struct rn_frame_scene {
+    const float* tris;
+    const float* normals;
+    const float* albedo;
+    uint32_t ntri;
+    float light_dir[3];
+    float light_intensity;
+    int has_light;
+} rn_frame_scene;
+typedef struct rn_frame_options {
+    float tolerance;
+    int rtao;        /* 0: no ray-traced pass; the frame is lit with SSAO (model 1), verdict unverifiable */
+    int lighting;    /* 2: sky and sun traced (the CLI default); 1: (0.2 + sun) x AO */
+    int spp;
+    float radius;
+    int ss_samples;
+} rn_frame_options;
+typedef struct rn_frame_out {
+    float* depth;      /* 1 float a pixel (screen-linear; +inf uncovered) */
+    float* position;   /* 3 */
+    float* normal;     /* 3 */
+    float* albedo;     /* 3 */
+    float* motion;     /* 2: current minus previous clip UV */
+    uint8_t* mask;     /* 1 byte */
+    float* ao_rt;      /* ray-traced AO */
+    float* sky;        /* lighting model 2 */
+    float* sun;
+    float* ao_ss;
+    float* error_map;
+    float* frame;      /* 3, clamped to [0, 1] */
+    float* hdr;        /* 3, unclamped linear radiance */
+    rn_reconcile_result rec;
+    int motion_valid, motion_total;
+    float view_proj[16];
+} rn_frame_out;
+int rn_render_frame(const rn_frame_scene* scene, const float* camera, const float* prev_view_proj, int w, int h,
+                    const rn_frame_options* options, int flags, rn_frame_out* out, rn_status* st);
+
 /* GTAO (ground-truth-based ambient occlusion, Jimenez et al. 2016): raw::post::gtao over
  * raw::post::viewGBuffer (raw/renderer/post.hpp:23-30; src/renderer/post_gtao.cpp:36-135),
  * the screen-space approximation judged, like SSAO, by the traced AO through rn_reconcile.

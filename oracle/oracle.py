@@ -73,6 +73,12 @@ def lib() -> C.CDLL:
         L.rno_test_scene.restype = C.c_int
         L.rno_test_scene.argtypes = [_F, _F, _F]
         L.rno_rasterize.argtypes = [_F, _F, C.c_int, _F, C.c_int, C.c_int, _F, _F, _F, _U8]
+        L.rno_rasterize_ex.argtypes = [_F, _F, C.c_int, _F, C.c_int, C.c_int, _F, _F, _F, _U8, _I32]
+        L.rno_test_scene_albedo.argtypes = [_F]
+        L.rno_view_proj.argtypes = [_F, C.c_int, C.c_int, _F]
+        L.rno_shade.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_int, _F, _F, _F, C.c_float, _F, _F]
+        L.rno_motion.restype = C.c_int
+        L.rno_motion.argtypes = [C.c_int, C.c_int, _F, _U8, _F, _F, _F]
         L.rno_view_gbuffer.argtypes = [C.c_int, C.c_int, _F, _F, _U8, _F, _F, _F, _F]
         L.rno_gtao.argtypes = [C.c_int, C.c_int, _F, _F, _F, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _D]
         L.rno_morton_keys.argtypes = [_F, C.c_int, _U64]
@@ -101,6 +107,8 @@ def ref() -> C.CDLL:
         R.ref_reconcile.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_float, _F, _F]
         R.ref_ploc.restype = C.c_int
         R.ref_ploc.argtypes = [_F, C.c_int, C.c_int, _I32, C.POINTER(C.c_uint32)]
+        R.ref_motion.restype = C.c_int
+        R.ref_motion.argtypes = [C.c_int, C.c_int, _F, _U8, _F, _F, _F]
         R.ref_view_gbuffer.argtypes = [C.c_int, C.c_int, _F, _F, _U8, _F, _F, _F, _F]
         R.ref_gtao.argtypes = [C.c_int, C.c_int, _F, _F, _F, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int,
                                _D]
@@ -241,6 +249,67 @@ def pgm_bytes(buf) -> bytes:
 
 def sha256(b: bytes) -> str:
     return hashlib.sha256(b).hexdigest()
+
+
+# ---------------------------------------------------------------- the whole frame
+def test_scene_albedo():
+    a = np.zeros((14, 3), np.float32)
+    lib().rno_test_scene_albedo(a)
+    return a
+
+
+def rasterize_ex(tris, nrm, cam, w: int, h: int):
+    """rasterize plus the triangle each covered pixel shows (-1 elsewhere)."""
+    tris = _f32(tris).reshape(-1, 9)
+    depth = np.zeros((h, w), np.float32)
+    pos = np.zeros((h, w, 3), np.float32)
+    nr = np.zeros((h, w, 3), np.float32)
+    mask = np.zeros((h, w), np.uint8)
+    tri = np.zeros((h, w), np.int32)
+    lib().rno_rasterize_ex(tris, _f32(nrm).reshape(-1, 9), len(tris), np.asarray(cam, np.float32), w, h, depth, pos,
+                           nr, mask, tri)
+    return depth, pos, nr, mask, tri
+
+
+def view_proj(cam, w: int, h: int):
+    vp = np.zeros(16, np.float32)
+    lib().rno_view_proj(np.asarray(cam, np.float32), w, h, vp)
+    return vp
+
+
+def shade(nrm, albedo, mask, model, a_or_sky, sun, ldir, li=1.0):
+    """(frame clamped, hdr) as shadeV2/shadeHDRV2 (model 2) or shade/shadeHDR (model 1)."""
+    mask = np.ascontiguousarray(mask, np.uint8)
+    h, w = mask.shape
+    frame = np.zeros((h, w, 3), np.float32)
+    hdr = np.zeros((h, w, 3), np.float32)
+    sun = _f32(sun) if sun is not None else np.zeros((h, w), np.float32)
+    lib().rno_shade(w, h, _f32(nrm), _f32(albedo), mask, int(model), _f32(a_or_sky), sun, _f32(ldir), float(li), frame,
+                    hdr)
+    return frame, hdr
+
+
+def motion(pos, mask, vp, prev_vp, use_ref=False):
+    mask = np.ascontiguousarray(mask, np.uint8)
+    h, w = mask.shape
+    m = np.zeros((h, w, 2), np.float32)
+    valid = (ref().ref_motion if use_ref else lib().rno_motion)(w, h, _f32(pos), mask, _f32(vp), _f32(prev_vp), m)
+    return m, valid
+
+
+def ppm_bytes(frame) -> bytes:
+    """frame.ppm of a clamped frame (src/core/image.cpp:9-18)."""
+    f = np.asarray(frame, np.float32)
+    h, w, _ = f.shape
+    v = (np.clip(f, 0.0, 1.0) * np.float32(255.0) + np.float32(0.5)).astype(np.uint8)
+    return b"P6\n%d %d\n255\n" % (w, h) + v.tobytes()
+
+
+def pfm3_bytes(img) -> bytes:
+    """frame_hdr.pfm (src/core/image.cpp:40-51): rows bottom to top, little-endian floats."""
+    f = np.asarray(img, np.float32)
+    h, w, _ = f.shape
+    return b"PF\n%d %d\n-1.0\n" % (w, h) + np.ascontiguousarray(f[::-1]).astype("<f4").tobytes()
 
 
 # ---------------------------------------------------------------- GTAO (raw::post)

@@ -15,6 +15,7 @@
 #include "raw/cert/reconcile.hpp"
 #include "raw/scene/scene.hpp"
 #include "raw/renderer/post.hpp"
+#include "raw/renderer/motion.hpp"
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -171,4 +172,22 @@ extern "C" void ref_gtao(int w, int h, const float* vpos, const float* vnrm, con
     p.radius = radius; p.slices = slices; p.steps = steps;
     const std::vector<double> r = post::gtao(v, p);
     std::memcpy(out, r.data(), n * sizeof(double));
+}
+
+// raw::computeMotion (src/renderer/motion.cpp:17-32) of a G-buffer's positions and mask between
+// two view-projections (16 floats each, row-major); returns the valid count.
+extern "C" int ref_motion(int w, int h, const float* pos, const uint8_t* mask, const float* vp16, const float* prev16,
+                          float* motion2) {
+    std::vector<float> nrm((std::size_t)w * h * 3, 0.0f);
+    GBuffer g = gbufferFrom(w, h, pos, nrm.data(), mask);
+    g.motion.resize(w, h);
+    Mat4 a, b;
+    std::memcpy(a.m, vp16, sizeof a.m);
+    std::memcpy(b.m, prev16, sizeof b.m);
+    const int valid = computeMotion(g, a, b);
+    for (std::size_t i = 0; i < (std::size_t)w * h; ++i) {
+        motion2[2 * i] = g.motion.px[i].x;
+        motion2[2 * i + 1] = g.motion.px[i].y;
+    }
+    return valid;
 }

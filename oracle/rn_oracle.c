@@ -487,7 +487,7 @@ static cvert lerp_vert(const cvert* a, const cvert* b, float t) {
     r.wn = v3m(a->wn.x + (b->wn.x - a->wn.x) * t, a->wn.y + (b->wn.y - a->wn.y) * t, a->wn.z + (b->wn.z - a->wn.z) * t);
     return r;
 }
-typedef struct { int w, h; float* depth; float* pos; float* nrm; uint8_t* mask; } rtarget;
+typedef struct { int w, h; float* depth; float* pos; float* nrm; uint8_t* mask; int32_t* tri; int cur; } rtarget;
 static void draw_tri(rtarget* T, const cvert v[3]) {
     const int w = T->w, h = T->h;
     float invw[3]; v3 sp[3];
@@ -529,13 +529,18 @@ static void draw_tri(rtarget* T, const cvert v[3]) {
         T->pos[3 * i] = P.x; T->pos[3 * i + 1] = P.y; T->pos[3 * i + 2] = P.z;
         T->nrm[3 * i] = Nn.x; T->nrm[3 * i + 1] = Nn.y; T->nrm[3 * i + 2] = Nn.z;
         T->mask[i] = 1;
+        if (T->tri) T->tri[i] = T->cur;
     }
 }
 /* cam10: eye(3) center(3) up(3) fovy; aspect = w / h as cameraFromParams
  * (src/tools/cli_params.cpp:12-18) sets it; nearZ 0.1, farZ 100. */
-RNO_API void rno_rasterize(const float* tris9, const float* nrm9, int ntri, const float* cam10,
-                           int w, int h, float* depth, float* pos, float* nrm, uint8_t* mask) {
+/* tri_out (may be NULL): the index of the triangle each covered pixel shows, -1 elsewhere;
+ * a mesh's material albedo is per triangle, so it gives the G-buffer's albedo plane
+ * (src/renderer/raster.cpp:76). */
+RNO_API void rno_rasterize_ex(const float* tris9, const float* nrm9, int ntri, const float* cam10,
+                              int w, int h, float* depth, float* pos, float* nrm, uint8_t* mask, int32_t* tri_out) {
     const size_t np = (size_t)w * h;
+    if (tri_out) for (size_t i = 0; i < np; ++i) tri_out[i] = -1;
     for (size_t i = 0; i < np; ++i) { depth[i] = INFINITY; mask[i] = 0; }
     memset(pos, 0, np * 3 * sizeof(float));
     memset(nrm, 0, np * 3 * sizeof(float));
@@ -544,8 +549,9 @@ RNO_API void rno_rasterize(const float* tris9, const float* nrm9, int ntri, cons
     const float aspect = h > 0 ? (float)w / (float)h : 1.0f, nearZ = 0.1f;
     const mat4 view = look_at(eye, ctr, up), proj = perspective(cam10[9], aspect, nearZ, 100.0f);
     const mat4 vp = mat_mul(&proj, &view);
-    rtarget T = {w, h, depth, pos, nrm, mask};
+    rtarget T = {w, h, depth, pos, nrm, mask, tri_out, 0};
     for (int t = 0; t < ntri; ++t) {
+        T.cur = t;
         cvert v[3]; int behind = 0;
         for (int k = 0; k < 3; ++k) {
             const float* p = tris9 + (size_t)t * 9 + 3 * k;
@@ -565,6 +571,83 @@ RNO_API void rno_rasterize(const float* tris9, const float* nrm9, int ntri, cons
         }
         for (int k = 1; k + 1 < n; ++k) { const cvert tt[3] = {c[0], c[k], c[k + 1]}; draw_tri(&T, tt); }
     }
+}
+RNO_API void rno_rasterize(const float* tris9, const float* nrm9, int ntri, const float* cam10,
+                           int w, int h, float* depth, float* pos, float* nrm, uint8_t* mask) {
+    rno_rasterize_ex(tris9, nrm9, ntri, cam10, w, h, depth, pos, nrm, mask, NULL);
+}
+/* The built-in scene's albedo per triangle (src/scene/scene.cpp:21-24): the plane's 2 then
+ * the box's 12, 3 floats each. */
+RNO_API void rno_test_scene_albedo(float* albedo3) {
+    for (int t = 0; t < 14; ++t) {
+        albedo3[3 * t] = t < 2 ? 0.7f : 0.8f;
+        albedo3[3 * t + 1] = t < 2 ? 0.7f : 0.3f;
+        albedo3[3 * t + 2] = t < 2 ? 0.7f : 0.2f;
+    }
+}
+/* The camera's view-projection (raw/scene/scene.hpp:21-22 with aspect w / h): 16 floats. */
+RNO_API void rno_view_proj(const float* cam10, int w, int h, float* vp16) {
+    const v3 eye = v3m(cam10[0], cam10[1], cam10[2]), ctr = v3m(cam10[3], cam10[4], cam10[5]);
+    const v3 up = v3m(cam10[6], cam10[7], cam10[8]);
+    const float aspect = h > 0 ? (float)w / (float)h : 1.0f;
+    const mat4 view = look_at(eye, ctr, up), proj = perspective(cam10[9], aspect, 0.1f, 100.0f);
+    const mat4 vp = mat_mul(&proj, &view);
+    memcpy(vp16, vp.m, sizeof vp.m);
+}
+
+/* ------------------------------------------------------------------ shading and motion
+ * src/renderer/composite.cpp:8-42 (radianceAt / radianceV2, shade / shadeV2 and their HDR
+ * forms): model 2 lights albedo x (0.2 sky + max(0, n . -l) li sun), model 1 albedo x
+ * (0.2 + max(0, n . -l) li) ao; the frame clamps to [0, 1], the HDR view does not; uncovered
+ * pixels are 0. src/renderer/motion.cpp:7-32 (projectToUV, computeMotion): current minus
+ * previous clip UV of the pixel's world position; returns the valid count. */
+RNO_API void rno_shade(int w, int h, const float* nrm, const float* albedo, const uint8_t* mask, int model,
+                       const float* a_or_sky, const float* sun, const float* ldir3, float li, float* frame,
+                       float* hdr) {
+    const v3 nl = mul3(v3m(ldir3[0], ldir3[1], ldir3[2]), -1.0f);
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+        float r[3] = {0, 0, 0};
+        if (mask[i]) {
+            const v3 n = v3m(nrm[3 * i], nrm[3 * i + 1], nrm[3 * i + 2]);
+            const float d = dot3(n, nl);
+            const float ndl = (d > 0.0f ? d : 0.0f) * li;
+            const float lit = model == 2 ? 0.2f * a_or_sky[i] + ndl * sun[i] : (0.2f + ndl) * a_or_sky[i];
+            for (int k = 0; k < 3; ++k) r[k] = albedo[3 * i + k] * lit;
+        }
+        for (int k = 0; k < 3; ++k) {
+            hdr[3 * i + k] = r[k];
+            frame[3 * i + k] = r[k] < 0.0f ? 0.0f : r[k] > 1.0f ? 1.0f : r[k];
+        }
+    }
+}
+static int project_uv(const mat4* vp, const float p[3], float uv[2]) {
+    const float hv[4] = {p[0], p[1], p[2], 1.0f};
+    float cs[4];
+    mat_vec(vp, hv, cs);
+    if (cs[3] <= 1e-6f) return 0;
+    const float invw = 1.0f / cs[3];
+    const float nx = cs[0] * invw, ny = cs[1] * invw;
+    uv[0] = nx * 0.5f + 0.5f;
+    uv[1] = 1.0f - (ny * 0.5f + 0.5f);
+    return 1;
+}
+RNO_API int rno_motion(int w, int h, const float* pos, const uint8_t* mask, const float* vp16, const float* prev16,
+                       float* motion2) {
+    mat4 cur, prev;
+    memcpy(cur.m, vp16, sizeof cur.m);
+    memcpy(prev.m, prev16, sizeof prev.m);
+    int valid = 0;
+    for (size_t i = 0; i < (size_t)w * h; ++i) {
+        motion2[2 * i] = motion2[2 * i + 1] = 0.0f;
+        if (!mask[i]) continue;
+        float a[2], b[2];
+        if (!project_uv(&cur, pos + 3 * i, a) || !project_uv(&prev, pos + 3 * i, b)) continue;
+        const float mx = a[0] - b[0], my = a[1] - b[1];
+        if (!isfinite(mx) || !isfinite(my)) continue;
+        motion2[2 * i] = mx; motion2[2 * i + 1] = my;
+        ++valid;
+    }
+    return valid;
 }
 
 /* ------------------------------------------------------------------ PLOC BVH

@@ -192,8 +192,10 @@ int trace_ao_device(const float* pos, const float* nrm, const uint8_t* mask, int
 void apply_tune(TraceParams& p, const rn_accel* accel) {
     const Tune& t = ctx().tune;
     p.frontier = t.trace_frontier && p.spp >= t.trace_frontier_min_spp;
-    p.packet_log2 = packet_log2(t.trace_packet);
     p.stack_need = 16 + 3 * (int)(accel ? accel->depth : 0);
+    // the frontier's seeds sit under the walk's own pushes: without room for both, walk from the root
+    if (p.stack_need > 96) p.frontier = 0;
+    p.packet_log2 = packet_log2(t.trace_packet);
 }
 
 int ensure_ctx(rn_status* st) {
@@ -298,6 +300,16 @@ int check_gbuf(const rn_gbuf* g, rn_status* st) {
 }
 
 struct StagedGbuf { const float* pos; const float* nrm; const uint8_t* mask; };
+
+// A buffer of the frame: the caller's device array when it passed one, else workspace.
+template <typename T>
+int frame_buf(T* p, size_t count, bool dev, Slot slot, T** out, rn_status* st) {
+    if (dev && p) { *out = p; return RN_OK; }
+    void* d = nullptr;
+    RN_TRY(ws_get(slot, count * sizeof(T), &d, st));
+    *out = (T*)d;
+    return RN_OK;
+}
 
 int stage_gbuf(const rn_gbuf* g, bool dev, StagedGbuf* s, rn_status* st) {
     const size_t np = (size_t)g->w * g->h;
@@ -664,6 +676,132 @@ int rn_ao_frame(const rn_gbuf* g, const rn_accel* accel, int spp, float radius, 
     }
     RN_TRY(check_device_error(st, "rn_ao_frame"));
     fill_result(r, tolerance, out);
+    return ok(st);
+}
+
+
+// raw::renderWithParams (src/renderer/render.cpp:99-137) on the GPU: the G-buffer with its
+// albedo plane, the ray-traced AO (lighting model 2: with sky and sun), SSAO and the
+// reconcile, the shaded frame and its HDR view, the motion plane. Every plane is the CPU
+// path's bit for bit.
+int rn_render_frame(const rn_frame_scene* sc, const float* camera, const float* prev_view_proj, int w, int h,
+                    const rn_frame_options* opt, int flags, rn_frame_out* out, rn_status* st) {
+    if (!sc || !camera || !out) return fail(st, RN_ERR_INVALID, "null argument");
+    if (sc->ntri > 0 && (!sc->tris || !sc->normals || !sc->albedo)) return fail(st, RN_ERR_INVALID, "null scene arrays");
+    if (w <= 0 || h <= 0 || (size_t)w * (size_t)h > ((size_t)1 << 31)) return fail(st, RN_ERR_INVALID, "size %dx%d", w, h);
+    if (sc->ntri >= (1u << 28)) return fail(st, RN_ERR_INVALID, "%u triangles: too many", sc->ntri);
+    rn_frame_options o{0.12f, 1, 2, 64, 2.0f, 24};
+    if (opt) o = *opt;
+    if (o.spp <= 0 || o.ss_samples < 0 || !(o.radius > 0.0f)) return fail(st, RN_ERR_INVALID, "spp %d ss %d radius %g", o.spp, o.ss_samples, o.radius);
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const size_t np = (size_t)w * h;
+    const int model = !o.rtao ? 1 : (o.lighting == 1 ? 1 : 2);
+    // scene in
+    const float *d_tris = nullptr, *d_nin = nullptr, *d_alb_in = nullptr;
+    RN_TRY(stage_in(sc->tris, (size_t)sc->ntri * 9, dev, WS_TRIS_IN, &d_tris, st));
+    RN_TRY(stage_in(sc->normals, (size_t)sc->ntri * 9, dev, WS_NRM_IN, &d_nin, st));
+    RN_TRY(stage_in(sc->albedo, (size_t)sc->ntri * 3, dev, WS_ALB_IN, &d_alb_in, st));
+    // G-buffer
+    float *d_depth, *d_pos, *d_nrm, *d_alb, *d_mot, *d_ao = nullptr, *d_sky = nullptr, *d_sun = nullptr, *d_ss, *d_err;
+    float *d_frame, *d_hdr;
+    uint8_t* d_mask;
+    RN_TRY(frame_buf(out->depth, np, dev, WS_DEPTH, &d_depth, st));
+    RN_TRY(frame_buf(out->position, np * 3, dev, WS_POS, &d_pos, st));
+    RN_TRY(frame_buf(out->normal, np * 3, dev, WS_NRM, &d_nrm, st));
+    RN_TRY(frame_buf(out->albedo, np * 3, dev, WS_ALB, &d_alb, st));
+    RN_TRY(frame_buf(out->mask, np, dev, WS_MASK, &d_mask, st));
+    RN_TRY(frame_buf(out->motion, np * 2, dev, WS_MOTION, &d_mot, st));
+    RN_TRY(frame_buf(out->ao_ss, np, dev, WS_SS, &d_ss, st));
+    RN_TRY(frame_buf(out->error_map, np, dev, WS_ERR, &d_err, st));
+    RN_TRY(frame_buf(out->frame, np * 3, dev, WS_FRAME, &d_frame, st));
+    RN_TRY(frame_buf(out->hdr, np * 3, dev, WS_HDR, &d_hdr, st));
+    if (o.rtao) {
+        RN_TRY(frame_buf(out->ao_rt, np, dev, WS_AO, &d_ao, st));
+        if (model == 2) {
+            RN_TRY(frame_buf(out->sky, np, dev, WS_SKY, &d_sky, st));
+            RN_TRY(frame_buf(out->sun, np, dev, WS_SUN, &d_sun, st));
+        }
+    }
+    const M4 vp = view_proj(camera, w, h, 0.1f, 100.0f);
+    void* small = nullptr;
+    RN_TRY(ws_get(WS_FRAME_SMALL, 256, &small, st));
+    float* d_vp = (float*)small;
+    unsigned* d_valid = (unsigned*)((char*)small + 128);
+    RN_CUDA(cudaMemcpyAsync(d_vp, vp.m, 64, cudaMemcpyHostToDevice, c.stream), st);
+    RN_CUDA(cudaMemsetAsync(d_valid, 0, 8, c.stream), st);
+    size_t pairs = (size_t)8 * sc->ntri + 1024;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        const size_t bytes = raster_scratch_bytes(sc->ntri, np, pairs);
+        void* scratch = nullptr;
+        RN_TRY(ws_get(WS_RASTER, bytes, &scratch, st));
+        size_t needed = 0;
+        const int rc = launch_raster(d_tris, d_nin, sc->ntri, d_vp, 0.1f, w, h, (char*)scratch, ctx().ws[WS_RASTER].cap,
+                                     d_depth, d_pos, d_nrm, d_mask, c.stream, &needed, d_alb_in, d_alb);
+        if (rc == RN_OK) break;
+        if (rc == RN_ERR_NO_MEMORY && attempt == 0) { pairs = needed + needed / 8 + 1024; continue; }
+        return rc == RN_ERR_NO_MEMORY ? fail(st, rc, "raster: %zu bin pairs", needed)
+                                      : cuda_fail(st, cudaGetLastError(), "raster kernels");
+    }
+    const float ldir[3] = {sc->has_light ? sc->light_dir[0] : 0.0f, sc->has_light ? sc->light_dir[1] : -1.0f,
+                           sc->has_light ? sc->light_dir[2] : 0.0f};
+    const float li = sc->has_light ? sc->light_intensity : 1.0f;
+    StagedGbuf sg{d_pos, d_nrm, d_mask};
+    rn_accel* acc = nullptr;
+    RecOut r{};
+    if (o.rtao) {
+        // the accelerator is built per frame from the scene's triangles, as the rtao pass does
+        RN_TRY(rn_accel_build(d_tris, sc->ntri, RN_DEVICE_PTRS, &acc, st));
+        const float tl[3] = {-ldir[0], -ldir[1], -ldir[2]};
+        int rc = do_visibility(sg, w, h, acc, o.spp, o.radius, tl, model == 2 ? RN_SKY : 0, d_ao, d_sky, d_sun, st);
+        if (rc == RN_OK) {
+            const int nb = ssao_blocks(w, h);
+            void *parts = nullptr, *ro = nullptr;
+            rc = ws_get(WS_PARTIALS, (size_t)nb * sizeof(RecPartial), &parts, st);
+            if (rc == RN_OK) rc = ws_get(WS_COUNTERS, sizeof(RecOut), &ro, st);
+            if (rc == RN_OK && launch_ssao(w, h, d_pos, d_nrm, d_mask, o.ss_samples, o.radius, c.trig_corr, d_ss, d_ao,
+                                           d_err, (RecPartial*)parts, (RecOut*)ro, c.stream) != RN_OK)
+                rc = cuda_fail(st, cudaGetLastError(), "ssao_kernel (fused reconcile)");
+            if (rc == RN_OK && cudaMemcpyAsync(&r, ro, sizeof r, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+                rc = cuda_fail(st, cudaGetLastError(), "reconcile read-back");
+        }
+        if (rc != RN_OK) { cudaStreamSynchronize(c.stream); rn_accel_free(acc); return rc; }
+    } else {
+        if (launch_ssao(w, h, d_pos, d_nrm, d_mask, o.ss_samples, o.radius, c.trig_corr, d_ss, nullptr, nullptr,
+                        nullptr, nullptr, c.stream) != RN_OK)
+            return cuda_fail(st, cudaGetLastError(), "ssao_kernel");
+        RN_CUDA(cudaMemsetAsync(d_err, 0, np * 4, c.stream), st);   // no reference: an empty reconcile
+    }
+    const float* light_ao = model == 2 ? d_sky : (o.rtao ? d_ao : d_ss);
+    int rc = launch_shade(w, h, d_nrm, d_alb, d_mask, model, light_ao, d_sun, ldir, li, d_frame, d_hdr, c.stream);
+    if (rc == RN_OK)
+        rc = launch_motion(w, h, d_pos, d_mask, vp.m, prev_view_proj ? prev_view_proj : vp.m, d_mot, d_valid, c.stream);
+    unsigned counts[2] = {0, 0};
+    if (rc == RN_OK && cudaMemcpyAsync(counts, d_valid, 8, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+        rc = cuda_fail(st, cudaGetLastError(), "motion counts");
+    if (rc == RN_OK && !dev) {
+        const struct { void* h; const void* d; size_t bytes; } outs[] = {
+            {out->depth, d_depth, np * 4}, {out->position, d_pos, np * 12}, {out->normal, d_nrm, np * 12},
+            {out->albedo, d_alb, np * 12}, {out->mask, d_mask, np}, {out->motion, d_mot, np * 8},
+            {out->ao_rt, d_ao, np * 4}, {o.rtao && model == 2 ? out->sky : nullptr, d_sky, np * 4},
+            {o.rtao && model == 2 ? out->sun : nullptr, d_sun, np * 4},
+            {out->ao_ss, d_ss, np * 4}, {out->error_map, d_err, np * 4}, {out->frame, d_frame, np * 12},
+            {out->hdr, d_hdr, np * 12}};
+        for (const auto& x : outs)
+            if (rc == RN_OK && x.h && x.d && cudaMemcpyAsync(x.h, x.d, x.bytes, cudaMemcpyDeviceToHost, c.stream) != cudaSuccess)
+                rc = cuda_fail(st, cudaGetLastError(), "frame read-back");
+    }
+    const cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (acc) rn_accel_free(acc);
+    if (rc != RN_OK) return rc;
+    if (e != cudaSuccess) return cuda_fail(st, e, "rn_render_frame");
+    RN_TRY(check_device_error(st, "rn_render_frame"));
+    if (o.rtao) fill_result(r, o.tolerance, &out->rec);
+    else out->rec = rn_reconcile_result{0.0f, 0.0f, 0, 0, 0.0};
+    out->motion_valid = (int)counts[0];
+    out->motion_total = (int)counts[1];
+    for (int k = 0; k < 16; ++k) out->view_proj[k] = vp.m[k];
     return ok(st);
 }
 

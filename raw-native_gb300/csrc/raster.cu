@@ -169,7 +169,8 @@ __global__ void raster_pairs(const RasterTri* __restrict__ recs, const uint2* __
 // raster.cpp:64-80 for the surviving fragment of each pixel.
 __global__ void raster_resolve(const RasterTri* __restrict__ recs, const unsigned long long* __restrict__ keys, int w,
                                int h, float* __restrict__ depth, float* __restrict__ pos, float* __restrict__ nrm,
-                               uint8_t* __restrict__ mask) {
+                               uint8_t* __restrict__ mask, const float* __restrict__ albedo_tri,
+                               float* __restrict__ albedo) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
     const size_t i = (size_t)y * w + x;
@@ -178,10 +179,16 @@ __global__ void raster_resolve(const RasterTri* __restrict__ recs, const unsigne
         if (depth) depth[i] = __int_as_float(0x7f800000);
         pos[3 * i] = pos[3 * i + 1] = pos[3 * i + 2] = 0.0f;
         nrm[3 * i] = nrm[3 * i + 1] = nrm[3 * i + 2] = 0.0f;
+        if (albedo) albedo[3 * i] = albedo[3 * i + 1] = albedo[3 * i + 2] = 0.0f;
         mask[i] = 0;
         return;
     }
-    const RasterTri& T = recs[(uint32_t)(key & 0xFFFFFFFFull)];
+    const uint32_t rec = (uint32_t)(key & 0xFFFFFFFFull);
+    const RasterTri& T = recs[rec];
+    if (albedo) {                   // a record's triangle is rec / 2 (two record slots per triangle)
+        const float* a = albedo_tri + 3 * (size_t)(rec >> 1);
+        albedo[3 * i] = a[0]; albedo[3 * i + 1] = a[1]; albedo[3 * i + 2] = a[2];
+    }
     float w0, w1, w2;
     weights(T, x, y, w0, w1, w2);
     if (depth) depth[i] = frag_depth(T, w0, w1, w2);
@@ -213,7 +220,7 @@ size_t raster_scratch_bytes(uint32_t ntri, size_t npx, size_t npairs) {
 
 int launch_raster(const float* tris, const float* nrm, uint32_t ntri, const float* d_vp, float nearZ, int w, int h,
                   char* scratch, size_t scratch_bytes, float* depth, float* pos, float* nrmo, uint8_t* mask,
-                  cudaStream_t s, size_t* pairs_needed) {
+                  cudaStream_t s, size_t* pairs_needed, const float* albedo_tri, float* albedo) {
     const uint32_t nrec = 2 * ntri;
     const size_t npx = (size_t)w * h;
     size_t off = 0;
@@ -239,7 +246,7 @@ int launch_raster(const float* tris, const float* nrm, uint32_t ntri, const floa
         if (npairs) raster_pairs<<<(npairs + 3) / 4, 256, 0, s>>>(recs, pairs, npairs, w, keys);
     }
     const dim3 blk(32, 8), grid((w + 31) / 32, (h + 7) / 8);
-    raster_resolve<<<grid, blk, 0, s>>>(recs, keys, w, h, depth, pos, nrmo, mask);
+    raster_resolve<<<grid, blk, 0, s>>>(recs, keys, w, h, depth, pos, nrmo, mask, albedo_tri, albedo);
     *pairs_needed = npairs;
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }

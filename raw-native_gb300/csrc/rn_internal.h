@@ -32,6 +32,7 @@ enum Slot {
     WS_PARTIALS, WS_WORKLIST, WS_COUNTERS, WS_RAYS, WS_TMAX, WS_HITS, WS_TRIS_IN,
     WS_NRM_IN, WS_RASTER, WS_DEPTH, WS_STATS,
     WS_SUR_AO4, WS_SUR_PRED, WS_SUR_FB, WS_SUR_AOFB, WS_SUR_STATS, WS_VPOS, WS_VNRM, WS_VDEPTH, WS_GTAO,
+    WS_ALB_IN, WS_ALB, WS_MOTION, WS_FRAME, WS_HDR, WS_FRAME_SMALL,
     WS_COUNT
 };
 
@@ -197,6 +198,16 @@ void apply_tune(TraceParams& p, const rn_accel* accel);
 int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned long long* counts = nullptr,
                  uint32_t stride = 1);
 
+// ---------------------------------------------------------------- shading and motion (frame.cu)
+// shadeV2 / shadeHDRV2 (model 2: a_or_sky = sky) or shade / shadeHDR (model 1: a_or_sky = the
+// AO), frame and hdr 3 floats a pixel; motion: current minus previous clip UV (2 floats a
+// pixel), the valid count added to valid[0] and the covered count to valid[1].
+int launch_shade(int w, int h, const float* nrm, const float* albedo, const uint8_t* mask, int model,
+                 const float* a_or_sky, const float* sun, const float ldir[3], float li, float* frame, float* hdr,
+                 cudaStream_t s);
+int launch_motion(int w, int h, const float* pos, const uint8_t* mask, const float* vp16, const float* prev16,
+                  float* motion, unsigned* valid, cudaStream_t s);
+
 // ---------------------------------------------------------------- GTAO (gtao.cu)
 // The view-space G-buffer (view16: the camera's row-major view matrix) into vpos/vnrm/vdepth,
 // then GTAO (radius, slices, steps; fovy and aspect w / h of the camera) into out.
@@ -210,7 +221,7 @@ size_t raster_scratch_bytes(uint32_t ntri, size_t npx, size_t npairs);
 // RN_ERR_NO_MEMORY with *pairs_needed set when the scratch holds too few pairs.
 int launch_raster(const float* tris, const float* nrm, uint32_t ntri, const float* d_vp, float nearZ, int w, int h,
                   char* scratch, size_t scratch_bytes, float* depth, float* pos, float* nrm_out, uint8_t* mask,
-                  cudaStream_t s, size_t* pairs_needed);
+                  cudaStream_t s, size_t* pairs_needed, const float* albedo_tri = nullptr, float* albedo = nullptr);
 int scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* bsum, uint32_t* total, cudaStream_t s);
 int launch_occluded(const Node4* nodes, const LeafTri* tris, int has_geometry, const float* rays,
                     const float* tmax, uint32_t n, uint8_t* hit, uint32_t* err_word, cudaStream_t s);

@@ -34,7 +34,8 @@ EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_ac
            "rn_unet_free", "rn_unet_param_count", "rn_unet_forward", "rn_unet_train_step", "rn_unet_get_params",
            "rn_unet_set_params", "rn_unet_get_grads", "rn_unet_get_state", "rn_unet_set_state",
            "rn_unet_set_clip", "rn_unet_last_grad_norm",
-           "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3", "rn_surrogate_ao", "rn_gtao", "rn_selftest_wait_budget")
+           "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3", "rn_surrogate_ao", "rn_gtao", "rn_selftest_wait_budget",
+           "rn_render_frame")
 
 
 class RnError(RuntimeError):
@@ -58,6 +59,16 @@ class SurrogateStats(C.Structure):
                 ("reserved", C.c_float)]
 
 
+class FrameScene(C.Structure):
+    _fields_ = [("tris", C.c_void_p), ("normals", C.c_void_p), ("albedo", C.c_void_p), ("ntri", C.c_uint32),
+                ("light_dir", C.c_float * 3), ("light_intensity", C.c_float), ("has_light", C.c_int)]
+
+
+class FrameOptions(C.Structure):
+    _fields_ = [("tolerance", C.c_float), ("rtao", C.c_int), ("lighting", C.c_int), ("spp", C.c_int),
+                ("radius", C.c_float), ("ss_samples", C.c_int)]
+
+
 class View(C.Structure):
     _fields_ = [("w", C.c_int), ("h", C.c_int), ("spp", C.c_int), ("radius", C.c_float), ("position", C.c_void_p),
                 ("normal", C.c_void_p), ("mask", C.c_void_p), ("ao", C.c_void_p), ("sky", C.c_void_p),
@@ -67,6 +78,17 @@ class View(C.Structure):
 class ReconcileOut(C.Structure):
     _fields_ = [("rmse", C.c_float), ("max_error", C.c_float), ("pixels", C.c_int32),
                 ("within_tolerance", C.c_int32), ("sum_sq", C.c_double)]
+
+
+FRAME_PLANES = (("depth", 1, np.float32), ("position", 3, np.float32), ("normal", 3, np.float32),
+                ("albedo", 3, np.float32), ("motion", 2, np.float32), ("mask", 1, np.uint8), ("ao_rt", 1, np.float32),
+                ("sky", 1, np.float32), ("sun", 1, np.float32), ("ao_ss", 1, np.float32),
+                ("error_map", 1, np.float32), ("frame", 3, np.float32), ("hdr", 3, np.float32))
+
+
+class FrameOut(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k, _, _ in FRAME_PLANES] + [
+        ("rec", ReconcileOut), ("motion_valid", C.c_int), ("motion_total", C.c_int), ("view_proj", C.c_float * 16)]
 
 
 _lib = None
@@ -115,6 +137,8 @@ def lib() -> C.CDLL:
         L.rn_unet_set_clip.argtypes = [vp, C.c_float, st]
         L.rn_tune_set.argtypes = [C.c_char_p, C.c_int, st]
         L.rn_selftest_wait_budget.argtypes = [C.c_uint32, st]
+        L.rn_render_frame.argtypes = [C.POINTER(FrameScene), vp, vp, C.c_int, C.c_int, C.POINTER(FrameOptions), C.c_int,
+                                      C.POINTER(FrameOut), st]
         L.rn_gtao.argtypes = [C.POINTER(GBuf), vp, C.c_float, C.c_int, C.c_int, C.c_int, vp, st]
         L.rn_surrogate_ao.argtypes = [vp, C.POINTER(GBuf), vp, vp, C.c_int, C.c_float, C.c_float, vp, vp, vp, vp,
                                       C.POINTER(SurrogateStats), st]
@@ -329,6 +353,34 @@ def compute_ssao(g: GBuffer, samples: int = SS_SAMPLES, radius: float = AO_RADIU
     flags = args.flags | (RN_DEVICE_TRIG if device_trig else 0)
     _check(lib().rn_ssao(C.byref(gb), int(samples), float(radius), flags, args.ptr(out, np.float32), C.byref(st)), st)
     return out
+
+
+def render_frame(tris, normals, albedo, camera, w: int, h: int, light=None, prev_view_proj=None, rtao: bool = True,
+                 lighting: int = 2, spp: int = RT_SAMPLES, radius: float = AO_RADIUS, ss_samples: int = SS_SAMPLES,
+                 tolerance: float = TOLERANCE):
+    """raw::renderWithParams on the GPU: dict of every plane (numpy for numpy inputs, CUDA
+    tensors for CUDA inputs) plus rec (ReconcileResult without its map), motion_valid,
+    motion_total and view_proj. light = (direction, intensity) of scene.lights[0] or None."""
+    args = _Args(tris, normals, albedo)
+    n = int(tris.shape[0])
+    like = tris
+    outs = {k: args.out(like, (h, w, c) if c > 1 else (h, w), dt) for k, c, dt in FRAME_PLANES}
+    sc = FrameScene(args.ptr(tris, np.float32), args.ptr(normals, np.float32), args.ptr(albedo, np.float32), n,
+                    (C.c_float * 3)(*(light[0] if light is not None else (0.0, -1.0, 0.0))),
+                    float(light[1]) if light is not None else 1.0, 1 if light is not None else 0)
+    opt = FrameOptions(float(tolerance), 1 if rtao else 0, int(lighting), int(spp), float(radius), int(ss_samples))
+    fo = FrameOut()
+    for k, _, dt in FRAME_PLANES:
+        setattr(fo, k, args.ptr(outs[k], dt))
+    cam = (C.c_float * 10)(*[float(v) for v in camera])
+    prev = (C.c_float * 16)(*[float(v) for v in prev_view_proj]) if prev_view_proj is not None else None
+    st = Status()
+    _check(lib().rn_render_frame(C.byref(sc), C.cast(cam, C.c_void_p), C.cast(prev, C.c_void_p) if prev is not None else None,
+                                 int(w), int(h), C.byref(opt), args.flags, C.byref(fo), C.byref(st)), st)
+    outs["rec"] = _result(None, fo.rec)
+    outs["motion_valid"], outs["motion_total"] = fo.motion_valid, fo.motion_total
+    outs["view_proj"] = np.array(list(fo.view_proj), np.float32)
+    return outs
 
 
 def selftest_wait_budget(spin_limit: int = 1 << 16) -> None:

@@ -75,6 +75,7 @@ def main(ref_dir):
                "ao_error.pgm": O.sha256(O.pgm_bytes(bufs["err"].reshape(h, w)))}
         assert got == files, (name, got, files)
         cases[name] = dict(args=case["args"], width=w, height=h, camera=cam, files=files,
+                           frame_files={f: case["files"][f] for f in ("frame.ppm", "frame_hdr.pfm")},
                            exact=dict(rmse=float(stats[0]), maxError=float(stats[1]), pixels=int(stats[2]),
                                       within=bool(stats[3])),
                            sky_sha256=O.sha256(O.pfm1_bytes(bufs["sky"].reshape(h, w))),

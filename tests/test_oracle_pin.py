@@ -170,3 +170,36 @@ def test_gtao_restatement_matches_reference_golden(oracle):
         a = oracle.gtao(vp, vn, vd, cam[9], case["radius"], case["slices"], case["steps"])
         assert int(mask.sum()) == case["covered"]
         assert oracle.sha256(np.ascontiguousarray(a).tobytes()) == case["sha256"], name
+
+
+@pytest.mark.parametrize("case", sorted(json.load(open(os.path.join(os.path.dirname(__file__), "golden",
+                                                                    "identity.json")))["cases"]))
+def test_oracle_frame_reproduces_reference_goldens(oracle, case):
+    """The shaded frame (shadeV2 / shadeHDRV2 over the G-buffer's albedo and the traced sky
+    and sun) reproduces the reference's committed frame.ppm and frame_hdr.pfm SHA-256."""
+    c = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "identity.json")))["cases"][case]
+    w, h, cam = c["width"], c["height"], c["camera"]
+    if w * h > 600 * 600 and platform.machine() != "x86_64":
+        pytest.skip("large case: CPU time")
+    tris, nrm9, light = oracle.test_scene()
+    alb = oracle.test_scene_albedo()
+    _, pos, nrm, mask, tri = oracle.rasterize_ex(tris, nrm9, cam, w, h)
+    albedo = np.where(mask[..., None] > 0, alb[np.maximum(tri, 0)], 0).astype(np.float32)
+    ao, sky, sun = oracle.trace(pos, nrm, mask, tris, oracle.RT_SAMPLES, oracle.AO_RADIUS, to_light=-light,
+                                threads=os.cpu_count() or 1)
+    frame, hdr = oracle.shade(nrm, albedo, mask, 2, sky, sun, light, 1.0)
+    assert oracle.sha256(oracle.ppm_bytes(frame)) == c["frame_files"]["frame.ppm"]
+    assert oracle.sha256(oracle.pfm3_bytes(hdr)) == c["frame_files"]["frame_hdr.pfm"]
+
+
+def test_motion_restatement_equals_reference_build(oracle):
+    if not oracle.ref_available():
+        pytest.skip("the reference build (oracle/_ref) is absent")
+    tris, nrm9, _ = oracle.test_scene()
+    cam = oracle.DEFAULT_CAMERA
+    prev = (4.3, 3.8, 5.7, 0.0, 1.0, 0.0, 0.0, 1.0, 0.0, 0.9)
+    _, pos, nrm, mask = oracle.rasterize(tris, nrm9, cam, 320, 200)
+    vp, pv = oracle.view_proj(cam, 320, 200), oracle.view_proj(prev, 320, 200)
+    a, na = oracle.motion(pos, mask, vp, pv)
+    b, nb = oracle.motion(pos, mask, vp, pv, use_ref=True)
+    assert na == nb == int(mask.sum()) and np.array_equal(a, b) and np.abs(a).max() > 0.01
