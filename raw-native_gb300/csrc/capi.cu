@@ -3,6 +3,7 @@
 // stage host buffers, launch the kernels and return results.
 #include "rn_internal.h"
 #include "rn_device.cuh"
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdlib>
@@ -119,6 +120,7 @@ const TuneKey kTuneKeys[] = {
     {"ssao_tile_h", "RN_TUNE_SSAO_TILE_H", &Tune::ssao_tile_h, {4, 8, 16}, 3},
     {"conv_bn_max", "RN_TUNE_CONV_BN_MAX", &Tune::conv_bn_max, {64, 128, 256}, 3},
     {"conv_halo", "RN_TUNE_CONV_HALO", &Tune::conv_halo, {0, 1}, 2},
+    {"frame_direct", "RN_TUNE_FRAME_DIRECT", &Tune::frame_direct, {0, 1}, 2},
 };
 
 const TuneKey* find_tune_key(const char* name) {
@@ -319,8 +321,8 @@ int stage_gbuf(const rn_gbuf* g, bool dev, StagedGbuf* s, rn_status* st) {
     return RN_OK;
 }
 
-int do_visibility(const StagedGbuf& g, int w, int h, const rn_accel* accel, int spp, float radius,
-                  const float* to_light, int flags, float* ao, float* sky, float* sun, rn_status* st) {
+TraceParams vis_params(const StagedGbuf& g, int w, int h, const rn_accel* accel, int spp, float radius,
+                       const float* to_light, int flags, float* ao, float* sky, float* sun) {
     Context& c = ctx();
     TraceParams p{};
     p.w = w; p.h = h;
@@ -336,8 +338,65 @@ int do_visibility(const StagedGbuf& g, int w, int h, const rn_accel* accel, int 
     p.ao = ao; p.sky = sky; p.sun = sun;
     p.err_word = c.dev_error;
     apply_tune(p, accel);
+    return p;
+}
+
+int do_visibility(const StagedGbuf& g, int w, int h, const rn_accel* accel, int spp, float radius,
+                  const float* to_light, int flags, float* ao, float* sky, float* sun, rn_status* st) {
+    Context& c = ctx();
+    const TraceParams p = vis_params(g, w, h, accel, spp, radius, to_light, flags, ao, sky, sun);
     if (launch_trace(p, c.sm_count, c.stream) != RN_OK) return cuda_fail(st, cudaGetLastError(), "trace_kernel");
     return RN_OK;
+}
+
+void fill_result(const RecOut& r, float tolerance, rn_reconcile_result* out);
+
+// The device address of a pinned, mapped host buffer (nullptr for any other kind).
+void* mapped(const void* p) {
+    cudaPointerAttributes a;
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// rn_ao_frame with pinned, mapped host buffers and no copies. The traversal reads each
+// pixel's G-buffer entry straight from host memory (25 bytes, once per pixel, against
+// hundreds of rays), writes AO (sky, sun) straight into the caller's host images, and
+// mirrors the G-buffer entry and the AO into HBM as it goes. The SSAO, whose taps re-read
+// neighbours, and the fused reconcile then run on the mirror and write the SSAO image and the
+// error map into host memory. No copy engine runs and nothing waits for one; every output is
+// the device-buffer frame's bit for bit.
+int direct_frame(const rn_gbuf* g, const rn_accel* accel, int spp, float radius, int ss_samples, float tolerance,
+                 const float tl[3], int flags, float* h_ao, float* h_sky, float* h_sun, float* h_ss, float* h_err,
+                 rn_reconcile_result* out, rn_status* st) {
+    Context& c = ctx();
+    const int w = g->w, h = g->h;
+    const size_t np = (size_t)w * h;
+    const bool want_sky = (flags & RN_SKY) != 0;
+    const StagedGbuf hg{(const float*)mapped(g->position), (const float*)mapped(g->normal),
+                        (const uint8_t*)mapped(g->mask)};
+    void *vm, *parts, *ro;
+    RN_TRY(ws_get(WS_MIRROR, np * 29, &vm, st));
+    const int nb = ssao_blocks(w, h);
+    RN_TRY(ws_get(WS_PARTIALS, (size_t)nb * sizeof(RecPartial), &parts, st));
+    RN_TRY(ws_get(WS_COUNTERS, sizeof(RecOut), &ro, st));
+    uint8_t* m = (uint8_t*)vm;
+    TraceParams p = vis_params(hg, w, h, accel, spp, radius, tl, flags, (float*)mapped(h_ao),
+                               want_sky ? (float*)mapped(h_sky) : nullptr, want_sky ? (float*)mapped(h_sun) : nullptr);
+    p.mirror = m;
+    if (launch_trace(p, c.sm_count, c.stream) != RN_OK) return cuda_fail(st, cudaGetLastError(), "trace_kernel");
+    const uint8_t* corr = (flags & RN_DEVICE_TRIG) ? nullptr : c.trig_corr;
+    if (launch_ssao(w, h, mirror_pos(m, np), mirror_nrm(m, np), mirror_mask(m, np), ss_samples, radius, corr,
+                    (float*)mapped(h_ss), mirror_ao(m, np), h_err ? (float*)mapped(h_err) : nullptr,
+                    (RecPartial*)parts, (RecOut*)ro, c.stream) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "ssao_kernel (fused reconcile)");
+    RecOut r;
+    RN_CUDA(cudaMemcpyAsync(&r, ro, sizeof r, cudaMemcpyDeviceToHost, c.stream), st);
+    RN_TRY(check_device_error(st, "rn_ao_frame"));
+    fill_result(r, tolerance, out);
+    return ok(st);
 }
 
 int check_vis_args(const rn_gbuf* g, const rn_accel* accel, int spp, const float* to_light, int flags, const float* ao,
@@ -645,11 +704,16 @@ int rn_ao_frame(const rn_gbuf* g, const rn_accel* accel, int spp, float radius, 
     Context& c = ctx();
     const bool dev = (flags & RN_DEVICE_PTRS) != 0;
     const size_t np = (size_t)g->w * g->h;
+    float tl[3] = {0.0f, 1.0f, 0.0f};
+    if (flags & RN_SKY) { tl[0] = to_light[0]; tl[1] = to_light[1]; tl[2] = to_light[2]; }
+    // host frames of 256k pixels and more, every buffer pinned and mapped: no copies
+    if (!dev && c.tune.frame_direct && np >= ((size_t)1 << 18) && mapped(g->position) && mapped(g->normal) &&
+        mapped(g->mask) && mapped(ao) && mapped(ao_ss) && (!err || mapped(err)) &&
+        (!(flags & RN_SKY) || (mapped(sky) && mapped(sun))))
+        return direct_frame(g, accel, spp, radius, ss_samples, tolerance, tl, flags, ao, sky, sun, ao_ss, err, out, st);
     StagedGbuf sg;
     RN_TRY(stage_gbuf(g, dev, &sg, st));
     float *d_ao, *d_sky = nullptr, *d_sun = nullptr, *d_ss, *d_err = nullptr;
-    float tl[3] = {0.0f, 1.0f, 0.0f};
-    if (flags & RN_SKY) { tl[0] = to_light[0]; tl[1] = to_light[1]; tl[2] = to_light[2]; }
     RN_TRY(stage_out(ao, np, dev, WS_AO, &d_ao, st));
     if (flags & RN_SKY) {
         RN_TRY(stage_out(sky, np, dev, WS_SKY, &d_sky, st));

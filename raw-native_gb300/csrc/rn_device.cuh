@@ -38,6 +38,7 @@ __device__ __forceinline__ v3 normalize(v3 v) {
     return l > 0.0f ? scale(v, fdiv(1.0f, l)) : v;
 }
 __device__ __forceinline__ v3 load3(const float* p) { return mk(p[0], p[1], p[2]); }
+__device__ __forceinline__ void store3(float* p, const v3& v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
 
 // ------------------------------------------------------------------ sampler
 // src/renderer/ray_ao.cpp:8-12 (and ssao.cpp:6-10): integer hash, exact float in [0,1).

@@ -32,7 +32,7 @@ enum Slot {
     WS_PARTIALS, WS_WORKLIST, WS_COUNTERS, WS_RAYS, WS_TMAX, WS_HITS, WS_TRIS_IN,
     WS_NRM_IN, WS_RASTER, WS_DEPTH, WS_STATS,
     WS_SUR_AO4, WS_SUR_PRED, WS_SUR_FB, WS_SUR_AOFB, WS_SUR_STATS, WS_VPOS, WS_VNRM, WS_VDEPTH, WS_GTAO,
-    WS_ALB_IN, WS_ALB, WS_MOTION, WS_FRAME, WS_HDR, WS_FRAME_SMALL,
+    WS_ALB_IN, WS_ALB, WS_MOTION, WS_FRAME, WS_HDR, WS_FRAME_SMALL, WS_MIRROR,
     WS_COUNT
 };
 
@@ -47,6 +47,7 @@ struct Tune {
     int ssao_tile_h = 8;        // SSAO tile: 32 x ssao_tile_h pixels, one thread each; 4, 8 or 16
     int conv_bn_max = 256;      // largest GEMM tile width (columns of C per CTA): 64, 128 or 256
     int conv_halo = 1;          // 128-pixel row tiles from one halo box per tile (where they fit)
+    int frame_direct = 1;       // host-buffer frames: the passes read and write mapped host memory
 };
 
 struct Context {
@@ -181,7 +182,15 @@ struct TraceParams {
     int frontier;         // AO-only walks start from a per-warp frontier (0: from the root)
     int packet_log2;      // log2 of the packet width (pixels per warp row): 2, 3 or 4
     int stack_need;       // entries the walk can push on this tree: 16 + 3 x wide depth
+    // copy-through of a G-buffer read from host memory (null: none): every pixel's position,
+    // normal, AO and mask are also written to a device buffer laid out as
+    // [position w*h*12 B][normal w*h*12 B][ao w*h*4 B][mask w*h B] (mirror_* below)
+    uint8_t* mirror;
 };
+__host__ __device__ inline float* mirror_pos(uint8_t* m, size_t) { return (float*)m; }
+__host__ __device__ inline float* mirror_nrm(uint8_t* m, size_t np) { return (float*)(m + np * 12); }
+__host__ __device__ inline float* mirror_ao(uint8_t* m, size_t np) { return (float*)(m + np * 24); }
+__host__ __device__ inline uint8_t* mirror_mask(uint8_t* m, size_t np) { return m + np * 28; }
 // Traced AO (AO only, the library's sampler and tuning) of a device G-buffer into a device
 // image, on the library's stream.
 int trace_ao_device(const float* pos, const float* nrm, const uint8_t* mask, int w, int h, const rn_accel* accel,

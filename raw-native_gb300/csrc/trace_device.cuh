@@ -251,12 +251,20 @@ __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, 
                                             const FrontierEntry* F = nullptr, int fn = 0) {
     const float kFar = 1e30f;
     const size_t i = (size_t)y * p.w + x;
-    if (!p.mask[i]) {
+    const uint8_t m = p.mask[i];
+    const v3 P = load3(p.pos + 3 * i), n = load3(p.nrm + 3 * i);
+    if (p.mirror) {
+        const size_t np = (size_t)p.w * p.h;
+        store3(mirror_pos(p.mirror, np) + 3 * i, P);
+        store3(mirror_nrm(p.mirror, np) + 3 * i, n);
+        mirror_mask(p.mirror, np)[i] = m;
+        if (!m) mirror_ao(p.mirror, np)[i] = 1.0f;
+    }
+    if (!m) {
         p.ao[i] = 1.0f;
         if (p.want_sky) { p.sky[i] = 1.0f; p.sun[i] = 1.0f; }
         return;
     }
-    const v3 P = load3(p.pos + 3 * i), n = load3(p.nrm + 3 * i);
     // basis (ray_ao.cpp:14-17)
     const v3 a = fabsf(n.x) > 0.9f ? mk(0.0f, 1.0f, 0.0f) : mk(1.0f, 0.0f, 0.0f);
     const v3 t = normalize(cross(a, n)), b = cross(n, t);
@@ -309,6 +317,7 @@ __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, 
         }
     }
     p.ao[i] = fdiv((float)open, (float)p.spp);
+    if (p.mirror) mirror_ao(p.mirror, (size_t)p.w * p.h)[i] = p.ao[i];
     if (p.want_sky) {
         p.sky[i] = fdiv((float)freec, (float)p.spp);
         p.sun[i] = lit ? 1.0f : 0.0f;

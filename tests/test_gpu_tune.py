@@ -62,3 +62,43 @@ def test_conv_tile_keeps_every_bit(rn, restore_tune):
     for v in rn.TUNE_KEYS["conv_bn_max"]:
         rn.tune_set("conv_bn_max", v)
         assert bool((net.forward(x) == ref).all()), v
+
+
+@pytest.mark.parametrize("sky", [False, True])
+def test_host_frame_keeps_every_bit(rn, restore_tune, sky):
+    """rn_ao_frame with pinned host buffers runs without copies: the traversal reads the
+    G-buffer from mapped host memory, mirrors it into HBM for the SSAO, and every pass writes
+    its image straight into host memory. Every image equals the device-pointer frame's bit for
+    bit, with the direct path and with the staged one, on a frame size that leaves ragged
+    packets and blocks, twice in a row (the mirror is reused); the reconcile agrees to the FP64
+    sum's last bits."""
+    import numpy as np
+    import torch
+    g, acc, tl = _scene(rn, 641, 487)
+    to_light = tl if sky else None
+    ref = rn.ao_frame(g, acc, 8, 1.0, 24, 0.12, to_light=to_light)
+    keys = ("ao", "ss", "err") + (("sky", "sun") if sky else ())
+    hg = rn.GBuffer(g.position.cpu().pin_memory().numpy(), g.normal.cpu().pin_memory().numpy(),
+                    g.mask.cpu().pin_memory().numpy())
+    for direct in rn.TUNE_KEYS["frame_direct"]:
+        rn.tune_set("frame_direct", direct)
+        for rep in range(2):
+            outs = {k: torch.full((487, 641), -7.0).pin_memory().numpy() for k in keys}
+            got = rn.ao_frame(hg, acc, 8, 1.0, 24, 0.12, to_light=to_light, outputs=outs)
+            for k in keys:
+                assert np.array_equal(got[k], ref[k].cpu().numpy()), (direct, rep, k)
+            r, q = got["rec"], ref["rec"]
+            assert r.pixels == q.pixels and r.max_error == q.max_error, direct
+            assert abs(r.sum_sq - q.sum_sq) <= 1e-12 * q.sum_sq, direct
+            assert r.rmse == pytest.approx(q.rmse, rel=1e-6) and r.within_tolerance == q.within_tolerance
+    # one pageable output (the error map the wrapper allocates) sends the frame down the staged path
+    rn.tune_set("frame_direct", 1)
+    outs = {k: torch.zeros(487, 641).pin_memory().numpy() for k in keys}
+    outs["err"] = None
+    got = rn.ao_frame(hg, acc, 8, 1.0, 24, 0.12, to_light=to_light, outputs=outs)
+    assert np.array_equal(got["ao"], ref["ao"].cpu().numpy())
+    # pageable host buffers take the staged path: the same images
+    pg = rn.GBuffer(g.position.cpu().numpy(), g.normal.cpu().numpy(), g.mask.cpu().numpy())
+    got = rn.ao_frame(pg, acc, 8, 1.0, 24, 0.12, to_light=to_light)
+    for k in keys:
+        assert np.array_equal(got[k], ref[k].cpu().numpy()), ("pageable", k)
