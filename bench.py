@@ -9,8 +9,10 @@ rasterized on the GPU by this library); no dataset is involved.
 
   value    AO Grays/s over all ranks, G-buffer resident in HBM, device pointers (the 207 MB
            G-buffer exceeds the 129 MB L2, so no flush is needed between steps)
-  e2e      the same metric through the C ABI with pinned host buffers: the G-buffer copied
-           in and ao, sky, sun, ss and the error map copied out every step
+  e2e      the same metric through the C ABI with pinned host buffers: every step the
+           G-buffer crosses from host memory and ao, sky, sun, ss and the error map cross
+           back (the library's passes read and write mapped host memory themselves, the
+           traversal mirroring the G-buffer into HBM for the SSAO; no copy-engine copy)
   roofline the traversal kernel (trace_kernel): algorithmic bytes per launch = 4-wide node
            fetches x 128 B + leaf-triangle fetches x 48 B, from the library's traversal
            counters over the whole frame, divided by the kernel's CUDA-event time

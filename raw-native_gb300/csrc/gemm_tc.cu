@@ -450,18 +450,21 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
 }
 
 
-// ------------------------------------------------------------------ implicit 3x3, halo tiles
+// ------------------------------------------------------------------ implicit 3x3, row ring
 // For 128-pixel tiles of one image row (W % 128 == 0) and a layer whose whole weight matrix
-// fits in shared memory: per tile ONE TMA box per source holds the 3 rows x 136 pixels
-// (x0 - 1 .. x0 + 134) of every input channel, and the 9 taps read it in place, each tap's
-// A operand starting 16 bytes (one pixel) further along a row or 136 pixels further down.
-// Layouts are the no-swizzle K-major canonical form: 8 rows x 16 bytes (8 channels) per
-// core matrix, core matrices 128 bytes apart along M (pixels) and one channel group apart
-// along K (3 x 136 x 16 bytes for A, N x 16 bytes for B). The weights are loaded once per
-// CTA. K order (tap outermost, then channel) and the K16 steps are the same as
-// tc_conv_kernel's, so the two kernels give identical results.
+// fits in shared memory. A work item is a strip of 128 pixels (x0 .. x0 + 127) over a chunk
+// of output rows [y0, y1); the CTA loads the chunk's input rows y0 - 1 .. y1 one at a time,
+// each as ONE TMA box per source holding 136 pixels (x0 - 1 .. x0 + 134) of every input
+// channel, into a ring of row slots. Output row y reads the slots of rows y - 1, y, y + 1
+// in place, each tap's A operand starting 16 bytes (one pixel) further along its row: every
+// input row crosses from L2 once per chunk instead of three times. Layouts are the
+// no-swizzle K-major canonical form: 8 rows x 16 bytes (8 channels) per core matrix, core
+// matrices 128 bytes apart along M (pixels) and one channel group apart along K (136 x 16
+// bytes for A, N x 16 bytes for B). The weights are loaded once per CTA. K order (tap
+// outermost, then channel) and the K16 steps are tc_conv_kernel's, so the two kernels give
+// identical results.
 constexpr int kHaloW = 136;                        // box width: 128 + 2 halo, rounded for alignment
-constexpr uint32_t kHaloGroup = 3 * kHaloW * 16;   // bytes of one 8-channel group of a box
+constexpr uint32_t kHaloGroup = kHaloW * 16;       // bytes of one 8-channel group of a row slot
 
 __device__ __forceinline__ uint64_t desc_plain(uint32_t addr, uint32_t lbo, uint32_t sbo) {
     uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
@@ -487,11 +490,25 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
 struct HaloArgs {
     int nsrc, C0, C1, cin;
     int B, H, W;
-    int tiles;                  // (W / 128) x H x B
-    int stages;
-    uint32_t a_bytes, b_bytes;  // one stage of A (all sources), the resident weights
+    int chunk, chunks_y;        // output rows per work item; items per strip column
+    int items;                  // (W / 128) x chunks_y x B
+    int stages;                 // row slots in the ring (>= 4)
+    uint32_t a_bytes, b_bytes;  // one row slot (all sources), the resident weights
     __nv_bfloat16* up16;
 };
+
+// Work item -> (image, strip, first row, rows).
+struct HaloItem { int b, tx, y0, rows; };
+__device__ __forceinline__ HaloItem halo_item(const HaloArgs& a, int item) {
+    const int tiles_x = a.W >> 7;
+    HaloItem it;
+    it.tx = item % tiles_x;
+    const int c = (item / tiles_x) % a.chunks_y;
+    it.b = item / (tiles_x * a.chunks_y);
+    it.y0 = c * a.chunk;
+    it.rows = min(a.chunk, a.H - it.y0);
+    return it;
+}
 
 template <int BN>
 __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __grid_constant__ CUtensorMap map0,
@@ -510,7 +527,6 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     __shared__ int s_abort;
     volatile int* abort_flag = &s_abort;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int tiles_x = a.W >> 7;
     auto full = [&](int s) { return smem_u32(&bars[s]); };
     auto empty = [&](int s) { return smem_u32(&bars[kSt + s]); };
     auto acc_full = [&](int b) { return smem_u32(&bars[2 * kSt + b]); };
@@ -538,23 +554,26 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
 
     if (warp == 0) {
         if (lane == 0) {
+            // loads in ring order: item by item, input rows y0 - 1 .. y0 + rows
             mbar_expect_tx(wbar, a.b_bytes);
             tma_load_3d(smem_u32(sB), &mapW, 0, 0, 0, wbar);
             uint32_t kc = 0;
-            for (int tile = blockIdx.x; tile < a.tiles && !*abort_flag; tile += gridDim.x, ++kc) {
-                const int s = kc % kSt;
-                const uint32_t ph = (kc / kSt) & 1u;
-                if (!mbar_wait_or_abort(empty(s), ph ^ 1u, abort_flag)) {
-                    atomicOr(e.err, DEV_GUARD);
-                    s_abort = 1;
-                    break;
+            for (int item = blockIdx.x; item < a.items && !*abort_flag; item += gridDim.x) {
+                const HaloItem it = halo_item(a, item);
+                for (int r = -1; r <= it.rows && !*abort_flag; ++r, ++kc) {
+                    const int s = kc % kSt;
+                    if (!mbar_wait_or_abort(empty(s), ((kc / kSt) & 1u) ^ 1u, abort_flag)) {
+                        atomicOr(e.err, DEV_GUARD);
+                        s_abort = 1;
+                        break;
+                    }
+                    mbar_expect_tx(full(s), a.a_bytes);
+                    const uint32_t dst = smem_u32(sA + s * a_stride);
+                    tma_load_5d(dst, &map0, 0, it.tx * 128 - 1, it.y0 + r, it.b, 0, full(s));
+                    if (a.nsrc > 1) tma_load_5d(dst + src1_off, &map1, 0, it.tx * 128 - 1, it.y0 + r, it.b, 0, full(s));
                 }
-                const int tx = tile % tiles_x, y = (tile / tiles_x) % a.H, b = tile / (tiles_x * a.H);
-                mbar_expect_tx(full(s), a.a_bytes);
-                const uint32_t dst = smem_u32(sA + s * a_stride);
-                tma_load_5d(dst, &map0, 0, tx * 128 - 1, y - 1, b, 0, full(s));
-                if (a.nsrc > 1) tma_load_5d(dst + src1_off, &map1, 0, tx * 128 - 1, y - 1, b, 0, full(s));
             }
+            // the copies this lane issued must land before the CTA can leave
             for (uint32_t k = kc > (uint32_t)kSt ? kc - kSt : 0; k < kc; ++k) mbar_wait(full(k % kSt), (k / kSt) & 1u);
             mbar_wait(wbar, 0);
         }
@@ -564,25 +583,39 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
             const uint32_t b0 = smem_u32(sB);
             const int q16 = a.cin / 16, g_tap = a.cin / 8;
             bool ok = mbar_wait_or_abort(wbar, 0, abort_flag);
-            uint32_t kc = 0, i = 0;
-            for (int tile = blockIdx.x; ok && tile < a.tiles && !*abort_flag; tile += gridDim.x, ++kc, ++i) {
-                const uint32_t buf = i & 1u, use = i >> 1;
-                if (!mbar_wait_or_abort(acc_empty(buf), (use & 1u) ^ 1u, abort_flag)) { ok = false; break; }
-                const int s = kc % kSt;
-                if (!mbar_wait_or_abort(full(s), (kc / kSt) & 1u, abort_flag)) { ok = false; break; }
-                tc_fence_after();
-                const uint32_t acc = tmem + buf * BN;
-                const uint32_t a0 = smem_u32(sA + s * a_stride);
-                for (int t = 0; t < 9; ++t) {
-                    const uint32_t a_tap = a0 + (uint32_t)((t / 3) * kHaloW + (t % 3)) * 16u;
-                    for (int q = 0; q < q16; ++q) {
-                        const uint64_t da = desc_plain(a_tap + (uint32_t)(2 * q) * kHaloGroup, kHaloGroup, 128);
-                        const uint64_t db = desc_plain(b0 + (uint32_t)(t * g_tap + 2 * q) * (BN * 16), BN * 16, 128);
-                        tc_mma(acc, da, db, idesc, (t | q) != 0 ? 1u : 0u);
+            uint32_t base = 0, i = 0;   // ring index of the item's first load; output rows so far
+            for (int item = blockIdx.x; ok && item < a.items && !*abort_flag; item += gridDim.x) {
+                const HaloItem it = halo_item(a, item);
+                for (int j = 0; ok && j < it.rows; ++j, ++i) {
+                    // output row y0 + j reads loads j, j + 1, j + 2 of the item
+                    const uint32_t buf = i & 1u, use = i >> 1;
+                    if (!mbar_wait_or_abort(acc_empty(buf), (use & 1u) ^ 1u, abort_flag)) { ok = false; break; }
+                    uint32_t row_addr[3];
+                    for (int d = 0; d < 3 && ok; ++d) {
+                        const uint32_t k = base + (uint32_t)(j + d);
+                        ok = mbar_wait_or_abort(full(k % kSt), (k / kSt) & 1u, abort_flag);
+                        row_addr[d] = smem_u32(sA + (k % kSt) * a_stride);
                     }
+                    if (!ok) break;
+                    tc_fence_after();
+                    const uint32_t acc = tmem + buf * BN;
+                    for (int t = 0; t < 9; ++t) {
+                        const uint32_t a_tap = row_addr[t / 3] + (uint32_t)(t % 3) * 16u;
+                        for (int q = 0; q < q16; ++q) {
+                            const uint64_t da = desc_plain(a_tap + (uint32_t)(2 * q) * kHaloGroup, kHaloGroup, 128);
+                            const uint64_t db = desc_plain(b0 + (uint32_t)(t * g_tap + 2 * q) * (BN * 16), BN * 16, 128);
+                            tc_mma(acc, da, db, idesc, (t | q) != 0 ? 1u : 0u);
+                        }
+                    }
+                    tc_commit(acc_full(buf));
+                    // load j (input row y0 + j - 1) has no later reader
+                    tc_commit(empty((base + (uint32_t)j) % kSt));
                 }
-                tc_commit(empty(s));
-                tc_commit(acc_full(buf));
+                if (!ok) break;
+                // the item's last two loads
+                tc_commit(empty((base + (uint32_t)it.rows) % kSt));
+                tc_commit(empty((base + (uint32_t)it.rows + 1) % kSt));
+                base += (uint32_t)it.rows + 2;
             }
             if (!ok) {
                 atomicOr(e.err, DEV_GUARD);
@@ -593,58 +626,61 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
         const int q = warp & 3;
         const int r = q * 32 + lane;
         uint32_t i = 0;
-        for (int tile = blockIdx.x; tile < a.tiles; tile += gridDim.x, ++i) {
-            const uint32_t buf = i & 1u, use = i >> 1;
-            const bool ok = __all_sync(0xffffffffu, mbar_wait_or_abort(acc_full(buf), use & 1u, abort_flag));
-            if (!ok) {
-                if (lane == 0) { atomicOr(e.err, DEV_GUARD); s_abort = 1; }
-                break;
-            }
-            tc_fence_after();
-            const int tx = tile % tiles_x, y = (tile / tiles_x) % a.H, b = tile / (tiles_x * a.H);
-            const int x = tx * 128 + r;
-            const size_t pix = ((size_t)b * a.H + y) * a.W + x;
-            const uint32_t tbase = tmem + buf * BN + ((uint32_t)(q * 32) << 16);
-#pragma unroll 1
-            for (int c0 = 0; c0 < BN; c0 += 16) {
-                uint32_t v[16];
-                tmem_ld16(tbase + (uint32_t)c0, v);
-                float f[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    float t = __uint_as_float(v[j]);
-                    if (e.bias) t += e.bias[c0 + j];
-                    if (e.relu) t = fmaxf(t, 0.0f);
-                    f[j] = t;
+        bool ok = true;
+        for (int item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
+            const HaloItem it = halo_item(a, item);
+            for (int j = 0; j < it.rows; ++j, ++i) {
+                const uint32_t buf = i & 1u, use = i >> 1;
+                ok = __all_sync(0xffffffffu, mbar_wait_or_abort(acc_full(buf), use & 1u, abort_flag));
+                if (!ok) {
+                    if (lane == 0) { atomicOr(e.err, DEV_GUARD); s_abort = 1; }
+                    break;
                 }
-                const size_t o = pix * e.ldc + c0;
-                if (e.c16) {
-                    uint4 out[2];
-                    __nv_bfloat16* ob = reinterpret_cast<__nv_bfloat16*>(out);
+                tc_fence_after();
+                const int y = it.y0 + j, x = it.tx * 128 + r;
+                const size_t pix = ((size_t)it.b * a.H + y) * a.W + x;
+                const uint32_t tbase = tmem + buf * BN + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+                for (int c0 = 0; c0 < BN; c0 += 16) {
+                    uint32_t v[16];
+                    tmem_ld16(tbase + (uint32_t)c0, v);
+                    float f[16];
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) ob[j] = __float2bfloat16_rn(f[j]);
-                    uint4* d4 = reinterpret_cast<uint4*>(e.c16 + o);
-                    d4[0] = out[0];
-                    d4[1] = out[1];
-                    if (a.up16) {
+                    for (int jj = 0; jj < 16; ++jj) {
+                        float t = __uint_as_float(v[jj]);
+                        if (e.bias) t += e.bias[c0 + jj];
+                        if (e.relu) t = fmaxf(t, 0.0f);
+                        f[jj] = t;
+                    }
+                    const size_t o = pix * e.ldc + c0;
+                    if (e.c16) {
+                        uint4 out[2];
+                        __nv_bfloat16* ob = reinterpret_cast<__nv_bfloat16*>(out);
 #pragma unroll
-                        for (int u = 0; u < 4; ++u) {
-                            const size_t up = ((size_t)b * 2 * a.H + 2 * y + (u >> 1)) * (2 * a.W) + 2 * x + (u & 1);
-                            uint4* d = reinterpret_cast<uint4*>(a.up16 + up * e.ldc + c0);
-                            d[0] = out[0];
-                            d[1] = out[1];
+                        for (int jj = 0; jj < 16; ++jj) ob[jj] = __float2bfloat16_rn(f[jj]);
+                        uint4* d4 = reinterpret_cast<uint4*>(e.c16 + o);
+                        d4[0] = out[0];
+                        d4[1] = out[1];
+                        if (a.up16) {
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                const size_t up = ((size_t)it.b * 2 * a.H + 2 * y + (u >> 1)) * (2 * a.W) + 2 * x + (u & 1);
+                                uint4* d = reinterpret_cast<uint4*>(a.up16 + up * e.ldc + c0);
+                                d[0] = out[0];
+                                d[1] = out[1];
+                            }
                         }
                     }
-                }
-                if (e.c32) {
-                    float4* d4 = reinterpret_cast<float4*>(e.c32 + o);
+                    if (e.c32) {
+                        float4* d4 = reinterpret_cast<float4*>(e.c32 + o);
 #pragma unroll
-                    for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
+                        for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
+                    }
                 }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(acc_empty(buf));
             }
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(acc_empty(buf));
         }
     }
     tc_fence_before();
@@ -734,15 +770,15 @@ int launch_conv(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap&
 }
 
 
-// The halo box of one source: a 5-D view of the NHWC tensor, (8 channels, W, H, B, C / 8
-// groups), read in boxes of 8 x 136 x 3 x 1 x C/8 without swizzle (the channel groups
+// The row box of one source: a 5-D view of the NHWC tensor, (8 channels, W, H, B, C / 8
+// groups), read in boxes of 8 x 136 x 1 x 1 x C/8 without swizzle (the channel groups
 // outermost in shared memory).
 bool make_map_halo(CUtensorMap* m, const void* base, int B, int H, int W, int C) {
     auto fn = encoder();
     if (!fn) return false;
     const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)B, (cuuint64_t)(C / 8)};
     const cuuint64_t strides[4] = {(cuuint64_t)C * 2, (cuuint64_t)W * C * 2, (cuuint64_t)H * W * C * 2, 16};
-    const cuuint32_t box[5] = {8, (cuuint32_t)kHaloW, 3, 1, (cuuint32_t)(C / 8)};
+    const cuuint32_t box[5] = {8, (cuuint32_t)kHaloW, 1, 1, (cuuint32_t)(C / 8)};
     const cuuint32_t elem[5] = {1, 1, 1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, elem,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -776,7 +812,7 @@ int launch_conv_halo(const CUtensorMap& m0, const CUtensorMap& m1, const CUtenso
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx().device);
     const int per_sm = std::max(1, std::min(std::min(smem_sm / (int)(smem + 1024), 512 / (2 * BN)), 3));
-    const int ctas = std::min(a.tiles, per_sm * ctx().sm_count);
+    const int ctas = std::min(a.items, per_sm * ctx().sm_count);
     tc_conv_halo_kernel<BN><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
@@ -859,16 +895,16 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     if (N % bn) return fail(st, RN_ERR_INVALID, "tc_conv3x3 N %d", N);
     while (bn > ctx().tune.conv_bn_max && bn > 32) bn /= 2;
     if (up16 && !epi.c16) return fail(st, RN_ERR_INVALID, "tc_conv3x3: the upsampled copy needs a BF16 output");
-    // halo tiles: rows of 128 pixels, channels in groups of 16, N 32 or 64 in one slice, the
-    // weights and at least two stages of boxes in shared memory
+    // row-ring tiles: rows of 128 pixels, channels in groups of 16, N 32 or 64 in one slice,
+    // the weights and a ring of at least four row slots in shared memory
     if (ctx().tune.conv_halo && t.tw_log2 == 7 && (N == 32 || N == 64) && (9 * cin) / 8 <= 256 && cin % 16 == 0) {
         const uint32_t b_bytes = (uint32_t)N * 9 * cin * 2;
         const uint32_t a_bytes = (uint32_t)cin / 8 * tc::kHaloGroup;
         const uint32_t a_stride = (a_bytes + 1023) & ~1023u, b_pad = (b_bytes + 1023) & ~1023u;
         const size_t budget = 220 * 1024;
-        int stages = (int)std::min<size_t>(4, (budget - std::min<size_t>(budget, b_pad + 2048)) / a_stride);
+        int stages = (int)std::min<size_t>(8, (budget - std::min<size_t>(budget, b_pad + 2048)) / a_stride);
         CUtensorMap hm[2], hw;
-        bool maps = stages >= 2;
+        bool maps = stages >= 4;
         for (int i = 0; maps && i < nsrc; ++i) maps = tc::make_map_halo(&hm[i], src[i].ptr, B, H, W, src[i].C);
         if (maps && nsrc == 1) hm[1] = hm[0];
         maps = maps && tc::make_map_wgroups(&hw, w, N, ldw, 9 * cin / 8);
@@ -876,7 +912,12 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
             tc::HaloArgs h{};
             h.nsrc = nsrc; h.C0 = src[0].C; h.C1 = nsrc > 1 ? src[1].C : 0; h.cin = cin;
             h.B = B; h.H = H; h.W = W;
-            h.tiles = (W / 128) * H * B;
+            // chunks of 16 output rows (2 halo rows re-read per chunk), fewer where that leaves
+            // less than two items per SM
+            h.chunk = 16;
+            while (h.chunk > 4 && (long)(W / 128) * B * ((H + h.chunk - 1) / h.chunk) < 2L * ctx().sm_count) h.chunk /= 2;
+            h.chunks_y = (H + h.chunk - 1) / h.chunk;
+            h.items = (W / 128) * h.chunks_y * B;
             h.stages = stages;
             h.a_bytes = a_bytes; h.b_bytes = b_bytes;
             h.up16 = up16;

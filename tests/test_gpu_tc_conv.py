@@ -76,11 +76,14 @@ def test_conv_rejects_untileable_and_bad_channels(rn):
 
 
 @pytest.mark.parametrize("B,H,W,c0,c1,N", [(2, 8, 128, 32, 0, 32), (1, 6, 256, 32, 0, 64), (1, 4, 1920, 32, 0, 32),
-                                            (2, 8, 128, 32, 64, 32), (1, 5, 384, 64, 0, 64)])
+                                            (2, 8, 128, 32, 64, 32), (1, 5, 384, 64, 0, 64),
+                                            # several row chunks per strip, a ragged last chunk
+                                            (1, 37, 256, 32, 0, 32), (2, 70, 128, 32, 64, 32),
+                                            (1, 333, 1920, 32, 0, 64)])
 def test_conv_halo_tiles_match_the_general_kernel(rn, B, H, W, c0, c1, N):
-    """Row tiles from one halo box (conv_halo 1) accumulate the same K16 steps in the same
-    order as the per-tap boxes (conv_halo 0): identical outputs, bias, ReLU and the
-    upsampled copy included."""
+    """Row tiles read from a ring of one-row boxes (conv_halo 1) accumulate the same K16 steps
+    in the same order as the per-tap boxes (conv_halo 0): identical outputs, bias, ReLU and
+    the upsampled copy included."""
     import torch
     saved = rn.tune_get("conv_halo")
     try:
