@@ -51,7 +51,7 @@ enum : int { HIT_NEAR = 1, HIT_FAR = 2 };
 // triangle a short ray of the warp's tile can reach. A triangle hit at t < radius lies within
 // radius of its ray's origin, so its leaf box, and every ancestor's, overlaps the box Q of
 // the tile's origins grown by the radius; the frontier is the set of Q-overlapping nodes
-// reached by expanding Q-overlapping nodes from the root (largest box first) while at most
+// reached by expanding Q-overlapping nodes from the root, level by level, while at most
 // kFrontier entries result. AO walks start from it instead of re-descending from the root.
 constexpr int kFrontier = 16;
 struct FrontierEntry {
@@ -65,41 +65,66 @@ __device__ __forceinline__ bool box_overlaps(float lx, float ly, float lz, float
     return lx <= qhi[0] && hx >= qlo[0] && ly <= qhi[1] && hy >= qlo[1] && lz <= qhi[2] && hz >= qlo[2];
 }
 
-// Lane 0 builds the frontier of box [qlo, qhi] into F; returns its size (0: start at the root).
+// The warp builds the frontier of box [qlo, qhi] into F (all 32 lanes call it); returns its
+// size (0: start at the root). Breadth first: each round every entry that is an interior
+// node is replaced by its Q-overlapping children, the lanes expanding their entries in
+// parallel (one node fetch per lane, a prefix sum over the lanes for the output slots),
+// while the result stays within kFrontier entries. A round costs one dependent node fetch,
+// so the build takes about the tree's depth in fetch latencies.
 __device__ inline int build_frontier(const Node4* __restrict__ nodes, const float* qlo, const float* qhi,
-                              FrontierEntry* F) {
-    int n = 0;
-    auto expand = [&](int32_t node, int slot) -> bool {
-        // replace F[slot] (or append when slot < 0) by node's Q-overlapping children
-        const Node4& N = nodes[node];
-        int add[4], na = 0;
-        for (int k = 0; k < N.meta[0]; ++k)
-            if (box_overlaps(N.lox[k], N.loy[k], N.loz[k], N.hix[k], N.hiy[k], N.hiz[k], qlo, qhi)) add[na++] = k;
-        if (n - (slot >= 0 ? 1 : 0) + na > kFrontier) return false;
-        for (int j = 0; j < na; ++j) {
-            const int k = add[j];
+                                     FrontierEntry* F) {
+    const int lane = (int)(threadIdx.x & 31u);
+    int32_t word = 0;                       // lane 0 starts with the root node
+    float lo[3] = {0.0f, 0.0f, 0.0f}, hi[3] = {0.0f, 0.0f, 0.0f};
+    int n = 1, built = 0;
+    for (int round = 0; round < 64; ++round) {
+        const bool mine = lane < n;
+        const bool inner = mine && word >= 0;
+        const Node4* N = nodes + (inner ? word : 0);
+        unsigned hit = 0;
+        if (inner)
+            for (int k = 0; k < N->meta[0]; ++k)
+                if (box_overlaps(N->lox[k], N->loy[k], N->loz[k], N->hix[k], N->hiy[k], N->hiz[k], qlo, qhi))
+                    hit |= 1u << k;
+        const int c = inner ? __popc(hit) : (mine ? 1 : 0);
+        int incl = c;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += v;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (!__any_sync(0xffffffffu, inner) || total > kFrontier) break;
+        __syncwarp();                       // every lane has read its entry of the last round
+        int pos = incl - c;
+        if (inner) {
+            for (int k = 0; k < 4; ++k)
+                if (hit & (1u << k)) {
+                    FrontierEntry e;
+                    e.lo[0] = N->lox[k]; e.lo[1] = N->loy[k]; e.lo[2] = N->loz[k];
+                    e.hi[0] = N->hix[k]; e.hi[1] = N->hiy[k]; e.hi[2] = N->hiz[k];
+                    e.word = N->child[k];
+                    e.pad = 0;
+                    F[pos++] = e;
+                }
+        } else if (mine) {
             FrontierEntry e;
-            e.lo[0] = N.lox[k]; e.lo[1] = N.loy[k]; e.lo[2] = N.loz[k];
-            e.hi[0] = N.hix[k]; e.hi[1] = N.hiy[k]; e.hi[2] = N.hiz[k];
-            e.word = N.child[k];
+            e.lo[0] = lo[0]; e.lo[1] = lo[1]; e.lo[2] = lo[2];
+            e.hi[0] = hi[0]; e.hi[1] = hi[1]; e.hi[2] = hi[2];
+            e.word = word;
             e.pad = 0;
-            if (j == 0 && slot >= 0) F[slot] = e; else F[n++] = e;
+            F[pos] = e;
         }
-        if (na == 0 && slot >= 0) F[slot] = F[--n];
-        return true;
-    };
-    expand(0, -1);
-    for (int iter = 0; iter < 4 * kFrontier; ++iter) {
-        int pick = -1;
-        float best = -1.0f;
-        for (int e = 0; e < n; ++e) {
-            if (F[e].word < 0) continue;
-            const float ext = fmaxf(fmaxf(F[e].hi[0] - F[e].lo[0], F[e].hi[1] - F[e].lo[1]), F[e].hi[2] - F[e].lo[2]);
-            if (ext > best) { best = ext; pick = e; }
+        __syncwarp();
+        n = total;
+        built = 1;
+        if (lane < n) {
+            const FrontierEntry& e = F[lane];
+            lo[0] = e.lo[0]; lo[1] = e.lo[1]; lo[2] = e.lo[2];
+            hi[0] = e.hi[0]; hi[1] = e.hi[1]; hi[2] = e.hi[2];
+            word = e.word;
         }
-        if (pick < 0 || !expand(F[pick].word, pick)) break;
     }
-    return n;
+    return built ? n : 0;
 }
 
 // One walk, two limits (tnear <= tfar): HIT_NEAR | HIT_FAR when some triangle is hit at
@@ -199,8 +224,8 @@ __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__
     return far_hit;
 }
 
-// The frontier of the warp's tile for AO walks of `radius` (all 32 lanes call it; lane 0
-// builds, the others wait). Returns its size, 0 when the tile has no covered pixel.
+// The frontier of the warp's tile for AO walks of `radius` (all 32 lanes call it and build
+// it together). Returns its size, 0 when the tile has no covered pixel.
 __device__ __forceinline__ int tile_frontier(const TraceParams& p, int x, int y, bool valid, FrontierEntry* F) {
     float lo[3] = {3.0e38f, 3.0e38f, 3.0e38f}, hi[3] = {-3.0e38f, -3.0e38f, -3.0e38f}, mag = 0.0f;
     if (valid) {
@@ -222,9 +247,7 @@ __device__ __forceinline__ int tile_frontier(const TraceParams& p, int x, int y,
     // grow by the radius with margin for the rounding of t, |d| and the hit point
     const float g = p.radius * 1.0001f + 1e-5f * (mag + 1.0f);
     for (int a = 0; a < 3; ++a) { lo[a] -= g; hi[a] += g; }
-    int n = 0;
-    if ((threadIdx.x & 31u) == 0) n = build_frontier(p.nodes, lo, hi, F);
-    n = __shfl_sync(0xffffffffu, n, 0);
+    const int n = build_frontier(p.nodes, lo, hi, F);
     __syncwarp();
     return n;
 }
