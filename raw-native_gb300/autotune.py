@@ -18,6 +18,7 @@ Workloads:
   conv           the surrogate U-Net: a forward at 1088 x 1920 and a training step on
                  64 crops of 128 x 128
   trace/low-spp  the synthetic scene's view at 4, 8, 16 and 32 spp (trace_frontier_min_spp)
+  trace/tail     the same view at 16, 64 and 256 spp (trace_frontier_tail)
 The traversal keys are searched jointly (every combination); the others one at a time.
 """
 from __future__ import annotations
@@ -117,6 +118,37 @@ def tune_frontier_min_spp(quick: bool, reps: int, log):
     return best["cfg"], rows
 
 
+def tune_frontier_tail(quick: bool, reps: int, log):
+    """Greedy largest-first steps after the level-by-level frontier build (the library takes at
+    most spp / 16 of them): AO-only traces of the synthetic scene at 16, 64 and 256 spp, each
+    candidate checked bit for bit against no tail; score: geometric mean of the time ratios to
+    no tail."""
+    import torch
+    big = scenes.build_synthetic_scene(7, 500 if quick else 2000, 100 if quick else 500)
+    bt, bn = torch.from_numpy(big.tris).cuda(), torch.from_numpy(big.normals).cuda()
+    g = rn.rasterize(bt, bn, scenes.orbit_views(7, 8)[0][3], 1920, 1080)
+    acc = rn.LinearAccel(bt)
+    spps = (16, 64, 256)
+    rows, ref = [], None
+    for v in rn.TUNE_KEYS["trace_frontier_tail"]:
+        rn.tune_set("trace_frontier_tail", v)
+        outs = [rn.compute_rtao(g, acc, spp, 1.0).clone() for spp in spps]
+        if ref is None:
+            ref = outs
+        elif not all(bool((a == b).all()) for a, b in zip(outs, ref)):
+            raise RuntimeError("trace_frontier_tail %d changed a traced result" % v)
+        ms = {"spp%d" % spp: _time(lambda: rn.compute_rtao(g, acc, spp, 1.0), max(2, reps // (1 + spp // 64)))
+              for spp in spps}
+        rows.append(dict(cfg={"trace_frontier_tail": v}, ms=ms))
+        log("trace_frontier_tail %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    base = rows[0]["ms"]
+    for r in rows:
+        r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
+    best = min(rows, key=lambda r: r["score"])
+    rn.tune_set("trace_frontier_tail", best["cfg"]["trace_frontier_tail"])
+    return best["cfg"], rows
+
+
 def tune_ssao(quick: bool, reps: int, log):
     import torch
     sc = scenes.build_test_scene()
@@ -195,6 +227,8 @@ def main(argv=None):
     c, report["trace"] = tune_trace(a.quick, a.reps, log)
     cfg.update(c)
     c, report["frontier_min_spp"] = tune_frontier_min_spp(a.quick, a.reps, log)
+    cfg.update(c)
+    c, report["frontier_tail"] = tune_frontier_tail(a.quick, a.reps, log)
     cfg.update(c)
     c, report["ssao"] = tune_ssao(a.quick, a.reps, log)
     cfg.update(c)

@@ -115,6 +115,7 @@ const TuneKey kTuneKeys[] = {
     {"trace_min_blocks", "RN_TUNE_TRACE_MIN_BLOCKS", &Tune::trace_min_blocks, {2, 3, 4}, 3},
     {"trace_frontier", "RN_TUNE_TRACE_FRONTIER", &Tune::trace_frontier, {0, 1}, 2},
     {"trace_frontier_min_spp", "RN_TUNE_TRACE_FRONTIER_MIN_SPP", &Tune::trace_frontier_min_spp, {1, 8, 16, 32}, 4},
+    {"trace_frontier_tail", "RN_TUNE_TRACE_FRONTIER_TAIL", &Tune::trace_frontier_tail, {0, 4, 8, 16}, 4},
     {"trace_packet", "RN_TUNE_TRACE_PACKET", &Tune::trace_packet, {4, 8, 16}, 3},
     {"trace_stack", "RN_TUNE_TRACE_STACK", &Tune::trace_stack, {48, 96}, 2},
     {"ssao_tile_h", "RN_TUNE_SSAO_TILE_H", &Tune::ssao_tile_h, {4, 8, 16}, 3},
@@ -198,6 +199,9 @@ void apply_tune(TraceParams& p, const rn_accel* accel) {
     // the frontier's seeds sit under the walk's own pushes: without room for both, walk from the root
     if (p.stack_need > 96) p.frontier = 0;
     p.packet_log2 = packet_log2(t.trace_packet);
+    // the greedy tail costs a node fetch per step and packet, and saves per ray: one step per
+    // 16 samples, up to the tuned count
+    p.frontier_tail = std::min(t.trace_frontier_tail, p.spp / 16);
 }
 
 int ensure_ctx(rn_status* st) {

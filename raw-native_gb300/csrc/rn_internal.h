@@ -42,6 +42,7 @@ struct Tune {
     int trace_min_blocks = 3;   // resident 256-thread traversal blocks per SM: 2, 3 or 4
     int trace_frontier = 1;     // per-warp frontier for AO-only walks
     int trace_frontier_min_spp = 16;  // ... built only when spp reaches this (its cost is per packet)
+    int trace_frontier_tail = 0;      // greedy largest-first steps after the level-by-level build (at most spp / 16)
     int trace_packet = 8;       // a warp's pixel packet: trace_packet x (32 / trace_packet); 4, 8 or 16
     int trace_stack = 96;       // traversal stack entries: 48 or 96 (48 only where the tree's depth allows)
     int ssao_tile_h = 8;        // SSAO tile: 32 x ssao_tile_h pixels, one thread each; 4, 8 or 16
@@ -181,6 +182,7 @@ struct TraceParams {
     uint32_t* err_word;
     int frontier;         // AO-only walks start from a per-warp frontier (0: from the root)
     int packet_log2;      // log2 of the packet width (pixels per warp row): 2, 3 or 4
+    int frontier_tail;    // greedy single-entry steps after the breadth-first frontier build
     int stack_need;       // entries the walk can push on this tree: 16 + 3 x wide depth
     // copy-through of a G-buffer read from host memory (null: none): every pixel's position,
     // normal, AO and mask are also written to a device buffer laid out as

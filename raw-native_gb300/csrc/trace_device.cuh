@@ -70,9 +70,10 @@ __device__ __forceinline__ bool box_overlaps(float lx, float ly, float lz, float
 // node is replaced by its Q-overlapping children, the lanes expanding their entries in
 // parallel (one node fetch per lane, a prefix sum over the lanes for the output slots),
 // while the result stays within kFrontier entries. A round costs one dependent node fetch,
-// so the build takes about the tree's depth in fetch latencies.
+// so the build takes about the tree's depth in fetch latencies. Up to `tail` greedy steps
+// follow, each replacing the largest interior entry by its children while the frontier fits.
 __device__ inline int build_frontier(const Node4* __restrict__ nodes, const float* qlo, const float* qhi,
-                                     FrontierEntry* F) {
+                                     FrontierEntry* F, int tail) {
     const int lane = (int)(threadIdx.x & 31u);
     int32_t word = 0;                       // lane 0 starts with the root node
     float lo[3] = {0.0f, 0.0f, 0.0f}, hi[3] = {0.0f, 0.0f, 0.0f};
@@ -117,6 +118,51 @@ __device__ inline int build_frontier(const Node4* __restrict__ nodes, const floa
         __syncwarp();
         n = total;
         built = 1;
+        if (lane < n) {
+            const FrontierEntry& e = F[lane];
+            lo[0] = e.lo[0]; lo[1] = e.lo[1]; lo[2] = e.lo[2];
+            hi[0] = e.hi[0]; hi[1] = e.hi[1]; hi[2] = e.hi[2];
+            word = e.word;
+        }
+    }
+    // then up to `tail` single steps, largest interior entry first, while the result fits
+    for (int step = 0; built && step < tail; ++step) {
+        const bool inner = lane < n && word >= 0;
+        float best = inner ? fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]) : -1.0f;
+        int bl = lane;
+        for (int off = 16; off > 0; off >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const int ol = __shfl_xor_sync(0xffffffffu, bl, off);
+            if (ob > best || (ob == best && ol < bl)) { best = ob; bl = ol; }
+        }
+        if (best < 0.0f) break;
+        unsigned hit = 0;
+        const Node4* N = nodes + (lane == bl ? word : 0);
+        if (lane == bl)
+            for (int k = 0; k < N->meta[0]; ++k)
+                if (box_overlaps(N->lox[k], N->loy[k], N->loz[k], N->hix[k], N->hiy[k], N->hiz[k], qlo, qhi))
+                    hit |= 1u << k;
+        const int c = __popc(__shfl_sync(0xffffffffu, hit, bl));
+        if (n - 1 + c > kFrontier) break;
+        __syncwarp();
+        if (lane == bl) {
+            // the children replace entry bl and append after the last entry; none: the last
+            // entry moves into slot bl
+            int pos = bl;
+            if (c == 0 && bl != n - 1) F[bl] = F[n - 1];
+            for (int k = 0; k < 4; ++k)
+                if (hit & (1u << k)) {
+                    FrontierEntry e;
+                    e.lo[0] = N->lox[k]; e.lo[1] = N->loy[k]; e.lo[2] = N->loz[k];
+                    e.hi[0] = N->hix[k]; e.hi[1] = N->hiy[k]; e.hi[2] = N->hiz[k];
+                    e.word = N->child[k];
+                    e.pad = 0;
+                    F[pos] = e;
+                    pos = pos == bl ? n : pos + 1;
+                }
+        }
+        __syncwarp();
+        n = n - 1 + c;
         if (lane < n) {
             const FrontierEntry& e = F[lane];
             lo[0] = e.lo[0]; lo[1] = e.lo[1]; lo[2] = e.lo[2];
@@ -247,7 +293,7 @@ __device__ __forceinline__ int tile_frontier(const TraceParams& p, int x, int y,
     // grow by the radius with margin for the rounding of t, |d| and the hit point
     const float g = p.radius * 1.0001f + 1e-5f * (mag + 1.0f);
     for (int a = 0; a < 3; ++a) { lo[a] -= g; hi[a] += g; }
-    const int n = build_frontier(p.nodes, lo, hi, F);
+    const int n = build_frontier(p.nodes, lo, hi, F, p.frontier_tail);
     __syncwarp();
     return n;
 }

@@ -24,17 +24,19 @@ def _scene(rn, w, h, n_boxes=300, n_spheres=60):
 
 def test_trace_keys_keep_every_bit(rn, restore_tune):
     g, acc, tl = _scene(rn, 333, 197)
-    for k, v in (("trace_min_blocks", 3), ("trace_packet", 8), ("trace_stack", 96), ("trace_frontier", 1)):
+    defaults = {"trace_min_blocks": 3, "trace_packet": 8, "trace_stack": 96, "trace_frontier": 1,
+                "trace_frontier_min_spp": 1, "trace_frontier_tail": 0}
+    for k, v in defaults.items():
         rn.tune_set(k, v)
     ref_ao = rn.compute_rtao(g, acc, 16, 1.0).clone()
     ref_vis = [t.clone() for t in rn.compute_rt_visibility(g, acc, 16, 1.0, tl)]
-    for k in ("trace_min_blocks", "trace_packet", "trace_stack", "trace_frontier"):
+    for k in defaults:
         for v in rn.TUNE_KEYS[k]:
             rn.tune_set(k, v)
             assert bool((rn.compute_rtao(g, acc, 16, 1.0) == ref_ao).all()), (k, v)
             vis = rn.compute_rt_visibility(g, acc, 16, 1.0, tl)
             assert all(bool((a == b).all()) for a, b in zip(vis, ref_vis)), (k, v)
-        rn.tune_set(k, {"trace_min_blocks": 3, "trace_packet": 8, "trace_stack": 96, "trace_frontier": 1}[k])
+        rn.tune_set(k, defaults[k])
 
 
 def test_ssao_tile_keeps_every_bit(rn, restore_tune):
