@@ -882,11 +882,12 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     const tc::ConvTiling t = tc::conv_tiling(H, W);
     if (!t.ok || B <= 0) return fail(st, RN_ERR_INVALID, "tc_conv3x3: %dx%d cannot be tiled", H, W);
     int cin = 0;
-    bool all64 = true;
+    bool all64 = true, all32 = true;
     for (int i = 0; i < nsrc; ++i) {
-        if (!src[i].ptr || src[i].C <= 0 || src[i].C % 32 || ((uintptr_t)src[i].ptr % 16))
+        if (!src[i].ptr || src[i].C <= 0 || src[i].C % 16 || ((uintptr_t)src[i].ptr % 16))
             return fail(st, RN_ERR_INVALID, "tc_conv3x3: source %d (C %d)", i, src[i].C);
         all64 = all64 && src[i].C % 64 == 0;
+        all32 = all32 && src[i].C % 32 == 0;
         cin += src[i].C;
     }
     if (ldw < 9 * cin || ldw % 8 || ((uintptr_t)w % 16)) return fail(st, RN_ERR_INVALID, "tc_conv3x3: weight stride %d", ldw);
@@ -896,8 +897,10 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     while (bn > ctx().tune.conv_bn_max && bn > 32) bn /= 2;
     if (up16 && !epi.c16) return fail(st, RN_ERR_INVALID, "tc_conv3x3: the upsampled copy needs a BF16 output");
     // row-ring tiles: rows of 128 pixels, channels in groups of 16, N 32 or 64 in one slice,
-    // the weights and a ring of at least four row slots in shared memory
-    if (ctx().tune.conv_halo && t.tw_log2 == 7 && (N == 32 || N == 64) && (9 * cin) / 8 <= 256 && cin % 16 == 0) {
+    // the weights and a ring of at least four row slots in shared memory. Sources of 16
+    // channels have only this kernel (the per-tap boxes take 32 or 64 channels).
+    if ((ctx().tune.conv_halo || !all32) && t.tw_log2 == 7 && (N == 32 || N == 64) && (9 * cin) / 8 <= 256 &&
+        cin % 16 == 0) {
         const uint32_t b_bytes = (uint32_t)N * 9 * cin * 2;
         const uint32_t a_bytes = (uint32_t)cin / 8 * tc::kHaloGroup;
         const uint32_t a_stride = (a_bytes + 1023) & ~1023u, b_pad = (b_bytes + 1023) & ~1023u;
@@ -928,6 +931,8 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
             return RN_OK;
         }
     }
+    if (!all32)
+        return fail(st, RN_ERR_INVALID, "tc_conv3x3: 16-channel sources need 128-pixel rows, N 32 or 64 and resident weights");
     const int cb = all64 ? 64 : 32;
     const int tw = 1 << t.tw_log2, th = tc::kBM >> t.tw_log2;
     CUtensorMap m[2], mw;

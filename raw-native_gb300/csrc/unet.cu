@@ -215,7 +215,7 @@ __global__ void head_kernel(const bf16* __restrict__ d0, const float* __restrict
     }
 }
 
-// fp32 features [M][5] -> bf16 [M][C] (C = 8 or 32; channels 5.. zero)
+// fp32 features [M][5] -> bf16 [M][C] (C = 8, 16 or 32; channels 5.. zero)
 __global__ void input_kernel(const float* __restrict__ in, size_t M, int C, bf16* __restrict__ out) {
     for (size_t m = (size_t)blockIdx.x * blockDim.x + threadIdx.x; m < M; m += (size_t)gridDim.x * blockDim.x) {
         uint4 v;
@@ -227,13 +227,15 @@ __global__ void input_kernel(const float* __restrict__ in, size_t M, int C, bf16
     }
 }
 
-// The first convolution's weights in the 32-channel input layout of the implicit path:
-// w0[co][tap * 32 + ci] = wq[co][tap * 8 + ci] (ci < 8; the other columns stay zero).
-__global__ void expand_w0_kernel(const bf16* __restrict__ wq, int kpad, bf16* __restrict__ w0, int kpad0, int cout) {
+// The first convolution's weights in the cin-channel input layout of the implicit path
+// (cin 16 or 32): w0[co][tap * cin + ci] = wq[co][tap * 8 + ci] (ci < 8; the other columns
+// stay zero, so the zero input channels add exact zeros).
+__global__ void expand_w0_kernel(const bf16* __restrict__ wq, int kpad, bf16* __restrict__ w0, int kpad0, int cout,
+                                 int cin) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cout * 72) return;
     const int co = i / 72, k = i % 72, tap = k / 8, ci = k % 8;
-    w0[(size_t)co * kpad0 + tap * 32 + ci] = wq[(size_t)co * kpad + k];
+    w0[(size_t)co * kpad0 + tap * cin + ci] = wq[(size_t)co * kpad + k];
 }
 
 struct AdamArgs { float lr, b1, b2, eps, c1, c2; const float* scale; };
@@ -456,7 +458,7 @@ struct rn_unet {
     bool inference = false;       // forward only: one shared im2col buffer, no gradient storage
     bool implicit = false;        // 3x3 convolutions of >= 32 input channels on the implicit GEMM
     bf16* UT[T_COUNT] = {};       // implicit: 2x upsampled copies of the tensors read upsampled
-    bf16* wq0 = nullptr;          // implicit: the first convolution's weights for a 32-channel input
+    bf16* wq0 = nullptr;          // implicit: the first convolution's weights for the 16/32-channel input
     int kpad0 = 0;
     // per layer
     struct Layer {
@@ -500,7 +502,7 @@ int conv_forward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
     const LayerSpec& sp = kSpec[l];
     const int H = u->H >> Ly.level, W = u->W >> Ly.level;
     const size_t M = pixels(u, Ly.level);
-    if (u->implicit && l == 0) {          // the input is stored with 32 channels (5 used)
+    if (u->implicit && l == 0) {          // the input is stored with 16 or 32 channels (5 used)
         const tc::ConvSrc src{u->T[T_IN], u->TC[T_IN]};
         tc::Epilogue e{};
         e.ldc = Ly.cout;
@@ -601,7 +603,7 @@ void refresh_weights(rn_unet* u, const AdamArgs* a, cudaStream_t s) {
     }
     if (u->wq0)
         expand_w0_kernel<<<(u->L[0].cout * 72 + 255) / 256, 256, 0, s>>>(u->L[0].wq, u->L[0].kpad, u->wq0, u->kpad0,
-                                                                          u->L[0].cout);
+                                                                          u->L[0].cout, u->TC[T_IN]);
     if (a) {
         adam_vec_kernel<<<1, 32, 0, s>>>(u->wh, u->mh, u->vh, u->gwh, 32, *a);
         adam_vec_kernel<<<1, 32, 0, s>>>(u->bh, u->mbh, u->vbh, u->gbh, 1, *a);
@@ -709,14 +711,16 @@ int rn_unet_create(int batch, int height, int width, uint64_t seed, uint32_t fla
     const int tch[T_COUNT] = {kInC, 32, 32, 64, 64, 128, 128, 256, 256, 128, 128, 64, 64, 32, 32, 32, 64, 128};
     for (int t = 0; t < T_COUNT; ++t) {
         u->Tlevel[t] = tlevel[t];
-        u->TC[t] = (t == T_IN && u->implicit) ? 32 : tch[t];
+        // the implicit path's input: 16 channels where the row-ring kernel takes level 0
+        // (128-pixel rows), else 32 (5 used)
+        u->TC[t] = (t == T_IN && u->implicit) ? (u->W % 128 == 0 ? 16 : 32) : tch[t];
         u->Tn[t] = pixels(u, tlevel[t]) * u->TC[t];
         if (ualloc(u, (void**)&u->T[t], u->Tn[t] * 2, st) ||
             (!u->inference && ualloc(u, (void**)&u->dT[t], u->Tn[t] * 4, st)))
             return bail(RN_ERR_NO_MEMORY);
     }
     if (u->implicit) {
-        u->kpad0 = round_up(9 * 32, 128);
+        u->kpad0 = round_up(9 * u->TC[T_IN], 128);
         if (ualloc(u, (void**)&u->wq0, (size_t)u->L[0].cout * u->kpad0 * 2, st)) return bail(RN_ERR_NO_MEMORY);
     }
     if (u->implicit)

@@ -14,6 +14,8 @@ CASES = [
     (4, 16, 16, 256, 0, 256),
     (1, 8, 1920, 32, 64, 32),
     (2, 32, 32, 64, 128, 64),
+    (2, 24, 256, 16, 0, 32),             # 16 input channels: the row-ring kernel only
+    (1, 8, 128, 16, 0, 64),
     (1, 16, 16, 128, 256, 128),
     (1, 16, 64, 64, 0, 384),
     (2, 24, 48, 96, 0, 64),
@@ -73,6 +75,9 @@ def test_conv_rejects_untileable_and_bad_channels(rn):
     y = torch.zeros(1, 16, 16, 40, device="cuda", dtype=torch.bfloat16)       # 40 channels
     with pytest.raises(rn.RnError):
         rn.tc_conv3x3(y, torch.zeros(32, 384, device="cuda", dtype=torch.bfloat16))
+    z = torch.zeros(1, 16, 64, 16, device="cuda", dtype=torch.bfloat16)       # 16 channels, 64-pixel rows
+    with pytest.raises(rn.RnError):
+        rn.tc_conv3x3(z, torch.zeros(32, 256, device="cuda", dtype=torch.bfloat16))
 
 
 @pytest.mark.parametrize("B,H,W,c0,c1,N", [(2, 8, 128, 32, 0, 32), (1, 6, 256, 32, 0, 64), (1, 4, 1920, 32, 0, 32),
