@@ -331,7 +331,8 @@ int rn_tc_gemm(const void* P, int ldp, const void* Q, int ldq, int M, int N, int
  * channels ci of in[b, y+dy, x+dx, ci] * w[n][t * Cin + ci], the input being src0's c0
  * channels followed by src1's c1 (src1 may be null). Sources are NHWC BF16 [B][H][W][c],
  * c a multiple of 32 (or of 16 when W is a multiple of 128, N is 32 or 64 and the weights
- * fit in shared memory); w is BF16 [N][ldw], ldw >= 9 Cin; outputs [B][H][W][N] as FP32 (c32)
+ * fit in shared memory); w is BF16 [N][ldw], ldw >= 9 Cin, N <= 512 (32, 64, 128, 256 or a
+ * multiple of 128); outputs [B][H][W][N] as FP32 (c32)
  * and/or BF16 (c16), optional ReLU; up16 (with c16) also receives the BF16 output upsampled
  * 2x by nearest neighbour, [B][2H][2W][N]. W's largest power-of-two divisor (at most 128),
  * TW, sets the tile (128 / TW rows must divide H). Device pointers, the library's stream. */

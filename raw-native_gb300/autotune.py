@@ -17,7 +17,8 @@ Workloads:
   ssao           the built-in scene at 4K: SSAO, 24 taps
   conv           the surrogate U-Net: a forward at 1088 x 1920 and a training step on
                  64 crops of 128 x 128
-  trace/low-spp  the synthetic scene's view at 4, 8, 16 and 32 spp (trace_frontier_min_spp)
+  trace/low-spp  the synthetic scene's view at 4, 8, 16 and 32 spp, and a 4K view of the
+                 7.88M-triangle scene at 4 and 16 spp (trace_frontier_min_spp)
   trace/tail     the same view at 16, 64 and 256 spp (trace_frontier_tail)
 The traversal keys are searched jointly (every combination); the others one at a time.
 """
@@ -101,20 +102,28 @@ def tune_trace(quick: bool, reps: int, log):
 
 def tune_frontier_min_spp(quick: bool, reps: int, log):
     """The spp from which the per-warp frontier pays for its build: AO-only traces of the
-    synthetic scene at 4, 8, 16 and 32 spp; the candidate with the least total time."""
+    synthetic scene at 4, 8, 16 and 32 spp (1920 x 1080), and of the 7.88M-triangle scene at
+    4 and 16 spp (3840 x 2160, radius 1: the surrogate's input trace); the candidate with the
+    least total time."""
     import torch
     big = scenes.build_synthetic_scene(7, 500 if quick else 2000, 100 if quick else 500)
     bt, bn = torch.from_numpy(big.tris).cuda(), torch.from_numpy(big.normals).cuda()
     g = rn.rasterize(bt, bn, scenes.orbit_views(7, 8)[0][3], 1920, 1080)
     acc = rn.LinearAccel(bt)
+    huge = scenes.build_synthetic_scene(5, 1000 if quick else 10000, 600 if quick else 6000)
+    ht, hn = torch.from_numpy(huge.tris).cuda(), torch.from_numpy(huge.normals).cuda()
+    gh = rn.rasterize(ht, hn, scenes.orbit_views(5, 16)[0][3], 1920 if quick else 3840, 1080 if quick else 2160)
+    acch = rn.LinearAccel(ht)
     rows = []
     for v in rn.TUNE_KEYS["trace_frontier_min_spp"]:
         rn.tune_set("trace_frontier_min_spp", v)
         ms = {"spp%d" % spp: _time(lambda: rn.compute_rtao(g, acc, spp, 1.0), reps) for spp in (4, 8, 16, 32)}
+        ms.update({"large_spp%d" % spp: _time(lambda: rn.compute_rtao(gh, acch, spp, 1.0), reps) for spp in (4, 16)})
         rows.append(dict(cfg={"trace_frontier_min_spp": v}, ms=ms, total=sum(ms.values())))
         log("trace_frontier_min_spp %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
     best = min(rows, key=lambda r: r["total"])
     rn.tune_set("trace_frontier_min_spp", best["cfg"]["trace_frontier_min_spp"])
+    del acch, gh, ht, hn
     return best["cfg"], rows
 
 

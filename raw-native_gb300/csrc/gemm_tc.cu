@@ -288,6 +288,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
     uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kSt * kBBytes);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 4);
     __shared__ int s_abort;
+    __shared__ float s_bias[512];       // the bias of every output channel, staged once
     volatile int* abort_flag = &s_abort;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tw = 1 << a.tw_log2, th = kBM >> a.tw_log2;
@@ -304,6 +305,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
+    if (e.bias)
+        for (int i = threadIdx.x; i < a.n_slices * BN; i += blockDim.x) s_bias[i] = e.bias[i];
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(kCols)
@@ -409,7 +412,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     float t = __uint_as_float(v[j]);
-                    if (e.bias) t += e.bias[col + j];
+                    if (e.bias) t += s_bias[col + j];
                     if (e.relu) t = fmaxf(t, 0.0f);
                     f[j] = t;
                 }
@@ -525,6 +528,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     uint64_t* bars = reinterpret_cast<uint64_t*>(sA + kSt * a_stride);     // full[kSt], empty[kSt], acc_full[2], acc_empty[2], w
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 5);
     __shared__ int s_abort;
+    __shared__ float s_bias[512];       // the bias of every output channel, staged once
     volatile int* abort_flag = &s_abort;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     auto full = [&](int s) { return smem_u32(&bars[s]); };
@@ -540,6 +544,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
+    if (e.bias)
+        for (int i = threadIdx.x; i < BN; i += blockDim.x) s_bias[i] = e.bias[i];
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(kCols)
@@ -648,7 +654,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
 #pragma unroll
                     for (int jj = 0; jj < 16; ++jj) {
                         float t = __uint_as_float(v[jj]);
-                        if (e.bias) t += e.bias[c0 + jj];
+                        if (e.bias) t += s_bias[c0 + jj];
                         if (e.relu) t = fmaxf(t, 0.0f);
                         f[jj] = t;
                     }
@@ -893,7 +899,7 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     if (ldw < 9 * cin || ldw % 8 || ((uintptr_t)w % 16)) return fail(st, RN_ERR_INVALID, "tc_conv3x3: weight stride %d", ldw);
     if (epi.atomic || epi.gate) return fail(st, RN_ERR_INVALID, "tc_conv3x3: no atomic or gated epilogue");
     int bn = (N == 32 || N == 64 || N == 128 || N == 256) ? N : 128;
-    if (N % bn) return fail(st, RN_ERR_INVALID, "tc_conv3x3 N %d", N);
+    if (N % bn || N > 512) return fail(st, RN_ERR_INVALID, "tc_conv3x3 N %d", N);
     while (bn > ctx().tune.conv_bn_max && bn > 32) bn /= 2;
     if (up16 && !epi.c16) return fail(st, RN_ERR_INVALID, "tc_conv3x3: the upsampled copy needs a BF16 output");
     // row-ring tiles: rows of 128 pixels, channels in groups of 16, N 32 or 64 in one slice,
