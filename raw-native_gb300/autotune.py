@@ -10,6 +10,10 @@ tune_sm103.txt when it exists.
   python autotune.py --out tune_sm103.txt [--report report.json] [--quick]
 
 Workloads:
+  accel          the traversal accelerator's PLOC radius and leaf size: builds of the
+                 7.88M-triangle scene (4K view at 4 and 16 spp) and of the 744k scene
+                 (1080p view at 64 spp); the leaf size of scenes under 65,536 triangles
+                 on the built-in scene's 4K frame (64 spp, AO + sky + sun)
   trace/model2   the reference's built-in scene and default camera at 3840 x 2160, 64 spp,
                  AO + sky + sun (lighting model 2, radius 2)
   trace/ao       a seeded synthetic scene (2,000 boxes, 500 spheres; 744k triangles),
@@ -158,6 +162,70 @@ def tune_frontier_tail(quick: bool, reps: int, log):
     return best["cfg"], rows
 
 
+def tune_accel(quick: bool, reps: int, log):
+    """The traversal accelerator's shape: PLOC search radius x largest leaf, each built for the
+    7.88M-triangle scene (4K view, AO radius 1, 4 and 16 spp: the surrogate's input trace and
+    a low-spp frame) and the 744k scene (1080p view, 64 spp), every traced image checked bit
+    for bit against the default shape; score: geometric mean of the time ratios to the
+    default (radius 16, leaves of 4)."""
+    import torch
+    huge = scenes.build_synthetic_scene(5, 1000 if quick else 10000, 600 if quick else 6000)
+    ht, hn = torch.from_numpy(huge.tris).cuda(), torch.from_numpy(huge.normals).cuda()
+    gh = rn.rasterize(ht, hn, scenes.orbit_views(5, 16)[0][3], 1920 if quick else 3840, 1080 if quick else 2160)
+    big = scenes.build_synthetic_scene(7, 500 if quick else 2000, 100 if quick else 500)
+    bt, bn = torch.from_numpy(big.tris).cuda(), torch.from_numpy(big.normals).cuda()
+    gb = rn.rasterize(bt, bn, scenes.orbit_views(7, 8)[0][3], 1920, 1080)
+    work = (("large_spp4", 0, 4), ("large_spp16", 0, 16), ("ao_spp64", 1, 64))
+    rows, ref = [], None
+    default = (16, 4)
+    combos = [default] + [(r, l) for r in rn.TUNE_KEYS["accel_radius"] for l in rn.TUNE_KEYS["accel_leaf"]
+                          if (r, l) != default]
+    for radius, leaf in combos:
+        rn.tune_set("accel_radius", radius)
+        rn.tune_set("accel_leaf", leaf)
+        t0 = time.perf_counter()
+        accs = (rn.LinearAccel(ht), rn.LinearAccel(bt))
+        torch.cuda.synchronize()
+        build_s = time.perf_counter() - t0
+        geo = (gh, gb)
+        outs = [rn.compute_rtao(geo[w], accs[w], spp, 1.0).clone() for _, w, spp in work]
+        if ref is None:
+            ref = outs
+        elif not all(bool((a == b).all()) for a, b in zip(outs, ref)):
+            raise RuntimeError("accel_radius %d accel_leaf %d changed a traced result" % (radius, leaf))
+        ms = {name: _time(lambda: rn.compute_rtao(geo[w], accs[w], spp, 1.0), reps) for name, w, spp in work}
+        rows.append(dict(cfg={"accel_radius": radius, "accel_leaf": leaf}, ms=ms, build_s=build_s))
+        log("accel_radius %d accel_leaf %d  build %.2f s  %s" % (radius, leaf, build_s,
+                                                                "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+        del accs
+    base = rows[0]["ms"]
+    for r in rows:
+        r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
+    best = min(rows, key=lambda r: r["score"])
+    for k, v in best["cfg"].items():
+        rn.tune_set(k, v)
+    # scenes under 65,536 triangles take their own leaf size: the built-in scene's 4K frame
+    sc = scenes.build_test_scene()
+    st_, sn_ = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+    w, h = (1920, 1080) if quick else (3840, 2160)
+    gs = rn.rasterize(st_, sn_, sc.camera, w, h)
+    ref_small = None
+    for leaf in rn.TUNE_KEYS["accel_leaf_small"]:
+        rn.tune_set("accel_leaf_small", leaf)
+        acc = rn.LinearAccel(st_)
+        out = [t.clone() for t in rn.compute_rt_visibility(gs, acc, 64, 2.0, sc.to_light)]
+        if ref_small is None:
+            ref_small = out
+        elif not all(bool((a == b).all()) for a, b in zip(out, ref_small)):
+            raise RuntimeError("accel_leaf_small %d changed a traced result" % leaf)
+        ms = {"model2": _time(lambda: rn.compute_rt_visibility(gs, acc, 64, 2.0, sc.to_light), reps)}
+        rows.append(dict(cfg={"accel_leaf_small": leaf}, ms=ms))
+        log("accel_leaf_small %d  model2 %.3f ms" % (leaf, ms["model2"]))
+    small = min((r for r in rows if "accel_leaf_small" in r["cfg"]), key=lambda r: r["ms"]["model2"])
+    rn.tune_set("accel_leaf_small", small["cfg"]["accel_leaf_small"])
+    return dict(best["cfg"], **small["cfg"]), rows
+
+
 def tune_ssao(quick: bool, reps: int, log):
     import torch
     sc = scenes.build_test_scene()
@@ -233,6 +301,8 @@ def main(argv=None):
     t0 = time.time()
     log = lambda m: print(m, flush=True)
     cfg, report = {}, {}
+    c, report["accel"] = tune_accel(a.quick, a.reps, log)
+    cfg.update(c)
     c, report["trace"] = tune_trace(a.quick, a.reps, log)
     cfg.update(c)
     c, report["frontier_min_spp"] = tune_frontier_min_spp(a.quick, a.reps, log)

@@ -121,6 +121,9 @@ const TuneKey kTuneKeys[] = {
     {"ssao_tile_h", "RN_TUNE_SSAO_TILE_H", &Tune::ssao_tile_h, {4, 8, 16}, 3},
     {"conv_bn_max", "RN_TUNE_CONV_BN_MAX", &Tune::conv_bn_max, {64, 128, 256}, 3},
     {"conv_halo", "RN_TUNE_CONV_HALO", &Tune::conv_halo, {0, 1}, 2},
+    {"accel_radius", "RN_TUNE_ACCEL_RADIUS", &Tune::accel_radius, {8, 16, 32, 64}, 4},
+    {"accel_leaf", "RN_TUNE_ACCEL_LEAF", &Tune::accel_leaf, {1, 2, 4, 8}, 4},
+    {"accel_leaf_small", "RN_TUNE_ACCEL_LEAF_SMALL", &Tune::accel_leaf_small, {1, 2, 4, 8}, 4},
     {"frame_direct", "RN_TUNE_FRAME_DIRECT", &Tune::frame_direct, {0, 1}, 2},
 };
 
@@ -561,8 +564,11 @@ int rn_accel_build(const float* tris, uint32_t ntri, int flags, rn_accel** out, 
     rn_accel* acc = new rn_accel();
     acc->device = c.device;
     PlocTree tree;
-    int rc = ploc_build(d_tris, ntri, 16, &tree, c.stream, st);
-    if (rc == RN_OK) rc = collapse_bvh4(tree, d_tris, acc, c.stream, st);
+    // the tree only prunes (every hit is the triangle test's): its shape is a tuning choice
+    int rc = ploc_build(d_tris, ntri, c.tune.accel_radius, &tree, c.stream, st);
+    if (rc == RN_OK)
+        rc = collapse_bvh4(tree, d_tris, acc, ntri < kSmallScene ? c.tune.accel_leaf_small : c.tune.accel_leaf,
+                           c.stream, st);
     if (rc == RN_OK) {
         cudaError_t e = cudaStreamSynchronize(c.stream);
         if (e != cudaSuccess) rc = cuda_fail(st, e, "rn_accel_build");

@@ -13,7 +13,7 @@
 //      rounds in batches and reads the survivor count once per batch, not once per round.
 //   6. collapse: subtree sizes bottom-up, then level by level each 4-wide node takes the
 //      binary node's children and opens the largest-area interior child until it has 4;
-//      subtrees of at most kLeafMax triangles become leaves with their triangles copied
+//      subtrees of at most leaf_max (<= 8) triangles become leaves with their triangles copied
 //      contiguously (48-byte records).
 #include "rn_internal.h"
 #include "rn_device.cuh"
@@ -483,14 +483,15 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
                                const float* __restrict__ box, const int32_t* __restrict__ left,
                                const int32_t* __restrict__ right, const int32_t* __restrict__ tri,
                                const uint32_t* __restrict__ count, const float* __restrict__ tris,
-                               Node4* __restrict__ nodes, LeafTri* __restrict__ leaf, uint32_t* err) {
+                               Node4* __restrict__ nodes, LeafTri* __restrict__ leaf, uint32_t leaf_max,
+                               uint32_t* err) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= *nin) return;
     const Task task = in[t];
     int32_t C[4];
     int nc = 0;
     const int32_t b = task.bnode;
-    if (tri[b] >= 0 || count[b] <= (uint32_t)kLeafMax) {
+    if (tri[b] >= 0 || count[b] <= leaf_max) {
         C[nc++] = b;
     } else {
         C[nc++] = left[b];
@@ -500,7 +501,7 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
             float best = -1.0f;
             for (int k = 0; k < nc; ++k) {
                 const int32_t c = C[k];
-                if (tri[c] >= 0 || count[c] <= (uint32_t)kLeafMax) continue;
+                if (tri[c] >= 0 || count[c] <= leaf_max) continue;
                 const float a = box_area(box + (size_t)c * 6);
                 if (a > best) { best = a; pick = k; }
             }
@@ -524,11 +525,11 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
         padded(box + (size_t)c * 6, lo, hi);
         nd.lox[k] = lo[0]; nd.loy[k] = lo[1]; nd.loz[k] = lo[2];
         nd.hix[k] = hi[0]; nd.hiy[k] = hi[1]; nd.hiz[k] = hi[2];
-        if (tri[c] >= 0 || count[c] <= (uint32_t)kLeafMax) {
+        if (tri[c] >= 0 || count[c] <= leaf_max) {
             const uint32_t cnt = count[c];
             const uint32_t first = atomicAdd(tri_ctr, cnt);
             // the subtree's leaves, left to right
-            int32_t stack[2 * kLeafMax];
+            int32_t stack[2 * kLeafCap];
             int sp = 0, w = 0;
             stack[sp++] = c;
             while (sp > 0) {
@@ -540,7 +541,7 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
                     lt.bx = v[3]; lt.by = v[4]; lt.bz = v[5]; lt.pad0 = 0.0f;
                     lt.cx = v[6]; lt.cy = v[7]; lt.cz = v[8]; lt.pad1 = 0.0f;
                     leaf[first + w++] = lt;
-                } else if (sp + 2 <= 2 * kLeafMax) {
+                } else if (sp + 2 <= 2 * kLeafCap) {
                     stack[sp++] = right[x];
                     stack[sp++] = left[x];
                 } else {
@@ -683,7 +684,9 @@ int ploc_export(const PlocTree& t, int32_t* d_nodes9, cudaStream_t s, rn_status*
     return ok(st);
 }
 
-int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, cudaStream_t s, rn_status* st) {
+int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, int leaf_max, cudaStream_t s,
+                  rn_status* st) {
+    if (leaf_max < 1 || leaf_max > kLeafCap) return fail(st, RN_ERR_INVALID, "leaf size %d outside [1, %d]", leaf_max, kLeafCap);
     const uint32_t n = t.n;
     acc->ntri = n;
     acc->rounds = t.rounds;
@@ -720,7 +723,8 @@ int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, cudaStr
         if (depth > 4096) { cudaFreeAsync(mem, s); return fail(st, RN_ERR_BUDGET, "collapse: more than 4096 levels"); }
         collapse_level<<<cdiv(level_tasks, 128), 128, 0, s>>>(q0, ctr + 0, q1, ctr + 1, n, ctr + 2, node_cap,
                                                               ctr + 3, t.box, t.left, t.right, t.tri, count,
-                                                              d_tris, acc->d_nodes, acc->d_tris, ctr + 4);
+                                                              d_tris, acc->d_nodes, acc->d_tris, (uint32_t)leaf_max,
+                                                              ctr + 4);
         ++depth;
         // next level: its tasks become the input, the output counter restarts at 0
         RN_CUDA(cudaMemcpyAsync(ctr + 0, ctr + 1, 4, cudaMemcpyDeviceToDevice, s), st);

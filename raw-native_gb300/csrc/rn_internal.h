@@ -48,8 +48,12 @@ struct Tune {
     int ssao_tile_h = 8;        // SSAO tile: 32 x ssao_tile_h pixels, one thread each; 4, 8 or 16
     int conv_bn_max = 256;      // largest GEMM tile width (columns of C per CTA): 64, 128 or 256
     int conv_halo = 1;          // 128-pixel row tiles from one halo box per tile (where they fit)
+    int accel_radius = 16;      // PLOC search radius of the traversal accelerators built next
+    int accel_leaf = 4;         // largest leaf (triangles) of the traversal accelerators built next
+    int accel_leaf_small = 4;   // ... of those with fewer than kSmallScene triangles
     int frame_direct = 1;       // host-buffer frames: the passes read and write mapped host memory
 };
+constexpr uint32_t kSmallScene = 1u << 16;
 
 struct Context {
     bool ready = false;
@@ -122,7 +126,7 @@ struct alignas(16) Node4 {
     int32_t meta[4];   // meta[0] = number of valid children
 };
 static_assert(sizeof(Node4) == 128, "Node4 layout");
-constexpr int kLeafMax = 4;
+constexpr int kLeafCap = 8;   // triangles a leaf may hold (the child word's 3-bit count)
 
 // A leaf triangle: vertices a, b, c as float4 (w of a = input triangle index).
 struct alignas(16) LeafTri {
@@ -160,7 +164,8 @@ struct PlocTree {
 int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaStream_t s, rn_status* st);
 void ploc_free(PlocTree* t);
 int ploc_export(const PlocTree& t, int32_t* d_nodes9, cudaStream_t s, rn_status* st);
-int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, cudaStream_t s, rn_status* st);
+int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, int leaf_max, cudaStream_t s,
+                  rn_status* st);
 
 // ---------------------------------------------------------------- traversal
 struct TraceParams {

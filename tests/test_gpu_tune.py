@@ -104,3 +104,43 @@ def test_host_frame_keeps_every_bit(rn, restore_tune, sky):
     got = rn.ao_frame(pg, acc, 8, 1.0, 24, 0.12, to_light=to_light)
     for k in keys:
         assert np.array_equal(got[k], ref[k].cpu().numpy()), ("pageable", k)
+
+
+def test_accel_shape_keeps_every_bit(rn, restore_tune):
+    """The traversal accelerator's PLOC radius and leaf size (accel_radius, accel_leaf) change
+    the tree, never a traced pixel: the BVH only prunes."""
+    import torch
+    import scene as scenes
+    sc = scenes.build_synthetic_scene(11, 300, 60)
+    tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+    g = rn.rasterize(tris, nrms, scenes.orbit_views(11, 8)[3][3], 333, 197)
+    rn.tune_set("accel_radius", 16)
+    rn.tune_set("accel_leaf", 4)
+    acc = rn.LinearAccel(tris)
+    ref_ao = rn.compute_rtao(g, acc, 16, 1.0).clone()
+    ref_vis = [t.clone() for t in rn.compute_rt_visibility(g, acc, 8, 1.0, sc.to_light)]
+    for radius, leaf in ((8, 4), (32, 4), (64, 4), (16, 1), (16, 2), (16, 8), (64, 8)):
+        rn.tune_set("accel_radius", radius)
+        rn.tune_set("accel_leaf", leaf)
+        a = rn.LinearAccel(tris)
+        assert bool((rn.compute_rtao(g, a, 16, 1.0) == ref_ao).all()), (radius, leaf)
+        vis = rn.compute_rt_visibility(g, a, 8, 1.0, sc.to_light)
+        assert all(bool((x == y).all()) for x, y in zip(vis, ref_vis)), (radius, leaf)
+
+
+def test_small_scene_leaf_keeps_every_bit(rn, restore_tune):
+    """Scenes under 65,536 triangles take accel_leaf_small: the built-in scene's frame is the
+    same for every leaf size."""
+    import torch
+    import scene as scenes
+    sc = scenes.build_test_scene()
+    tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+    g = rn.rasterize(tris, nrms, sc.camera, 320, 240)
+    ref = None
+    for leaf in rn.TUNE_KEYS["accel_leaf_small"]:
+        rn.tune_set("accel_leaf_small", leaf)
+        acc = rn.LinearAccel(tris)
+        out = [t.clone() for t in rn.compute_rt_visibility(g, acc, 32, 2.0, sc.to_light)]
+        if ref is None:
+            ref = out
+        assert all(bool((a == b).all()) for a, b in zip(out, ref)), leaf
