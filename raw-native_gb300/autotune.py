@@ -18,6 +18,8 @@ Workloads:
                  AO + sky + sun (lighting model 2, radius 2)
   trace/ao       a seeded synthetic scene (2,000 boxes, 500 spheres; 744k triangles),
                  1920 x 1080 orbit view, 64 spp AO only (radius 1)
+  trace/large    the 7.88M-triangle scene, one 3840 x 2160 orbit view, 16 spp AO only
+  batch          16 orbit views of the 744k scene in one captured batch (batch_min_blocks)
   ssao           the built-in scene at 4K: SSAO, 24 taps
   conv           the surrogate U-Net: a forward at 1088 x 1920 and a training step on
                  64 crops of 128 x 128
@@ -77,6 +79,11 @@ def trace_workloads(quick: bool):
     g2 = rn.rasterize(bt, bn, cam, 1920, 1080)
     acc2 = rn.LinearAccel(bt)
     out.append(("trace/ao", lambda: rn.compute_rtao(g2, acc2, 64, 1.0), (g2, acc2)))
+    huge = scenes.build_synthetic_scene(5, 1000 if quick else 10000, 600 if quick else 6000)
+    ht, hn = torch.from_numpy(huge.tris).cuda(), torch.from_numpy(huge.normals).cuda()
+    g3 = rn.rasterize(ht, hn, scenes.orbit_views(5, 16)[0][3], 1920 if quick else 3840, 1080 if quick else 2160)
+    acc3 = rn.LinearAccel(ht)
+    out.append(("trace/large", lambda: rn.compute_rtao(g3, acc3, 16, 1.0), (g3, acc3)))
     return out
 
 
@@ -226,6 +233,34 @@ def tune_accel(quick: bool, reps: int, log):
     return dict(best["cfg"], **small["cfg"]), rows
 
 
+def tune_batch(quick: bool, reps: int, log):
+    """Residency of the batched multi-view traversal: 16 orbit views (resolutions and spp as
+    drawn) of the 744k scene in one captured batch; every view's AO checked bit for bit."""
+    import torch
+    sc = scenes.build_synthetic_scene(1, 500 if quick else 2000, 100 if quick else 500)
+    tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+    acc = rn.LinearAccel(tris)
+    views = [dict(g=rn.rasterize(tris, nrms, cam, w, h), spp=spp, radius=1.0)
+             for (w, h, spp, cam) in scenes.orbit_views(1, 8 if quick else 16)]
+    rows, ref = [], None
+    for v in rn.TUNE_KEYS["batch_min_blocks"]:
+        rn.tune_set("batch_min_blocks", v)
+        b = rn.Batch(acc, views)
+        b.run()
+        out = [o["ao"].clone() for o in b.outputs]
+        if ref is None:
+            ref = out
+        elif not all(bool((x == y).all()) for x, y in zip(out, ref)):
+            raise RuntimeError("batch_min_blocks %d changed a traced result" % v)
+        ms = _time(b.run, max(2, reps // 2))
+        rows.append(dict(cfg={"batch_min_blocks": v}, ms={"batch": ms}))
+        log("batch_min_blocks %d  %.3f ms" % (v, ms))
+        del b
+    best = min(rows, key=lambda r: r["ms"]["batch"])
+    rn.tune_set("batch_min_blocks", best["cfg"]["batch_min_blocks"])
+    return best["cfg"], rows
+
+
 def tune_ssao(quick: bool, reps: int, log):
     import torch
     sc = scenes.build_test_scene()
@@ -308,6 +343,8 @@ def main(argv=None):
     c, report["frontier_min_spp"] = tune_frontier_min_spp(a.quick, a.reps, log)
     cfg.update(c)
     c, report["frontier_tail"] = tune_frontier_tail(a.quick, a.reps, log)
+    cfg.update(c)
+    c, report["batch"] = tune_batch(a.quick, a.reps, log)
     cfg.update(c)
     c, report["ssao"] = tune_ssao(a.quick, a.reps, log)
     cfg.update(c)

@@ -206,7 +206,7 @@ int rn_batch_create(const rn_accel* accel, const rn_view* views, int nviews, int
     if (rc == RN_OK) {
         cudaMemsetAsync(d_ctr, 0, 4, b->capture);
         cudaMemsetAsync(d_outs, 0, (size_t)nviews * sizeof(RecOut), b->capture);
-        const int mb = c.tune.trace_min_blocks;
+        const int mb = c.tune.batch_min_blocks;
         if (mb == 2) trace_batch_kernel<2><<<c.sm_count * 2, 256, 0, b->capture>>>(d_views, nviews, tiles, d_ctr);
         else if (mb == 4) trace_batch_kernel<4><<<c.sm_count * 4, 256, 0, b->capture>>>(d_views, nviews, tiles, d_ctr);
         else trace_batch_kernel<3><<<c.sm_count * 3, 256, 0, b->capture>>>(d_views, nviews, tiles, d_ctr);

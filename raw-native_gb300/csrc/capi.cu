@@ -113,6 +113,7 @@ struct TuneKey {
 };
 const TuneKey kTuneKeys[] = {
     {"trace_min_blocks", "RN_TUNE_TRACE_MIN_BLOCKS", &Tune::trace_min_blocks, {2, 3, 4}, 3},
+    {"batch_min_blocks", "RN_TUNE_BATCH_MIN_BLOCKS", &Tune::batch_min_blocks, {2, 3, 4}, 3},
     {"trace_frontier", "RN_TUNE_TRACE_FRONTIER", &Tune::trace_frontier, {0, 1}, 2},
     {"trace_frontier_min_spp", "RN_TUNE_TRACE_FRONTIER_MIN_SPP", &Tune::trace_frontier_min_spp, {1, 8, 16, 32}, 4},
     {"trace_frontier_tail", "RN_TUNE_TRACE_FRONTIER_TAIL", &Tune::trace_frontier_tail, {0, 4, 8, 16}, 4},

@@ -40,6 +40,7 @@ enum Slot {
 // environment variables at the first rn_init). None of them changes a result bit.
 struct Tune {
     int trace_min_blocks = 3;   // resident 256-thread traversal blocks per SM: 2, 3 or 4
+    int batch_min_blocks = 3;   // ... of the batched multi-view traversal
     int trace_frontier = 1;     // per-warp frontier for AO-only walks
     int trace_frontier_min_spp = 16;  // ... built only when spp reaches this (its cost is per packet)
     int trace_frontier_tail = 0;      // greedy largest-first steps after the level-by-level build (at most spp / 16)

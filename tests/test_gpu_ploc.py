@@ -81,8 +81,17 @@ def test_any_hit_equals_scan(rn, oracle, scene):
 
 
 def test_accel_info(rn, oracle):
-    tris = oracle.soup(20000, 7)
-    acc = rn.LinearAccel(tris)
-    info = acc.info()
-    assert info["leaf_tris"] == 20000 and info["ploc_rounds"] == 40
-    assert 20000 // 4 // 4 <= info["wide_nodes"] < 20000
+    """The accelerator of a 20,000-triangle soup with the default shape (PLOC radius 16, leaves
+    of at most 4 triangles): the PLOC round count and the 4-wide node count."""
+    saved = {k: rn.tune_get(k) for k in ("accel_radius", "accel_leaf")}
+    try:
+        rn.tune_set("accel_radius", 16)
+        rn.tune_set("accel_leaf", 4)
+        tris = oracle.soup(20000, 7)
+        acc = rn.LinearAccel(tris)
+        info = acc.info()
+        assert info["leaf_tris"] == 20000 and info["ploc_rounds"] == 40
+        assert 20000 // 4 // 4 <= info["wide_nodes"] < 20000
+    finally:
+        for k, v in saved.items():
+            rn.tune_set(k, v)
