@@ -26,16 +26,28 @@ __device__ __forceinline__ float max_nan(float a, float b) {
 // inverse(d) of src/renderer/bvh.cpp:29-33: 1/x, or a signed infinity for a zero component.
 __device__ __forceinline__ float safe_inv(float x) { return x != 0.0f ? __frcp_rn(x) : copysignf(__int_as_float(0x7f800000), x); }
 
-struct Inv { float x, y, z; };
-__device__ __forceinline__ Inv make_inv(const v3& d) { return Inv{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)}; }
+// The ray's inverse direction and origin x inverse direction, formed once per walk.
+struct Inv { float x, y, z, ox, oy, oz; };
+__device__ __forceinline__ Inv make_inv(const v3& o, const v3& d) {
+    Inv r;
+    r.x = safe_inv(d.x); r.y = safe_inv(d.y); r.z = safe_inv(d.z);
+    r.ox = o.x * r.x; r.oy = o.y * r.y; r.oz = o.z * r.z;
+    return r;
+}
 
-// Slab entry of one child box. An axis whose distances are NaN (origin on the plane, zero
-// direction component) constrains nothing, as in the reference's entry().
+// Slab entry of one child box, each plane distance as one fused multiply-add,
+// lo * inv - o * inv. The BVH only prunes, so the test has to be conservative, not exact:
+// against (lo - o) * inv the fused form is off by at most about 2^-24 |o| in position, far
+// inside the child boxes' outward padding (2^-19 of the coordinate plus 1e-6 of the
+// extent), so no box a triangle hit lies in is culled. An axis whose distances are NaN
+// (origin on the plane, zero or vanishing direction component) constrains nothing, as in
+// the reference's entry(); that only keeps more boxes.
 __device__ __forceinline__ bool slab(float lox, float hix, float loy, float hiy, float loz, float hiz,
                                      const v3& o, const Inv& iv, float tmax, float& tnear) {
-    const float ax = (lox - o.x) * iv.x, bx = (hix - o.x) * iv.x;
-    const float ay = (loy - o.y) * iv.y, by = (hiy - o.y) * iv.y;
-    const float az = (loz - o.z) * iv.z, bz = (hiz - o.z) * iv.z;
+    (void)o;
+    const float ax = __fmaf_rn(lox, iv.x, -iv.ox), bx = __fmaf_rn(hix, iv.x, -iv.ox);
+    const float ay = __fmaf_rn(loy, iv.y, -iv.oy), by = __fmaf_rn(hiy, iv.y, -iv.oy);
+    const float az = __fmaf_rn(loz, iv.z, -iv.oz), bz = __fmaf_rn(hiz, iv.z, -iv.oz);
     const float t0 = fmaxf(fmaxf(fmaxf(0.0f, min_nan(ax, bx)), min_nan(ay, by)), min_nan(az, bz));
     const float t1 = fminf(fminf(fminf(tmax, max_nan(ax, bx)), max_nan(ay, by)), max_nan(az, bz));
     tnear = t0;
@@ -181,7 +193,7 @@ template <bool kCount, int kStackN = kStack>
 __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, const v3& o, const v3& d,
                     float tnear, float tfar, uint32_t* err, Counts& cn, const FrontierEntry* F = nullptr,
                     int fn = 0) {
-    const Inv iv = make_inv(d);
+    const Inv iv = make_inv(o, d);
     WRay wr;                             // the watertight set-up: formed at the first leaf
     bool wr_ready = false;
     float tmax = tfar;
