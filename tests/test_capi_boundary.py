@@ -125,3 +125,20 @@ def test_tuning_keys_without_a_device(lib, tmp_path, monkeypatch):
     finally:
         for k, v in saved.items():
             rn_ao.tune_set(k, v)
+
+
+def test_package_tune_file_loads(lib):
+    """The autotuner's committed file for GB300 names known keys with allowed values only."""
+    import rn_ao
+    saved = rn_ao.tune_all()
+    try:
+        rn_ao.tune_load(rn_ao.TUNE_FILE)
+        keys = [ln.split("=")[0].strip() for ln in open(rn_ao.TUNE_FILE) if "=" in ln and not ln.startswith("#")]
+        assert keys and set(keys) <= set(rn_ao.TUNE_KEYS)
+        for ln in open(rn_ao.TUNE_FILE):
+            if "=" in ln and not ln.startswith("#"):
+                k, v = (x.strip() for x in ln.split("=", 1))
+                assert rn_ao.tune_get(k) == int(v)
+    finally:
+        for k, v in saved.items():
+            rn_ao.tune_set(k, v)
