@@ -304,13 +304,19 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
 /* Launch-shape tuning (no counterpart in the reference; no key changes a per-pixel result).
  * Keys and values:
  *   trace_min_blocks  2 | 3 | 4      resident traversal blocks per SM (register budget)
+ *   batch_min_blocks  2 | 3 | 4      ... of the batched multi-view traversal (rn_batch_*)
  *   trace_frontier    0 | 1          per-warp frontier for AO-only walks
  *   trace_frontier_min_spp 1|8|16|32 ... built only at this spp or more
+ *   trace_frontier_tail 0|4|8|16     greedy steps after the level-by-level build (<= spp / 16)
  *   trace_packet      4 | 8 | 16     a warp's pixel packet: packet x (32 / packet)
  *   trace_stack       48 | 96        traversal stack entries (48 only where the tree allows)
  *   ssao_tile_h       4 | 8 | 16     SSAO tile 32 x h (the fused FP64 sum follows the tiling)
  *   conv_bn_max       64 | 128 | 256 widest GEMM tile of the surrogate's convolutions
- *   conv_halo         0 | 1          row tiles of 128 pixels from one halo box each (where they fit)
+ *   conv_halo         0 | 1          128-pixel row tiles from a ring of one-row boxes (where they fit)
+ *   accel_radius      8|16|32|64     PLOC search radius of accelerators built afterwards
+ *   accel_leaf        1 | 2 | 4 | 8  their largest leaf (triangles), 65,536 triangles or more
+ *   accel_leaf_small  1 | 2 | 4 | 8  ... below 65,536 triangles
+ *   frame_direct      0 | 1          rn_ao_frame on pinned, mapped host buffers without copies
  * Process-wide; RN_TUNE_<KEY> environment variables apply before the first call.
  * rn_tune_load reads "key = value" lines ('#' comments), all or nothing. */
 int rn_tune_set(const char* key, int value, rn_status* st);
