@@ -403,6 +403,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
             const int y = ty * th + (r >> a.tw_log2), x = tx * tw + (r & (tw - 1));
             const size_t pix = ((size_t)b * a.H + y) * a.W + x;
             const uint32_t tbase = tmem + buf * BN + ((uint32_t)(q * 32) << 16);
+            float hz = e.head_out ? e.head_b[0] : 0.0f;
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 uint32_t v[16];
@@ -416,6 +417,9 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
                     if (e.relu) t = fmaxf(t, 0.0f);
                     f[j] = t;
                 }
+                if (e.head_out)
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) hz += __bfloat162float(__float2bfloat16_rn(f[j])) * e.head_w[col + j];
                 const size_t o = pix * e.ldc + col;
                 if (e.c16) {
                     uint4 out[2];
@@ -441,6 +445,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
                     for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
                 }
             }
+            if (e.head_out) e.head_out[pix] = 1.0f / (1.0f + __expf(-hz));
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(acc_empty(buf));
@@ -646,6 +651,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                 const int y = it.y0 + j, x = it.tx * 128 + r;
                 const size_t pix = ((size_t)it.b * a.H + y) * a.W + x;
                 const uint32_t tbase = tmem + buf * BN + ((uint32_t)(q * 32) << 16);
+                float hz = e.head_out ? e.head_b[0] : 0.0f;
 #pragma unroll 1
                 for (int c0 = 0; c0 < BN; c0 += 16) {
                     uint32_t v[16];
@@ -658,6 +664,10 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                         if (e.relu) t = fmaxf(t, 0.0f);
                         f[jj] = t;
                     }
+                    if (e.head_out)
+#pragma unroll
+                        for (int jj = 0; jj < 16; ++jj)
+                            hz += __bfloat162float(__float2bfloat16_rn(f[jj])) * e.head_w[c0 + jj];
                     const size_t o = pix * e.ldc + c0;
                     if (e.c16) {
                         uint4 out[2];
@@ -683,6 +693,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                         for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
                     }
                 }
+                if (e.head_out) e.head_out[pix] = 1.0f / (1.0f + __expf(-hz));
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(acc_empty(buf));
@@ -898,6 +909,8 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     }
     if (ldw < 9 * cin || ldw % 8 || ((uintptr_t)w % 16)) return fail(st, RN_ERR_INVALID, "tc_conv3x3: weight stride %d", ldw);
     if (epi.atomic || epi.gate) return fail(st, RN_ERR_INVALID, "tc_conv3x3: no atomic or gated epilogue");
+    if (epi.head_out && (N != 32 || !epi.head_w || !epi.head_b || up16))
+        return fail(st, RN_ERR_INVALID, "tc_conv3x3: the fused head needs N 32, its weights and no upsampled copy");
     int bn = (N == 32 || N == 64 || N == 128 || N == 256) ? N : 128;
     if (N % bn || N > 512) return fail(st, RN_ERR_INVALID, "tc_conv3x3 N %d", N);
     while (bn > ctx().tune.conv_bn_max && bn > 32) bn /= 2;

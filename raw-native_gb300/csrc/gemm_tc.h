@@ -21,6 +21,11 @@ struct Epilogue {
     uint32_t* err;
     uint32_t spin;                   // try_wait rounds before a wait gives up (0: the default)
     int withhold;                    // self-test only: the first K block's copies are never issued
+    // convolutions with N = 32 in one slice: the U-Net head fused into the epilogue,
+    // head_out[pixel] = sigmoid(head_b[0] + sum over c of bf16(out[c]) * head_w[c]), c in order
+    const float* head_w;
+    const float* head_b;
+    float* head_out;
 };
 
 // One input of an implicit-GEMM 3x3 convolution: an NHWC BF16 tensor at the output's

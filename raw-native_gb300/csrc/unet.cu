@@ -497,7 +497,9 @@ size_t pixels(const rn_unet* u, int level) { return (size_t)u->B * (u->H >> leve
 // The upsampled copy a layer's output feeds (implicit path), or null.
 bf16* up_target(rn_unet* u, int l) { return u->implicit ? u->UT[l + 1] : nullptr; }
 
-int conv_forward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
+// head_out (implicit path, the last layer): the head's sigmoid output straight from the
+// layer's epilogue; the layer's own activation is then not stored.
+int conv_forward(rn_unet* u, int l, cudaStream_t s, rn_status* st, float* head_out = nullptr) {
     auto& Ly = u->L[l];
     const LayerSpec& sp = kSpec[l];
     const int H = u->H >> Ly.level, W = u->W >> Ly.level;
@@ -521,6 +523,12 @@ int conv_forward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
         e.bias = Ly.b;
         e.relu = 1;
         e.err = ctx().dev_error;
+        if (head_out) {
+            e.c16 = nullptr;
+            e.head_w = u->wh;
+            e.head_b = u->bh;
+            e.head_out = head_out;
+        }
         return tc_conv3x3(src, sp.nsrc, u->B, H, W, Ly.wq, Ly.kpad, Ly.cout, e, up_target(u, l), s, st);
     }
     Im2col a{u->T[sp.s0.tensor], u->TC[sp.s0.tensor], sp.s0.up, nullptr, 0, 0, u->B, H, W, Ly.kpad, Ly.A};
@@ -535,12 +543,14 @@ int conv_forward(rn_unet* u, int l, cudaStream_t s, rn_status* st) {
     return tc_gemm(Ly.A, Ly.kpad, Ly.wq, Ly.kpad, (int)M, Ly.cout, Ly.kpad, 1, e, s, st);
 }
 
-int forward_all(rn_unet* u, cudaStream_t s, rn_status* st) {
+// The forward pass; with head_out (implicit path only) the head's sigmoid output is written
+// by the last layer's epilogue, else the caller runs head_kernel on T[14].
+int forward_all(rn_unet* u, cudaStream_t s, rn_status* st, float* head_out = nullptr) {
     for (int l = 0; l < kLayers; ++l) {
         if (l == 2) pool_kernel<<<grid_for(pixels(u, 1) * 4), 256, 0, s>>>(u->T[2], u->B, u->H, u->W, 32, u->T[T_P0]);
         if (l == 4) pool_kernel<<<grid_for(pixels(u, 2) * 8), 256, 0, s>>>(u->T[4], u->B, u->H >> 1, u->W >> 1, 64, u->T[T_P1]);
         if (l == 6) pool_kernel<<<grid_for(pixels(u, 3) * 16), 256, 0, s>>>(u->T[6], u->B, u->H >> 2, u->W >> 2, 128, u->T[T_P2]);
-        RN_TRY(conv_forward(u, l, s, st));
+        RN_TRY(conv_forward(u, l, s, st, l == kLayers - 1 && u->implicit ? head_out : nullptr));
     }
     return RN_OK;
 }
@@ -774,9 +784,13 @@ int rn_unet_forward(rn_unet* u, const float* input, int batch, float* output, rn
     cudaStream_t s = ctx().stream;
     const size_t M = pixels(u, 0);
     input_kernel<<<grid_for(M), 256, 0, s>>>(input, M, u->TC[T_IN], u->T[T_IN]);
-    RN_TRY(forward_all(u, s, st));
-    head_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(u->T[14], u->wh, u->bh, M, output, nullptr, 0.0f, nullptr,
-                                                           nullptr, nullptr, nullptr);
+    if (u->implicit) {
+        RN_TRY(forward_all(u, s, st, output));         // the head in the last layer's epilogue
+    } else {
+        RN_TRY(forward_all(u, s, st));
+        head_kernel<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(u->T[14], u->wh, u->bh, M, output, nullptr, 0.0f,
+                                                               nullptr, nullptr, nullptr, nullptr);
+    }
     RN_CUDA(cudaGetLastError(), st);
     return ok(st);
 }
@@ -901,9 +915,13 @@ int rn_surrogate_ao(rn_unet* u, const rn_gbuf* g, const float* depth, const rn_a
     depth_mean_kernel<<<1, 32, 0, s>>>(psum, pcnt, kDepthBlocks, mean);
     features_kernel<<<grid_for(npad), 256, 0, s>>>(depth, g->normal, g->mask, a4, w, h, u->W, u->H, mean, radius,
                                                     u->TC[T_IN], u->T[T_IN]);
-    RN_TRY(forward_all(u, s, st));
-    head_kernel<<<(unsigned)((npad + 255) / 256), 256, 0, s>>>(u->T[14], u->wh, u->bh, npad, pr, nullptr, 0.0f, nullptr,
-                                                              nullptr, nullptr, nullptr);
+    if (u->implicit) {
+        RN_TRY(forward_all(u, s, st, pr));             // the head in the last layer's epilogue
+    } else {
+        RN_TRY(forward_all(u, s, st));
+        head_kernel<<<(unsigned)((npad + 255) / 256), 256, 0, s>>>(u->T[14], u->wh, u->bh, npad, pr, nullptr, 0.0f,
+                                                                  nullptr, nullptr, nullptr, nullptr);
+    }
     // 4. the band test, 5. the fallback trace, 6. the composite
     band_kernel<<<dim3(tx, ty), kTile * kTile, 0, s>>>(pr, u->W, a4, g->mask, w, h, k, tf, fbm, counts, fb_list);
     // the fallback pixels' rays, one thread per (pixel, sample): a few tiles' worth of work
