@@ -313,6 +313,7 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *   ssao_tile_h       4 | 8 | 16     SSAO tile 32 x h (the fused FP64 sum follows the tiling)
  *   conv_bn_max       64 | 128 | 256 widest GEMM tile of the surrogate's convolutions
  *   conv_halo         0 | 1          128-pixel row tiles from a ring of one-row boxes (where they fit)
+ *   conv_pair         0 | 1          per-tap convolutions: two 128-pixel tiles per weight box
  *   accel_radius      8|16|32|64     PLOC search radius of accelerators built afterwards
  *   accel_leaf        1 | 2 | 4 | 8  their largest leaf (triangles), 65,536 triangles or more
  *   accel_leaf_small  1 | 2 | 4 | 8  ... below 65,536 triangles

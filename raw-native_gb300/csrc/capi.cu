@@ -122,6 +122,7 @@ const TuneKey kTuneKeys[] = {
     {"ssao_tile_h", "RN_TUNE_SSAO_TILE_H", &Tune::ssao_tile_h, {4, 8, 16}, 3},
     {"conv_bn_max", "RN_TUNE_CONV_BN_MAX", &Tune::conv_bn_max, {64, 128, 256}, 3},
     {"conv_halo", "RN_TUNE_CONV_HALO", &Tune::conv_halo, {0, 1}, 2},
+    {"conv_pair", "RN_TUNE_CONV_PAIR", &Tune::conv_pair, {0, 1}, 2},
     {"accel_radius", "RN_TUNE_ACCEL_RADIUS", &Tune::accel_radius, {8, 16, 32, 64}, 4},
     {"accel_leaf", "RN_TUNE_ACCEL_LEAF", &Tune::accel_leaf, {1, 2, 4, 8}, 4},
     {"accel_leaf_small", "RN_TUNE_ACCEL_LEAF_SMALL", &Tune::accel_leaf_small, {1, 2, 4, 8}, 4},

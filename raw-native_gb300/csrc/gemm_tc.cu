@@ -273,7 +273,10 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
-template <int BN, int CB>
+// kT tiles per work item (1 or 2): with 2, every weight box feeds two 128-pixel tiles (two
+// A boxes per stage, two TMEM accumulators per buffer), halving the weights' L2 traffic;
+// each tile's MMAs are the same in the same order.
+template <int BN, int CB, int kT>
 __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_constant__ CUtensorMap map0,
                                                                   const __grid_constant__ CUtensorMap map1,
                                                                   const __grid_constant__ CUtensorMap mapW,
@@ -282,9 +285,9 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr uint32_t kABytes = kBM * CB * 2, kBBytes = BN * CB * 2;
-    constexpr uint32_t kCols = 2 * BN;                       // two accumulator buffers
-    uint8_t* sA = smem;
-    uint8_t* sB = smem + kSt * kABytes;
+    constexpr uint32_t kCols = 2 * kT * BN;                  // two buffers of kT accumulators
+    uint8_t* sA = smem;                                      // kSt stages of kT A boxes
+    uint8_t* sB = smem + kSt * kT * kABytes;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kSt * kBBytes);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 4);
     __shared__ int s_abort;
@@ -334,14 +337,17 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
                     break;
                 }
                 const int item = (int)blockIdx.x + (int)(kc / nkb) * (int)gridDim.x, kb = (int)(kc % nkb);
-                const int tile = item / a.n_slices, n0 = (item % a.n_slices) * BN;
-                const int tx = tile % a.tiles_x, ty = (tile / a.tiles_x) % a.tiles_y, b = tile / (a.tiles_x * a.tiles_y);
+                const int group = item / a.n_slices, n0 = (item % a.n_slices) * BN;
                 const int tap = kb / per_tap, r = kb % per_tap;
                 const bool second = r >= nb0;
                 const int cb = second ? r - nb0 : r;
-                mbar_expect_tx(full(lane), kABytes + kBBytes);
-                tma_load_4d(smem_u32(sA + lane * kABytes), second ? &map1 : &map0, cb * CB, tx * tw + tap % 3 - 1,
-                            ty * th + tap / 3 - 1, b, full(lane));
+                mbar_expect_tx(full(lane), kT * kABytes + kBBytes);
+                for (int t = 0; t < kT; ++t) {
+                    const int tile = group * kT + t;
+                    const int tx = tile % a.tiles_x, ty = (tile / a.tiles_x) % a.tiles_y, b = tile / (a.tiles_x * a.tiles_y);
+                    tma_load_4d(smem_u32(sA + (lane * kT + t) * kABytes), second ? &map1 : &map0, cb * CB,
+                                tx * tw + tap % 3 - 1, ty * th + tap / 3 - 1, b, full(lane));
+                }
                 tma_load_2d(smem_u32(sB + lane * kBBytes), &mapW, tap * a.cin + (second ? a.C0 : 0) + cb * CB, n0,
                             full(lane));
                 last = kc;
@@ -361,19 +367,23 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
                     break;
                 }
                 tc_fence_after();
-                const uint32_t acc = tmem + buf * BN;
+                const uint32_t acc = tmem + buf * kT * BN;
                 bool ok = true;
                 for (int kb = 0; kb < nkb; ++kb, ++kc) {
                     const int s = kc % kSt;
                     const uint32_t ph = (kc / kSt) & 1u;
                     if (!mbar_wait_or_abort(full(s), ph, abort_flag)) { ok = false; break; }
                     tc_fence_after();
-                    const uint32_t a0 = smem_u32(sA + s * kABytes), b0 = smem_u32(sB + s * kBBytes);
+                    const uint32_t b0 = smem_u32(sB + s * kBBytes);
 #pragma unroll
                     for (int k = 0; k < CB / 16; ++k) {
-                        const uint64_t da = CB == 64 ? smem_desc(a0 + k * 32) : smem_desc64(a0 + k * 32);
                         const uint64_t db = CB == 64 ? smem_desc(b0 + k * 32) : smem_desc64(b0 + k * 32);
-                        tc_mma(acc, da, db, idesc, (kb | k) != 0 ? 1u : 0u);
+#pragma unroll
+                        for (int t = 0; t < kT; ++t) {
+                            const uint32_t a0 = smem_u32(sA + (s * kT + t) * kABytes);
+                            const uint64_t da = CB == 64 ? smem_desc(a0 + k * 32) : smem_desc64(a0 + k * 32);
+                            tc_mma(acc + (uint32_t)(t * BN), da, db, idesc, (kb | k) != 0 ? 1u : 0u);
+                        }
                     }
                     tc_commit(empty(s));
                 }
@@ -398,11 +408,14 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
                 break;
             }
             tc_fence_after();
-            const int tile = item / a.n_slices, n0 = (item % a.n_slices) * BN;
+            const int group = item / a.n_slices, n0 = (item % a.n_slices) * BN;
+#pragma unroll 1
+            for (int t = 0; t < kT; ++t) {
+            const int tile = group * kT + t;
             const int tx = tile % a.tiles_x, ty = (tile / a.tiles_x) % a.tiles_y, b = tile / (a.tiles_x * a.tiles_y);
             const int y = ty * th + (r >> a.tw_log2), x = tx * tw + (r & (tw - 1));
             const size_t pix = ((size_t)b * a.H + y) * a.W + x;
-            const uint32_t tbase = tmem + buf * BN + ((uint32_t)(q * 32) << 16);
+            const uint32_t tbase = tmem + buf * kT * BN + (uint32_t)(t * BN) + ((uint32_t)(q * 32) << 16);
             float hz = e.head_out ? e.head_b[0] : 0.0f;
 #pragma unroll 1
             for (int c0 = 0; c0 < BN; c0 += 16) {
@@ -446,6 +459,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_c
                 }
             }
             if (e.head_out) e.head_out[pix] = 1.0f / (1.0f + __expf(-hz));
+            }
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(acc_empty(buf));
@@ -762,16 +776,16 @@ bool make_map_nhwc(CUtensorMap* m, const void* base, int B, int H, int W, int C,
               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int BN, int CB>
+template <int BN, int CB, int kT>
 int launch_conv(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap& mw, const ConvArgs& a,
                 const Epilogue& e, cudaStream_t s) {
     constexpr int kSt = CB == 32 ? 8 : 4;
-    const size_t smem = 1024 + kSt * (kBM * CB * 2 + BN * CB * 2) + (2 * kSt + 4) * 8 + 16;
+    const size_t smem = 1024 + kSt * (kT * kBM * CB * 2 + BN * CB * 2) + (2 * kSt + 4) * 8 + 16;
     static int per_sm = 0;
     if (!per_sm) {
-        if (cudaFuncSetAttribute(tc_conv_kernel<BN, CB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        if (cudaFuncSetAttribute(tc_conv_kernel<BN, CB, kT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
                 cudaSuccess ||
-            cudaFuncSetAttribute(tc_conv_kernel<BN, CB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+            cudaFuncSetAttribute(tc_conv_kernel<BN, CB, kT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return RN_ERR_CUDA;
         // residency: shared memory (228 KB per SM, 1 KB reserved per CTA), TMEM (512 columns per
@@ -779,10 +793,10 @@ int launch_conv(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap&
         int smem_sm = 0;
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx().device);
         const int by_smem = smem_sm / (int)(smem + 1024);
-        per_sm = std::max(1, std::min(std::min(by_smem, 512 / (2 * BN)), 3));
+        per_sm = std::max(1, std::min(std::min(by_smem, 512 / (2 * kT * BN)), 3));
     }
     const int ctas = std::min(a.items, per_sm * ctx().sm_count);
-    tc_conv_kernel<BN, CB><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
+    tc_conv_kernel<BN, CB, kT><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 
@@ -969,19 +983,38 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     a.tiles_x = W / tw; a.tiles_y = H / th;
     a.cin = cin;
     a.n_slices = N / bn;
-    a.items = a.tiles_x * a.tiles_y * B * a.n_slices;
+    // two tiles per item where the tile count is even, both accumulator pairs fit in TMEM and
+    // the doubled A stages keep as many CTAs per SM as single tiles do
+    const long tiles = (long)a.tiles_x * a.tiles_y * B;
+    auto resident = [&](int kt) {
+        const int st_n = cb == 32 ? 8 : 4;
+        const int smem = 1024 + st_n * (kt * tc::kBM * cb * 2 + bn * cb * 2) + (2 * st_n + 4) * 8 + 16;
+        int smem_sm = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx().device);
+        return std::min(std::min(smem_sm / (smem + 1024), 512 / (2 * kt * bn)), 3);
+    };
+    const bool pair = ctx().tune.conv_pair && tiles % 2 == 0 && bn <= 128 && resident(2) >= std::max(1, resident(1));
+    a.items = (int)(tiles / (pair ? 2 : 1)) * a.n_slices;
     a.up16 = up16;
     int rc;
-#define RN_CONV_CASE(BNV)                                                                             \
+#define RN_CONV_CASE(BNV, KT)                                                                         \
     case BNV:                                                                                         \
-        rc = cb == 64 ? tc::launch_conv<BNV, 64>(m[0], m[1], mw, a, epi, s)                           \
-                      : tc::launch_conv<BNV, 32>(m[0], m[1], mw, a, epi, s);                          \
+        rc = cb == 64 ? tc::launch_conv<BNV, 64, KT>(m[0], m[1], mw, a, epi, s)                       \
+                      : tc::launch_conv<BNV, 32, KT>(m[0], m[1], mw, a, epi, s);                      \
         break;
-    switch (bn) {
-        RN_CONV_CASE(32)
-        RN_CONV_CASE(64)
-        RN_CONV_CASE(256)
-        default: RN_CONV_CASE(128)
+    if (pair) {
+        switch (bn) {
+            RN_CONV_CASE(32, 2)
+            RN_CONV_CASE(64, 2)
+            default: RN_CONV_CASE(128, 2)
+        }
+    } else {
+        switch (bn) {
+            RN_CONV_CASE(32, 1)
+            RN_CONV_CASE(64, 1)
+            RN_CONV_CASE(256, 1)
+            default: RN_CONV_CASE(128, 1)
+        }
     }
 #undef RN_CONV_CASE
     if (rc != RN_OK) return cuda_fail(st, cudaGetLastError(), "tc_conv_kernel");

@@ -49,6 +49,7 @@ struct Tune {
     int ssao_tile_h = 8;        // SSAO tile: 32 x ssao_tile_h pixels, one thread each; 4, 8 or 16
     int conv_bn_max = 256;      // largest GEMM tile width (columns of C per CTA): 64, 128 or 256
     int conv_halo = 1;          // 128-pixel row tiles from a ring of one-row boxes (where they fit)
+    int conv_pair = 1;          // per-tap convolutions: two 128-pixel tiles per weight box
     int accel_radius = 16;      // PLOC search radius of the traversal accelerators built next
     int accel_leaf = 4;         // largest leaf (triangles) of the traversal accelerators built next
     int accel_leaf_small = 4;   // ... of those with fewer than kSmallScene triangles

@@ -169,7 +169,7 @@ def _check(rc: int, st: Status) -> None:
 TUNE_KEYS = {"trace_min_blocks": (2, 3, 4), "batch_min_blocks": (2, 3, 4), "trace_frontier": (0, 1), "trace_frontier_min_spp": (1, 8, 16, 32),
              "trace_frontier_tail": (0, 4, 8, 16),
              "trace_packet": (4, 8, 16),
-             "trace_stack": (48, 96), "ssao_tile_h": (4, 8, 16), "conv_bn_max": (64, 128, 256), "conv_halo": (0, 1),
+             "trace_stack": (48, 96), "ssao_tile_h": (4, 8, 16), "conv_bn_max": (64, 128, 256), "conv_halo": (0, 1), "conv_pair": (0, 1),
              "accel_radius": (8, 16, 32, 64), "accel_leaf": (1, 2, 4, 8), "accel_leaf_small": (1, 2, 4, 8),
              "frame_direct": (0, 1)}
 

@@ -56,14 +56,20 @@ def test_ssao_tile_keeps_every_bit(rn, restore_tune):
 
 
 def test_conv_tile_keeps_every_bit(rn, restore_tune):
+    """The GEMM tile width, the row ring and two tiles per weight box change no output bit,
+    on a network whose levels take every convolution kernel (128-pixel rows at levels 0-1)."""
     import torch
-    net = rn.UNet(2, 64, 64, seed=4, inference=True)
-    x = torch.rand(2, 64, 64, 5, device="cuda", generator=torch.Generator(device="cuda").manual_seed(1))
-    rn.tune_set("conv_bn_max", 256)
-    ref = net.forward(x).clone()
-    for v in rn.TUNE_KEYS["conv_bn_max"]:
-        rn.tune_set("conv_bn_max", v)
-        assert bool((net.forward(x) == ref).all()), v
+    for H, W in ((64, 64), (128, 256)):
+        net = rn.UNet(2, H, W, seed=4, inference=True)
+        x = torch.rand(2, H, W, 5, device="cuda", generator=torch.Generator(device="cuda").manual_seed(1))
+        rn.tune_set("conv_bn_max", 256)
+        rn.tune_set("conv_pair", 0)
+        ref = net.forward(x).clone()
+        for k in ("conv_bn_max", "conv_pair", "conv_halo"):
+            for v in rn.TUNE_KEYS[k]:
+                rn.tune_set(k, v)
+                assert bool((net.forward(x) == ref).all()), (H, W, k, v)
+            rn.tune_set(k, {"conv_bn_max": 256, "conv_pair": 0, "conv_halo": 1}[k])
 
 
 @pytest.mark.parametrize("sky", [False, True])
