@@ -276,12 +276,17 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
 // kT tiles per work item (1 or 2): with 2, every weight box feeds two 128-pixel tiles (two
 // A boxes per stage, two TMEM accumulators per buffer), halving the weights' L2 traffic;
 // each tile's MMAs are the same in the same order.
+// Pipeline stages of tc_conv_kernel: 8 of 32 channels or 4 of 64; pairs of tiles with a
+// 64-column or narrower slice take half as many, so that two CTAs still share an SM.
+template <int BN, int CB, int kT>
+__host__ __device__ constexpr int conv_stages() { return (CB == 32 ? 8 : 4) / (kT == 2 && BN <= 64 ? 2 : 1); }
+
 template <int BN, int CB, int kT>
 __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_kernel(const __grid_constant__ CUtensorMap map0,
                                                                   const __grid_constant__ CUtensorMap map1,
                                                                   const __grid_constant__ CUtensorMap mapW,
                                                                   const ConvArgs a, const Epilogue e) {
-    constexpr int kSt = CB == 32 ? 8 : 4;
+    constexpr int kSt = conv_stages<BN, CB, kT>();
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     constexpr uint32_t kABytes = kBM * CB * 2, kBBytes = BN * CB * 2;
@@ -779,7 +784,7 @@ bool make_map_nhwc(CUtensorMap* m, const void* base, int B, int H, int W, int C,
 template <int BN, int CB, int kT>
 int launch_conv(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap& mw, const ConvArgs& a,
                 const Epilogue& e, cudaStream_t s) {
-    constexpr int kSt = CB == 32 ? 8 : 4;
+    constexpr int kSt = conv_stages<BN, CB, kT>();
     const size_t smem = 1024 + kSt * (kT * kBM * CB * 2 + BN * CB * 2) + (2 * kSt + 4) * 8 + 16;
     static int per_sm = 0;
     if (!per_sm) {
@@ -987,7 +992,7 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     // the doubled A stages keep as many CTAs per SM as single tiles do
     const long tiles = (long)a.tiles_x * a.tiles_y * B;
     auto resident = [&](int kt) {
-        const int st_n = cb == 32 ? 8 : 4;
+        const int st_n = (cb == 32 ? 8 : 4) / (kt == 2 && bn <= 64 ? 2 : 1);
         const int smem = 1024 + st_n * (kt * tc::kBM * cb * 2 + bn * cb * 2) + (2 * st_n + 4) * 8 + 16;
         int smem_sm = 0;
         cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx().device);
