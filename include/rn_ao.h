@@ -372,6 +372,17 @@ int rn_unet_train_step(rn_unet* net, const float* input, const float* target, in
                        rn_status* st);
 /* Parameters / last gradients as FP32 host arrays: per convolution w[cout][9 cin] (tap-major,
  * input channel fastest) then b[cout], then the head's w[32] and b. */
+/* Data-parallel training: a step in two halves with the gradients exchanged between them
+ * (rn_unet_train_step is rn_unet_backward then rn_unet_apply). rn_unet_backward runs the
+ * forward and backward passes on this rank's batch and leaves the gradients in the network
+ * (loss: the batch's mean squared error); rn_unet_grads_flat copies them to (to_flat 1) or
+ * from (0) a flat DEVICE FP32 array of rn_unet_grad_count values, asynchronously on the
+ * library's stream, for an all-reduce between the ranks; rn_unet_apply clips and takes the
+ * Adam step (lr 0: no update) from the gradients the network then holds. */
+int rn_unet_backward(rn_unet* net, const float* input, const float* target, int batch, float* loss, rn_status* st);
+int rn_unet_grad_count(const rn_unet* net, uint64_t* count, rn_status* st);
+int rn_unet_grads_flat(rn_unet* net, float* dev, int to_flat, rn_status* st);
+int rn_unet_apply(rn_unet* net, float lr, rn_status* st);
 int rn_unet_get_params(rn_unet* net, float* host, rn_status* st);
 int rn_unet_set_params(rn_unet* net, const float* host, rn_status* st);
 int rn_unet_get_grads(rn_unet* net, float* host, rn_status* st);

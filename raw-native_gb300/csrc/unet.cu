@@ -479,6 +479,7 @@ struct rn_unet {
     float* gstats;                // device: see clip_kernel
     GradSeg* segs;                // device table of the gradient arrays
     int nsegs = 0;
+    std::vector<GradSeg> hsegs;   // the same table on the host (flat gradient copies)
     float clip_ratio = 0.0f;
     std::vector<void*> allocs;
     size_t param_count = 0;
@@ -754,6 +755,7 @@ int rn_unet_create(int batch, int height, int width, uint64_t seed, uint32_t fla
         segs.push_back({u->gwh, 32});
         segs.push_back({u->gbh, 1});
         u->nsegs = (int)segs.size();
+        u->hsegs = segs;
         if (ualloc(u, (void**)&u->segs, segs.size() * sizeof(GradSeg), st)) return bail(RN_ERR_NO_MEMORY);
         if (cudaMemcpy(u->segs, segs.data(), segs.size() * sizeof(GradSeg), cudaMemcpyHostToDevice) != cudaSuccess)
             return bail(fail(st, RN_ERR_CUDA, "gradient table upload"));
@@ -795,8 +797,9 @@ int rn_unet_forward(rn_unet* u, const float* input, int batch, float* output, rn
     return ok(st);
 }
 
-int rn_unet_train_step(rn_unet* u, const float* input, const float* target, int batch, float lr, float* loss,
-                       rn_status* st) {
+// Forward and backward on one batch: the gradients are left in the network, *loss (if
+// given) receives the batch's mean squared error.
+int rn_unet_backward(rn_unet* u, const float* input, const float* target, int batch, float* loss, rn_status* st) {
     if (!u || !input || !target) return fail(st, RN_ERR_INVALID, "null argument");
     if (u->inference) return fail(st, RN_ERR_INVALID, "network created for inference only");
     RN_TRY(check_shape(u, batch, st));
@@ -822,7 +825,19 @@ int rn_unet_train_step(rn_unet* u, const float* input, const float* target, int 
         if (l == 4) pool_back_kernel<<<grid_for(u->Tn[4]), 256, 0, s>>>(u->dT[T_P1], u->B, u->H >> 1, u->W >> 1, 64, u->dT[4]);
         if (l == 2) pool_back_kernel<<<grid_for(u->Tn[2]), 256, 0, s>>>(u->dT[T_P0], u->B, u->H, u->W, 32, u->dT[2]);
     }
-    // global gradient norm and the clip factor Adam applies
+    RN_CUDA(cudaMemcpyAsync(u->host_loss, u->loss, 4, cudaMemcpyDeviceToHost, s), st);
+    RN_CUDA(cudaStreamSynchronize(s), st);
+    RN_TRY(check_device_error(st, "rn_unet_backward"));
+    if (loss) *loss = *u->host_loss / (float)M;
+    return ok(st);
+}
+
+// The update from the gradients the network holds: their global norm, the adaptive clip
+// factor, and (lr > 0) one Adam step with the BF16 copies refreshed.
+int rn_unet_apply(rn_unet* u, float lr, rn_status* st) {
+    if (!u) return fail(st, RN_ERR_INVALID, "null argument");
+    if (u->inference) return fail(st, RN_ERR_INVALID, "network created for inference only");
+    cudaStream_t s = ctx().stream;
     RN_CUDA(cudaMemsetAsync(u->gstats, 0, 4, s), st);
     grad_sumsq_kernel<<<dim3(64, u->nsegs), 256, 0, s>>>(u->segs, u->gstats);
     clip_kernel<<<1, 1, 0, s>>>(u->gstats, u->clip_ratio);
@@ -832,11 +847,40 @@ int rn_unet_train_step(rn_unet* u, const float* input, const float* target, int 
                          1.0f / (1.0f - std::pow(0.999f, (float)u->step)), u->gstats + 2};
         refresh_weights(u, &a, s);
     }
-    RN_CUDA(cudaMemcpyAsync(u->host_loss, u->loss, 4, cudaMemcpyDeviceToHost, s), st);
     RN_CUDA(cudaMemcpyAsync(u->host_loss + 1, u->gstats + 1, 8, cudaMemcpyDeviceToHost, s), st);
     RN_CUDA(cudaStreamSynchronize(s), st);
-    RN_TRY(check_device_error(st, "rn_unet_train_step"));
-    if (loss) *loss = *u->host_loss / (float)M;
+    RN_TRY(check_device_error(st, "rn_unet_apply"));
+    return ok(st);
+}
+
+int rn_unet_train_step(rn_unet* u, const float* input, const float* target, int batch, float lr, float* loss,
+                       rn_status* st) {
+    RN_TRY(rn_unet_backward(u, input, target, batch, loss, st));
+    return rn_unet_apply(u, lr, st);
+}
+
+// The gradients as one flat FP32 array (the gradient table's order: per layer the weight
+// gradient [kpad][cout] then the bias, then the head's 32 + 1), for an exchange between
+// data-parallel ranks: copied to (to_flat != 0) or from a DEVICE array of
+// rn_unet_grad_count values on the library's stream (asynchronous).
+int rn_unet_grad_count(const rn_unet* u, uint64_t* count, rn_status* st) {
+    if (!u || !count) return fail(st, RN_ERR_INVALID, "null argument");
+    uint64_t n = 0;
+    for (const GradSeg& g : u->hsegs) n += g.n;
+    *count = n;
+    return ok(st);
+}
+int rn_unet_grads_flat(rn_unet* u, float* dev, int to_flat, rn_status* st) {
+    if (!u || !dev) return fail(st, RN_ERR_INVALID, "null argument");
+    if (u->inference) return fail(st, RN_ERR_INVALID, "network created for inference only");
+    cudaStream_t s = ctx().stream;
+    size_t o = 0;
+    for (const GradSeg& g : u->hsegs) {
+        float* seg = const_cast<float*>(g.p);
+        if (to_flat) RN_CUDA(cudaMemcpyAsync(dev + o, seg, (size_t)g.n * 4, cudaMemcpyDeviceToDevice, s), st);
+        else RN_CUDA(cudaMemcpyAsync(seg, dev + o, (size_t)g.n * 4, cudaMemcpyDeviceToDevice, s), st);
+        o += g.n;
+    }
     return ok(st);
 }
 

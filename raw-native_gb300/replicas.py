@@ -7,6 +7,9 @@ deterministic), works on its own share, and the host combines the shares.
     coordinates (the sampler hashes frame x, y), reading the whole G-buffer so SSAO's
     6-pixel neighbourhood crosses band edges; its reconcile covers its rows only;
   - a set of views splits round-robin by view;
+  - surrogate training splits each step's crops by rank (data parallel): every rank runs the
+    backward pass on its crops, the gradients are averaged with one all-reduce of a flat
+    tensor, and every rank takes the same Adam step;
   - the reconcile's parts (FP64 sum of squared errors, covered pixels, max error) combine on
     the host in rank order, and the RMSE and verdict follow as raw::reconcile derives them
     (src/cert/reconcile.cpp:17-20): rmse = (float)sqrt(sum / n), within = rmse <= tolerance.
@@ -97,6 +100,43 @@ def max_over_ranks(x: float, pg=None, device=None) -> float:
     t = torch.tensor([x], dtype=torch.float64, device=device)
     pg.all_reduce(t, op=pg.ReduceOp.MAX)
     return float(t.item())
+
+
+def batch_indices(perm, pos: int, batch: int, rank: int, world: int):
+    """This rank's crops of one data-parallel step: the step takes world x batch consecutive
+    entries of the shared permutation from `pos` and rank r the r-th run of `batch` (every
+    rank holds the same permutation, drawn from the same seed)."""
+    if not (0 <= rank < world):
+        raise ValueError("rank %d of %d" % (rank, world))
+    return perm[pos + rank * batch: pos + (rank + 1) * batch]
+
+
+def allreduce_mean_(t, pg=None):
+    """In place: the mean of `t` over the ranks (a sum all-reduce, then / world)."""
+    if pg is None or not pg.is_initialized() or pg.get_world_size() == 1:
+        return t
+    pg.all_reduce(t)
+    t /= pg.get_world_size()
+    return t
+
+
+def dp_train_step(net, x, y, lr: float, flat, pg=None) -> float:
+    """One data-parallel step of the surrogate network: backward on this rank's batch, the
+    gradients averaged over the ranks (all-reduce of one flat CUDA tensor), then the same
+    clipped Adam update on every rank, so the replicas stay identical. Returns the mean of
+    the ranks' batch losses."""
+    import torch
+    loss = net.backward(x, y)
+    if pg is None or not pg.is_initialized() or pg.get_world_size() == 1:
+        net.apply(lr)
+        return loss
+    net.grads_to(flat)
+    allreduce_mean_(flat, pg)
+    net.grads_from(flat)
+    net.apply(lr)
+    lt = torch.tensor([loss], dtype=torch.float64, device=flat.device)
+    allreduce_mean_(lt, pg)
+    return float(lt.item())
 
 
 def band_frame(g, accel, rank: int, world: int, samples: int, radius: float, ss_samples: int, tolerance: float,

@@ -33,7 +33,8 @@ EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_ac
            "rn_batch_run", "rn_batch_info", "rn_batch_free", "rn_ao_batch", "rn_tc_gemm", "rn_unet_create",
            "rn_unet_free", "rn_unet_param_count", "rn_unet_forward", "rn_unet_train_step", "rn_unet_get_params",
            "rn_unet_set_params", "rn_unet_get_grads", "rn_unet_get_state", "rn_unet_set_state",
-           "rn_unet_set_clip", "rn_unet_last_grad_norm",
+           "rn_unet_set_clip", "rn_unet_last_grad_norm", "rn_unet_backward", "rn_unet_grad_count",
+           "rn_unet_grads_flat", "rn_unet_apply",
            "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3", "rn_surrogate_ao", "rn_gtao", "rn_selftest_wait_budget",
            "rn_render_frame")
 
@@ -152,6 +153,10 @@ def lib() -> C.CDLL:
         L.rn_unet_param_count.argtypes = [vp, C.POINTER(C.c_uint64), st]
         L.rn_unet_forward.argtypes = [vp, vp, C.c_int, vp, st]
         L.rn_unet_train_step.argtypes = [vp, vp, vp, C.c_int, C.c_float, C.POINTER(C.c_float), st]
+        L.rn_unet_backward.argtypes = [vp, vp, vp, C.c_int, C.POINTER(C.c_float), st]
+        L.rn_unet_grad_count.argtypes = [vp, C.POINTER(C.c_uint64), st]
+        L.rn_unet_grads_flat.argtypes = [vp, vp, C.c_int, st]
+        L.rn_unet_apply.argtypes = [vp, C.c_float, st]
         for f in (L.rn_unet_get_params, L.rn_unet_set_params, L.rn_unet_get_grads):
             f.argtypes = [vp, vp, st]
         L.rn_ao_trace_stats.argtypes = [C.POINTER(GBuf), vp, C.c_int, C.c_float, vp, C.c_int, C.c_uint32,
@@ -648,6 +653,44 @@ class UNet:
 
     def get_grads(self):
         return self._io(lib().rn_unet_get_grads)
+
+    # data-parallel training: backward on this rank's batch, the gradients exchanged through a
+    # flat CUDA tensor, then apply (train_step is backward + apply)
+    def backward(self, x, y) -> float:
+        _use_torch_stream()
+        loss = C.c_float()
+        st = Status()
+        _check(lib().rn_unet_backward(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), self.shape[0],
+                                      C.byref(loss), C.byref(st)), st)
+        return loss.value
+
+    @property
+    def grad_count(self) -> int:
+        n = C.c_uint64()
+        st = Status()
+        _check(lib().rn_unet_grad_count(self._h, C.byref(n), C.byref(st)), st)
+        return n.value
+
+    def grads_to(self, flat):
+        """Copy the gradients into `flat` (a contiguous CUDA float32 tensor of grad_count)."""
+        self._flat(flat, 1)
+
+    def grads_from(self, flat):
+        """Replace the gradients by `flat` (as grads_to lays them out)."""
+        self._flat(flat, 0)
+
+    def _flat(self, flat, to_flat: int):
+        import torch
+        if not (flat.is_cuda and flat.dtype == torch.float32 and flat.is_contiguous() and flat.numel() == self.grad_count):
+            raise ValueError("a contiguous CUDA float32 tensor of %d values is needed" % self.grad_count)
+        _use_torch_stream()
+        st = Status()
+        _check(lib().rn_unet_grads_flat(self._h, C.c_void_p(flat.data_ptr()), int(to_flat), C.byref(st)), st)
+
+    def apply(self, lr: float) -> None:
+        _use_torch_stream()
+        st = Status()
+        _check(lib().rn_unet_apply(self._h, float(lr), C.byref(st)), st)
 
     def set_clip(self, ratio: float):
         """Adaptive gradient clipping at `ratio` x the running mean norm (0: off)."""

@@ -16,6 +16,10 @@ traced at the full spp and the traced values replace the prediction there.
 Command line (one GPU):
   python surrogate.py train --out DIR [--seeds 2000 --crops 20000 --steps 20000 ...]
   python surrogate.py eval --ckpt FILE [--seeds 200 ...]
+Data-parallel training on N GPUs of one node (each rank renders the same crops from the same
+seeds, takes its share of every step's N x batch crops, and the ranks average their
+gradients with one NCCL all-reduce per step; rank 0 writes the files):
+  python -m torch.distributed.run --nproc-per-node N --master-addr 127.0.0.1 surrogate.py train --out DIR
 """
 from __future__ import annotations
 
@@ -178,22 +182,33 @@ def lr_at(step: int, total: int, peak: float, warmup: int = 100) -> float:
 
 
 def train(net, data: Dataset, steps: int, batch: int = 64, lr: float = 1e-3, seed: int = 0, log=print,
-          log_every: int = 500, start: int = 0, total: int = 0):
+          log_every: int = 500, start: int = 0, total: int = 0, pg=None):
     """Adam on the MSE for `steps` mini-batches of a seeded shuffle, learning rate from lr_at
-    over `total` steps (0: constant lr); returns the losses."""
+    over `total` steps (0: constant lr); returns the losses. With a process group of several
+    ranks (one GPU each, the same data and seed on every rank), each step takes world x batch
+    crops, rank r its r-th run of `batch`, and the gradients are averaged over the ranks
+    before the shared Adam step (replicas.dp_train_step)."""
     import torch
+    import replicas
+    world = pg.get_world_size() if pg is not None and pg.is_initialized() else 1
+    rank = pg.get_rank() if world > 1 else 0
     gen = torch.Generator(device="cuda").manual_seed(seed)
     n = data.x.shape[0]
     losses = []
     t0 = time.time()
+    flat = torch.empty(net.grad_count, device="cuda") if world > 1 else None
     perm, pos = torch.randperm(n, device="cuda", generator=gen), 0
     for step in range(start, start + steps):
-        if pos + batch > n:
+        if pos + world * batch > n:
             perm, pos = torch.randperm(n, device="cuda", generator=gen), 0
-        idx = perm[pos:pos + batch]
-        pos += batch
+        idx = replicas.batch_indices(perm, pos, batch, rank, world)
+        pos += world * batch
         step_lr = lr_at(step, total, lr) if total else lr
-        losses.append(net.train_step(data.x[idx].contiguous(), data.y[idx].contiguous(), step_lr))
+        if world > 1:
+            losses.append(replicas.dp_train_step(net, data.x[idx].contiguous(), data.y[idx].contiguous(), step_lr,
+                                                 flat, pg))
+        else:
+            losses.append(net.train_step(data.x[idx].contiguous(), data.y[idx].contiguous(), step_lr))
         if log and (step + 1) % log_every == 0:
             gn, sc = net.last_grad_norm()
             log("train: step %d loss %.6f lr %.2e |g| %.3e clip %.3f (%.1f s)" % (
@@ -367,13 +382,23 @@ def main(argv=None):
     e.add_argument("--density", choices=["fixed", "mixed"], default="fixed")
     a = ap.parse_args(argv)
     import torch
+    import replicas
+    rank, world, local = replicas.rank_env()
+    pg = None
+    if world > 1:
+        # data-parallel training under torchrun: one GPU per rank, NCCL for the gradients
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        pg = dist
     rn.init()
     if a.cmd == "train":
         os.makedirs(a.out, exist_ok=True)
-        log_f = open(os.path.join(a.out, "train.log"), "a")
+        log_f = open(os.path.join(a.out, "train.log" if rank == 0 else "train.rank%d.log" % rank), "a")
 
         def log(msg):
-            print(msg, flush=True)
+            if rank == 0:
+                print(msg, flush=True)
             log_f.write(msg + "\n")
             log_f.flush()
         t0 = time.time()
@@ -387,13 +412,17 @@ def main(argv=None):
         t1 = time.time()
         while done < a.steps:
             n = min(a.ckpt_every, a.steps - done)
-            train(net, data, n, a.batch, a.lr, seed=a.init_seed + done, log=log, start=done, total=a.steps)
+            train(net, data, n, a.batch, a.lr, seed=a.init_seed + done, log=log, start=done, total=a.steps, pg=pg)
             done += n
-            save_checkpoint(net, os.path.join(a.out, "surrogate_ckpt.npz"), a.init_seed, data.manifest)
+            if rank == 0:
+                save_checkpoint(net, os.path.join(a.out, "surrogate_ckpt.npz"), a.init_seed, data.manifest)
         train_s = time.time() - t1
         log("train: %d steps in %.1f s (%.2f ms/step)" % (a.steps, train_s, 1e3 * train_s / max(1, a.steps)))
         meta = dict(data=data.manifest, data_digest=data.digest, steps=a.steps, batch=a.batch, lr=a.lr,
-                    schedule="warmup 100, cosine", clip=a.clip, init_seed=a.init_seed, train_seconds=round(train_s, 1))
+                    schedule="warmup 100, cosine", clip=a.clip, init_seed=a.init_seed, train_seconds=round(train_s, 1),
+                    ranks=world)
+        if rank != 0:
+            return 0
         save_weights(net, os.path.join(a.out, "surrogate_bf16.npz"), meta)
         del data
         if a.eval_seeds:

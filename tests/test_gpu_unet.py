@@ -159,3 +159,44 @@ def test_unet_implicit_and_explicit_convolutions_agree(rn):
     inf = rn.UNet(B, H, W, inference=True)
     inf.set_params(imp.get_params())
     assert torch.equal(inf.forward(x), imp.forward(x))
+
+
+def test_unet_step_in_halves_and_data_parallel_average(rn):
+    """rn_unet_backward + rn_unet_apply is rn_unet_train_step (up to the order of the loss and
+    weight-gradient atomics); the flat gradient copy round-trips; and two data-parallel
+    replicas that average their gradients (as the ranks' all-reduce does) take the same step
+    bit for bit, with the gradient of the joint batch."""
+    import torch
+    import replicas
+    B, H, W = 2, 128, 128
+    a = rn.UNet(B, H, W, seed=8)
+    b = rn.UNet(B, H, W, seed=8)
+    x, y = _batch(B, H, W, 21)
+    la = a.train_step(x, y, lr=1e-3)
+    lb = b.backward(x, y)
+    flat = torch.empty(b.grad_count, device="cuda")
+    b.grads_to(flat)
+    b.grads_from(flat)
+    b.apply(1e-3)
+    assert abs(la - lb) <= 1e-6 * abs(la)
+    assert np.allclose(a.get_params(), b.get_params(), rtol=1e-4, atol=1e-6)
+    # two replicas, one batch each, gradients averaged; a batch-4 network on both batches
+    x1, y1 = _batch(B, H, W, 22)
+    r0, r1 = rn.UNet(B, H, W, seed=9), rn.UNet(B, H, W, seed=9)
+    both = rn.UNet(2 * B, H, W, seed=9)
+    r0.backward(x, y)
+    r1.backward(x1, y1)
+    g0, g1 = torch.empty(r0.grad_count, device="cuda"), torch.empty(r1.grad_count, device="cuda")
+    r0.grads_to(g0)
+    r1.grads_to(g1)
+    mean = (g0 + g1) / 2
+    replicas.allreduce_mean_(mean, None)              # one rank: unchanged
+    both.backward(torch.cat([x, x1]).contiguous(), torch.cat([y, y1]).contiguous())
+    gb = torch.empty(both.grad_count, device="cuda")
+    both.grads_to(gb)
+    assert torch.allclose(mean, gb, rtol=1e-3, atol=1e-6 * gb.abs().max().item())
+    r0.grads_from(mean)
+    r1.grads_from(mean.clone())
+    r0.apply(1e-3)
+    r1.apply(1e-3)
+    assert np.array_equal(r0.get_params(), r1.get_params())

@@ -105,3 +105,53 @@ def test_two_gloo_ranks_combine_a_banded_reconcile(oracle):
         assert slowest == 11.0
         assert sum(per_rank) == whole["pixels"]
     assert results[0][4] == results[1][4]              # every rank combined the same sum
+
+
+def test_data_parallel_batches_partition_each_step():
+    import torch
+    perm = torch.randperm(1000, generator=torch.Generator().manual_seed(1))
+    for world in (1, 2, 4):
+        pos = 0
+        for _ in range(3):
+            got = torch.cat([replicas.batch_indices(perm, pos, 16, r, world) for r in range(world)])
+            assert torch.equal(got, perm[pos:pos + 16 * world])
+            pos += 16 * world
+    with pytest.raises(ValueError):
+        replicas.batch_indices(perm, 0, 16, 2, 2)
+
+
+def _dp_rank_main(rank, world, port, q):
+    import sys
+    import torch
+    import torch.distributed as dist
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for p in (root, os.path.join(root, "raw-native_gb300")):
+        sys.path.insert(0, p)
+    import replicas as R
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        # each rank's "gradients" (a stand-in flat tensor); the mean over the ranks reaches all
+        g = torch.arange(6, dtype=torch.float32) * (rank + 1)
+        R.allreduce_mean_(g, dist)
+        q.put((rank, g.tolist()))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_average_gradients():
+    """The data-parallel gradient exchange (one all-reduce of a flat tensor, / world) gives
+    every rank the same mean."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_dp_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    results = dict(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    want = [1.5 * i for i in range(6)]
+    assert results[0] == want and results[1] == want
