@@ -57,7 +57,7 @@ def parse():
                    help="run only this pass `--steps` times after `--warmup` (for ncu), print nothing")
     p.add_argument("--spp", type=int, default=SPP, help="samples per pixel (the benchmark uses 256)")
     p.add_argument("--tris", type=int, default=1000000, help="--profile build: soup triangles")
-    p.add_argument("--workload", default="4k", choices=["4k", "batch", "large", "surrogate"],
+    p.add_argument("--workload", default="4k", choices=["4k", "batch", "large", "surrogate", "hybrid"],
                    help="4k: the benchmark (built-in scene, 3840x2160, 256 spp); batch: 64 orbit views of the "
                         "seeded 744k-triangle scene in one batch; large: 16 4K views of the 7.88M-triangle scene")
     p.add_argument("--views", type=int, default=0, help="batch/large: number of views (default 64 / 16)")
@@ -537,8 +537,79 @@ def run_surrogate(args):
     print(json.dumps(out), flush=True)
 
 
+def run_hybrid(args):
+    """The closest-hit consumers: the hybrid pass (a sun shadow ray and a mirror reflection ray
+    per covered pixel, rn_hybrid) on 3840x2160 views of the built-in scene and of the seeded
+    7.88M-triangle scene, G-buffers resident; and rn_closest on the reflection rays of the
+    first large view (the same rays as a flat list). Timed per frame with CUDA events."""
+    import numpy as np
+    import torch
+    import rn_ao as rn
+    import scene as scenes
+    torch.cuda.set_device(0)
+    rn.init()
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    W, H = 3840, 2160
+    out = {"metric": "hybrid shadow + reflection rays per second", "unit": "G rays/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "scenes": []}
+    with Clocks(0) as clk:
+        for name, sc, views in (("built-in scene (14 triangles)", scenes.build_test_scene(), None),
+                                ("seeded 7.88M-triangle scene", scenes.build_synthetic_scene(5, 10000, 6000), 4)):
+            tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+            acc = rn.LinearAccel(tris)
+            cams = [sc.camera] if views is None else [v[3] for v in scenes.orbit_views(5, views)]
+            ms, rays = [], 0
+            for cam in cams:
+                g = rn.rasterize(tris, nrms, cam, W, H)
+                eye = cam[:3]
+                ms.append(timed(lambda: rn.hybrid(g, acc, eye, sc.to_light)))
+                lit, tri, _ = rn.hybrid(g, acc, eye, sc.to_light)
+                rays += 2 * int(g.mask.sum().item())
+                cov = g.mask != 0
+                shadowed = float((lit[cov] == 0).float().mean().item())
+                reflected = float((tri[cov] >= 0).float().mean().item())
+            row = {"scene": name, "views": len(cams), "ms_per_frame": float(np.mean(ms)),
+                   "grays_per_s": rays / (sum(ms) * 1e-3) / 1e9, "shadowed_fraction_last_view": shadowed,
+                   "reflected_fraction_last_view": reflected}
+            if views is not None:
+                # the last view's reflection rays as a flat list through rn_closest
+                pos, nrm = g.position.reshape(-1, 3), g.normal.reshape(-1, 3)
+                keep = g.mask.reshape(-1) != 0
+                p, n = pos[keep], nrm[keep]
+                d = torch.nn.functional.normalize(p - torch.tensor(eye, device="cuda"), dim=1)
+                n = torch.where(((n * d).sum(1, keepdim=True) > 0), -n, n)
+                r = d - n * (2 * (d * n).sum(1, keepdim=True))
+                rays6 = torch.cat([p + n * 1e-3, r], 1).contiguous()
+                tmax = torch.full((len(rays6),), 1e30, device="cuda")
+                cms = timed(lambda: rn.closest(acc, rays6, tmax))
+                row["closest"] = {"rays": len(rays6), "ms": cms, "grays_per_s": len(rays6) / (cms * 1e-3) / 1e9}
+            out["scenes"].append(row)
+    big = out["scenes"][-1]
+    out.update(value=big["grays_per_s"], ms_per_step=big["ms_per_frame"], clocks=clk.summary(),
+               config={"workload": "hybrid pass, 3840x2160, seeded 7.88M-triangle scene, 4 orbit views",
+                       "inputs": "G-buffers resident in HBM (64 MB per view with its outputs)"})
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "hybrid":
+        run_hybrid(args)
+        return
     if args.workload == "surrogate" and not args.profile:
         run_surrogate(args)
         return

@@ -163,6 +163,23 @@ int rn_ploc_build(const float* tris, uint32_t ntri, int radius, int flags, int32
 int rn_occluded(const rn_accel* accel, const float* rays, const float* t_max, uint32_t nrays,
                 int flags, uint8_t* hit, rn_status* st);
 
+/* raw::rt::closest (src/renderer/rt_bvh.cpp:125-152): for each of nrays rays (origin xyz,
+ * direction xyz: 6 floats) the nearest triangle hit with 1e-4 < t < t_max[i] under the
+ * reference's watertight test, ties to the lowest triangle index; tri[i] its index in the
+ * accelerator's input order (-1: none), t[i] its t (-1: none). Host or device pointers. */
+int rn_closest(const rn_accel* accel, const float* rays, const float* t_max, uint32_t nrays, int flags, int32_t* tri,
+               float* t, rn_status* st);
+
+/* The hybrid pass (raw::gpu_check::hybridGpu, src/renderer/gpu/rt_hybrid.cpp:43-83, with the
+ * per-pixel rule of its CPU reference, src/renderer/gpu/rt_hybrid_parity.cpp:14-82) over a
+ * G-buffer: for each covered pixel, d = normalize(position - eye), the normal turned to face
+ * the viewer, the origin pushed off the surface by 2e-4 (1 + max |position|) along the normal
+ * toward the ray; lit = 1 when nothing is hit toward normalize(to_sun) below 1e30, else 0;
+ * refl_tri / refl_t = the nearest hit of the mirror ray d - 2 (d.n) n (-1 / -1: none).
+ * Uncovered pixels: lit -1, refl_tri -1, refl_t -1. */
+int rn_hybrid(const rn_gbuf* g, const rn_accel* accel, const float* eye, const float* to_sun, int flags, float* lit,
+              int32_t* refl_tri, float* refl_t, rn_status* st);
+
 /* One view of a batch: its G-buffer and outputs, all DEVICE pointers. `sky`/`sun` are used
  * with RN_SKY; `ao_ss` (and `err`, optional) turn on SSAO and the reconcile for the view. */
 typedef struct rn_view {

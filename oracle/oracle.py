@@ -63,6 +63,8 @@ def lib() -> C.CDLL:
         L.rno_occluded.argtypes = [C.c_void_p, _F, C.c_float]
         L.rno_occluded_scan.argtypes = [_F, C.c_int, _F, C.c_float]
         L.rno_occluded_scan_batch.argtypes = [_F, C.c_int, _F, _F, C.c_int, _U8, C.c_int]
+        L.rno_closest_scan_batch.argtypes = [_F, C.c_int, _F, _F, C.c_int, _I32, _F, C.c_int]
+        L.rno_hybrid.argtypes = [C.c_int, C.c_int, _F, _F, _U8, _F, C.c_int, _F, _F, _F, _I32, _F, C.c_int]
         L.rno_trace.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_void_p, _F, C.c_int, C.c_int,
                                 C.c_float, C.c_void_p, C.c_int, _F, C.c_void_p, C.c_void_p,
                                 C.c_int, C.c_int, C.c_int]
@@ -107,6 +109,7 @@ def ref() -> C.CDLL:
         R.ref_reconcile.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_float, _F, _F]
         R.ref_ploc.restype = C.c_int
         R.ref_ploc.argtypes = [_F, C.c_int, C.c_int, _I32, C.POINTER(C.c_uint32)]
+        R.ref_closest.argtypes = [_F, C.c_int, _F, _F, C.c_int, _I32, _F]
         R.ref_motion.restype = C.c_int
         R.ref_motion.argtypes = [C.c_int, C.c_int, _F, _U8, _F, _F, _F]
         R.ref_view_gbuffer.argtypes = [C.c_int, C.c_int, _F, _F, _U8, _F, _F, _F, _F]
@@ -175,6 +178,29 @@ def occluded_scan(tris, rays, tmax, threads=1):
     hit = np.zeros(len(rays), np.uint8)
     lib().rno_occluded_scan_batch(tris, len(tris), rays, _f32(tmax), len(rays), hit, int(threads))
     return hit
+
+
+def closest_scan(tris, rays, tmax, threads=1):
+    """rt::closest by scanning every triangle (ties to the lowest index) for rays (n, 6):
+    (triangle index or -1, t or -1)."""
+    tris = _f32(tris).reshape(-1, 9)
+    rays = _f32(rays).reshape(-1, 6)
+    tri = np.zeros(len(rays), np.int32)
+    t = np.zeros(len(rays), np.float32)
+    lib().rno_closest_scan_batch(tris, len(tris), rays, _f32(tmax), len(rays), tri, t, int(threads))
+    return tri, t
+
+
+def hybrid(pos, nrm, mask, tris, eye, sun, threads=1):
+    """The hybrid pass's per-pixel rule over a G-buffer (scans): (lit, refl_tri, refl_t)."""
+    mask = np.ascontiguousarray(mask, np.uint8)
+    h, w = mask.shape
+    tris = _f32(tris).reshape(-1, 9)
+    lit = np.zeros((h, w), np.float32)
+    tri = np.zeros((h, w), np.int32)
+    t = np.zeros((h, w), np.float32)
+    lib().rno_hybrid(w, h, _f32(pos), _f32(nrm), mask, tris, len(tris), _f32(eye), _f32(sun), lit, tri, t, int(threads))
+    return lit, tri, t
 
 
 def ssao(pos, nrm, mask, samples=SS_SAMPLES, radius=AO_RADIUS, threads=1):

@@ -138,6 +138,25 @@ int ref_ploc(const float* tris9, int n, int radius, int32_t* out9, uint32_t* rou
     return T.root;
 }
 
+// rt::closest (src/renderer/rt_bvh.cpp:125-152) on rt::buildPloc's tree (default radius) for
+// rays (n, 6): the triangle index (-1: none) and t (-1: none).
+void ref_closest(const float* tris9, int ntri, const float* rays6, const float* tmax, int n, int32_t* tri, float* t) {
+    std::vector<Tri> tv((std::size_t)ntri);
+    std::memcpy(tv.data(), tris9, (std::size_t)ntri * 36);
+    const rt::Tree T = rt::buildPloc(tv);
+    for (int i = 0; i < n; ++i) {
+        const float* r = rays6 + (std::size_t)i * 6;
+        Hit h;
+        if (rt::closest(T, tv, Ray{Vec3{r[0], r[1], r[2]}, Vec3{r[3], r[4], r[5]}}, tmax[i], h)) {
+            tri[i] = h.tri;
+            t[i] = h.t;
+        } else {
+            tri[i] = -1;
+            t[i] = -1.0f;
+        }
+    }
+}
+
 }  // extern "C"
 
 

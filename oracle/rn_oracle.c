@@ -810,6 +810,76 @@ RNO_API void rno_occluded_scan_batch(const float* tris9, int ntri, const float* 
     parallel_rows(n, threads, scan_row, &c);
 }
 
+/* ------------------------------------------------------------------ closest hit, hybrid
+ * rt::closest (src/renderer/rt_bvh.cpp:125-152) by its definition: the smallest t of the
+ * watertight test below tMax, ties to the lowest triangle index (the rule its walk keeps:
+ * tt < best, or tt == best with a lower index); here by scanning every triangle in index
+ * order, as the reference's own hybrid check does (src/renderer/gpu/rt_hybrid_parity.cpp:66-71). */
+static int scan_closest(const tri_t* tris, int ntri, v3 o, v3 d, float tmax, float* tout) {
+    int best_tri = -1;
+    float best = tmax;
+    for (int i = 0; i < ntri; ++i) {
+        float t;
+        if (!intersect_tri(o, d, &tris[i], &t)) continue;
+        if (t < best) { best = t; best_tri = i; }      /* in index order a tie keeps the lower index */
+    }
+    *tout = best;
+    return best_tri;
+}
+typedef struct { const tri_t* tris; int ntri; const float* rays; const float* tmax; int32_t* tri; float* t; } closest_ctx;
+static void closest_row(void* p, int i) {
+    const closest_ctx* c = (const closest_ctx*)p;
+    const float* r = c->rays + (size_t)i * 6;
+    float t;
+    const int id = scan_closest(c->tris, c->ntri, v3m(r[0], r[1], r[2]), v3m(r[3], r[4], r[5]), c->tmax[i], &t);
+    c->tri[i] = id;
+    c->t[i] = id >= 0 ? t : -1.0f;
+}
+RNO_API void rno_closest_scan_batch(const float* tris9, int ntri, const float* rays6, const float* tmax, int n,
+                                    int32_t* tri, float* t, int threads) {
+    closest_ctx c = {(const tri_t*)tris9, ntri, rays6, tmax, tri, t};
+    parallel_rows(n, threads, closest_row, &c);
+}
+
+/* The hybrid pass's per-pixel rule (src/renderer/gpu/rt_hybrid_parity.cpp:38-41, 57-80) over a
+ * G-buffer whose normal serves as both the geometric and the shading normal: d =
+ * normalize(pos - eye), the normal turned to face the viewer, origins pushed off by
+ * 2e-4 (1 + max |pos|) along it toward each ray; lit = no hit toward normalize(sun) below 1e30
+ * (1, else 0); the mirror ray d - n (2 d.n) and its nearest hit below 1e30. Uncovered: -1. */
+typedef struct {
+    int w; const float* pos; const float* nrm; const uint8_t* mask; const tri_t* tris; int ntri;
+    v3 eye, sun; float* lit; int32_t* tri; float* t;
+} hybrid_ctx;
+static v3 offset_of(v3 p, v3 n, v3 dir) {
+    const float e = 2e-4f * (1.0f + smax(fabsf(p.x), smax(fabsf(p.y), fabsf(p.z))));
+    return add3(p, mul3(n, dot3(n, dir) > 0.0f ? e : -e));
+}
+static void hybrid_row(void* p, int y) {
+    const hybrid_ctx* c = (const hybrid_ctx*)p;
+    for (int x = 0; x < c->w; ++x) {
+        const size_t i = (size_t)y * c->w + x;
+        if (!c->mask[i]) { c->lit[i] = -1.0f; c->tri[i] = -1; c->t[i] = -1.0f; continue; }
+        const v3 pos = v3m(c->pos[3 * i], c->pos[3 * i + 1], c->pos[3 * i + 2]);
+        v3 n = v3m(c->nrm[3 * i], c->nrm[3 * i + 1], c->nrm[3 * i + 2]);
+        const v3 d = norm3(sub3(pos, c->eye));
+        if (dot3(n, d) > 0.0f) n = mul3(n, -1.0f);
+        const v3 l = norm3(c->sun);
+        c->lit[i] = scan_occluded(c->tris, c->ntri, offset_of(pos, n, l), l, 1e30f) ? 0.0f : 1.0f;
+        const v3 r = sub3(d, mul3(n, 2.0f * dot3(d, n)));
+        float t;
+        const int id = scan_closest(c->tris, c->ntri, offset_of(pos, n, r), r, 1e30f, &t);
+        c->tri[i] = id;
+        c->t[i] = id >= 0 ? t : -1.0f;
+    }
+}
+RNO_API void rno_hybrid(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, const float* tris9,
+                        int ntri, const float* eye3, const float* sun3, float* lit, int32_t* tri, float* t,
+                        int threads) {
+    hybrid_ctx c = {w, pos, nrm, mask, (const tri_t*)tris9, ntri, v3m(eye3[0], eye3[1], eye3[2]),
+                    v3m(sun3[0], sun3[1], sun3[2]), lit, tri, t};
+    parallel_rows(h, threads, hybrid_row, &c);
+}
+
 /* ------------------------------------------------------------------ GTAO (raw::post)
  * The view-space G-buffer (src/renderer/post_gtao.cpp:36-53, in float as there), the screen
  * projection (:55-61), the depth sample between pixel centres (:14-33) and GTAO itself

@@ -1022,4 +1022,60 @@ int rn_occluded(const rn_accel* accel, const float* rays, const float* t_max, ui
     return ok(st);
 }
 
+// raw::rt::closest (src/renderer/rt_bvh.cpp:125-152) on the GPU: for each ray (origin,
+// direction: 6 floats) the nearest hit below t_max, ties to the lowest triangle index.
+int rn_closest(const rn_accel* accel, const float* rays, const float* t_max, uint32_t nrays, int flags, int32_t* tri,
+               float* t, rn_status* st) {
+    if (!accel || (nrays > 0 && (!rays || !t_max || !tri || !t))) return fail(st, RN_ERR_INVALID, "null argument");
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    if (accel->device != c.device) return fail(st, RN_ERR_STATE, "accelerator belongs to device %d", accel->device);
+    if (nrays == 0) return ok(st);
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const float *d_rays, *d_tm;
+    int32_t* d_tri;
+    float* d_t;
+    RN_TRY(stage_in(rays, (size_t)nrays * 6, dev, WS_RAYS, &d_rays, st));
+    RN_TRY(stage_in(t_max, (size_t)nrays, dev, WS_TMAX, &d_tm, st));
+    RN_TRY(stage_out(tri, (size_t)nrays, dev, WS_CLOSEST_TRI, &d_tri, st));
+    RN_TRY(stage_out(t, (size_t)nrays, dev, WS_CLOSEST_T, &d_t, st));
+    if (launch_closest(accel->d_nodes, accel->d_tris, accel->ntri > 0, d_rays, d_tm, nrays, d_tri, d_t, c.dev_error,
+                       c.stream) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "closest_kernel");
+    if (dev) return ok(st);
+    RN_TRY(copy_back(tri, d_tri, nrays, st));
+    RN_TRY(copy_back(t, d_t, nrays, st));
+    RN_TRY(check_device_error(st, "rn_closest"));
+    return ok(st);
+}
+
+// The hybrid pass of raw::gpu_check::hybridGpu (src/renderer/gpu/rt_hybrid.cpp:43-83) over a
+// G-buffer: per covered pixel a sun shadow ray and a mirror reflection ray (closest hit).
+int rn_hybrid(const rn_gbuf* g, const rn_accel* accel, const float* eye, const float* to_sun, int flags, float* lit,
+              int32_t* refl_tri, float* refl_t, rn_status* st) {
+    RN_TRY(ensure_ctx(st));
+    RN_TRY(check_gbuf(g, st));
+    if (!accel || !eye || !to_sun || !lit || !refl_tri || !refl_t) return fail(st, RN_ERR_INVALID, "null argument");
+    Context& c = ctx();
+    if (accel->device != c.device) return fail(st, RN_ERR_STATE, "accelerator belongs to device %d", accel->device);
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const size_t np = (size_t)g->w * g->h;
+    StagedGbuf sg;
+    RN_TRY(stage_gbuf(g, dev, &sg, st));
+    float *d_lit, *d_t;
+    int32_t* d_tri;
+    RN_TRY(stage_out(lit, np, dev, WS_HYB_LIT, &d_lit, st));
+    RN_TRY(stage_out(refl_tri, np, dev, WS_HYB_TRI, &d_tri, st));
+    RN_TRY(stage_out(refl_t, np, dev, WS_HYB_T, &d_t, st));
+    if (launch_hybrid(g->w, g->h, sg.pos, sg.nrm, sg.mask, accel, eye, to_sun, d_lit, d_tri, d_t, c.dev_error,
+                      c.stream) != RN_OK)
+        return cuda_fail(st, cudaGetLastError(), "hybrid_kernel");
+    if (dev) return ok(st);
+    RN_TRY(copy_back(lit, d_lit, np, st));
+    RN_TRY(copy_back(refl_tri, d_tri, np, st));
+    RN_TRY(copy_back(refl_t, d_t, np, st));
+    RN_TRY(check_device_error(st, "rn_hybrid"));
+    return ok(st);
+}
+
 }  // extern "C"

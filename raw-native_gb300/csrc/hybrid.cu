@@ -1,0 +1,179 @@
+// hybrid.cu -- closest-hit consumers of the AO path's BVH: the nearest-hit query of
+// raw::rt::closest (src/renderer/rt_bvh.cpp:125-152) on the 4-wide tree, and the hybrid pass
+// of raw::gpu_check::hybridGpu / cpuReference (src/renderer/gpu/rt_hybrid.cpp:43-83,
+// src/renderer/gpu/rt_hybrid_parity.cpp:14-82): per covered G-buffer pixel a sun shadow ray
+// (any hit) and a mirror reflection ray (closest hit), both from an origin pushed off the
+// surface along the normal.
+//
+// Nearest hit: the smallest t > 1e-4 below t_max of the reference's watertight triangle test
+// over all triangles, ties to the lowest triangle index, exactly as the reference's ordered
+// walk defines it. The 4-wide walk visits children nearest first and culls a box only when
+// its slab entry exceeds the best t found so far (with the same conservative padding and
+// widened exit as the AO walk), so no triangle that could hold the answer is skipped, and
+// the hit test is the AO path's: the answer is the scan's bit for bit.
+#include "rn_internal.h"
+#include "rn_device.cuh"
+#include "trace_device.cuh"
+
+namespace rn {
+namespace {
+
+using namespace trace_dev;
+
+// The nearest hit of ray (o, d) below tmax: returns the triangle index (input order) or -1,
+// and its t.
+__device__ int walk_closest(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, const v3& o,
+                            const v3& d, float tmax, float& t_hit, uint32_t* err) {
+    const Inv iv = make_inv(o, d);
+    const WRay wr = make_wray(o, d);
+    float best = tmax;
+    int best_tri = -1;
+    int32_t stack[kStack];
+    int sp = 0;
+    int32_t cur = 0;
+    for (uint32_t guard = 0; guard < kGuard; ++guard) {
+        const float4* q = reinterpret_cast<const float4*>(nodes + cur);
+        const float4 lx = __ldg(q + 0), hx = __ldg(q + 1), ly = __ldg(q + 2), hy = __ldg(q + 3);
+        const float4 lz = __ldg(q + 4), hz = __ldg(q + 5);
+        const int4 ch = __ldg(reinterpret_cast<const int4*>(q + 6));
+        const int cnt = __ldg(reinterpret_cast<const int*>(q + 7));
+        const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
+        const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
+        const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+        const int32_t CH[4] = {ch.x, ch.y, ch.z, ch.w};
+        // interior children that the ray enters before `best`, nearest first
+        int32_t kid[4];
+        float kt[4];
+        int nk = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float tn;
+            if (k >= cnt || !slab(LX[k], HX[k], LY[k], HY[k], LZ[k], HZ[k], o, iv, best, tn)) continue;
+            const int32_t c = CH[k];
+            if (c < 0) {
+                const uint32_t u = (uint32_t)~c;
+                const uint32_t first = u >> 3, count = (u & 7u) + 1u;
+                for (uint32_t i = 0; i < count; ++i) {
+                    const float4* tq = reinterpret_cast<const float4*>(tris + first + i);
+                    const float4 A = __ldg(tq), B = __ldg(tq + 1), C = __ldg(tq + 2);
+                    float t;
+                    if (!hit_tri(wr, mk(A.x, A.y, A.z), mk(B.x, B.y, B.z), mk(C.x, C.y, C.z), t)) continue;
+                    const int id = __float_as_int(A.w);
+                    if (t < best || (best_tri >= 0 && t == best && id < best_tri)) {
+                        best = t;
+                        best_tri = id;
+                    }
+                }
+                continue;
+            }
+            int j = nk++;
+            while (j > 0 && kt[j - 1] < tn) { kt[j] = kt[j - 1]; kid[j] = kid[j - 1]; --j; }
+            kt[j] = tn;
+            kid[j] = c;
+        }
+        // push the farther children, descend into the nearest
+        for (int j = 0; j + 1 < nk; ++j) {
+            if (sp >= kStack) { atomicOr(err, DEV_STACK_OVERFLOW); t_hit = best; return best_tri; }
+            stack[sp++] = kid[j];
+        }
+        if (nk > 0) { cur = kid[nk - 1]; continue; }
+        // pop the next pushed node: its children meet the best hit found since
+        if (sp == 0) { t_hit = best; return best_tri; }
+        cur = stack[--sp];
+    }
+    atomicOr(err, DEV_GUARD);
+    t_hit = best;
+    return best_tri;
+}
+
+__global__ void closest_kernel(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, int has_geometry,
+                               const float* __restrict__ rays, const float* __restrict__ tmax, uint32_t n,
+                               int32_t* __restrict__ tri, float* __restrict__ t_out, uint32_t* err) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const v3 o = load3(rays + (size_t)i * 6), d = load3(rays + (size_t)i * 6 + 3);
+    float t = tmax[i];
+    const int id = has_geometry ? walk_closest(nodes, tris, o, d, tmax[i], t, err) : -1;
+    tri[i] = id;
+    t_out[i] = id >= 0 ? t : -1.0f;
+}
+
+// rt_hybrid_parity.cpp:38-41: the origin pushed off the surface along the normal, toward the
+// ray's side, by 2e-4 (1 + the position's largest magnitude).
+__device__ __forceinline__ v3 offset_of(const v3& pos, const v3& ng, const v3& dir) {
+    const float e = fmul(2e-4f, fadd(1.0f, fmaxf(fabsf(pos.x), fmaxf(fabsf(pos.y), fabsf(pos.z)))));
+    return add(pos, scale(ng, dot(ng, dir) > 0.0f ? e : -e));
+}
+
+struct HybridArgs {
+    int w, h;
+    const float* pos;
+    const float* nrm;
+    const uint8_t* mask;
+    const Node4* nodes;
+    const LeafTri* tris;
+    int has_geometry;
+    float ex, ey, ez;     // the eye
+    float lx, ly, lz;     // toward the sun (normalized on the device)
+    float* lit;           // 1 lit, 0 in shadow, -1 uncovered
+    int32_t* refl_tri;    // the reflected triangle, -1 none
+    float* refl_t;        // its t, -1 none
+    uint32_t* err;
+};
+
+// rt_hybrid_parity.cpp:57-80 over the library's G-buffer: d = normalize(pos - eye); the
+// normal faces the viewer (the G-buffer's normal serves as both the geometric and the
+// shading normal); lit = no hit toward the sun below 1e30; the reflection r = d - 2 (d.n) n
+// and its nearest hit below 1e30.
+__global__ void hybrid_kernel(const HybridArgs a) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= a.w || y >= a.h) return;
+    const size_t i = (size_t)y * a.w + x;
+    if (!a.mask[i]) {
+        a.lit[i] = -1.0f;
+        a.refl_tri[i] = -1;
+        a.refl_t[i] = -1.0f;
+        return;
+    }
+    const v3 pos = load3(a.pos + 3 * i);
+    v3 n = load3(a.nrm + 3 * i);
+    const v3 d = normalize(sub(pos, mk(a.ex, a.ey, a.ez)));
+    if (dot(n, d) > 0.0f) n = scale(n, -1.0f);
+    const v3 l = normalize(mk(a.lx, a.ly, a.lz));
+    Counts cn;
+    const bool shadow =
+        a.has_geometry && walk<false>(a.nodes, a.tris, offset_of(pos, n, l), l, 1e30f, 1e30f, a.err, cn) != 0;
+    a.lit[i] = shadow ? 0.0f : 1.0f;
+    const v3 r = sub(d, scale(n, fmul(2.0f, dot(d, n))));
+    float t = 1e30f;
+    const int id = a.has_geometry ? walk_closest(a.nodes, a.tris, offset_of(pos, n, r), r, 1e30f, t, a.err) : -1;
+    a.refl_tri[i] = id;
+    a.refl_t[i] = id >= 0 ? t : -1.0f;
+}
+
+}  // namespace
+
+int launch_closest(const Node4* nodes, const LeafTri* tris, int has_geometry, const float* rays, const float* tmax,
+                   uint32_t n, int32_t* tri, float* t, uint32_t* err, cudaStream_t s) {
+    if (n == 0) return RN_OK;
+    closest_kernel<<<(n + 127) / 128, 128, 0, s>>>(nodes, tris, has_geometry, rays, tmax, n, tri, t, err);
+    return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
+}
+
+int launch_hybrid(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, const rn_accel* accel,
+                  const float eye[3], const float to_sun[3], float* lit, int32_t* refl_tri, float* refl_t,
+                  uint32_t* err, cudaStream_t s) {
+    HybridArgs a{};
+    a.w = w; a.h = h;
+    a.pos = pos; a.nrm = nrm; a.mask = mask;
+    a.nodes = accel->d_nodes; a.tris = accel->d_tris;
+    a.has_geometry = accel->ntri > 0;
+    a.ex = eye[0]; a.ey = eye[1]; a.ez = eye[2];
+    a.lx = to_sun[0]; a.ly = to_sun[1]; a.lz = to_sun[2];
+    a.lit = lit; a.refl_tri = refl_tri; a.refl_t = refl_t;
+    a.err = err;
+    hybrid_kernel<<<dim3((w + 127) / 128, h), 128, 0, s>>>(a);
+    return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
+}
+
+}  // namespace rn

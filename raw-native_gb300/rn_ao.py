@@ -29,7 +29,7 @@ ERROR_NAMES = {0: "RN_OK", 1: "RN_ERR_INVALID", 2: "RN_ERR_NO_DEVICE", 3: "RN_ER
 # Every symbol include/rn_ao.h declares.
 EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_accel_build", "rn_accel_free",
            "rn_accel_info", "rn_ao_visibility", "rn_ssao", "rn_reconcile", "rn_ao_frame", "rn_ploc_build",
-           "rn_occluded", "rn_raster_gbuffer", "rn_ao_trace_stats", "rn_reconcile_noalloc", "rn_batch_create",
+           "rn_occluded", "rn_closest", "rn_hybrid", "rn_raster_gbuffer", "rn_ao_trace_stats", "rn_reconcile_noalloc", "rn_batch_create",
            "rn_batch_run", "rn_batch_info", "rn_batch_free", "rn_ao_batch", "rn_tc_gemm", "rn_unet_create",
            "rn_unet_free", "rn_unet_param_count", "rn_unet_forward", "rn_unet_train_step", "rn_unet_get_params",
            "rn_unet_set_params", "rn_unet_get_grads", "rn_unet_get_state", "rn_unet_set_state",
@@ -119,6 +119,8 @@ def lib() -> C.CDLL:
         L.rn_ploc_build.argtypes = [vp, C.c_uint32, C.c_int, C.c_int, vp, C.POINTER(C.c_int32),
                                     C.POINTER(C.c_uint32), st]
         L.rn_occluded.argtypes = [vp, vp, vp, C.c_uint32, C.c_int, vp, st]
+        L.rn_closest.argtypes = [vp, vp, vp, C.c_uint32, C.c_int, vp, vp, st]
+        L.rn_hybrid.argtypes = [C.POINTER(GBuf), vp, vp, vp, C.c_int, vp, vp, vp, st]
         L.rn_raster_gbuffer.argtypes = [vp, vp, C.c_uint32, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, st]
         L.rn_reconcile_noalloc.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, vp, vp,
                                            C.POINTER(ReconcileOut), st]
@@ -782,3 +784,33 @@ def occluded(accel: LinearAccel, rays, t_max):
     _check(lib().rn_occluded(accel.handle, args.ptr(rays, np.float32), args.ptr(t_max, np.float32), n, args.flags,
                              args.ptr(hit, np.uint8), C.byref(st)), st)
     return hit
+
+
+def closest(accel: LinearAccel, rays, t_max):
+    """rt::closest for a list of rays (n, 6): (triangle index int32, -1 for none; t, -1 for
+    none), the nearest hit below t_max with ties to the lowest index."""
+    args = _Args(rays, t_max)
+    n = int(rays.shape[0])
+    tri = args.out(rays, (n,), np.int32)
+    t = args.out(rays, (n,), np.float32)
+    st = Status()
+    _check(lib().rn_closest(accel.handle, args.ptr(rays, np.float32), args.ptr(t_max, np.float32), n, args.flags,
+                            args.ptr(tri, np.int32), args.ptr(t, np.float32), C.byref(st)), st)
+    return tri, t
+
+
+def hybrid(g: GBuffer, accel: LinearAccel, eye, to_sun):
+    """The hybrid pass over a G-buffer: (lit, refl_tri, refl_t), each (h, w); lit 1 / 0 / -1
+    (lit, shadowed, uncovered), refl_tri / refl_t the mirror ray's nearest hit (-1: none)."""
+    args = _Args(g.position, g.normal, g.mask)
+    gb = _gbuf(g, args)
+    h, w = g.shape
+    lit = args.out(g.mask, (h, w), np.float32)
+    tri = args.out(g.mask, (h, w), np.int32)
+    t = args.out(g.mask, (h, w), np.float32)
+    e = (C.c_float * 3)(*[float(v) for v in eye])
+    l = (C.c_float * 3)(*[float(v) for v in to_sun])
+    st = Status()
+    _check(lib().rn_hybrid(C.byref(gb), accel.handle, C.cast(e, C.c_void_p), C.cast(l, C.c_void_p), args.flags,
+                           args.ptr(lit, np.float32), args.ptr(tri, np.int32), args.ptr(t, np.float32), C.byref(st)), st)
+    return lit, tri, t

@@ -1,0 +1,120 @@
+"""Closest-hit consumers of the AO path's accelerator against the oracle, through the C ABI.
+
+rn_closest is rt::closest (src/renderer/rt_bvh.cpp:125-152): the nearest hit below t_max,
+ties to the lowest triangle index. rn_hybrid is the hybrid pass's per-pixel rule
+(src/renderer/gpu/rt_hybrid_parity.cpp:38-41, 57-80) over a G-buffer: a sun shadow ray and
+a mirror reflection ray per covered pixel. Both use the reference's hit test on the same
+operands as the oracle's scans, so the bar is bit-exact: the same triangle, the same t, the
+same lit flag.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 1
+
+
+def _soup(seed, n):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-4, 4, (n, 1, 3))
+    tris = (c + rng.normal(0, 0.6, (n, 3, 3))).reshape(n, 9).astype(np.float32)
+    return tris
+
+
+def _rays(seed, n, spread=6.0):
+    rng = np.random.default_rng(seed)
+    o = rng.uniform(-spread, spread, (n, 3))
+    d = rng.normal(0, 1, (n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([o, d], 1).astype(np.float32)
+
+
+def test_closest_matches_scan_on_a_soup(rn, oracle):
+    tris = _soup(1, 3000)
+    # exact duplicates at higher indices: equal t, the lower index must win
+    tris = np.concatenate([tris, tris[:200]]).astype(np.float32)
+    rays = _rays(2, 20000)
+    rng = np.random.default_rng(3)
+    tmax = np.where(rng.random(len(rays)) < 0.3, rng.uniform(0.5, 4.0, len(rays)), 1e30).astype(np.float32)
+    acc = rn.LinearAccel(tris)
+    tri, t = rn.closest(acc, rays, tmax)
+    rtri, rt = oracle.closest_scan(tris, rays, tmax, threads=THREADS)
+    assert np.array_equal(tri, rtri), int((tri != rtri).sum())
+    assert np.array_equal(t, rt)
+    hits = tri >= 0
+    assert 0.2 < hits.mean() < 1.0 and (tri[hits] < 3000).all()
+    assert (t[hits] < tmax[hits]).all() and (t[~hits] == -1).all()
+    # any hit below t_max is exactly a closest hit below it
+    assert np.array_equal(rn.occluded(acc, rays, tmax) != 0, hits)
+
+
+def test_closest_device_pointers_and_empty_inputs(rn, oracle):
+    import torch
+    tris = _soup(4, 500)
+    rays = _rays(5, 4096)
+    tmax = np.full(len(rays), 1e30, np.float32)
+    acc = rn.LinearAccel(tris)
+    tri, t = rn.closest(acc, rays, tmax)
+    dtri, dt = rn.closest(acc, torch.from_numpy(rays).cuda(), torch.from_numpy(tmax).cuda())
+    assert np.array_equal(dtri.cpu().numpy(), tri) and np.array_equal(dt.cpu().numpy(), t)
+    none = rn.closest(acc, rays[:0], tmax[:0])
+    assert none[0].size == 0
+    empty = rn.LinearAccel(np.zeros((0, 9), np.float32))
+    etri, et = rn.closest(empty, rays, tmax)
+    assert (etri == -1).all() and (et == -1).all()
+
+
+def _hybrid_case(oracle, sc, w, h):
+    _, pos, nrm, mask = oracle.rasterize(sc.tris, sc.normals, sc.camera, w, h)
+    return pos, nrm, mask, np.asarray(sc.camera[:3], np.float32), sc.to_light
+
+
+def _check_hybrid(rn, oracle, tris, pos, nrm, mask, eye, sun):
+    acc = rn.LinearAccel(tris)
+    lit, tri, t = rn.hybrid(rn.GBuffer(pos, nrm, mask), acc, eye, sun)
+    rlit, rtri, rt = oracle.hybrid(pos, nrm, mask, tris, eye, sun, threads=THREADS)
+    assert np.array_equal(lit, rlit), int((lit != rlit).sum())
+    assert np.array_equal(tri, rtri), int((tri != rtri).sum())
+    assert np.array_equal(t, rt)
+    cov = mask != 0
+    assert (lit[~cov] == -1).all() and (tri[~cov] == -1).all()
+    return lit, tri, cov
+
+
+def test_hybrid_test_scene_bit_exact(rn, oracle):
+    import scene as scenes
+    sc = scenes.build_test_scene()
+    pos, nrm, mask, eye, sun = _hybrid_case(oracle, sc, 160, 128)
+    lit, tri, cov = _check_hybrid(rn, oracle, sc.tris, pos, nrm, mask, eye, sun)
+    # the box shadows part of the plane, and the plane reflects the box
+    assert 0.0 < (lit[cov] == 0).mean() < 0.5 and (tri[cov] >= 2).any()
+
+
+def test_hybrid_synthetic_scene_bit_exact(rn, oracle):
+    """A seeded city of boxes and spheres on a 20 x 20 ground grid (about 2,200 triangles),
+    320 x 240 from its default view."""
+    import scene as scenes
+    sc = scenes.build_synthetic_scene(11, 40, 3, grid=20, subdiv=2)
+    pos, nrm, mask, eye, sun = _hybrid_case(oracle, sc, 320, 240)
+    lit, tri, cov = _check_hybrid(rn, oracle, sc.tris, pos, nrm, mask, eye, sun)
+    assert 0.0 < (lit[cov] == 0).mean() < 0.9 and 0.0 < (tri[cov] >= 0).mean()
+
+
+def test_hybrid_device_pointers_equal_host_path(rn, oracle):
+    import torch
+    import scene as scenes
+    sc = scenes.build_test_scene()
+    pos, nrm, mask, eye, sun = _hybrid_case(oracle, sc, 96, 64)
+    acc = rn.LinearAccel(sc.tris)
+    host = rn.hybrid(rn.GBuffer(pos, nrm, mask), acc, eye, sun)
+    g = rn.GBuffer(*(torch.from_numpy(a).cuda() for a in (pos, nrm, mask)))
+    dev = rn.hybrid(g, acc, eye, sun)
+    for a, b in zip(host, dev):
+        assert np.array_equal(a, b.cpu().numpy())
+    empty = rn.LinearAccel(np.zeros((0, 9), np.float32))
+    lit, tri, _ = rn.hybrid(rn.GBuffer(pos, nrm, mask), empty, eye, sun)
+    cov = mask != 0
+    assert (lit[cov] == 1).all() and (tri == -1).all()

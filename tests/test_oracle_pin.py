@@ -104,6 +104,46 @@ def test_bvh_equals_scan_on_random_rays(oracle):
         L.rno_accel_free(h)
 
 
+def test_closest_scan_semantics(oracle):
+    """The closest scan: a hit exactly where the any-hit scan finds one, the smallest t of the
+    hit test below t_max, and duplicates resolved to the lower index."""
+    tris = oracle.soup(800, 3)
+    tris = np.concatenate([tris, tris[:100]]).astype(np.float32)
+    rng = np.random.default_rng(9)
+    o = rng.uniform(-14, 14, (3000, 3))
+    d = rng.normal(size=(3000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    tmax = np.where(rng.random(3000) < 0.5, 3.0, 1e30).astype(np.float32)
+    tri, t = oracle.closest_scan(tris, rays, tmax, threads=4)
+    hit = oracle.occluded_scan(tris, rays, tmax, threads=4)
+    assert np.array_equal(tri >= 0, hit != 0) and 0 < hit.mean() < 1
+    assert (tri < 800).all() and (t[tri >= 0] < tmax[tri >= 0]).all()
+    import ctypes as C
+    tt = C.c_float()
+    for i in np.flatnonzero(tri >= 0)[:200]:
+        assert oracle.lib().rno_intersect(rays[i].copy(), tris[tri[i]].copy(), C.byref(tt)) and tt.value == t[i]
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libref_ao.so")),
+                    reason="the reference's own sources are not compiled on this host")
+def test_closest_scan_equals_reference_closest(oracle):
+    """rt::closest of the reference (its PLOC tree, its ordered walk) against the scan."""
+    tris = oracle.soup(2000, 17)
+    tris = np.concatenate([tris, tris[:150]]).astype(np.float32)
+    rng = np.random.default_rng(4)
+    o = rng.uniform(-14, 14, (4000, 3))
+    d = rng.normal(size=(4000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.concatenate([o, d], 1).astype(np.float32)
+    tmax = np.where(rng.random(4000) < 0.4, rng.uniform(0.5, 5, 4000), 1e30).astype(np.float32)
+    tri, t = oracle.closest_scan(tris, rays, tmax, threads=4)
+    rtri = np.zeros(4000, np.int32)
+    rt = np.zeros(4000, np.float32)
+    oracle.ref().ref_closest(tris, len(tris), rays, tmax, 4000, rtri, rt)
+    assert np.array_equal(tri, rtri) and np.array_equal(t, rt)
+
+
 def test_thread_count_invariance(oracle):
     # tests/test_verify.cpp:40-43: output identical for any thread count
     a = oracle.render_default(128, 96, threads=1)
