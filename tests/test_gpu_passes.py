@@ -1,6 +1,6 @@
 """GPU parity of the three AO passes against the oracle, through the C ABI.
 
-Bar (spec parity rules): the sampler's hash sequence, mask and pixel counts
+Bar (the parity rules of the path): the sampler's hash sequence, mask and pixel counts
 bit-exact; with the host-libm calibration (the default) RT AO, sky, sun and SSAO are
 bit-identical to the oracle, the error map too, RMSE within 1e-6 and the verdict equal.
 Where this host's oracle reproduces the reference's x86-64 goldens, the GPU's outputs must
