@@ -125,8 +125,12 @@ struct HybridArgs {
 // normal faces the viewer (the G-buffer's normal serves as both the geometric and the
 // shading normal); lit = no hit toward the sun below 1e30; the reflection r = d - 2 (d.n) n
 // and its nearest hit below 1e30.
+// A block covers 16 x 8 pixels, each warp an 8 x 4 packet: neighbouring rays share more of
+// their walks than a 32-pixel row does.
 __global__ void hybrid_kernel(const HybridArgs a) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
+    const int y = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
     if (x >= a.w || y >= a.h) return;
     const size_t i = (size_t)y * a.w + x;
     if (!a.mask[i]) {
@@ -172,7 +176,7 @@ int launch_hybrid(int w, int h, const float* pos, const float* nrm, const uint8_
     a.lx = to_sun[0]; a.ly = to_sun[1]; a.lz = to_sun[2];
     a.lit = lit; a.refl_tri = refl_tri; a.refl_t = refl_t;
     a.err = err;
-    hybrid_kernel<<<dim3((w + 127) / 128, h), 128, 0, s>>>(a);
+    hybrid_kernel<<<dim3((w + 15) / 16, (h + 7) / 8), 128, 0, s>>>(a);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 
