@@ -70,6 +70,29 @@ def build_test_scene(camera=DEFAULT_CAMERA) -> Scene:
 #   build_synthetic_scene(seed, 200, 50)      146,400 triangles (surrogate training scenes)
 #   build_synthetic_scene(seed, 10000, 6000)  ~7,880,000 triangles (4K head-to-head)
 
+def _soup_hash(x: int) -> int:
+    x ^= x >> 16
+    x = (x * 0x7FEB352D) & 0xFFFFFFFF
+    x ^= x >> 15
+    x = (x * 0x846CA68B) & 0xFFFFFFFF
+    return x ^ (x >> 16)
+
+
+def soup(count: int, seed: int) -> np.ndarray:
+    """raw::rt::soup (src/renderer/rt_scenes.cpp:52-63), the reference's PLOC check input:
+    `count` triangles, each a centre uniform in [-12, 12)^3 plus three corners within +-1 of
+    it, all drawn from one integer-hash sequence. (count, 9) float32."""
+    r = (seed * 2654435761 + 1) & 0xFFFFFFFF
+    u = np.empty(12 * count, np.float64)
+    for k in range(12 * count):
+        r = _soup_hash((r + 0x9E3779B9) & 0xFFFFFFFF)
+        u[k] = r >> 8
+    v = (u / 16777216.0).astype(np.float32).reshape(count, 4, 3)   # exact: 24-bit integers / 2^24
+    c = np.float32(24.0) * v[:, 0] - np.float32(12.0)
+    corners = c[:, None, :] + (np.float32(2.0) * v[:, 1:] - np.float32(1.0))
+    return np.ascontiguousarray(corners.reshape(count, 9), np.float32)
+
+
 def _icosphere(subdiv: int):
     """Unit icosphere: 20 * 4^subdiv triangles (vertices, faces), outward winding."""
     t = (1.0 + 5.0 ** 0.5) / 2.0

@@ -185,6 +185,12 @@ def test_product_scene_equals_reference_scene(oracle):
     assert np.array_equal(sc.tris, tris) and np.array_equal(sc.normals, nrm) and np.array_equal(sc.light, light)
 
 
+def test_product_soup_equals_oracle_soup(oracle):
+    import scene
+    for n, seed in ((20000, 7), (513, 11)):
+        assert np.array_equal(scene.soup(n, seed), oracle.soup(n, seed))
+
+
 def test_synthetic_scenes_are_seeded_and_sized():
     import scene as scenes
     a = scenes.build_synthetic_scene(1, 2000, 500)
