@@ -62,6 +62,9 @@ def test_no_device_fails_loudly(lib):
     g = rn_ao.GBuffer(np.zeros((2, 2, 3), np.float32), np.zeros((2, 2, 3), np.float32), m)
     with pytest.raises(rn_ao.RnError):
         rn_ao.compute_ssao(g, 24, 2.0)
+    st = rn_ao.Status()
+    eye = (C.c_float * 3)(0, 0, 0)
+    assert lib.rn_hybrid(None, None, eye, eye, 0, None, None, None, C.byref(st)) == 2
 
 
 def test_argument_errors_before_any_device_work(lib):
@@ -72,6 +75,7 @@ def test_argument_errors_before_any_device_work(lib):
     assert b"null" in st.message
     assert lib.rn_accel_build(None, 5, 0, C.byref(C.c_void_p()), C.byref(st)) == 1
     assert lib.rn_ploc_build(None, 3, 16, 0, None, None, None, C.byref(st)) == 1
+    assert lib.rn_closest(None, None, None, 4, 0, None, None, C.byref(st)) == 1
 
 
 def test_host_and_device_arrays_do_not_mix():
