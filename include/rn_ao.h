@@ -335,6 +335,7 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *   accel_leaf        1 | 2 | 4 | 8  their largest leaf (triangles), 65,536 triangles or more
  *   accel_leaf_small  1 | 2 | 4 | 8  ... below 65,536 triangles
  *   frame_direct      0 | 1          rn_ao_frame on pinned, mapped host buffers without copies
+ *   hybrid_min_blocks 5 | 6 | 8      resident rn_hybrid blocks per SM (register budget)
  * Process-wide; RN_TUNE_<KEY> environment variables apply before the first call.
  * rn_tune_load reads "key = value" lines ('#' comments), all or nothing. */
 int rn_tune_set(const char* key, int value, rn_status* st);

@@ -127,7 +127,10 @@ struct HybridArgs {
 // and its nearest hit below 1e30.
 // A block covers 16 x 8 pixels, each warp an 8 x 4 packet: neighbouring rays share more of
 // their walks than a 32-pixel row does.
-__global__ void hybrid_kernel(const HybridArgs a) {
+// kMinBlocks: resident 128-thread blocks per SM asked of the register allocator (the
+// walk's latency is hidden by more warps where the cap costs no spills).
+template <int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) hybrid_kernel(const HybridArgs a) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int x = blockIdx.x * 16 + (warp & 1) * 8 + (lane & 7);
     const int y = blockIdx.y * 8 + (warp >> 1) * 4 + (lane >> 3);
@@ -176,7 +179,12 @@ int launch_hybrid(int w, int h, const float* pos, const float* nrm, const uint8_
     a.lx = to_sun[0]; a.ly = to_sun[1]; a.lz = to_sun[2];
     a.lit = lit; a.refl_tri = refl_tri; a.refl_t = refl_t;
     a.err = err;
-    hybrid_kernel<<<dim3((w + 15) / 16, (h + 7) / 8), 128, 0, s>>>(a);
+    const dim3 grid((w + 15) / 16, (h + 7) / 8);
+    switch (ctx().tune.hybrid_min_blocks) {
+        case 5: hybrid_kernel<5><<<grid, 128, 0, s>>>(a); break;
+        case 8: hybrid_kernel<8><<<grid, 128, 0, s>>>(a); break;
+        default: hybrid_kernel<6><<<grid, 128, 0, s>>>(a); break;
+    }
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 

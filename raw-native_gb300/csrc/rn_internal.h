@@ -55,6 +55,7 @@ struct Tune {
     int accel_leaf = 4;         // largest leaf (triangles) of the traversal accelerators built next
     int accel_leaf_small = 4;   // ... of those with fewer than kSmallScene triangles
     int frame_direct = 1;       // host-buffer frames: the passes read and write mapped host memory
+    int hybrid_min_blocks = 6;  // resident 128-thread hybrid-pass blocks per SM: 5, 6 or 8
 };
 constexpr uint32_t kSmallScene = 1u << 16;
 

@@ -118,3 +118,22 @@ def test_hybrid_device_pointers_equal_host_path(rn, oracle):
     lit, tri, _ = rn.hybrid(rn.GBuffer(pos, nrm, mask), empty, eye, sun)
     cov = mask != 0
     assert (lit[cov] == 1).all() and (tri == -1).all()
+
+
+def test_hybrid_residency_keys_change_no_result(rn, oracle):
+    import scene as scenes
+    sc = scenes.build_synthetic_scene(12, 30, 2, grid=16, subdiv=2)
+    pos, nrm, mask, eye, sun = _hybrid_case(oracle, sc, 128, 96)
+    acc = rn.LinearAccel(sc.tris)
+    g = rn.GBuffer(pos, nrm, mask)
+    saved = rn.tune_get("hybrid_min_blocks")
+    try:
+        outs = []
+        for v in rn.TUNE_KEYS["hybrid_min_blocks"]:
+            rn.tune_set("hybrid_min_blocks", v)
+            outs.append(rn.hybrid(g, acc, eye, sun))
+    finally:
+        rn.tune_set("hybrid_min_blocks", saved)
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            assert np.array_equal(a, b)
