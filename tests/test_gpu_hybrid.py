@@ -137,3 +137,30 @@ def test_hybrid_residency_keys_change_no_result(rn, oracle):
     for o in outs[1:]:
         for a, b in zip(outs[0], o):
             assert np.array_equal(a, b)
+
+
+def test_closest_ties_on_shared_edges_and_axis_rays(rn, oracle):
+    """Rays straight down through the vertices, edges and cells of a triangulated ground grid:
+    axis-aligned directions (zero components, infinite inverses) and hits on edges that 2-6
+    triangles share at the same t, which the lowest index must win; t_max at or below the hit
+    distance leaves no hit."""
+    import scene as scenes
+    g = scenes.build_synthetic_scene(0, 0, 0, grid=8, half=4.0).tris     # 128 ground triangles, y = 0
+    xs = np.linspace(-4.0, 4.0, 17, dtype=np.float32)                    # vertices and edge midpoints
+    ox, oz = np.meshgrid(xs, xs, indexing="ij")
+    n = ox.size
+    down = np.stack([ox.ravel(), np.full(n, 3.0, np.float32), oz.ravel(), np.zeros(n), -np.ones(n), np.zeros(n)], 1)
+    slant = down.copy()
+    slant[:, 3:] = np.array([0.6, -0.8, 0.0], np.float32)                # exact unit vector, y component -0.8
+    slant[:, 0] -= np.float32(2.25)                                      # 3 / 0.8 * 0.6: lands on the same points
+    rays = np.concatenate([down, slant]).astype(np.float32)
+    for tmax in (np.full(len(rays), 1e30, np.float32), np.full(len(rays), 3.0, np.float32),
+                 np.zeros(len(rays), np.float32)):
+        acc = rn.LinearAccel(g)
+        tri, t = rn.closest(acc, rays, tmax)
+        rtri, rt = oracle.closest_scan(g, rays, tmax, threads=THREADS)
+        assert np.array_equal(tri, rtri), int((tri != rtri).sum())
+        assert np.array_equal(t, rt)
+    tri, t = rn.closest(rn.LinearAccel(g), rays, np.full(len(rays), 1e30, np.float32))
+    inside = (np.abs(rays[:, 0]) < 4) & (np.abs(rays[:, 2]) < 4)
+    assert (tri[:n][inside[:n]] >= 0).all() and (t[:n][inside[:n]] == 3.0).all()
