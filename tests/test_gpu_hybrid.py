@@ -164,3 +164,60 @@ def test_closest_ties_on_shared_edges_and_axis_rays(rn, oracle):
     tri, t = rn.closest(rn.LinearAccel(g), rays, np.full(len(rays), 1e30, np.float32))
     inside = (np.abs(rays[:, 0]) < 4) & (np.abs(rays[:, 2]) < 4)
     assert (tri[:n][inside[:n]] >= 0).all() and (t[:n][inside[:n]] == 3.0).all()
+
+
+class _XorShift:
+    """tests/test_bvh.cpp's generator: xorshift64 (13, 7, 17), 53-bit doubles rounded to float."""
+
+    def __init__(self, seed):
+        self.s = seed
+
+    def next(self):
+        s = self.s
+        s ^= (s << 13) & 0xFFFFFFFFFFFFFFFF
+        s ^= s >> 7
+        s ^= (s << 17) & 0xFFFFFFFFFFFFFFFF
+        self.s = s
+        return np.float32((s >> 11) * (1.0 / 9007199254740992.0))
+
+    def vec(self, lo, hi):
+        lo, span = np.float32(lo), np.float32(hi) - np.float32(lo)
+        return np.array([lo + span * self.next() for _ in range(3)], np.float32)
+
+
+def _seeded_rays(count, seed):
+    """tests/test_bvh.cpp:31-35: origins in [-12, 12)^3, normalized directions from [-1, 1)^3,
+    t_max 4 u on every third ray and 1e30 on the rest."""
+    r = _XorShift(seed)
+    rays = np.empty((count, 6), np.float32)
+    tmax = np.empty(count, np.float32)
+    for k in range(count):
+        o = r.vec(-12.0, 12.0)
+        d = r.vec(-1.0, 1.0)
+        l = np.sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2], dtype=np.float32)
+        d = d * (np.float32(1.0) / l) if l > 0 else d
+        rays[k, :3], rays[k, 3:] = o, d
+        tmax[k] = np.float32(1e30) if k % 3 else np.float32(4.0) * r.next()
+    return rays, tmax
+
+
+def test_closest_and_occluded_equal_the_scan_on_seeded_rays(rn, oracle):
+    """The reference's BVH check (tests/test_bvh.cpp): 10,000 seeded rays through a
+    20,000-triangle soup and 100,000 through the built-in scene; the nearest triangle, its t
+    and the occlusion answer all equal the scan's."""
+    import scene as scenes
+    r = _XorShift(7)
+    soup = np.empty((20000, 9), np.float32)
+    for i in range(20000):
+        c = r.vec(-10.0, 10.0)
+        soup[i] = np.concatenate([c + r.vec(-0.6, 0.6), c + r.vec(-0.6, 0.6), c + r.vec(-0.6, 0.6)])
+    for tris, count, seed in ((soup, 10000, 11), (scenes.build_test_scene().tris, 100000, 13)):
+        rays, tmax = _seeded_rays(count, seed)
+        acc = rn.LinearAccel(tris)
+        tri, t = rn.closest(acc, rays, tmax)
+        rtri, rt = oracle.closest_scan(tris, rays, tmax, threads=THREADS)
+        assert np.array_equal(tri, rtri), int((tri != rtri).sum())
+        assert np.array_equal(t, rt)
+        occ = rn.occluded(acc, rays, tmax)
+        assert np.array_equal(occ, oracle.occluded_scan(tris, rays, tmax, threads=THREADS))
+        assert 0.01 < (tri >= 0).mean() < 0.95
