@@ -84,11 +84,12 @@ int build_trig_correction(Context& c, rn_status* st) {
             }
         });
     for (auto& th : pool) th.join();
-    float2* d_host = nullptr;
-    uint32_t* d_bad = nullptr;
+    ScopedDev host_buf, bad_buf;
     RN_CUDA(cudaMalloc((void**)&c.trig_corr, kAngles), st);
-    RN_CUDA(cudaMalloc((void**)&d_host, (size_t)kAngles * sizeof(float2)), st);
-    RN_CUDA(cudaMalloc((void**)&d_bad, 4), st);
+    RN_CUDA(cudaMalloc(&host_buf.p, (size_t)kAngles * sizeof(float2)), st);
+    RN_CUDA(cudaMalloc(&bad_buf.p, 4), st);
+    float2* d_host = (float2*)host_buf.p;
+    uint32_t* d_bad = (uint32_t*)bad_buf.p;
     RN_CUDA(cudaMemsetAsync(d_bad, 0, 4, c.stream), st);
     RN_CUDA(cudaMemcpyAsync(d_host, host.data(), (size_t)kAngles * sizeof(float2), cudaMemcpyHostToDevice, c.stream), st);
     trig_corr_kernel<<<kAngles / 256, 256, 0, c.stream>>>(d_host, c.trig_corr, d_bad);
@@ -96,8 +97,6 @@ int build_trig_correction(Context& c, rn_status* st) {
     uint32_t bad = 0;
     RN_CUDA(cudaMemcpyAsync(&bad, d_bad, 4, cudaMemcpyDeviceToHost, c.stream), st);
     RN_CUDA(cudaStreamSynchronize(c.stream), st);
-    cudaFree(d_host);
-    cudaFree(d_bad);
     if (bad) return fail(st, RN_ERR_STATE, "sampler calibration: %u angles differ by more than 7 ulp", bad);
     return RN_OK;
 }

@@ -1072,10 +1072,11 @@ extern "C" int rn_tc_conv3x3(const void* src0, int c0, const void* src1, int c1,
 extern "C" int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st) {
     RN_TRY(ensure_ctx(st));
     if (spin_limit == 0 || spin_limit > (1u << 24)) return fail(st, RN_ERR_INVALID, "spin limit %u", spin_limit);
-    void *p = nullptr, *q = nullptr, *c = nullptr;
-    RN_CUDA(cudaMalloc(&p, 128 * 64 * 2), st);
-    RN_CUDA(cudaMalloc(&q, 32 * 64 * 2), st);
-    RN_CUDA(cudaMalloc(&c, 128 * 32 * 4), st);
+    ScopedDev pb, qb, cb;
+    RN_CUDA(cudaMalloc(&pb.p, 128 * 64 * 2), st);
+    RN_CUDA(cudaMalloc(&qb.p, 32 * 64 * 2), st);
+    RN_CUDA(cudaMalloc(&cb.p, 128 * 32 * 4), st);
+    void *p = pb.p, *q = qb.p, *c = cb.p;
     cudaMemsetAsync(p, 0, 128 * 64 * 2, ctx().stream);
     cudaMemsetAsync(q, 0, 32 * 64 * 2, ctx().stream);
     tc::Epilogue e{};
@@ -1087,8 +1088,5 @@ extern "C" int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st) {
     int rc = tc_gemm((const __nv_bfloat16*)p, 64, (const __nv_bfloat16*)q, 64, 128, 32, 64, 1, e, ctx().stream, st);
     if (rc == RN_OK) rc = check_device_error(st, "rn_selftest_wait_budget");
     cudaStreamSynchronize(ctx().stream);
-    cudaFree(p);
-    cudaFree(q);
-    cudaFree(c);
     return rc;
 }

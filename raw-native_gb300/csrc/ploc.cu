@@ -702,6 +702,12 @@ int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, int lea
     const size_t o_ctr = take(8 * 4);
     char* mem = nullptr;
     RN_CUDA(cudaMallocAsync((void**)&mem, off, s), st);
+    // the scratch goes back to the stream's pool on every return path
+    struct ScratchGuard {
+        char* p;
+        cudaStream_t s;
+        ~ScratchGuard() { cudaFreeAsync(p, s); }
+    } guard{mem, s};
     int32_t* parent = (int32_t*)(mem + o_parent);
     uint32_t* visits = (uint32_t*)(mem + o_visits);
     uint32_t* count = (uint32_t*)(mem + o_count);
@@ -720,7 +726,7 @@ int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, int lea
     uint32_t level_tasks = 1, depth = 0;
     uint32_t hc[5] = {0, 0, 0, 0, 0};
     while (level_tasks > 0) {
-        if (depth > 4096) { cudaFreeAsync(mem, s); return fail(st, RN_ERR_BUDGET, "collapse: more than 4096 levels"); }
+        if (depth > 4096) return fail(st, RN_ERR_BUDGET, "collapse: more than 4096 levels");
         collapse_level<<<cdiv(level_tasks, 128), 128, 0, s>>>(q0, ctr + 0, q1, ctr + 1, n, ctr + 2, node_cap,
                                                               ctr + 3, t.box, t.left, t.right, t.tri, count,
                                                               d_tris, acc->d_nodes, acc->d_tris, (uint32_t)leaf_max,
@@ -735,7 +741,6 @@ int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, int lea
         std::swap(q0, q1);
     }
     RN_CUDA(cudaGetLastError(), st);
-    cudaFreeAsync(mem, s);
     if (hc[4]) return fail(st, RN_ERR_OVERFLOW, "BVH collapse error word 0x%x", hc[4]);
     if (hc[3] != n) return fail(st, RN_ERR_STATE, "collapse placed %u of %u triangles", hc[3], n);
     acc->nodes = hc[2];

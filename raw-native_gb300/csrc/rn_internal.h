@@ -25,6 +25,15 @@ struct DevBuf {
     size_t cap = 0;
 };
 
+// A call-local device allocation, freed on every return path.
+struct ScopedDev {
+    void* p = nullptr;
+    ScopedDev() = default;
+    ScopedDev(const ScopedDev&) = delete;
+    ScopedDev& operator=(const ScopedDev&) = delete;
+    ~ScopedDev() { if (p) cudaFree(p); }
+};
+
 // Workspace slots of the context. Each entry point uses fixed slots, so repeated calls of
 // the same size allocate nothing.
 enum Slot {
