@@ -172,13 +172,15 @@ int rn_closest(const rn_accel* accel, const float* rays, const float* t_max, uin
 
 /* The hybrid pass (raw::gpu_check::hybridGpu, src/renderer/gpu/rt_hybrid.cpp:43-83, with the
  * per-pixel rule of its CPU reference, src/renderer/gpu/rt_hybrid_parity.cpp:14-82) over a
- * G-buffer: for each covered pixel, d = normalize(position - eye), the normal turned to face
- * the viewer, the origin pushed off the surface by 2e-4 (1 + max |position|) along the normal
- * toward the ray; lit = 1 when nothing is hit toward normalize(to_sun) below 1e30, else 0;
- * refl_tri / refl_t = the nearest hit of the mirror ray d - 2 (d.n) n (-1 / -1: none).
- * Uncovered pixels: lit -1, refl_tri -1, refl_t -1. */
-int rn_hybrid(const rn_gbuf* g, const rn_accel* accel, const float* eye, const float* to_sun, int flags, float* lit,
-              int32_t* refl_tri, float* refl_t, rn_status* st);
+ * G-buffer: for each covered pixel, d = normalize(position - eye); the geometric normal ng
+ * (`geo_normal`, w x h x 3 floats, the surface triangle's normalize(cross(b - a, c - a));
+ * NULL: the G-buffer normal) turned to face the viewer, and the shading normal n (the
+ * G-buffer normal) turned to ng's side; each ray's origin pushed off the surface by
+ * 2e-4 (1 + max |position|) along ng toward the ray; lit = 1 when nothing is hit toward
+ * normalize(to_sun) below 1e30, else 0; refl_tri / refl_t = the nearest hit of the mirror
+ * ray d - 2 (d.n) n (-1 / -1: none). Uncovered pixels: lit -1, refl_tri -1, refl_t -1. */
+int rn_hybrid(const rn_gbuf* g, const float* geo_normal, const rn_accel* accel, const float* eye, const float* to_sun,
+              int flags, float* lit, int32_t* refl_tri, float* refl_t, rn_status* st);
 
 /* One view of a batch: its G-buffer and outputs, all DEVICE pointers. `sky`/`sun` are used
  * with RN_SKY; `ao_ss` (and `err`, optional) turn on SSAO and the reconcile for the view. */

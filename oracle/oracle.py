@@ -64,7 +64,8 @@ def lib() -> C.CDLL:
         L.rno_occluded_scan.argtypes = [_F, C.c_int, _F, C.c_float]
         L.rno_occluded_scan_batch.argtypes = [_F, C.c_int, _F, _F, C.c_int, _U8, C.c_int]
         L.rno_closest_scan_batch.argtypes = [_F, C.c_int, _F, _F, C.c_int, _I32, _F, C.c_int]
-        L.rno_hybrid.argtypes = [C.c_int, C.c_int, _F, _F, _U8, _F, C.c_int, _F, _F, _F, _I32, _F, C.c_int]
+        L.rno_hybrid.argtypes = [C.c_int, C.c_int, _F, _F, C.c_void_p, _U8, _F, C.c_int, _F, _F, _F, _I32, _F,
+                                 C.c_int]
         L.rno_trace.argtypes = [C.c_int, C.c_int, _F, _F, _U8, C.c_void_p, _F, C.c_int, C.c_int,
                                 C.c_float, C.c_void_p, C.c_int, _F, C.c_void_p, C.c_void_p,
                                 C.c_int, C.c_int, C.c_int]
@@ -191,15 +192,18 @@ def closest_scan(tris, rays, tmax, threads=1):
     return tri, t
 
 
-def hybrid(pos, nrm, mask, tris, eye, sun, threads=1):
-    """The hybrid pass's per-pixel rule over a G-buffer (scans): (lit, refl_tri, refl_t)."""
+def hybrid(pos, nrm, mask, tris, eye, sun, geo_normal=None, threads=1):
+    """The hybrid pass's per-pixel rule over a G-buffer (scans): (lit, refl_tri, refl_t).
+    geo_normal: the geometric normals (h, w, 3), or None for the G-buffer normals."""
     mask = np.ascontiguousarray(mask, np.uint8)
     h, w = mask.shape
     tris = _f32(tris).reshape(-1, 9)
     lit = np.zeros((h, w), np.float32)
     tri = np.zeros((h, w), np.int32)
     t = np.zeros((h, w), np.float32)
-    lib().rno_hybrid(w, h, _f32(pos), _f32(nrm), mask, tris, len(tris), _f32(eye), _f32(sun), lit, tri, t, int(threads))
+    ng = _f32(geo_normal) if geo_normal is not None else None
+    lib().rno_hybrid(w, h, _f32(pos), _f32(nrm), ng.ctypes.data if ng is not None else None, mask, tris, len(tris),
+                     _f32(eye), _f32(sun), lit, tri, t, int(threads))
     return lit, tri, t
 
 

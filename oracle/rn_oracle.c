@@ -841,13 +841,14 @@ RNO_API void rno_closest_scan_batch(const float* tris9, int ntri, const float* r
     parallel_rows(n, threads, closest_row, &c);
 }
 
-/* The hybrid pass's per-pixel rule (src/renderer/gpu/rt_hybrid_parity.cpp:38-41, 57-80) over a
- * G-buffer whose normal serves as both the geometric and the shading normal: d =
- * normalize(pos - eye), the normal turned to face the viewer, origins pushed off by
- * 2e-4 (1 + max |pos|) along it toward each ray; lit = no hit toward normalize(sun) below 1e30
- * (1, else 0); the mirror ray d - n (2 d.n) and its nearest hit below 1e30. Uncovered: -1. */
+/* The hybrid pass's per-pixel rule (src/renderer/gpu/rt_hybrid_parity.cpp:35-41, 57-80) over
+ * a G-buffer: d = normalize(pos - eye); the geometric normal (a plane of its own, or the
+ * G-buffer normal when none is given) turned to face the viewer, the shading normal (the
+ * G-buffer normal) turned to its side; origins pushed off by 2e-4 (1 + max |pos|) along the
+ * geometric normal toward each ray; lit = no hit toward normalize(sun) below 1e30 (1, else
+ * 0); the mirror ray d - n (2 d.n) and its nearest hit below 1e30. Uncovered: -1. */
 typedef struct {
-    int w; const float* pos; const float* nrm; const uint8_t* mask; const tri_t* tris; int ntri;
+    int w; const float* pos; const float* nrm; const float* ng; const uint8_t* mask; const tri_t* tris; int ntri;
     v3 eye, sun; float* lit; int32_t* tri; float* t;
 } hybrid_ctx;
 static v3 offset_of(v3 p, v3 n, v3 dir) {
@@ -861,21 +862,23 @@ static void hybrid_row(void* p, int y) {
         if (!c->mask[i]) { c->lit[i] = -1.0f; c->tri[i] = -1; c->t[i] = -1.0f; continue; }
         const v3 pos = v3m(c->pos[3 * i], c->pos[3 * i + 1], c->pos[3 * i + 2]);
         v3 n = v3m(c->nrm[3 * i], c->nrm[3 * i + 1], c->nrm[3 * i + 2]);
+        v3 ng = c->ng ? v3m(c->ng[3 * i], c->ng[3 * i + 1], c->ng[3 * i + 2]) : n;
         const v3 d = norm3(sub3(pos, c->eye));
-        if (dot3(n, d) > 0.0f) n = mul3(n, -1.0f);
+        if (dot3(ng, d) > 0.0f) ng = mul3(ng, -1.0f);
+        if (dot3(n, ng) < 0.0f) n = mul3(n, -1.0f);
         const v3 l = norm3(c->sun);
-        c->lit[i] = scan_occluded(c->tris, c->ntri, offset_of(pos, n, l), l, 1e30f) ? 0.0f : 1.0f;
+        c->lit[i] = scan_occluded(c->tris, c->ntri, offset_of(pos, ng, l), l, 1e30f) ? 0.0f : 1.0f;
         const v3 r = sub3(d, mul3(n, 2.0f * dot3(d, n)));
         float t;
-        const int id = scan_closest(c->tris, c->ntri, offset_of(pos, n, r), r, 1e30f, &t);
+        const int id = scan_closest(c->tris, c->ntri, offset_of(pos, ng, r), r, 1e30f, &t);
         c->tri[i] = id;
         c->t[i] = id >= 0 ? t : -1.0f;
     }
 }
-RNO_API void rno_hybrid(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, const float* tris9,
-                        int ntri, const float* eye3, const float* sun3, float* lit, int32_t* tri, float* t,
-                        int threads) {
-    hybrid_ctx c = {w, pos, nrm, mask, (const tri_t*)tris9, ntri, v3m(eye3[0], eye3[1], eye3[2]),
+RNO_API void rno_hybrid(int w, int h, const float* pos, const float* nrm, const float* ng, const uint8_t* mask,
+                        const float* tris9, int ntri, const float* eye3, const float* sun3, float* lit, int32_t* tri,
+                        float* t, int threads) {
+    hybrid_ctx c = {w, pos, nrm, ng, mask, (const tri_t*)tris9, ntri, v3m(eye3[0], eye3[1], eye3[2]),
                     v3m(sun3[0], sun3[1], sun3[2]), lit, tri, t};
     parallel_rows(h, threads, hybrid_row, &c);
 }

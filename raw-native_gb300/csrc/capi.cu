@@ -1051,8 +1051,8 @@ int rn_closest(const rn_accel* accel, const float* rays, const float* t_max, uin
 
 // The hybrid pass of raw::gpu_check::hybridGpu (src/renderer/gpu/rt_hybrid.cpp:43-83) over a
 // G-buffer: per covered pixel a sun shadow ray and a mirror reflection ray (closest hit).
-int rn_hybrid(const rn_gbuf* g, const rn_accel* accel, const float* eye, const float* to_sun, int flags, float* lit,
-              int32_t* refl_tri, float* refl_t, rn_status* st) {
+int rn_hybrid(const rn_gbuf* g, const float* geo_normal, const rn_accel* accel, const float* eye, const float* to_sun,
+              int flags, float* lit, int32_t* refl_tri, float* refl_t, rn_status* st) {
     RN_TRY(ensure_ctx(st));
     RN_TRY(check_gbuf(g, st));
     if (!accel || !eye || !to_sun || !lit || !refl_tri || !refl_t) return fail(st, RN_ERR_INVALID, "null argument");
@@ -1062,12 +1062,14 @@ int rn_hybrid(const rn_gbuf* g, const rn_accel* accel, const float* eye, const f
     const size_t np = (size_t)g->w * g->h;
     StagedGbuf sg;
     RN_TRY(stage_gbuf(g, dev, &sg, st));
+    const float* d_ng = nullptr;
+    if (geo_normal) RN_TRY(stage_in(geo_normal, np * 3, dev, WS_HYB_NG, &d_ng, st));
     float *d_lit, *d_t;
     int32_t* d_tri;
     RN_TRY(stage_out(lit, np, dev, WS_HYB_LIT, &d_lit, st));
     RN_TRY(stage_out(refl_tri, np, dev, WS_HYB_TRI, &d_tri, st));
     RN_TRY(stage_out(refl_t, np, dev, WS_HYB_T, &d_t, st));
-    if (launch_hybrid(g->w, g->h, sg.pos, sg.nrm, sg.mask, accel, eye, to_sun, d_lit, d_tri, d_t, c.dev_error,
+    if (launch_hybrid(g->w, g->h, sg.pos, sg.nrm, d_ng, sg.mask, accel, eye, to_sun, d_lit, d_tri, d_t, c.dev_error,
                       c.stream) != RN_OK)
         return cuda_fail(st, cudaGetLastError(), "hybrid_kernel");
     if (dev) return ok(st);

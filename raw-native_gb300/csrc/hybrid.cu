@@ -109,6 +109,7 @@ struct HybridArgs {
     int w, h;
     const float* pos;
     const float* nrm;
+    const float* geo;     // geometric normals, or null: the G-buffer normals
     const uint8_t* mask;
     const Node4* nodes;
     const LeafTri* tris;
@@ -121,10 +122,10 @@ struct HybridArgs {
     uint32_t* err;
 };
 
-// rt_hybrid_parity.cpp:57-80 over the library's G-buffer: d = normalize(pos - eye); the
-// normal faces the viewer (the G-buffer's normal serves as both the geometric and the
-// shading normal); lit = no hit toward the sun below 1e30; the reflection r = d - 2 (d.n) n
-// and its nearest hit below 1e30.
+// rt_hybrid_parity.cpp:35-37, 57-80 over the library's G-buffer: d = normalize(pos - eye);
+// the geometric normal faces the viewer and the shading normal lies on its side; lit = no
+// hit toward the sun below 1e30; the reflection r = d - 2 (d.n) n and its nearest hit below
+// 1e30; both origins pushed off along the geometric normal.
 // A block covers 16 x 8 pixels, each warp an 8 x 4 packet: neighbouring rays share more of
 // their walks than a 32-pixel row does.
 // kMinBlocks: resident 128-thread blocks per SM asked of the register allocator (the
@@ -144,16 +145,18 @@ __global__ void __launch_bounds__(128, kMinBlocks) hybrid_kernel(const HybridArg
     }
     const v3 pos = load3(a.pos + 3 * i);
     v3 n = load3(a.nrm + 3 * i);
+    v3 ng = a.geo ? load3(a.geo + 3 * i) : n;
     const v3 d = normalize(sub(pos, mk(a.ex, a.ey, a.ez)));
-    if (dot(n, d) > 0.0f) n = scale(n, -1.0f);
+    if (dot(ng, d) > 0.0f) ng = scale(ng, -1.0f);
+    if (dot(n, ng) < 0.0f) n = scale(n, -1.0f);
     const v3 l = normalize(mk(a.lx, a.ly, a.lz));
     Counts cn;
     const bool shadow =
-        a.has_geometry && walk<false>(a.nodes, a.tris, offset_of(pos, n, l), l, 1e30f, 1e30f, a.err, cn) != 0;
+        a.has_geometry && walk<false>(a.nodes, a.tris, offset_of(pos, ng, l), l, 1e30f, 1e30f, a.err, cn) != 0;
     a.lit[i] = shadow ? 0.0f : 1.0f;
     const v3 r = sub(d, scale(n, fmul(2.0f, dot(d, n))));
     float t = 1e30f;
-    const int id = a.has_geometry ? walk_closest(a.nodes, a.tris, offset_of(pos, n, r), r, 1e30f, t, a.err) : -1;
+    const int id = a.has_geometry ? walk_closest(a.nodes, a.tris, offset_of(pos, ng, r), r, 1e30f, t, a.err) : -1;
     a.refl_tri[i] = id;
     a.refl_t[i] = id >= 0 ? t : -1.0f;
 }
@@ -167,12 +170,13 @@ int launch_closest(const Node4* nodes, const LeafTri* tris, int has_geometry, co
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 
-int launch_hybrid(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, const rn_accel* accel,
+int launch_hybrid(int w, int h, const float* pos, const float* nrm, const float* geo_nrm, const uint8_t* mask,
+                  const rn_accel* accel,
                   const float eye[3], const float to_sun[3], float* lit, int32_t* refl_tri, float* refl_t,
                   uint32_t* err, cudaStream_t s) {
     HybridArgs a{};
     a.w = w; a.h = h;
-    a.pos = pos; a.nrm = nrm; a.mask = mask;
+    a.pos = pos; a.nrm = nrm; a.geo = geo_nrm; a.mask = mask;
     a.nodes = accel->d_nodes; a.tris = accel->d_tris;
     a.has_geometry = accel->ntri > 0;
     a.ex = eye[0]; a.ey = eye[1]; a.ez = eye[2];

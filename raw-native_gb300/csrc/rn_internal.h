@@ -42,7 +42,7 @@ enum Slot {
     WS_NRM_IN, WS_RASTER, WS_DEPTH, WS_STATS,
     WS_SUR_AO4, WS_SUR_PRED, WS_SUR_FB, WS_SUR_AOFB, WS_SUR_STATS, WS_VPOS, WS_VNRM, WS_VDEPTH, WS_GTAO,
     WS_ALB_IN, WS_ALB, WS_MOTION, WS_FRAME, WS_HDR, WS_FRAME_SMALL, WS_MIRROR,
-    WS_HYB_LIT, WS_HYB_TRI, WS_HYB_T, WS_CLOSEST_TRI, WS_CLOSEST_T,
+    WS_HYB_LIT, WS_HYB_TRI, WS_HYB_T, WS_HYB_NG, WS_CLOSEST_TRI, WS_CLOSEST_T,
     WS_COUNT
 };
 
@@ -232,7 +232,8 @@ int launch_trace(const TraceParams& p, int sm_count, cudaStream_t s, unsigned lo
 int launch_closest(const Node4* nodes, const LeafTri* tris, int has_geometry, const float* rays, const float* tmax,
                    uint32_t n, int32_t* tri, float* t, uint32_t* err, cudaStream_t s);
 // The hybrid pass over a G-buffer: sun shadows and mirror reflections per covered pixel.
-int launch_hybrid(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, const rn_accel* accel,
+int launch_hybrid(int w, int h, const float* pos, const float* nrm, const float* geo_nrm, const uint8_t* mask,
+                  const rn_accel* accel,
                   const float eye[3], const float to_sun[3], float* lit, int32_t* refl_tri, float* refl_t,
                   uint32_t* err, cudaStream_t s);
 

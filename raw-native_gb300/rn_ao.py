@@ -120,7 +120,7 @@ def lib() -> C.CDLL:
                                     C.POINTER(C.c_uint32), st]
         L.rn_occluded.argtypes = [vp, vp, vp, C.c_uint32, C.c_int, vp, st]
         L.rn_closest.argtypes = [vp, vp, vp, C.c_uint32, C.c_int, vp, vp, st]
-        L.rn_hybrid.argtypes = [C.POINTER(GBuf), vp, vp, vp, C.c_int, vp, vp, vp, st]
+        L.rn_hybrid.argtypes = [C.POINTER(GBuf), vp, vp, vp, vp, C.c_int, vp, vp, vp, st]
         L.rn_raster_gbuffer.argtypes = [vp, vp, C.c_uint32, vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, st]
         L.rn_reconcile_noalloc.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_float, vp, vp,
                                            C.POINTER(ReconcileOut), st]
@@ -799,10 +799,12 @@ def closest(accel: LinearAccel, rays, t_max):
     return tri, t
 
 
-def hybrid(g: GBuffer, accel: LinearAccel, eye, to_sun):
+def hybrid(g: GBuffer, accel: LinearAccel, eye, to_sun, geo_normal=None):
     """The hybrid pass over a G-buffer: (lit, refl_tri, refl_t), each (h, w); lit 1 / 0 / -1
-    (lit, shadowed, uncovered), refl_tri / refl_t the mirror ray's nearest hit (-1: none)."""
-    args = _Args(g.position, g.normal, g.mask)
+    (lit, shadowed, uncovered), refl_tri / refl_t the mirror ray's nearest hit (-1: none).
+    geo_normal: the surface triangles' normals (h, w, 3) for the offsets and the facing test;
+    None uses the G-buffer normals."""
+    args = _Args(g.position, g.normal, g.mask, geo_normal)
     gb = _gbuf(g, args)
     h, w = g.shape
     lit = args.out(g.mask, (h, w), np.float32)
@@ -811,6 +813,7 @@ def hybrid(g: GBuffer, accel: LinearAccel, eye, to_sun):
     e = (C.c_float * 3)(*[float(v) for v in eye])
     l = (C.c_float * 3)(*[float(v) for v in to_sun])
     st = Status()
-    _check(lib().rn_hybrid(C.byref(gb), accel.handle, C.cast(e, C.c_void_p), C.cast(l, C.c_void_p), args.flags,
+    _check(lib().rn_hybrid(C.byref(gb), args.ptr(geo_normal, np.float32), accel.handle, C.cast(e, C.c_void_p),
+                           C.cast(l, C.c_void_p), args.flags,
                            args.ptr(lit, np.float32), args.ptr(tri, np.int32), args.ptr(t, np.float32), C.byref(st)), st)
     return lit, tri, t

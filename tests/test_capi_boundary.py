@@ -64,7 +64,7 @@ def test_no_device_fails_loudly(lib):
         rn_ao.compute_ssao(g, 24, 2.0)
     st = rn_ao.Status()
     eye = (C.c_float * 3)(0, 0, 0)
-    assert lib.rn_hybrid(None, None, eye, eye, 0, None, None, None, C.byref(st)) == 2
+    assert lib.rn_hybrid(None, None, None, eye, eye, 0, None, None, None, C.byref(st)) == 2
 
 
 def test_argument_errors_before_any_device_work(lib):

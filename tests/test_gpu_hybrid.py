@@ -221,3 +221,32 @@ def test_closest_and_occluded_equal_the_scan_on_seeded_rays(rn, oracle):
         occ = rn.occluded(acc, rays, tmax)
         assert np.array_equal(occ, oracle.occluded_scan(tris, rays, tmax, threads=THREADS))
         assert 0.01 < (tri >= 0).mean() < 0.95
+
+
+def test_hybrid_geometric_normals_bit_exact(rn, oracle):
+    """Smooth-shaded spheres: the shading normal (the G-buffer's, interpolated) differs from
+    the surface triangle's normal, which places the ray origins and decides the facing
+    (rt_hybrid_parity.cpp:35-41). The plane of triangle normals comes from the rasterizer's
+    per-pixel triangle."""
+    import torch
+    import scene as scenes
+    sc = scenes.build_synthetic_scene(13, 20, 12, grid=12, half=12.0, subdiv=2)
+    cam = (14.0, 6.0, 10.0, 0.0, 1.0, 0.0, 0.0, 1.0, 0.0, 0.9)
+    _, pos, nrm, mask, ptri = oracle.rasterize_ex(sc.tris, sc.normals, cam, 256, 192)
+    t9 = sc.tris[np.maximum(ptri, 0)].reshape(192, 256, 3, 3)
+    ng = np.cross(t9[..., 1, :] - t9[..., 0, :], t9[..., 2, :] - t9[..., 0, :]).astype(np.float32)
+    ng = (ng * (np.float32(1.0) / np.sqrt((ng * ng).sum(-1, keepdims=True, dtype=np.float32)))).astype(np.float32)
+    ng[mask == 0] = 0.0
+    eye = np.asarray(cam[:3], np.float32)
+    acc = rn.LinearAccel(sc.tris)
+    got = rn.hybrid(rn.GBuffer(pos, nrm, mask), acc, eye, sc.to_light, geo_normal=ng)
+    ref = oracle.hybrid(pos, nrm, mask, sc.tris, eye, sc.to_light, geo_normal=ng, threads=THREADS)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b), int((a != b).sum())
+    # the geometric normals change the answer somewhere: they are not the shading normals
+    alt = oracle.hybrid(pos, nrm, mask, sc.tris, eye, sc.to_light, threads=THREADS)
+    assert any(not np.array_equal(a, b) for a, b in zip(ref, alt))
+    dev = rn.hybrid(rn.GBuffer(*(torch.from_numpy(a).cuda() for a in (pos, nrm, mask))), acc, eye, sc.to_light,
+                    geo_normal=torch.from_numpy(ng).cuda())
+    for a, b in zip(got, dev):
+        assert np.array_equal(a, b.cpu().numpy())
