@@ -144,6 +144,64 @@ def test_closest_scan_equals_reference_closest(oracle):
     assert np.array_equal(tri, rtri) and np.array_equal(t, rt)
 
 
+def test_hybrid_rule_restated_in_python(oracle):
+    """The oracle's hybrid pass against a scalar float32 restatement of the reference's
+    per-pixel rule (src/renderer/gpu/rt_hybrid_parity.cpp:35-41, 57-80; raw/math/vec.hpp
+    normalize and dot) on a small G-buffer, with and without separate geometric normals; the
+    ray queries scan with the oracle's pinned triangle test."""
+    import ctypes as C
+    import scene
+    f = np.float32
+    sc = scene.build_test_scene()
+    _, pos, nrm, mask, ptri = oracle.rasterize_ex(sc.tris, sc.normals, sc.camera, 24, 18)
+    tris = sc.tris
+    t9 = tris[np.maximum(ptri, 0)].reshape(18, 24, 3, 3)
+    geo = np.cross(t9[..., 1, :] - t9[..., 0, :], t9[..., 2, :] - t9[..., 0, :]).astype(f)
+    geo = geo * (f(1) / np.sqrt((geo * geo).sum(-1, keepdims=True, dtype=f)))
+    geo[mask == 0] = 0
+    eye = np.asarray(sc.camera[:3], f)
+    tt = C.c_float()
+
+    def dot(a, b):
+        return f(f(f(a[0] * b[0]) + f(a[1] * b[1])) + f(a[2] * b[2]))
+
+    def normalize(v):
+        l = f(np.sqrt(dot(v, v)))
+        return (v * (f(1) / l)).astype(f) if l > 0 else v
+
+    def offset(p, ng, d):
+        e = f(f(2e-4) * f(f(1) + max(abs(p[0]), max(abs(p[1]), abs(p[2])))))
+        return (p + ng * (e if dot(ng, d) > 0 else -e)).astype(f)
+
+    def scan(o, d):
+        ray = np.concatenate([o, d]).astype(f)
+        best, best_i = f(1e30), -1
+        for i in range(len(tris)):
+            if oracle.lib().rno_intersect(ray, np.ascontiguousarray(tris[i]), C.byref(tt)) and f(tt.value) < best:
+                best, best_i = f(tt.value), i
+        return best_i, best
+
+    l = normalize(np.asarray(sc.to_light, f))
+    for g in (None, geo):
+        lit, tri, t = oracle.hybrid(pos, nrm, mask, tris, eye, sc.to_light, geo_normal=g)
+        for y in range(18):
+            for x in range(24):
+                if not mask[y, x]:
+                    assert lit[y, x] == -1 and tri[y, x] == -1
+                    continue
+                p, n = pos[y, x], nrm[y, x]
+                ng = g[y, x] if g is not None else n
+                d = normalize((p - eye).astype(f))
+                if dot(ng, d) > 0:
+                    ng = (ng * f(-1)).astype(f)
+                if dot(n, ng) < 0:
+                    n = (n * f(-1)).astype(f)
+                assert lit[y, x] == (0.0 if scan(offset(p, ng, l), l)[0] >= 0 else 1.0)
+                r = (d - n * f(f(2) * dot(d, n))).astype(f)
+                i, best = scan(offset(p, ng, r), r)
+                assert tri[y, x] == i and t[y, x] == (best if i >= 0 else -1.0)
+
+
 def test_thread_count_invariance(oracle):
     # tests/test_verify.cpp:40-43: output identical for any thread count
     a = oracle.render_default(128, 96, threads=1)
