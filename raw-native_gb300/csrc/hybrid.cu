@@ -2,8 +2,8 @@
 // raw::rt::closest (src/renderer/rt_bvh.cpp:125-152) on the 4-wide tree, and the hybrid pass
 // of raw::gpu_check::hybridGpu / cpuReference (src/renderer/gpu/rt_hybrid.cpp:43-83,
 // src/renderer/gpu/rt_hybrid_parity.cpp:14-82): per covered G-buffer pixel a sun shadow ray
-// (any hit) and a mirror reflection ray (closest hit), both from an origin pushed off the
-// surface along the normal.
+// (any hit) and a mirror reflection ray (closest hit, about the shading normal), both from
+// an origin pushed off the surface along the geometric normal.
 //
 // Nearest hit: the smallest t > 1e-4 below t_max of the reference's watertight triangle test
 // over all triangles, ties to the lowest triangle index, exactly as the reference's ordered
