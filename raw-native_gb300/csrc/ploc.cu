@@ -485,79 +485,89 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
                                const uint32_t* __restrict__ count, const float* __restrict__ tris,
                                Node4* __restrict__ nodes, LeafTri* __restrict__ leaf, uint32_t leaf_max,
                                uint32_t* err) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= *nin) return;
-    const Task task = in[t];
-    int32_t C[4];
-    int nc = 0;
-    const int32_t b = task.bnode;
-    if (tri[b] >= 0 || count[b] <= leaf_max) {
-        C[nc++] = b;
-    } else {
-        C[nc++] = left[b];
-        C[nc++] = right[b];
-        while (nc < 4) {
-            int pick = -1;
-            float best = -1.0f;
-            for (int k = 0; k < nc; ++k) {
-                const int32_t c = C[k];
-                if (tri[c] >= 0 || count[c] <= leaf_max) continue;
-                const float a = box_area(box + (size_t)c * 6);
-                if (a > best) { best = a; pick = k; }
-            }
-            if (pick < 0) break;
-            const int32_t c = C[pick];
-            C[pick] = left[c];
-            C[nc++] = right[c];
-        }
-    }
-    Node4 nd;
-    for (int k = 0; k < 4; ++k) {
-        nd.lox[k] = nd.loy[k] = nd.loz[k] = 1e30f;
-        nd.hix[k] = nd.hiy[k] = nd.hiz[k] = -1e30f;
-        nd.child[k] = 0;
-        nd.meta[k] = 0;
-    }
-    nd.meta[0] = nc;
-    for (int k = 0; k < nc; ++k) {
-        const int32_t c = C[k];
-        float lo[3], hi[3];
-        padded(box + (size_t)c * 6, lo, hi);
-        nd.lox[k] = lo[0]; nd.loy[k] = lo[1]; nd.loz[k] = lo[2];
-        nd.hix[k] = hi[0]; nd.hiy[k] = hi[1]; nd.hiz[k] = hi[2];
-        if (tri[c] >= 0 || count[c] <= leaf_max) {
-            const uint32_t cnt = count[c];
-            const uint32_t first = atomicAdd(tri_ctr, cnt);
-            // the subtree's leaves, left to right
-            int32_t stack[2 * kLeafCap];
-            int sp = 0, w = 0;
-            stack[sp++] = c;
-            while (sp > 0) {
-                const int32_t x = stack[--sp];
-                if (tri[x] >= 0) {
-                    const float* v = tris + (size_t)tri[x] * 9;
-                    LeafTri lt;
-                    lt.ax = v[0]; lt.ay = v[1]; lt.az = v[2]; lt.id = __int_as_float(tri[x]);
-                    lt.bx = v[3]; lt.by = v[4]; lt.bz = v[5]; lt.pad0 = 0.0f;
-                    lt.cx = v[6]; lt.cy = v[7]; lt.cz = v[8]; lt.pad1 = 0.0f;
-                    leaf[first + w++] = lt;
-                } else if (sp + 2 <= 2 * kLeafCap) {
-                    stack[sp++] = right[x];
-                    stack[sp++] = left[x];
-                } else {
-                    atomicOr(err, DEV_STACK_OVERFLOW);
-                }
-            }
-            nd.child[k] = ~(int32_t)((first << 3) | (cnt - 1));
+    // grid-stride over the level's tasks: the grid is fixed, the count is read on the device
+    const uint32_t m = *nin;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x) {
+        const Task task = in[t];
+        int32_t C[4];
+        int nc = 0;
+        const int32_t b = task.bnode;
+        if (tri[b] >= 0 || count[b] <= leaf_max) {
+            C[nc++] = b;
         } else {
-            const uint32_t id = atomicAdd(node_ctr, 1u);
-            const uint32_t q = atomicAdd(nout, 1u);
-            if (id >= node_cap || q >= out_cap) { atomicOr(err, DEV_QUEUE_OVERFLOW); nd.child[k] = 0; continue; }
-            out[q] = Task{c, (int32_t)id};
-            nd.child[k] = (int32_t)id;
+            C[nc++] = left[b];
+            C[nc++] = right[b];
+            while (nc < 4) {
+                int pick = -1;
+                float best = -1.0f;
+                for (int k = 0; k < nc; ++k) {
+                    const int32_t c = C[k];
+                    if (tri[c] >= 0 || count[c] <= leaf_max) continue;
+                    const float a = box_area(box + (size_t)c * 6);
+                    if (a > best) { best = a; pick = k; }
+                }
+                if (pick < 0) break;
+                const int32_t c = C[pick];
+                C[pick] = left[c];
+                C[nc++] = right[c];
+            }
         }
+        Node4 nd;
+        for (int k = 0; k < 4; ++k) {
+            nd.lox[k] = nd.loy[k] = nd.loz[k] = 1e30f;
+            nd.hix[k] = nd.hiy[k] = nd.hiz[k] = -1e30f;
+            nd.child[k] = 0;
+            nd.meta[k] = 0;
+        }
+        nd.meta[0] = nc;
+        for (int k = 0; k < nc; ++k) {
+            const int32_t c = C[k];
+            float lo[3], hi[3];
+            padded(box + (size_t)c * 6, lo, hi);
+            nd.lox[k] = lo[0]; nd.loy[k] = lo[1]; nd.loz[k] = lo[2];
+            nd.hix[k] = hi[0]; nd.hiy[k] = hi[1]; nd.hiz[k] = hi[2];
+            if (tri[c] >= 0 || count[c] <= leaf_max) {
+                const uint32_t cnt = count[c];
+                const uint32_t first = atomicAdd(tri_ctr, cnt);
+                // the subtree's leaves, left to right
+                int32_t stack[2 * kLeafCap];
+                int sp = 0, w = 0;
+                stack[sp++] = c;
+                while (sp > 0) {
+                    const int32_t x = stack[--sp];
+                    if (tri[x] >= 0) {
+                        const float* v = tris + (size_t)tri[x] * 9;
+                        LeafTri lt;
+                        lt.ax = v[0]; lt.ay = v[1]; lt.az = v[2]; lt.id = __int_as_float(tri[x]);
+                        lt.bx = v[3]; lt.by = v[4]; lt.bz = v[5]; lt.pad0 = 0.0f;
+                        lt.cx = v[6]; lt.cy = v[7]; lt.cz = v[8]; lt.pad1 = 0.0f;
+                        leaf[first + w++] = lt;
+                    } else if (sp + 2 <= 2 * kLeafCap) {
+                        stack[sp++] = right[x];
+                        stack[sp++] = left[x];
+                    } else {
+                        atomicOr(err, DEV_STACK_OVERFLOW);
+                    }
+                }
+                nd.child[k] = ~(int32_t)((first << 3) | (cnt - 1));
+            } else {
+                const uint32_t id = atomicAdd(node_ctr, 1u);
+                const uint32_t q = atomicAdd(nout, 1u);
+                if (id >= node_cap || q >= out_cap) { atomicOr(err, DEV_QUEUE_OVERFLOW); nd.child[k] = 0; continue; }
+                out[q] = Task{c, (int32_t)id};
+                nd.child[k] = (int32_t)id;
+            }
+        }
+        nodes[task.wnode] = nd;
     }
-    nodes[task.wnode] = nd;
+}
+
+// Between two levels: count the level just processed if it had tasks (ctr[5], the 4-wide
+// depth), make its output the next input (ctr[0] = ctr[1]) and restart the output count.
+__global__ void collapse_next(uint32_t* ctr) {
+    if (ctr[0] > 0) ++ctr[5];
+    ctr[0] = ctr[1];
+    ctr[1] = 0;
 }
 
 inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
@@ -723,22 +733,25 @@ int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, int lea
     const uint32_t init[4] = {1u, 0u, 1u, 0u};
     RN_CUDA(cudaMemcpyAsync(q0, &root, sizeof root, cudaMemcpyHostToDevice, s), st);
     RN_CUDA(cudaMemcpyAsync(ctr, init, sizeof init, cudaMemcpyHostToDevice, s), st);
+    // levels in batches of kLevels per host read; a level after the last one finds no task
+    constexpr int kLevels = 8;
+    const uint32_t grid = std::max(1u, std::min(cdiv(n, 128), (uint32_t)ctx().sm_count * 16u));
     uint32_t level_tasks = 1, depth = 0;
-    uint32_t hc[5] = {0, 0, 0, 0, 0};
+    uint32_t hc[6] = {0, 0, 0, 0, 0, 0};
     while (level_tasks > 0) {
         if (depth > 4096) return fail(st, RN_ERR_BUDGET, "collapse: more than 4096 levels");
-        collapse_level<<<cdiv(level_tasks, 128), 128, 0, s>>>(q0, ctr + 0, q1, ctr + 1, n, ctr + 2, node_cap,
-                                                              ctr + 3, t.box, t.left, t.right, t.tri, count,
-                                                              d_tris, acc->d_nodes, acc->d_tris, (uint32_t)leaf_max,
-                                                              ctr + 4);
-        ++depth;
-        // next level: its tasks become the input, the output counter restarts at 0
-        RN_CUDA(cudaMemcpyAsync(ctr + 0, ctr + 1, 4, cudaMemcpyDeviceToDevice, s), st);
-        RN_CUDA(cudaMemsetAsync(ctr + 1, 0, 4, s), st);
+        for (int k = 0; k < kLevels; ++k) {
+            collapse_level<<<grid, 128, 0, s>>>(q0, ctr + 0, q1, ctr + 1, n, ctr + 2, node_cap, ctr + 3, t.box,
+                                                t.left, t.right, t.tri, count, d_tris, acc->d_nodes, acc->d_tris,
+                                                (uint32_t)leaf_max, ctr + 4);
+            collapse_next<<<1, 1, 0, s>>>(ctr);
+            std::swap(q0, q1);
+        }
+        RN_CUDA(cudaGetLastError(), st);
         RN_CUDA(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), st);
         RN_CUDA(cudaStreamSynchronize(s), st);
         level_tasks = hc[0];
-        std::swap(q0, q1);
+        depth = hc[5];
     }
     RN_CUDA(cudaGetLastError(), st);
     if (hc[4]) return fail(st, RN_ERR_OVERFLOW, "BVH collapse error word 0x%x", hc[4]);
