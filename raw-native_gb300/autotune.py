@@ -1,5 +1,6 @@
 """Autotuner for the library's launch shapes (rn_tune_* keys): the traversal's packet shape,
-stack depth, residency and frontier; the SSAO tile; the convolution GEMM's tile width.
+stack depth, residency and frontier; the accelerator's shape; the SSAO tile; the convolution
+GEMM's tile width; the hybrid pass's residency.
 
 Every candidate is timed with CUDA events on the library's stream over representative
 workloads, after a check that it reproduces the default configuration's outputs bit for bit
@@ -26,6 +27,8 @@ Workloads:
   trace/low-spp  the synthetic scene's view at 4, 8, 16 and 32 spp, and a 4K view of the
                  7.88M-triangle scene at 4 and 16 spp (trace_frontier_min_spp)
   trace/tail     the same view at 16, 64 and 256 spp (trace_frontier_tail)
+  hybrid         the hybrid pass (shadow + mirror ray per pixel) on the built-in scene and
+                 the 744k scene at 4K (hybrid_min_blocks)
 The traversal keys are searched jointly (every combination); the others one at a time.
 """
 from __future__ import annotations
@@ -284,6 +287,41 @@ def tune_ssao(quick: bool, reps: int, log):
     return best["cfg"], rows
 
 
+def tune_hybrid(quick: bool, reps: int, log):
+    """Residency of the hybrid pass: the built-in scene from its camera and the 744k scene from
+    an orbit view, each candidate's outputs (lit, triangle, t) checked bit for bit; scored by
+    the geometric mean of the time ratios to the current setting."""
+    import torch
+    w, h = (1920, 1080) if quick else (3840, 2160)
+    big = scenes.build_synthetic_scene(1, 500 if quick else 2000, 100 if quick else 500)
+    wls = []
+    for name, sc, cam in (("hybrid/model2", scenes.build_test_scene(), None),
+                          ("hybrid/744k", big, scenes.orbit_views(1, 8)[0][3])):
+        cam = cam if cam is not None else sc.camera
+        tris, nrms = torch.from_numpy(sc.tris).cuda(), torch.from_numpy(sc.normals).cuda()
+        g = rn.rasterize(tris, nrms, cam, w, h)
+        acc = rn.LinearAccel(tris)
+        wls.append((name, lambda g=g, acc=acc, eye=cam[:3], tl=sc.to_light: rn.hybrid(g, acc, eye, tl)))
+    current = rn.tune_get("hybrid_min_blocks")
+    rows, ref = [], None
+    for v in rn.TUNE_KEYS["hybrid_min_blocks"]:
+        rn.tune_set("hybrid_min_blocks", v)
+        outs = [[o.clone() for o in fn()] for _, fn in wls]
+        if ref is None:
+            ref = outs
+        elif not all(bool((a == b).all()) for out, r in zip(outs, ref) for a, b in zip(out, r)):
+            raise RuntimeError("hybrid_min_blocks %d changed a hybrid result" % v)
+        ms = {name: _time(fn, reps) for name, fn in wls}
+        rows.append(dict(cfg={"hybrid_min_blocks": v}, ms=ms))
+        log("hybrid_min_blocks %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    base = next(r for r in rows if r["cfg"]["hybrid_min_blocks"] == current)["ms"]
+    for r in rows:
+        r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
+    best = min(rows, key=lambda r: r["score"])
+    rn.tune_set("hybrid_min_blocks", best["cfg"]["hybrid_min_blocks"])
+    return best["cfg"], rows
+
+
 def tune_conv(quick: bool, reps: int, log):
     import torch
     H, W = (544, 960) if quick else (1088, 1920)
@@ -349,6 +387,8 @@ def main(argv=None):
     c, report["ssao"] = tune_ssao(a.quick, a.reps, log)
     cfg.update(c)
     c, report["conv"] = tune_conv(a.quick, a.reps, log)
+    cfg.update(c)
+    c, report["hybrid"] = tune_hybrid(a.quick, a.reps, log)
     cfg.update(c)
     dev = torch.cuda.get_device_name(0)
     note = "%s, %d SMs, %s workloads, %.0f s" % (dev, torch.cuda.get_device_properties(0).multi_processor_count,
