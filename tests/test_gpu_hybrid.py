@@ -84,10 +84,12 @@ def _check_hybrid(rn, oracle, tris, pos, nrm, mask, eye, sun):
     return lit, tri, cov
 
 
-def test_hybrid_test_scene_bit_exact(rn, oracle):
+@pytest.mark.parametrize("w,h", [(160, 128), (101, 37)])
+def test_hybrid_test_scene_bit_exact(rn, oracle, w, h):
+    """160 x 128 and a ragged 101 x 37 (partial 16 x 8 blocks on both edges)."""
     import scene as scenes
     sc = scenes.build_test_scene()
-    pos, nrm, mask, eye, sun = _hybrid_case(oracle, sc, 160, 128)
+    pos, nrm, mask, eye, sun = _hybrid_case(oracle, sc, w, h)
     lit, tri, cov = _check_hybrid(rn, oracle, sc.tris, pos, nrm, mask, eye, sun)
     # the box shadows part of the plane, and the plane reflects the box
     assert 0.0 < (lit[cov] == 0).mean() < 0.5 and (tri[cov] >= 2).any()
