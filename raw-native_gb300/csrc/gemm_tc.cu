@@ -1077,8 +1077,8 @@ extern "C" int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st) {
     RN_CUDA(cudaMalloc(&qb.p, 32 * 64 * 2), st);
     RN_CUDA(cudaMalloc(&cb.p, 128 * 32 * 4), st);
     void *p = pb.p, *q = qb.p, *c = cb.p;
-    cudaMemsetAsync(p, 0, 128 * 64 * 2, ctx().stream);
-    cudaMemsetAsync(q, 0, 32 * 64 * 2, ctx().stream);
+    RN_CUDA(cudaMemsetAsync(p, 0, 128 * 64 * 2, ctx().stream), st);
+    RN_CUDA(cudaMemsetAsync(q, 0, 32 * 64 * 2, ctx().stream), st);
     tc::Epilogue e{};
     e.ldc = 32;
     e.c32 = (float*)c;

@@ -234,13 +234,14 @@ int launch_raster(const float* tris, const float* nrm, uint32_t ntri, const floa
     uint2* pairs = (uint2*)(scratch + off);
     const size_t cap = off < scratch_bytes ? (scratch_bytes - off) / sizeof(uint2) : 0;
     uint32_t npairs = 0;
-    cudaMemsetAsync(keys, 0xFF, npx * 8, s);
+    if (cudaMemsetAsync(keys, 0xFF, npx * 8, s) != cudaSuccess) return RN_ERR_CUDA;
     if (ntri) {
         raster_setup<<<(ntri + 127) / 128, 128, 0, s>>>(tris, nrm, ntri, d_vp, nearZ, w, h, recs);
         count_tiles<<<(nrec + 255) / 256, 256, 0, s>>>(recs, nrec, cnt);
         scan_exclusive_u32(cnt, ofs, nrec, bsum, total, s);
-        cudaMemcpyAsync(&npairs, total, 4, cudaMemcpyDeviceToHost, s);
-        if (cudaStreamSynchronize(s) != cudaSuccess) return RN_ERR_CUDA;
+        if (cudaMemcpyAsync(&npairs, total, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return RN_ERR_CUDA;
         if (npairs > cap) { *pairs_needed = npairs; return RN_ERR_NO_MEMORY; }
         emit_pairs<<<(nrec + 255) / 256, 256, 0, s>>>(recs, nrec, ofs, pairs, (uint32_t)cap);
         if (npairs) raster_pairs<<<(npairs + 3) / 4, 256, 0, s>>>(recs, pairs, npairs, w, keys);

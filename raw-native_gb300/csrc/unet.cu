@@ -714,7 +714,8 @@ int rn_unet_create(int batch, int height, int width, uint64_t seed, uint32_t fla
     {
         std::vector<float> wh(32);
         for (auto& x : wh) x = nd(rng) * std::sqrt(1.0f / 32.0f);
-        cudaMemcpy(u->wh, wh.data(), 32 * 4, cudaMemcpyHostToDevice);
+        const cudaError_t e = cudaMemcpy(u->wh, wh.data(), 32 * 4, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return bail(cuda_fail(st, e, "unet head weights"));
     }
     u->param_count += 33;
     // tensors
@@ -1028,15 +1029,15 @@ int rn_unet_get_grads(rn_unet* u, float* host, rn_status* st) {
     for (int l = 0; l < kLayers; ++l) {
         auto& Ly = u->L[l];
         gt.resize((size_t)Ly.kpad * Ly.cout);
-        cudaMemcpy(gt.data(), Ly.gw, gt.size() * 4, cudaMemcpyDeviceToHost);
+        RN_CUDA(cudaMemcpy(gt.data(), Ly.gw, gt.size() * 4, cudaMemcpyDeviceToHost), st);
         for (int co = 0; co < Ly.cout; ++co)
             for (int k = 0; k < 9 * Ly.cin; ++k) host[o++] = gt[(size_t)k * Ly.cout + co];
-        cudaMemcpy(host + o, Ly.gb, (size_t)Ly.cout * 4, cudaMemcpyDeviceToHost);
+        RN_CUDA(cudaMemcpy(host + o, Ly.gb, (size_t)Ly.cout * 4, cudaMemcpyDeviceToHost), st);
         o += Ly.cout;
     }
-    cudaMemcpy(host + o, u->gwh, 32 * 4, cudaMemcpyDeviceToHost);
+    RN_CUDA(cudaMemcpy(host + o, u->gwh, 32 * 4, cudaMemcpyDeviceToHost), st);
     o += 32;
-    cudaMemcpy(host + o, u->gbh, 4, cudaMemcpyDeviceToHost);
+    RN_CUDA(cudaMemcpy(host + o, u->gbh, 4, cudaMemcpyDeviceToHost), st);
     return ok(st);
 }
 
