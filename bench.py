@@ -18,8 +18,13 @@ rasterized on the GPU by this library); no dataset is involved.
            counters over the whole frame, divided by the kernel's CUDA-event time
   cpu_baseline  the oracle (a C restatement of the reference's CPU path) on this host's
            cores, on every 4th row of the same frame
+  surrogate_4k  (one GPU) the surrogate-versus-plain-RT head-to-head on the 7.88M-triangle
+           scene, measured after the frame's timed region; RN_BENCH_NO_SURROGATE=1 leaves
+           this separate report out (for a launch list of the frame alone) and changes
+           nothing in the frame's measurement
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py --workload batch|large|surrogate|hybrid|build   (the other workloads)
 """
 from __future__ import annotations
 
