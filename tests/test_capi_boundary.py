@@ -146,3 +146,24 @@ def test_package_tune_file_loads(lib):
     finally:
         for k, v in saved.items():
             rn_ao.tune_set(k, v)
+
+
+def test_autotuner_file_round_trip(lib, tmp_path):
+    """A tune file the autotuner writes (every key, one line each, known values) loads back
+    as written."""
+    import rn_ao
+    import autotune
+    saved = rn_ao.tune_all()
+    try:
+        pick = {k: v[-1] for k, v in rn_ao.TUNE_KEYS.items()}
+        path = tmp_path / "tune.txt"
+        autotune.write_tune_file(str(path), pick, "test")
+        lines = [ln for ln in path.read_text().splitlines() if ln and not ln.startswith("#")]
+        assert len(lines) == len(rn_ao.TUNE_KEYS)
+        for k, v in saved.items():
+            rn_ao.tune_set(k, v)
+        rn_ao.tune_load(str(path))
+        assert rn_ao.tune_all() == pick
+    finally:
+        for k, v in saved.items():
+            rn_ao.tune_set(k, v)
