@@ -251,8 +251,11 @@ int rn_ao_trace_stats(const rn_gbuf* g, const rn_accel* accel, int spp, float ra
  * pointer (err may be NULL); work goes to `stream` (NULL = the legacy default stream) and
  * the call returns when `out` is filled. Scratch comes from a fixed 33 KiB device array in
  * the library, held on every GPU that loads it until exit; at most 2^31-1 pixels. The first
- * call on a device looks the array's address up (make it before any stream capture). Calls
- * share the array: calls that overlap on the GPU race and must be serialized. */
+ * call on a device looks the array's address up and keeps it (not valid across a
+ * cudaDeviceReset of that device: do not call it again there after a reset). No call may be
+ * made on a stream under capture: each reads its result back to host memory and synchronizes
+ * the stream. Calls share the array: calls that overlap on the GPU race and must be
+ * serialized. */
 int rn_reconcile_noalloc(const float* approx, const float* truth, const uint8_t* mask, int w, int h,
                          float tolerance, void* stream, float* err, rn_reconcile_result* out,
                          rn_status* st);

@@ -34,13 +34,25 @@ _D = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 
 
 def build(with_ref: bool | None = None) -> None:
-    """Compile the oracle (and the reference harness when the raw-native tree exists)."""
+    """Compile the oracle (and the reference harness when the raw-native tree exists: the
+    tree named by RN_REFERENCE_DIR, else the location oracle/Makefile names)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref_dir = os.environ.get("RN_REFERENCE_DIR", "/root/reference")
-    if with_ref is None:
-        with_ref = os.path.isdir(os.path.join(ref_dir, "src", "renderer"))
-    if with_ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_dir}"], check=True)
+    if with_ref is False:
+        return
+    extra = ["REF=" + os.environ["RN_REFERENCE_DIR"]] if os.environ.get("RN_REFERENCE_DIR") else []
+    subprocess.run(["make", "-s", "-C", HERE, "ref" if with_ref else "ref-if-present"] + extra, check=True)
+
+
+def reference_dir() -> str | None:
+    """The raw-native tree the reference harness was built from (RN_REFERENCE_DIR first), or
+    None where no tree is present (the GPU host)."""
+    d = os.environ.get("RN_REFERENCE_DIR")
+    if not d:
+        try:
+            d = open(os.path.join(HERE, "_ref", "reference_dir")).read().strip()
+        except OSError:
+            return None
+    return d if os.path.isdir(os.path.join(d, "src", "renderer")) else None
 
 
 _lib = None

@@ -696,8 +696,8 @@ int rn_reconcile(const float* approx, const float* truth, const uint8_t* mask, i
     void *parts = nullptr, *ro = nullptr;
     RN_TRY(ws_get(WS_PARTIALS, (size_t)nb * sizeof(RecPartial), &parts, st));
     RN_TRY(ws_get(WS_COUNTERS, sizeof(RecOut), &ro, st));
-    if (launch_reconcile(d_a, d_t, d_m, np, d_e, (RecPartial*)parts, nb, (RecOut*)ro, c.stream) != RN_OK)
-        return cuda_fail(st, cudaGetLastError(), "reconcile_kernel");
+    const cudaError_t le = launch_reconcile(d_a, d_t, d_m, np, d_e, (RecPartial*)parts, nb, (RecOut*)ro, c.stream);
+    if (le != cudaSuccess) return cuda_fail(st, le, "reconcile_kernel");
     RecOut r;
     RN_CUDA(cudaMemcpyAsync(&r, ro, sizeof r, cudaMemcpyDeviceToHost, c.stream), st);
     if (!dev) RN_TRY(copy_back(err, d_e, np, st));

@@ -63,15 +63,15 @@ int reconcile_blocks(size_t npx) {
     return (int)nb;
 }
 
-int launch_reconcile(const float* approx, const float* truth, const uint8_t* mask, size_t npx, float* err,
-                     RecPartial* partials, int nblocks, RecOut* out, cudaStream_t s) {
+cudaError_t launch_reconcile(const float* approx, const float* truth, const uint8_t* mask, size_t npx, float* err,
+                             RecPartial* partials, int nblocks, RecOut* out, cudaStream_t s) {
     const bool vec = ((uintptr_t)approx % 16 == 0) && ((uintptr_t)truth % 16 == 0) && ((uintptr_t)mask % 4 == 0) &&
                      (err == nullptr || (uintptr_t)err % 16 == 0);
     if (vec)
         reconcile_kernel<true><<<nblocks, kThreads, 0, s>>>(approx, truth, mask, npx, err, partials, out);
     else
         reconcile_kernel<false><<<nblocks, kThreads, 0, s>>>(approx, truth, mask, npx, err, partials, out);
-    return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
+    return cudaGetLastError();
 }
 
 }  // namespace rn

@@ -14,9 +14,12 @@
 // reconcile never launches more than kMaxBlocks blocks, whatever the image size) and the
 // completion counter. Host code cannot use the array's name as a device address, so each
 // device's address comes from cudaGetSymbolAddress, once per device, on that device's first
-// call (that first call must come before any stream capture). Every call shares the array:
-// the counter is cleared at each call, and calls that overlap on the GPU (two streams, or
-// two host threads) race on it and must be serialized by the caller.
+// call, and is kept for the life of the process: it is not valid across a cudaDeviceReset of
+// that device (the module and its array are loaded anew), so a process that resets a device
+// must not call this entry point on it again. No call may be made on a stream under capture:
+// it reads its result back into host memory and synchronizes the stream. Every call shares
+// the array: the counter is cleared at each call, and calls that overlap on the GPU (two
+// streams, or two host threads) race on it and must be serialized by the caller.
 #include "rn_internal.h"
 #include <cmath>
 #include <mutex>
@@ -78,8 +81,8 @@ extern "C" int rn_reconcile_noalloc(const float* approx, const float* truth, con
     RecOut* ro = (RecOut*)((char*)base + kPartialBytes);
     const cudaStream_t s = (cudaStream_t)stream;
     RN_CUDA(cudaMemsetAsync(ro, 0, sizeof(RecOut), s), st);   // the completion counter starts at zero
-    if (launch_reconcile(approx, truth, mask, np, err, parts, nb, ro, s) != RN_OK)
-        return cuda_fail(st, cudaGetLastError(), "reconcile_kernel (allocation-free)");
+    const cudaError_t le = launch_reconcile(approx, truth, mask, np, err, parts, nb, ro, s);
+    if (le != cudaSuccess) return cuda_fail(st, le, "reconcile_kernel (allocation-free)");
     RecOut r;
     RN_CUDA(cudaMemcpyAsync(&r, ro, sizeof r, cudaMemcpyDeviceToHost, s), st);
     RN_CUDA(cudaStreamSynchronize(s), st);

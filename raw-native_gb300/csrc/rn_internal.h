@@ -121,8 +121,9 @@ struct RecOut {       // the reduction's device-side result
     uint32_t done;    // blocks finished (the last block reduces, then resets it to 0)
     uint32_t pad;
 };
-int launch_reconcile(const float* approx, const float* truth, const uint8_t* mask, size_t npx,
-                     float* err, RecPartial* partials, int nblocks, RecOut* out, cudaStream_t s);
+// Returns the launch's error (read once with cudaGetLastError, so the caller reports it).
+cudaError_t launch_reconcile(const float* approx, const float* truth, const uint8_t* mask, size_t npx,
+                             float* err, RecPartial* partials, int nblocks, RecOut* out, cudaStream_t s);
 int reconcile_blocks(size_t npx);
 int launch_ssao(int w, int h, const float* pos, const float* nrm, const uint8_t* mask, int samples,
                 float radius, const uint8_t* corr, float* ao, const float* truth, float* err,

@@ -70,14 +70,18 @@ class Combined:
 
 
 def combine_reconcile(parts, tolerance: float) -> Combined:
-    """The whole frame's reconcile from its parts, summed in the order given (rank order)."""
+    """The whole frame's reconcile from its parts, summed in the order given (rank order).
+
+    With no masked pixel at all the rmse is 0 and the verdict is rmse <= tolerance, i.e. true,
+    as src/cert/reconcile.cpp:18-19 decides it (the certificate turns pixels == 0 into
+    "unverifiable" on its own, src/cert/certificate_from.cpp)."""
     total, n, mx = 0.0, 0, 0.0
     for p in parts:
         total += p.sum_sq
         n += p.pixels
         mx = max(mx, p.max_error)
     rmse = float(np.float32(math.sqrt(total / n))) if n else 0.0
-    return Combined(rmse, float(np.float32(mx)), n, bool(n > 0 and rmse <= tolerance), total)
+    return Combined(rmse, float(np.float32(mx)), n, bool(rmse <= np.float32(tolerance)), total)
 
 
 def gather_parts(part: ReconcilePart, pg=None, device=None):

@@ -73,7 +73,7 @@ def build_library(verbose: bool = False) -> str:
 def build_shim(verbose: bool = False) -> str:
     """The reference-facing C++23 shim (computeRTAO & co. over the C ABI), built stand-alone
     against host/mirror's headers with a C test API (librn_ao_shim.so). Inside a raw-native
-    build the same ao_shim.cpp compiles against the reference's headers."""
+    build the same ao_shim.cpp compiles against the reference's headers instead."""
     mirror = os.path.join(HOST, "mirror")
     srcs = [os.path.join(HOST, "ao_shim.cpp")] + sorted(
         os.path.join(mirror, f) for f in os.listdir(mirror) if f.endswith(".cpp"))

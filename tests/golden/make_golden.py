@@ -112,4 +112,7 @@ def main(ref_dir):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    _ref = sys.argv[1] if len(sys.argv) > 1 else O.reference_dir()
+    if not _ref:
+        sys.exit("usage: make_golden.py RAW_NATIVE_TREE (or set RN_REFERENCE_DIR)")
+    main(_ref)

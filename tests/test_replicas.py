@@ -53,7 +53,24 @@ def test_combined_parts_equal_the_whole_frame(oracle):
         assert c.rmse == whole["rmse"] and c.within_tolerance == whole["within"]
         assert abs(c.sum_sq - whole["sumSq"]) <= 1e-12 * whole["sumSq"]
     empty = replicas.combine_reconcile([replicas.ReconcilePart(0.0, 0, 0.0)] * 2, 0.3)
-    assert empty.pixels == 0 and not empty.within_tolerance
+    assert empty.pixels == 0 and empty.rmse == 0.0 and empty.within_tolerance
+
+
+def test_combined_verdict_equals_oracle_on_empty_partial_and_full_masks(oracle):
+    """src/cert/reconcile.cpp:18-19: with no masked pixel rmse is 0 and the verdict is true."""
+    a, t, m = _synthetic()
+    masks = {"empty": np.zeros_like(m), "partial": m, "full": np.ones_like(m)}
+    for name, mk in masks.items():
+        for tol in (0.0, 0.05, 0.3):
+            _, whole = oracle.reconcile(a, t, mk, tol)
+            parts = []
+            for r in range(3):
+                y0, y1 = replicas.row_band(a.shape[0], r, 3)
+                _, d = oracle.reconcile(a[y0:y1], t[y0:y1], np.ascontiguousarray(mk[y0:y1]), tol)
+                parts.append(replicas.ReconcilePart(d["sumSq"], d["pixels"], d["maxError"]))
+            c = replicas.combine_reconcile(parts, tol)
+            assert c.pixels == whole["pixels"], name
+            assert c.rmse == whole["rmse"] and c.within_tolerance == whole["within"], (name, tol, c, whole)
 
 
 def _free_port():

@@ -10,11 +10,13 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("RN_REFERENCE_DIR", "/root/reference")
+from oracle import oracle as _O
+
+REF = _O.reference_dir() or ""
 PKG = os.path.join(ROOT, "raw-native_gb300")
 REF_SOURCES = ["src/renderer/raster.cpp", "src/scene/scene.cpp", "src/core/arena.cpp", "src/renderer/bvh.cpp"]
 
-pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src", "renderer")),
+pytestmark = pytest.mark.skipif(not REF,
                                 reason="the raw-native tree is not on this host")
 
 
