@@ -69,3 +69,27 @@ def test_gpu_arm_fails_without_a_gpu():
                        timeout=600, cwd=ROOT)
     assert r.returncode != 0
     assert not _json_lines(r.stdout)
+
+
+def test_equal_rmse_spp_is_the_smallest_passing_integer():
+    """The head-to-head's spp rule: the smallest integer spp meeting the RMSE bar on every
+    view, found by powers of two and bisection, on monotone curves whose answer is known."""
+    sys.path.insert(0, ROOT)
+    import bench
+    for c in (0.08, 0.25, 0.2368, 0.3, 0.64, 0.02, 0.0199):
+        def worst(s, c=c):
+            return c / s ** 0.5
+        got, seen = bench.equal_rmse_spp(worst, 0.02, 16, 1024)
+        want = next(k for k in range(1, 5000) if worst(k) <= 0.02)
+        assert got == max(16, want), (c, got, want)
+        assert worst(got) <= 0.02 and len(seen) <= 20
+    got, _ = bench.equal_rmse_spp(lambda s: 1.0, 0.02, 16, 1024)     # never meets the bar: the cap
+    assert got == 1024
+
+
+def test_reference_arm_config_is_the_gpu_arms(oracle):
+    """Both arms print the same config dict (covered pixels of the 4K default view included)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    cfg = bench.frame_config(1, bench.covered_pixels_cpu())
+    assert cfg["covered_px"] == 3992795 and cfg["ao_rays_per_step"] == 3992795 * 256
