@@ -102,6 +102,19 @@ int rn_set_stream(void* stream, rn_status* st);
 /* Wait for all work queued on the library's stream. */
 int rn_synchronize(rn_status* st);
 
+/* The device the library runs on, for the reference's adapter record (rhi::AdapterInfo,
+ * raw/rhi/rhi.hpp:39-41, which raw::gpuInit fills: raw/renderer/gpu.hpp:27). Opens the
+ * context as rn_init does (RN_ERR_NO_DEVICE without a usable GPU). */
+typedef struct rn_device_desc {
+    char name[256];
+    int cc_major, cc_minor;   /* compute capability (10.3 on GB300) */
+    int sm_count;
+    int driver_version;       /* cudaDriverGetVersion: 1000 x major + 10 x minor */
+    int runtime_version;      /* cudaRuntimeGetVersion, same encoding */
+    uint64_t total_bytes;     /* device memory */
+} rn_device_desc;
+int rn_device_info(rn_device_desc* out, rn_status* st);
+
 /* Build the accelerator for `ntri` triangles (9 floats each). Replaces
  * raw::LinearAccel::build + raw::Bvh::build (src/renderer/accel.cpp:13-25,
  * src/renderer/bvh.cpp:35-92): on the GPU a PLOC binary tree (Morton codes, radix sort,

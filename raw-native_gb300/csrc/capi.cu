@@ -553,6 +553,22 @@ int rn_synchronize(rn_status* st) {
     return ok(st);
 }
 
+int rn_device_info(rn_device_desc* out, rn_status* st) {
+    if (!out) return fail(st, RN_ERR_INVALID, "null output");
+    RN_TRY(ensure_ctx(st));
+    cudaDeviceProp p;
+    RN_CUDA(cudaGetDeviceProperties(&p, ctx().device), st);
+    std::memset(out, 0, sizeof *out);
+    std::snprintf(out->name, sizeof out->name, "%s", p.name);
+    out->cc_major = p.major;
+    out->cc_minor = p.minor;
+    out->sm_count = p.multiProcessorCount;
+    out->total_bytes = (uint64_t)p.totalGlobalMem;
+    RN_CUDA(cudaDriverGetVersion(&out->driver_version), st);
+    RN_CUDA(cudaRuntimeGetVersion(&out->runtime_version), st);
+    return ok(st);
+}
+
 int rn_accel_build(const float* tris, uint32_t ntri, int flags, rn_accel** out, rn_status* st) {
     if (!out) return fail(st, RN_ERR_INVALID, "null output handle");
     *out = nullptr;

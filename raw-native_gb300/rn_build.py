@@ -75,7 +75,7 @@ def build_shim(verbose: bool = False) -> str:
     against host/mirror's headers with a C test API (librn_ao_shim.so). Inside a raw-native
     build the same ao_shim.cpp compiles against the reference's headers instead."""
     mirror = os.path.join(HOST, "mirror")
-    srcs = [os.path.join(HOST, "ao_shim.cpp")] + sorted(
+    srcs = [os.path.join(HOST, "ao_shim.cpp"), os.path.join(HOST, "gpu_shim.cpp")] + sorted(
         os.path.join(mirror, f) for f in os.listdir(mirror) if f.endswith(".cpp"))
     hdrs = [os.path.join(dp, f) for dp, _, fs in os.walk(HOST) for f in fs if f.endswith(".hpp")]
     if _stale(SHIM, srcs + hdrs + [LIB]):
