@@ -5,7 +5,7 @@ Times, on this host's cores, the reference's computeRTVisibility + computeSSAO +
 src/cert/reconcile.cpp:4-21 compiled where they lie) against the port's rno_trace + rno_ssao +
 rno_reconcile (oracle/rn_oracle.c) on the same G-buffer: the built-in scene from the CLI's
 camera, lighting model 2 (AO + sky + sun), SSAO 24 taps, tolerance 0.12. Each pass is timed
-separately, median of `reps` runs, the same thread count on both sides; the outputs are
+separately, median of `reps` alternating runs, the same thread count on both sides; the outputs are
 checked equal first. Prints one JSON object. Needs oracle/_ref (a host with the raw-native
 tree); the GPU host has none.
 
@@ -89,19 +89,22 @@ def main():
 
     assert np.array_equal(port_rec()[0], ref_rec())
 
-    def med(fn):
-        ts = []
+    def med2(fp, fr):
+        """Medians of alternating runs (port, reference, port, ...): drift of the host's clock or
+        load falls on both sides alike."""
+        tp, tr = [], []
         for _ in range(a.reps):
-            t0 = time.perf_counter()
-            fn()
-            ts.append(time.perf_counter() - t0)
-        return statistics.median(ts)
+            for fn, ts in ((fp, tp), (fr, tr)):
+                t0 = time.perf_counter()
+                fn()
+                ts.append(time.perf_counter() - t0)
+        return statistics.median(tp), statistics.median(tr)
 
     res = {"host": os.uname().machine, "threads": T, "w": w, "h": h, "spp": spp, "covered_px": covered,
            "reps": a.reps, "outputs_equal": True, "passes": {}}
     for name, fp, fr in (("visibility (AO + sky + sun)", port_trace, ref_trace), ("ssao", port_ssao, ref_ssao),
                          ("reconcile", port_rec, ref_rec)):
-        tp, tr = med(fp), med(fr)
+        tp, tr = med2(fp, fr)
         res["passes"][name] = {"port_s": tp, "reference_s": tr, "port_over_reference": tp / tr}
     tp = sum(v["port_s"] for v in res["passes"].values())
     tr = sum(v["reference_s"] for v in res["passes"].values())

@@ -36,7 +36,7 @@ EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_ac
            "rn_unet_set_clip", "rn_unet_last_grad_norm", "rn_unet_backward", "rn_unet_grad_count",
            "rn_unet_grads_flat", "rn_unet_apply",
            "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3", "rn_surrogate_ao", "rn_gtao", "rn_selftest_wait_budget",
-           "rn_render_frame")
+           "rn_render_frame", "rn_device_info")
 
 
 class RnError(RuntimeError):
@@ -48,6 +48,19 @@ class RnError(RuntimeError):
 
 class Status(C.Structure):
     _fields_ = [("code", C.c_int), ("message", C.c_char * 240)]
+
+
+class DeviceDesc(C.Structure):
+    _fields_ = [("name", C.c_char * 256), ("cc_major", C.c_int), ("cc_minor", C.c_int), ("sm_count", C.c_int),
+                ("driver_version", C.c_int), ("runtime_version", C.c_int), ("total_bytes", C.c_uint64)]
+
+
+def device_info() -> dict:
+    """rn_device_info: the device the library runs on."""
+    d, st = DeviceDesc(), Status()
+    _check(lib().rn_device_info(C.byref(d), C.byref(st)), st)
+    return dict(name=d.name.decode(), cc=(d.cc_major, d.cc_minor), sm_count=d.sm_count,
+                driver_version=d.driver_version, runtime_version=d.runtime_version, total_bytes=d.total_bytes)
 
 
 class GBuf(C.Structure):

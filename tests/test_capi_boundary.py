@@ -167,3 +167,21 @@ def test_autotuner_file_round_trip(lib, tmp_path):
     finally:
         for k, v in saved.items():
             rn_ao.tune_set(k, v)
+
+
+@pytest.mark.skipif(_cuda_present(), reason="checks the behaviour without a GPU")
+def test_device_info_and_gpu_renderer_without_a_device(lib):
+    """rn_device_info and raw::gpuInit / raw::renderGpu (gpu_shim.cpp, through the stand-alone
+    shim build) report no device instead of answering: gpu_run.cpp then exits 4."""
+    import rn_ao
+    with pytest.raises(rn_ao.RnError) as e:
+        rn_ao.device_info()
+    assert e.value.code == 2
+    import rn_build
+    shim = C.CDLL(rn_build.build_shim())
+    msg = C.create_string_buffer(512)
+    z = np.zeros(64, np.float32)
+    p = z.ctypes.data_as(C.c_void_p)
+    args = [8, 8, p, p, p, p, p, 0, None, 1, 2, C.c_float(0.12), 0] + [None] * 14 + [None, 0, msg, 512]
+    assert shim.shim_render_gpu(*args) == -1
+    assert msg.value.startswith(b"gpuInit: ")
