@@ -40,7 +40,8 @@ def build(with_ref: bool | None = None) -> None:
     if with_ref is False:
         return
     extra = ["REF=" + os.environ["RN_REFERENCE_DIR"]] if os.environ.get("RN_REFERENCE_DIR") else []
-    subprocess.run(["make", "-s", "-C", HERE, "ref" if with_ref else "ref-if-present"] + extra, check=True)
+    jobs = "-j%d" % (os.cpu_count() or 4)
+    subprocess.run(["make", "-s", jobs, "-C", HERE, "ref" if with_ref else "ref-if-present"] + extra, check=True)
 
 
 def reference_dir() -> str | None:
@@ -388,3 +389,104 @@ def render_default(w, h, cam=DEFAULT_CAMERA, spp=RT_SAMPLES, radius=AO_RADIUS, s
     err, st = reconcile(ss, ao, mask, tolerance)
     return dict(tris=tris, pos=pos, nrm=nrm, mask=mask, ao=ao, sky=sky, sun=sun, ss=ss, err=err, stats=st,
                 light=light)
+
+
+# ---------------------------------------------------------------- path tracer (raw::rt, interface v4)
+PT_FLOATS = 64 * 128 * 2 + 128 * 2          # the lobe's energy table (rt_pt_math.hpp:86-90)
+PT_CONTROLS = dict(drop_lambert_cosine=1, mis_weight_one=2, aov_drop_specular_indirect=4,
+                   aov_emission_to_diffuse=8, legacy_lobe_v2=16)
+PT_AOVS = (("radiance", 3, np.float32), ("albedo", 3, np.float32), ("normal", 3, np.float32),
+           ("depth", 1, np.float32), ("variance", 1, np.float32), ("triangle", 1, np.int32),
+           ("motion", 2, np.float32), ("diffuse", 3, np.float32), ("specular", 3, np.float32),
+           ("emission", 3, np.float32), ("diffuse_albedo", 3, np.float32), ("specular_albedo", 3, np.float32),
+           ("diffuse_variance", 1, np.float32), ("specular_variance", 1, np.float32))
+
+
+class PtSceneC(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("nrm", C.c_void_p), ("uv", C.c_void_p), ("nvert", C.c_uint32),
+                ("idx", C.c_void_p), ("tri_tex", C.c_void_p), ("ntri", C.c_uint32),
+                ("tex_entries", C.c_void_p), ("ntex", C.c_uint32), ("texels", C.c_void_p), ("ntexels", C.c_uint32),
+                ("materials", C.c_void_p), ("sun_dir", C.c_float * 3), ("sun_irr", C.c_float * 3),
+                ("sky", C.c_float * 3)]
+
+
+class PtDescC(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("spp", C.c_uint32), ("spp_begin", C.c_uint32), ("max_bounces", C.c_uint32),
+                ("width", C.c_int32), ("height", C.c_int32), ("camera", C.c_float * 10), ("previous", C.c_float * 10),
+                ("jitter", C.c_int32), ("rr", C.c_int32), ("controls", C.c_uint32)]
+
+
+class PtOutC(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name, _, _ in PT_AOVS]
+
+
+def pt_scene_struct(sc: dict):
+    """A path-tracer scene dict (pos (n,3), nrm (n,3), uv (n,2), idx (t,3) u32, tri_tex (t,) u32,
+    tex_entries (k,3) u32, texels u32, materials (k,7), sun_dir, sun_irr, sky) as the C struct;
+    returns (struct, the arrays it points into)."""
+    keep = dict(pos=_f32(sc["pos"]), nrm=_f32(sc["nrm"]), uv=_f32(sc["uv"]),
+                idx=np.ascontiguousarray(sc["idx"], np.uint32), tri_tex=np.ascontiguousarray(sc["tri_tex"], np.uint32),
+                tex_entries=np.ascontiguousarray(sc["tex_entries"], np.uint32),
+                texels=np.ascontiguousarray(sc["texels"], np.uint32), materials=_f32(sc["materials"]))
+    s = PtSceneC(_ptr(keep["pos"]), _ptr(keep["nrm"]), _ptr(keep["uv"]), keep["pos"].size // 3,
+                 _ptr(keep["idx"]), _ptr(keep["tri_tex"]), keep["tri_tex"].size, _ptr(keep["tex_entries"]),
+                 keep["tex_entries"].size // 3, _ptr(keep["texels"]), keep["texels"].size, _ptr(keep["materials"]),
+                 (C.c_float * 3)(*sc["sun_dir"]), (C.c_float * 3)(*sc["sun_irr"]), (C.c_float * 3)(*sc["sky"]))
+    return s, keep
+
+
+def pt_desc_struct(d: dict):
+    controls = 0
+    for k in d.get("controls", ()):
+        controls |= PT_CONTROLS[k]
+    return PtDescC(int(d.get("seed", 1)), int(d.get("spp", 16)), int(d.get("spp_begin", 0)),
+                   int(d.get("max_bounces", 64)), int(d["width"]), int(d["height"]), (C.c_float * 10)(*d["camera"]),
+                   (C.c_float * 10)(*d.get("previous", d["camera"])), int(d.get("jitter", True)),
+                   int(d.get("russian_roulette", True)), controls)
+
+
+def pt_energy_table(threads=None, use_ref=False):
+    t = np.zeros(PT_FLOATS, np.float32)
+    if use_ref:
+        ref().ref_pt_energy_table(t.ctypes.data_as(C.c_void_p))
+    else:
+        lib().rno_pt_energy_table(t.ctypes.data_as(C.c_void_p), int(threads or os.cpu_count() or 1))
+    return t
+
+
+def pathtrace(scene: dict, desc: dict, threads=None, use_ref=False, table=None):
+    """raw::rt::pathTraceCpu of a v2 scene: a dict of every AOV ((h, w[, k]) arrays) and the
+    emitter count. use_ref runs the reference's own build (oracle/_ref)."""
+    s, keep = pt_scene_struct(scene)
+    d = pt_desc_struct(desc)
+    h, w = int(desc["height"]), int(desc["width"])
+    outs = {name: np.zeros((h, w, k) if k > 1 else (h, w), dt) for name, k, dt in PT_AOVS}
+    o = PtOutC(*[_ptr(outs[name]) for name, _, _ in PT_AOVS])
+    T = int(threads or os.cpu_count() or 1)
+    if use_ref:
+        n = ref().ref_pathtrace(C.byref(s), C.byref(d), T, C.byref(o))
+    else:
+        tab = None if table is None else np.ascontiguousarray(table, np.float32)
+        n = lib().rno_pathtrace(C.byref(s), C.byref(d), _ptr(tab), T, C.byref(o))
+    outs["emitters"] = n
+    return outs
+
+
+def pt_reference_scene(name: str, emission=1.0, albedo=0.5, material=None, sky=(1.0, 1.0, 1.0)):
+    """The reference's own lit scene by name (retro_room, iso_street, dense_block, furnace,
+    white_plane) from its build (oracle/_ref): (scene dict, camera 10 floats)."""
+    R = ref()
+    counts = (C.c_uint32 * 5)()
+    mat7 = np.asarray(material if material is not None else (1.0, 0.8, 0.0, 0.5, 0, 0, 0), np.float32)
+    sky3 = np.asarray(sky, np.float32)
+    args = [name.encode(), C.c_float(emission), C.c_float(albedo), _ptr(mat7), _ptr(sky3), counts]
+    assert R.ref_pt_scene(*args, *([None] * 10)) == 0, name
+    nv, nt, nk, nx = counts[0], counts[1], counts[2], counts[3]
+    sc = dict(pos=np.zeros((nv, 3), np.float32), nrm=np.zeros((nv, 3), np.float32), uv=np.zeros((nv, 2), np.float32),
+              idx=np.zeros((nt, 3), np.uint32), tri_tex=np.zeros(nt, np.uint32), tex_entries=np.zeros((nk, 3), np.uint32),
+              texels=np.zeros(nx, np.uint32), materials=np.zeros((nk, 7), np.float32))
+    light9, cam10 = np.zeros(9, np.float32), np.zeros(10, np.float32)
+    R.ref_pt_scene(*args, *[_ptr(sc[k]) for k in ("pos", "nrm", "uv", "idx", "tri_tex", "tex_entries", "texels",
+                                                    "materials")], _ptr(light9), _ptr(cam10))
+    sc.update(sun_dir=light9[0:3].copy(), sun_irr=light9[3:6].copy(), sky=light9[6:9].copy())
+    return sc, cam10

@@ -1013,3 +1013,7 @@ RNO_API void rno_gtao(int w, int h, const float* vpos, const float* vnrm, const 
             out[i] = sum / slices;
         }
 }
+
+/* ------------------------------------------------------------------ the path tracer
+ * raw::rt::pathTraceCpu (interface v4, v2 scenes): in its own file, built into this library. */
+#include "rn_oracle_pt.c"
