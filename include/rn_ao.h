@@ -354,6 +354,8 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *   accel_leaf_small  1 | 2 | 4 | 8  ... below 65,536 triangles
  *   frame_direct      0 | 1          rn_ao_frame on pinned, mapped host buffers without copies
  *   hybrid_min_blocks 5 | 6 | 8      resident rn_hybrid blocks per SM (register budget)
+ *   pt_slice          0|1|4|16       rn_pathtrace: samples traced per slice at most (0: as many
+ *                                    as 2 GiB of per-sample terms hold)
  * Process-wide; RN_TUNE_<KEY> environment variables apply before the first call.
  * rn_tune_load reads "key = value" lines ('#' comments), all or nothing. */
 int rn_tune_set(const char* key, int value, rn_status* st);
@@ -450,6 +452,94 @@ typedef struct rn_surrogate_stats {
 int rn_surrogate_ao(rn_unet* net, const rn_gbuf* g, const float* depth, const rn_accel* accel, int spp_full,
                     float radius, float k, float* ao, float* ao4, float* pred, uint8_t* tile_flags,
                     rn_surrogate_stats* stats, rn_status* st);
+
+/* ------------------------------------------------------------------ path tracer
+ * raw-native's path tracer, interface v4 (raw/renderer/rt_pathtrace.hpp), for scenes that set
+ * no v3 field: the v4 lobe (Lambert base under GGX with height-correlated Smith, Schlick
+ * Fresnel and Kulla-Conty multiple scattering, weighted by the float64-built energy table of
+ * src/renderer/rt_pt_energy.cpp), next-event estimation for the sun and for emissive
+ * triangles with MIS, Russian roulette after bounce 3, and every AOV, each equal to
+ * raw::rt::pathTraceCpu's (src/renderer/rt_pt_cpu.cpp) bit for bit for the same scene and
+ * description: counter-based random numbers, the CPU's float32 operation order, the host
+ * libm's cos/sin bits and the moments in float64. Scenes with v3 fields (punctual lights,
+ * an environment, full glTF materials) are CPU-only in the reference too. */
+typedef struct rn_pt_material {   /* raw::rt::PtMaterial (rt_pathtrace.hpp:43-49) */
+    float base_factor;            /* base colour = texel / 255 x base_factor */
+    float roughness;              /* GGX alpha = roughness^2 */
+    float metallic;
+    float specular;               /* scales the dielectric F0 of 0.04; 0: pure Lambert */
+    float emission[3];            /* two-sided radiance */
+} rn_pt_material;
+/* The scene as raw::rt::PtScene holds it (swr::Geometry, swr::TextureSet, one material per
+ * texture id, sun and sky; rt_pathtrace.hpp:50-63): vertex positions, normals and uvs;
+ * three vertex indices and one texture id a triangle; per texture its texel offset, width
+ * and height (powers of two), RGBA8 texels with red in the low byte. HOST pointers. */
+typedef struct rn_pt_scene_desc {
+    const float* pos;             /* 3 a vertex */
+    const float* nrm;             /* 3 a vertex */
+    const float* uv;              /* 2 a vertex */
+    uint32_t nvert;
+    const uint32_t* idx;          /* 3 a triangle */
+    const uint32_t* tri_texture;  /* 1 a triangle */
+    uint32_t ntri;
+    const uint32_t* tex_entries;  /* offset, width, height a texture */
+    uint32_t ntex;
+    const uint32_t* texels;
+    uint32_t ntexels;
+    const rn_pt_material* materials;   /* ntex of them */
+    float sun_dir[3];             /* toward the sun; normalized by the tracer */
+    float sun_irradiance[3];      /* 0: no sun */
+    float sky[3];                 /* constant radiance on escape */
+} rn_pt_scene_desc;
+typedef struct rn_ptscene rn_ptscene;
+/* raw::rt::finishPtScene (src/renderer/rt_pt_scene.cpp:31-45) on the GPU: the scene copied to
+ * the device, its triangle list's accelerator (rn_accel_build), the emitter list and its
+ * inclusive area CDF (float, in triangle order, formed on the host as the reference forms it),
+ * and the lobe's energy table (built once per process on the host in float64, the
+ * reference's construction, then kept on the device). */
+int rn_pt_scene_create(const rn_pt_scene_desc* scene, rn_ptscene** out, rn_status* st);
+void rn_pt_scene_free(rn_ptscene* scene);
+/* Emitter count and total emitter area of a scene (finishPtScene's emitters / emitterArea). */
+int rn_pt_scene_info(const rn_ptscene* scene, uint32_t* emitters, float* emitter_area, rn_status* st);
+
+#define RN_PT_DROP_LAMBERT_COSINE     0x01   /* raw::rt::PtControls (rt_pathtrace.hpp:72-80) */
+#define RN_PT_MIS_WEIGHT_ONE          0x02
+#define RN_PT_AOV_DROP_SPECULAR_INDIRECT 0x04
+#define RN_PT_AOV_EMISSION_TO_DIFFUSE 0x08
+#define RN_PT_LEGACY_LOBE_V2          0x10
+/* raw::rt::PathTraceDesc (rt_pathtrace.hpp:82-92). Cameras: eye(3), target(3), up(3), fovy. */
+typedef struct rn_pt_desc {
+    uint64_t seed;
+    uint32_t spp, spp_begin, max_bounces;
+    int32_t width, height;
+    float camera[10];
+    float previous[10];           /* for motion; equal to camera for a still frame */
+    int32_t jitter;
+    int32_t russian_roulette;
+    uint32_t controls;            /* RN_PT_* */
+} rn_pt_desc;
+/* raw::rt::PathTraceOutput's planes (rt_pathtrace.hpp:94-104); any may be NULL. */
+typedef struct rn_pt_out {
+    float* radiance;              /* 3 a pixel */
+    float* albedo;                /* 3 */
+    float* normal;                /* 3 */
+    float* depth;                 /* 1 */
+    float* variance;              /* 1 */
+    int32_t* triangle;            /* 1 */
+    float* motion;                /* 2 */
+    float* diffuse;               /* 3 */
+    float* specular;              /* 3 */
+    float* emission;              /* 3 */
+    float* diffuse_albedo;        /* 3 */
+    float* specular_albedo;       /* 3 */
+    float* diffuse_variance;      /* 1 */
+    float* specular_variance;     /* 1 */
+} rn_pt_out;
+/* raw::rt::pathTraceCpu / raw::gpu_check::pathTraceGpu (rt_pathtrace.hpp:135-136,
+ * rt_pt_gpu.hpp:13) on the GPU. Output planes are host pointers unless flags has
+ * RN_DEVICE_PTRS. Samples are traced in parallel and summed per pixel in sample order, so
+ * the result is pathTraceCpu's for any launch shape. */
+int rn_pathtrace(const rn_ptscene* scene, const rn_pt_desc* desc, int flags, rn_pt_out* out, rn_status* st);
 
 #ifdef __cplusplus
 }  /* extern "C" */

@@ -127,6 +127,7 @@ const TuneKey kTuneKeys[] = {
     {"accel_leaf_small", "RN_TUNE_ACCEL_LEAF_SMALL", &Tune::accel_leaf_small, {1, 2, 4, 8}, 4},
     {"frame_direct", "RN_TUNE_FRAME_DIRECT", &Tune::frame_direct, {0, 1}, 2},
     {"hybrid_min_blocks", "RN_TUNE_HYBRID_MIN_BLOCKS", &Tune::hybrid_min_blocks, {5, 6, 8}, 3},
+    {"pt_slice", "RN_TUNE_PT_SLICE", &Tune::pt_slice, {0, 1, 4, 16}, 4},
 };
 
 const TuneKey* find_tune_key(const char* name) {

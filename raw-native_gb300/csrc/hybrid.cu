@@ -20,72 +20,6 @@ namespace {
 
 using namespace trace_dev;
 
-// The nearest hit of ray (o, d) below tmax: returns the triangle index (input order) or -1,
-// and its t.
-__device__ int walk_closest(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, const v3& o,
-                            const v3& d, float tmax, float& t_hit, uint32_t* err) {
-    const Inv iv = make_inv(o, d);
-    const WRay wr = make_wray(o, d);
-    float best = tmax;
-    int best_tri = -1;
-    int32_t stack[kStack];
-    int sp = 0;
-    int32_t cur = 0;
-    for (uint32_t guard = 0; guard < kGuard; ++guard) {
-        const float4* q = reinterpret_cast<const float4*>(nodes + cur);
-        const float4 lx = __ldg(q + 0), hx = __ldg(q + 1), ly = __ldg(q + 2), hy = __ldg(q + 3);
-        const float4 lz = __ldg(q + 4), hz = __ldg(q + 5);
-        const int4 ch = __ldg(reinterpret_cast<const int4*>(q + 6));
-        const int cnt = __ldg(reinterpret_cast<const int*>(q + 7));
-        const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
-        const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
-        const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
-        const int32_t CH[4] = {ch.x, ch.y, ch.z, ch.w};
-        // interior children that the ray enters before `best`, nearest first
-        int32_t kid[4];
-        float kt[4];
-        int nk = 0;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            float tn;
-            if (k >= cnt || !slab(LX[k], HX[k], LY[k], HY[k], LZ[k], HZ[k], o, iv, best, tn)) continue;
-            const int32_t c = CH[k];
-            if (c < 0) {
-                const uint32_t u = (uint32_t)~c;
-                const uint32_t first = u >> 3, count = (u & 7u) + 1u;
-                for (uint32_t i = 0; i < count; ++i) {
-                    const float4* tq = reinterpret_cast<const float4*>(tris + first + i);
-                    const float4 A = __ldg(tq), B = __ldg(tq + 1), C = __ldg(tq + 2);
-                    float t;
-                    if (!hit_tri(wr, mk(A.x, A.y, A.z), mk(B.x, B.y, B.z), mk(C.x, C.y, C.z), t)) continue;
-                    const int id = __float_as_int(A.w);
-                    if (t < best || (best_tri >= 0 && t == best && id < best_tri)) {
-                        best = t;
-                        best_tri = id;
-                    }
-                }
-                continue;
-            }
-            int j = nk++;
-            while (j > 0 && kt[j - 1] < tn) { kt[j] = kt[j - 1]; kid[j] = kid[j - 1]; --j; }
-            kt[j] = tn;
-            kid[j] = c;
-        }
-        // push the farther children, descend into the nearest
-        for (int j = 0; j + 1 < nk; ++j) {
-            if (sp >= kStack) { atomicOr(err, DEV_STACK_OVERFLOW); t_hit = best; return best_tri; }
-            stack[sp++] = kid[j];
-        }
-        if (nk > 0) { cur = kid[nk - 1]; continue; }
-        // pop the next pushed node: its children meet the best hit found since
-        if (sp == 0) { t_hit = best; return best_tri; }
-        cur = stack[--sp];
-    }
-    atomicOr(err, DEV_GUARD);
-    t_hit = best;
-    return best_tri;
-}
-
 __global__ void closest_kernel(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, int has_geometry,
                                const float* __restrict__ rays, const float* __restrict__ tmax, uint32_t n,
                                int32_t* __restrict__ tri, float* __restrict__ t_out, uint32_t* err) {

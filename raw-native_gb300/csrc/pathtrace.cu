@@ -1,0 +1,928 @@
+// pathtrace.cu -- raw-native's path tracer (interface v4, v2 scenes) on the GPU, bit for bit.
+//
+// The reference: raw::rt::pathTraceCpu (src/renderer/rt_pt_cpu.cpp) over the scene queries
+// and next-event estimation of src/renderer/rt_pt_ctx.hpp and the random numbers and lobe of
+// src/renderer/rt_pt_math.hpp; its GPU counterpart is raw::gpu_check::pathTraceGpu
+// (raw/renderer/rt_pt_gpu.hpp, a WGSL pass), judged there only statistically. Here every
+// AOV equals the CPU's bytes:
+//   - every float32 operation is the CPU's, in its order, one rounding each (the explicit
+//     round-to-nearest intrinsics of rn_device.cuh; no contraction);
+//   - the sampler angles 2 pi u (u = k / 2^24 from PCG2D) take their cos and sin from the
+//     device function plus the host libm's correction table (the AO sampler's: the same
+//     2^24 angles);
+//   - the closest hit is rt::closest's (nearest t, ties to the lowest triangle index; the
+//     4-wide walk of trace_device.cuh) and visibility its any-hit answer;
+//   - the lobe's energy table is built on the host in float64 exactly as
+//     src/renderer/rt_pt_energy.cpp builds it, then read on the device;
+//   - per pixel the samples are summed in sample order and the moments kept in float64.
+//
+// Work: samples of a slice are traced in parallel, one thread per (pixel, sample), a warp
+// on an 8 x 4 pixel tile for one sample index (coherent primary rays); each sample's eight
+// colour terms go to a slice buffer, and a second kernel adds them per pixel in sample
+// order into running sums that persist across slices (the CPU's loop order, so any slice
+// size gives the same bits). The last slice's pass also scales the sums, forms the
+// variances and traces the pixel-centre ray (depth, triangle, motion).
+#include "rn_internal.h"
+#include "rn_device.cuh"
+#include "trace_device.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+struct rn_ptscene {
+    int device = -1;
+    uint32_t nvert = 0, ntri = 0, ntex = 0, ntexels = 0, nemit = 0;
+    float area = 0.0f;
+    float sun_dir[3] = {0, 0, 0}, sun_irr[3] = {0, 0, 0}, sky[3] = {0, 0, 0};
+    void* block = nullptr;     // one device allocation holding every array below
+    float* nrm = nullptr;      // 3 a vertex
+    float* uv = nullptr;       // 2 a vertex
+    uint32_t* idx = nullptr;   // 3 a triangle
+    uint32_t* tritex = nullptr;
+    uint32_t* texent = nullptr;
+    uint32_t* texels = nullptr;
+    float* mat = nullptr;      // 7 a texture
+    float* tris = nullptr;     // 9 a triangle, input order (trianglesOf)
+    uint32_t* emit = nullptr;
+    float* cdf = nullptr;
+    rn_accel* accel = nullptr;
+};
+
+namespace rn {
+namespace {
+
+using namespace trace_dev;
+
+constexpr int kMu = 64, kRough = 128;
+constexpr int kNodes = kMu * kRough * 2, kTableFloats = kNodes + kRough * 2;
+constexpr float kPiF = 3.14159265f;
+
+// ================================================================ the energy table (host, float64)
+// src/renderer/rt_pt_energy.cpp:11-40 with the split albedo of src/renderer/pbr_tables.cpp:23-50
+// and the Gauss-Legendre nodes of src/renderer/brdf.cpp:95-109. Host code is built without
+// contraction (-ffp-contract=off), as the reference's is.
+constexpr double kPiD = 3.14159265358979323846;
+
+double radical_inverse(uint32_t b) {
+    b = (b << 16) | (b >> 16);
+    b = ((b & 0x55555555u) << 1) | ((b & 0xAAAAAAAAu) >> 1);
+    b = ((b & 0x33333333u) << 2) | ((b & 0xCCCCCCCCu) >> 2);
+    b = ((b & 0x0F0F0F0Fu) << 4) | ((b & 0xF0F0F0F0u) >> 4);
+    b = ((b & 0x00FF00FFu) << 8) | ((b & 0xFF00FF00u) >> 8);
+    return b * 2.3283064365386963e-10;
+}
+double lambda_d(double mu, double a) {
+    const double m2 = mu * mu;
+    return 0.5 * (-1.0 + std::sqrt(1.0 + a * a * (1.0 - m2) / m2));
+}
+void albedo_split(double mu, double a, int n, double& outA, double& outB) {
+    const double vx = std::sqrt(std::max(0.0, 1.0 - mu * mu)), vy = 0.0, vz = mu;
+    const double hx = a * vx, hz = vz;
+    const double lv = std::sqrt(hx * hx + hz * hz);
+    const double nx = hx / lv, ny = 0.0, nz = hz / lv;
+    const double t1x = 0.0, t1y = 1.0, t1z = 0.0;
+    const double t2x = ny * t1z - nz * t1y, t2y = nz * t1x - nx * t1z, t2z = nx * t1y - ny * t1x;
+    const double g1 = 1.0 / (1.0 + lambda_d(mu, a));
+    double sa = 0.0, sb = 0.0;
+    for (int k = 0; k < n; ++k) {
+        const double u1 = (k + 0.5) / n, u2 = radical_inverse((uint32_t)k);
+        const double r = std::sqrt(u1), phi = 2.0 * kPiD * u2, s = 0.5 * (1.0 + nz);
+        const double p1 = r * std::cos(phi), p2 = (1.0 - s) * std::sqrt(1.0 - p1 * p1) + s * r * std::sin(phi);
+        const double p3 = std::sqrt(std::max(0.0, 1.0 - p1 * p1 - p2 * p2));
+        double mx = t1x * p1 + t2x * p2 + nx * p3, my = t1y * p1 + t2y * p2 + ny * p3, mz = t1z * p1 + t2z * p2 + nz * p3;
+        mx = a * mx; my = a * my; mz = std::max(1e-12, mz);
+        const double lm = std::sqrt(mx * mx + my * my + mz * mz);
+        mx = mx / lm; my = my / lm; mz = mz / lm;
+        const double vom = vx * mx + vy * my + vz * mz, li = 2.0 * vom * mz - vz;
+        if (li <= 0.0) continue;
+        const double w = (1.0 / (1.0 + lambda_d(mu, a) + lambda_d(li, a))) / g1;
+        const double c = 1.0 - vom, c5 = c * c * c * c * c;
+        sa += w * (1.0 - c5); sb += w * c5;
+    }
+    outA = sa / n; outB = sb / n;
+}
+void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w) {
+    x.assign(n, 0.0); w.assign(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        double z = std::cos(kPiD * (i + 0.75) / (n + 0.5)), pp = 0.0;
+        for (int it = 0; it < 100; ++it) {
+            double p1 = 1.0, p2 = 0.0;
+            for (int j = 1; j <= n; ++j) { const double p3 = p2; p2 = p1; p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j; }
+            pp = n * (z * p1 - p2) / (z * z - 1.0);
+            const double z1 = z;
+            z = z1 - p1 / pp;
+            if (std::fabs(z - z1) < 1e-15) break;
+        }
+        x[i] = 0.5 * (1.0 - z); w[i] = 1.0 / ((1.0 - z * z) * pp * pp);
+    }
+}
+// rt_pt_math.hpp:93-107 on the host (the means are formed from the float table as read).
+void table_ab_host(const float* t, float mu, float rough, float& A, float& B) {
+    const float x = std::sqrt(std::clamp(mu, 0.0f, 1.0f)) * float(kMu - 1), y = std::clamp(rough, 0.0f, 1.0f) * float(kRough - 1);
+    const int x0 = std::min(int(x), kMu - 2), y0 = std::min(int(y), kRough - 2);
+    const float fx = x - float(x0), fy = y - float(y0);
+    const float* p = t + (std::size_t(y0) * kMu + std::size_t(x0)) * 2;
+    const float* q = p + std::size_t(kMu) * 2;
+    const float a0 = p[0] * (1.0f - fx) + p[2] * fx, b0 = p[1] * (1.0f - fx) + p[3] * fx;
+    const float a1 = q[0] * (1.0f - fx) + q[2] * fx, b1 = q[1] * (1.0f - fx) + q[3] * fx;
+    A = a0 * (1.0f - fy) + a1 * fy; B = b0 * (1.0f - fy) + b1 * fy;
+}
+const std::vector<float>& energy_table_host() {
+    static std::vector<float> t;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        t.assign(kTableFloats, 0.0f);
+        // rows are independent and each is written by one thread: identical for any count
+        const int threads = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        for (int th = 0; th < threads; ++th)
+            pool.emplace_back([th, threads] {
+                for (int i = th; i < kRough; i += threads) {
+                    const double r = double(i) / (kRough - 1), a = std::max(1e-4, r * r);
+                    for (int j = 0; j < kMu; ++j) {
+                        const double u = double(j) / (kMu - 1), mu = std::max(u * u, 1e-4);
+                        double A = 0.0, B = 0.0;
+                        albedo_split(mu, a, 1 << 12, A, B);
+                        t[(std::size_t(i) * kMu + std::size_t(j)) * 2] = float(A);
+                        t[(std::size_t(i) * kMu + std::size_t(j)) * 2 + 1] = float(B);
+                    }
+                }
+            });
+        for (auto& p : pool) p.join();
+        std::vector<double> x, w;
+        gauss_legendre01(64, x, w);
+        for (int i = 0; i < kRough; ++i) {
+            const float r = float(i) / float(kRough - 1);
+            double sa = 0.0, sb = 0.0;
+            for (std::size_t k = 0; k < x.size(); ++k) {
+                float A, B;
+                table_ab_host(t.data(), float(x[k]), r, A, B);
+                sa += w[k] * double(A) * x[k]; sb += w[k] * double(B) * x[k];
+            }
+            t[kNodes + std::size_t(i) * 2] = float(2.0 * sa);
+            t[kNodes + std::size_t(i) * 2 + 1] = float(2.0 * sb);
+        }
+    });
+    return t;
+}
+// The table on each device, uploaded once (held until the process exits).
+std::mutex g_table_mutex;
+float* g_table_dev[64] = {};
+int device_table(int dev, const float** out, rn_status* st) {
+    if (dev < 0 || dev >= 64) return fail(st, RN_ERR_STATE, "device ordinal %d", dev);
+    const std::vector<float>& t = energy_table_host();
+    std::lock_guard<std::mutex> lock(g_table_mutex);
+    if (!g_table_dev[dev]) {
+        void* p = nullptr;
+        RN_CUDA(cudaMalloc(&p, t.size() * sizeof(float)), st);
+        const cudaError_t e = cudaMemcpy(p, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) { cudaFree(p); return cuda_fail(st, e, "energy table upload"); }
+        g_table_dev[dev] = (float*)p;
+    }
+    *out = g_table_dev[dev];
+    return RN_OK;
+}
+
+// ================================================================ host vector math (camera)
+struct hv3 { float x, y, z; };
+hv3 hsub(hv3 a, hv3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+float hdot(hv3 a, hv3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+hv3 hcross(hv3 a, hv3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+hv3 hnorm(hv3 v) {
+    const float l = std::sqrt(hdot(v, v));
+    if (!(l > 0.0f)) return v;
+    const float s = 1.0f / l;
+    return {v.x * s, v.y * s, v.z * s};
+}
+
+// ================================================================ device
+struct PtCam { v3 eye, f, s, u; float th, aspect; };
+
+// rt_pt_cpu.cpp:14-20 on the host (std::tan of a float: the host libm's tanf).
+PtCam cam_of(const float* c, int w, int h) {
+    PtCam k;
+    const hv3 eye{c[0], c[1], c[2]}, tgt{c[3], c[4], c[5]}, up{c[6], c[7], c[8]};
+    const hv3 f = hnorm(hsub(tgt, eye)), s = hnorm(hcross(f, up)), u = hcross(s, f);
+    k.eye = v3{eye.x, eye.y, eye.z};
+    k.f = v3{f.x, f.y, f.z}; k.s = v3{s.x, s.y, s.z}; k.u = v3{u.x, u.y, u.z};
+    k.th = std::tan(c[9] * 0.5f);
+    k.aspect = float(w) / float(h);
+    return k;
+}
+
+struct PtParams {
+    const Node4* nodes;
+    const LeafTri* ltris;
+    int has_geometry;
+    const float* tris;        // 9 a triangle, input order
+    const float* nrm;
+    const float* uv;
+    const uint32_t* idx;
+    const uint32_t* tritex;
+    const uint32_t* texent;
+    const uint32_t* texels;
+    const float* mat;         // 7 a texture
+    const uint32_t* emit;
+    const float* cdf;
+    uint32_t nemit;
+    float area;
+    const float* table;
+    const uint8_t* corr;
+    v3 sun_dir, sun_irr, sky;
+    uint32_t seed_lo, seed_hi, spp, spp_begin, max_bounces, controls;
+    int w, h, jitter, rr;
+    PtCam cam, prev;
+    uint32_t k0, kn;          // this slice: samples [k0, k0 + kn) of the pixel's spp
+    uint32_t npix;
+    float* samp;              // kSampleFloats x kn x npix (component-major)
+    float* acc;               // kAccFloats x npix running sums (component-major)
+    double* mom;              // 6 x npix running moments
+    int first, last;          // slice flags
+    uint32_t* err;
+};
+constexpr int kSampleFloats = 24;   // L, D, S, E, alb, nrm, dAlb, sAlb
+
+// ---------------------------------------------------------------- random numbers (rt_pt_math.hpp:18-35)
+struct R2 { float a, b; uint32_t ka, kb; };
+__device__ __forceinline__ R2 rand2(const PtParams& P, uint32_t pixel, uint32_t sample, uint32_t dim) {
+    uint32_t x = pixel ^ (P.seed_lo * 0x9E3779B9u), y = (sample * 64u + dim) ^ P.seed_hi;
+    x = x * 1664525u + 1013904223u; y = y * 1664525u + 1013904223u;
+    x += y * 1664525u; y += x * 1664525u;
+    x ^= x >> 16; y ^= y >> 16;
+    x += y * 1664525u; y += x * 1664525u;
+    x ^= x >> 16; y ^= y >> 16;
+    R2 r;
+    r.ka = x >> 8; r.kb = y >> 8;
+    r.a = unit24(r.ka); r.b = unit24(r.kb);   // float(k) x 5.96046448e-8f = k / 2^24 exactly
+    return r;
+}
+
+// ---------------------------------------------------------------- small float helpers
+__device__ __forceinline__ v3 mulv(v3 a, v3 b) { return mk(fmul(a.x, b.x), fmul(a.y, b.y), fmul(a.z, b.z)); }
+__device__ __forceinline__ float maxc(v3 a) { return smax(a.x, smax(a.y, a.z)); }
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return (v < lo) ? lo : (hi < v) ? hi : v; }
+__device__ __forceinline__ float lum(v3 c) { return fadd(fadd(fmul(0.2126f, c.x), fmul(0.7152f, c.y)), fmul(0.0722f, c.z)); }
+
+struct Frame { v3 t, b, n; };
+// Duff et al. 2017 (rt_pt_math.hpp:38-42)
+__device__ __forceinline__ Frame basis(v3 n) {
+    const float s = n.z >= 0.0f ? 1.0f : -1.0f;
+    const float a = fdiv(-1.0f, fadd(s, n.z)), c = fmul(fmul(n.x, n.y), a);
+    Frame f;
+    f.t = mk(fadd(1.0f, fmul(fmul(fmul(s, n.x), n.x), a)), fmul(s, c), -fmul(s, n.x));
+    f.b = mk(c, fadd(s, fmul(fmul(n.y, n.y), a)), -n.y);
+    f.n = n;
+    return f;
+}
+__device__ __forceinline__ v3 to_local(const Frame& f, v3 v) { return mk(dot(v, f.t), dot(v, f.b), dot(v, f.n)); }
+__device__ __forceinline__ v3 to_world(const Frame& f, v3 v) { return add(add(scale(f.t, v.x), scale(f.b, v.y)), scale(f.n, v.z)); }
+
+// ---------------------------------------------------------------- the lobe (rt_pt_math.hpp:45-210)
+__device__ __forceinline__ float ggx_d(float a2, float cosH) {
+    const float d = fadd(fmul(fmul(cosH, cosH), fsub(a2, 1.0f)), 1.0f);
+    return fdiv(a2, fmul(fmul(kPiF, d), d));
+}
+__device__ __forceinline__ float lambda_f(float a2, float cosT) {
+    const float c2 = fmul(cosT, cosT);
+    return fmul(fadd(-1.0f, fsqrt(fadd(1.0f, fdiv(fmul(a2, fsub(1.0f, c2)), c2)))), 0.5f);
+}
+// VNDF sampling (Heitz 2018); u2 = kb / 2^24, so phi is the sampler angle kb.
+__device__ v3 sample_vndf(const PtParams& P, v3 wo, float a, float u1, uint32_t kb) {
+    const v3 vh = normalize(mk(fmul(a, wo.x), fmul(a, wo.y), wo.z));
+    const float lensq = fadd(fmul(vh.x, vh.x), fmul(vh.y, vh.y));
+    const v3 t1 = lensq > 0.0f ? scale(mk(-vh.y, vh.x, 0.0f), fdiv(1.0f, fsqrt(lensq))) : mk(1.0f, 0.0f, 0.0f);
+    const v3 t2 = cross(vh, t1);
+    float cphi, sphi;
+    sample_sincos(kb, P.corr, cphi, sphi);
+    const float r = fsqrt(u1);
+    const float p1 = fmul(r, cphi), s = fmul(0.5f, fadd(1.0f, vh.z));
+    const float p2 = fadd(fmul(fsub(1.0f, s), fsqrt(smax(0.0f, fsub(1.0f, fmul(p1, p1))))), fmul(s, fmul(r, sphi)));
+    const float q = fsub(fsub(1.0f, fmul(p1, p1)), fmul(p2, p2));
+    const v3 nh = add(add(scale(t1, p1), scale(t2, p2)), scale(vh, fsqrt(smax(0.0f, q))));
+    return normalize(mk(fmul(a, nh.x), fmul(a, nh.y), smax(0.0f, nh.z)));
+}
+struct Bsdf { v3 base; float rough, metallic, specular; bool legacy; };
+__device__ __forceinline__ float lobe_prob(const Bsdf& m) {
+    return fadd(m.metallic, fmul(fmul(fsub(1.0f, m.metallic), 0.5f), m.specular));
+}
+__device__ __forceinline__ v3 f0_of(const Bsdf& m) {
+    const float d = fmul(0.04f, m.specular);
+    return mk(fadd(d, fmul(fsub(m.base.x, d), m.metallic)), fadd(d, fmul(fsub(m.base.y, d), m.metallic)),
+              fadd(d, fmul(fsub(m.base.z, d), m.metallic)));
+}
+__device__ __forceinline__ float kms(float favg, float eavg) {
+    return fdiv(fmul(fmul(favg, favg), eavg), fsub(1.0f, fmul(favg, fsub(1.0f, eavg))));
+}
+__device__ __forceinline__ void table_ab(const float* __restrict__ t, float mu, float rough, float& A, float& B) {
+    const float x = fmul(fsqrt(clampf(mu, 0.0f, 1.0f)), float(kMu - 1)), y = fmul(clampf(rough, 0.0f, 1.0f), float(kRough - 1));
+    const int x0 = min((int)x, kMu - 2), y0 = min((int)y, kRough - 2);
+    const float fx = fsub(x, float(x0)), fy = fsub(y, float(y0));
+    const float* p = t + ((size_t)y0 * kMu + (size_t)x0) * 2;
+    const float* q = p + (size_t)kMu * 2;
+    const float gx = fsub(1.0f, fx);
+    const float a0 = fadd(fmul(__ldg(p), gx), fmul(__ldg(p + 2), fx)), b0 = fadd(fmul(__ldg(p + 1), gx), fmul(__ldg(p + 3), fx));
+    const float a1 = fadd(fmul(__ldg(q), gx), fmul(__ldg(q + 2), fx)), b1 = fadd(fmul(__ldg(q + 1), gx), fmul(__ldg(q + 3), fx));
+    const float gy = fsub(1.0f, fy);
+    A = fadd(fmul(a0, gy), fmul(a1, fy)); B = fadd(fmul(b0, gy), fmul(b1, fy));
+}
+__device__ __forceinline__ void table_avg(const float* __restrict__ t, float rough, float& A, float& B) {
+    const float y = fmul(clampf(rough, 0.0f, 1.0f), float(kRough - 1));
+    const int y0 = min((int)y, kRough - 2);
+    const float fy = fsub(y, float(y0)), gy = fsub(1.0f, fy);
+    const float* p = t + kNodes + (size_t)y0 * 2;
+    A = fadd(fmul(__ldg(p), gy), fmul(__ldg(p + 2), fy)); B = fadd(fmul(__ldg(p + 1), gy), fmul(__ldg(p + 3), fy));
+}
+struct Energy { float ms, wd, kd, eavg; };
+__device__ Energy energy_of(const PtParams& P, const Bsdf& m, float muO, float muI) {
+    float oa, ob, ia, ib, aa, ab;
+    table_ab(P.table, muO, m.rough, oa, ob);
+    table_ab(P.table, muI, m.rough, ia, ib);
+    table_avg(P.table, m.rough, aa, ab);
+    const float eo = smin(1.0f, fadd(oa, ob)), ei = smin(1.0f, fadd(ia, ib)), ea = smin(1.0f, fadd(aa, ab));
+    Energy e;
+    e.eavg = ea;
+    e.ms = ea < 1.0f ? fdiv(fmul(fsub(1.0f, eo), fsub(1.0f, ei)), fmul(kPiF, fsub(1.0f, ea))) : 0.0f;
+    const float on = m.specular > 0.0f ? 1.0f : 0.0f, d = fmul(0.04f, m.specular);
+    e.kd = kms(fmul(on, fadd(d, fdiv(fsub(1.0f, d), 21.0f))), ea);
+    const float eso = fadd(fmul(on, fadd(fmul(d, oa), ob)), fmul(e.kd, fsub(1.0f, eo)));
+    const float esi = fadd(fmul(on, fadd(fmul(d, ia), ib)), fmul(e.kd, fsub(1.0f, ei)));
+    const float esa = fadd(fmul(on, fadd(fmul(d, aa), ab)), fmul(e.kd, fsub(1.0f, ea)));
+    e.wd = fdiv(fmul(fsub(1.0f, eso), fsub(1.0f, esi)), fsub(1.0f, esa));
+    return e;
+}
+struct Eval { v3 fcos; float pdf; };
+// The shared specular part of both lobes: h, D, G1, G2, the Fresnel weight x1^5.
+struct Spec { float D, G1, G2, fw, spec; };
+__device__ __forceinline__ Spec spec_terms(const Bsdf& m, v3 wo, v3 wi) {
+    const float a = smax(1e-4f, fmul(m.rough, m.rough)), a2 = fmul(a, a);
+    const v3 h = normalize(add(wo, wi));
+    const float oh = dot(wo, h);
+    Spec s;
+    s.D = ggx_d(a2, h.z);
+    const float lo = lambda_f(a2, wo.z);
+    s.G2 = fdiv(1.0f, fadd(fadd(1.0f, lo), lambda_f(a2, wi.z)));
+    s.G1 = fdiv(1.0f, fadd(1.0f, lo));
+    const float x1 = clampf(fsub(1.0f, oh), 0.0f, 1.0f);
+    s.fw = fmul(fmul(fmul(fmul(x1, x1), x1), x1), x1);
+    s.spec = fdiv(fmul(s.D, s.G2), fmul(fmul(4.0f, wo.z), wi.z));
+    return s;
+}
+__device__ __forceinline__ float km_of(const Bsdf& m, float b, const Energy& en) {
+    return fadd(fmul(m.metallic, kms(fadd(b, fdiv(fsub(1.0f, b), 21.0f)), en.eavg)), fmul(fsub(1.0f, m.metallic), en.kd));
+}
+__device__ Eval eval_bsdf(const PtParams& P, const Bsdf& m, v3 wo, v3 wi, bool dropCosine) {
+    Eval r{mk(0.0f, 0.0f, 0.0f), 0.0f};
+    if (wo.z <= 0.0f || wi.z <= 0.0f) return r;
+    const float ps = lobe_prob(m), cosI = dropCosine ? 1.0f : wi.z;
+    const float kd = fdiv(fsub(1.0f, m.metallic), kPiF);
+    v3 f = mk(fmul(m.base.x, kd), fmul(m.base.y, kd), fmul(m.base.z, kd));
+    float pdf = fdiv(fmul(fsub(1.0f, ps), wi.z), kPiF);
+    if (ps > 0.0f) {
+        const v3 F0 = f0_of(m);
+        if (m.legacy) {
+            const Spec s = spec_terms(m, wo, wi);
+            const v3 F = mk(fadd(F0.x, fmul(fsub(1.0f, F0.x), s.fw)), fadd(F0.y, fmul(fsub(1.0f, F0.y), s.fw)),
+                            fadd(F0.z, fmul(fsub(1.0f, F0.z), s.fw)));
+            f = add(f, scale(F, s.spec));
+            pdf = fadd(pdf, fmul(ps, fdiv(fmul(s.G1, s.D), fmul(4.0f, wo.z))));
+        } else {
+            const Energy en = energy_of(P, m, wo.z, wi.z);
+            f = scale(f, en.wd);
+            const Spec s = spec_terms(m, wo, wi);
+            const float f90 = fadd(m.metallic, fmul(fsub(1.0f, m.metallic), m.specular > 0.0f ? 1.0f : 0.0f));
+            const v3 F = mk(fadd(F0.x, fmul(fsub(f90, F0.x), s.fw)), fadd(F0.y, fmul(fsub(f90, F0.y), s.fw)),
+                            fadd(F0.z, fmul(fsub(f90, F0.z), s.fw)));
+            const v3 km = mk(km_of(m, m.base.x, en), km_of(m, m.base.y, en), km_of(m, m.base.z, en));
+            f = add(add(f, scale(F, s.spec)), scale(km, en.ms));
+            pdf = fadd(pdf, fmul(ps, fdiv(fmul(s.G1, s.D), fmul(4.0f, wo.z))));
+        }
+    }
+    r.fcos = scale(f, cosI);
+    r.pdf = pdf;
+    return r;
+}
+__device__ v3 lambert_cos(const PtParams& P, const Bsdf& m, v3 wo, v3 wi, bool dropCosine) {
+    if (wo.z <= 0.0f || wi.z <= 0.0f) return mk(0.0f, 0.0f, 0.0f);
+    const float cosI = dropCosine ? 1.0f : wi.z, kd = fdiv(fsub(1.0f, m.metallic), kPiF);
+    v3 f = mk(fmul(m.base.x, kd), fmul(m.base.y, kd), fmul(m.base.z, kd));
+    if (!m.legacy && lobe_prob(m) > 0.0f) f = scale(f, energy_of(P, m, wo.z, wi.z).wd);
+    return scale(f, cosI);
+}
+__device__ __forceinline__ v3 spec_albedo(const Bsdf& m, float cosO) {
+    if (lobe_prob(m) <= 0.0f) return mk(0.0f, 0.0f, 0.0f);
+    const float x1 = clampf(fsub(1.0f, cosO), 0.0f, 1.0f), fw = fmul(fmul(fmul(fmul(x1, x1), x1), x1), x1);
+    const v3 F0 = f0_of(m);
+    return mk(fadd(F0.x, fmul(fsub(1.0f, F0.x), fw)), fadd(F0.y, fmul(fsub(1.0f, F0.y), fw)),
+              fadd(F0.z, fmul(fsub(1.0f, F0.z), fw)));
+}
+// one-sample mixture; u = (u1, kb / 2^24)
+__device__ bool sample_bsdf(const PtParams& P, const Bsdf& m, v3 wo, float pick, float u1, uint32_t kb, v3& wi) {
+    if (pick < lobe_prob(m)) {
+        const float a = smax(1e-4f, fmul(m.rough, m.rough));
+        const v3 h = sample_vndf(P, wo, a, u1, kb);
+        wi = sub(scale(h, fmul(2.0f, dot(wo, h))), wo);
+    } else {
+        float c, s;
+        sample_sincos(kb, P.corr, c, s);
+        const float r = fsqrt(u1);
+        wi = mk(fmul(r, c), fmul(r, s), fsqrt(smax(0.0f, fsub(1.0f, u1))));
+    }
+    return wi.z > 0.0f;
+}
+
+// ---------------------------------------------------------------- scene queries (rt_pt_ctx.hpp:18-79)
+struct Surf { v3 p, n, ng, base; const float* m; float t; int tri; };
+__device__ __forceinline__ v3 tri_corner(const PtParams& P, int t, int k) { return load3(P.tris + (size_t)t * 9 + 3 * k); }
+
+__device__ bool hit(const PtParams& P, v3 o, v3 d, float tmax, Surf& x) {
+    if (!P.has_geometry) return false;
+    float t;
+    const int tri = walk_closest(P.nodes, P.ltris, o, d, tmax, t, P.err);
+    if (tri < 0) return false;
+    const v3 a = tri_corner(P, tri, 0), b = tri_corner(P, tri, 1), c = tri_corner(P, tri, 2);
+    float tt, u, v;
+    hit_tri_uv(make_wray(o, d), a, b, c, tt, u, v);      // the winner's u, v (its t is the walk's)
+    const uint32_t i0 = __ldg(P.idx + (size_t)tri * 3), i1 = __ldg(P.idx + (size_t)tri * 3 + 1),
+                   i2 = __ldg(P.idx + (size_t)tri * 3 + 2);
+    const float b0 = fsub(fsub(1.0f, u), v);
+    x.t = t; x.tri = tri;
+    x.p = add(o, scale(d, t));
+    x.ng = normalize(cross(sub(b, a), sub(c, a)));
+    const v3 n0 = load3(P.nrm + 3 * (size_t)i0), n1 = load3(P.nrm + 3 * (size_t)i1), n2 = load3(P.nrm + 3 * (size_t)i2);
+    x.n = normalize(add(add(scale(n0, b0), scale(n1, u)), scale(n2, v)));
+    const float tu = fadd(fadd(fmul(__ldg(P.uv + 2 * (size_t)i0), b0), fmul(__ldg(P.uv + 2 * (size_t)i1), u)),
+                          fmul(__ldg(P.uv + 2 * (size_t)i2), v));
+    const float tv = fadd(fadd(fmul(__ldg(P.uv + 2 * (size_t)i0 + 1), b0), fmul(__ldg(P.uv + 2 * (size_t)i1 + 1), u)),
+                          fmul(__ldg(P.uv + 2 * (size_t)i2 + 1), v));
+    const uint32_t tex = __ldg(P.tritex + tri);
+    const uint32_t off = __ldg(P.texent + 3 * tex), tw = __ldg(P.texent + 3 * tex + 1), th = __ldg(P.texent + 3 * tex + 2);
+    const uint32_t tx = (uint32_t)(int32_t)floorf(fmul(tu, (float)tw)) & (tw - 1);
+    const uint32_t ty = (uint32_t)(int32_t)floorf(fmul(tv, (float)th)) & (th - 1);
+    const uint32_t col = __ldg(P.texels + off + ty * tw + tx);
+    x.m = P.mat + 7 * (size_t)tex;
+    const float k = fdiv(__ldg(x.m), 255.0f);
+    x.base = mk(fmul((float)(col & 255u), k), fmul((float)((col >> 8) & 255u), k), fmul((float)((col >> 16) & 255u), k));
+    if (dot(x.ng, d) > 0.0f) x.ng = scale(x.ng, -1.0f);
+    if (dot(x.n, x.ng) < 0.0f) x.n = scale(x.n, -1.0f);
+    (void)tt;
+    return true;
+}
+__device__ __forceinline__ bool visible(const PtParams& P, v3 p, v3 dir, float tmax) {
+    if (!P.has_geometry) return true;
+    Counts cn;
+    return walk<false>(P.nodes, P.ltris, p, dir, tmax, tmax, P.err, cn) == 0;
+}
+__device__ __forceinline__ v3 offset_of(const Surf& x, v3 dir) {
+    const float e = fmul(2e-4f, fadd(1.0f, smax(fabsf(x.p.x), smax(fabsf(x.p.y), fabsf(x.p.z)))));
+    return add(x.p, scale(x.ng, dot(x.ng, dir) > 0.0f ? e : -e));
+}
+__device__ v3 nee(const PtParams& P, const Surf& x, const Frame& fr, const Bsdf& bs, v3 woL, uint32_t px, uint32_t smp,
+                  uint32_t base, v3& diff) {
+    v3 L = mk(0.0f, 0.0f, 0.0f);
+    diff = L;
+    const bool dc = (P.controls & RN_PT_DROP_LAMBERT_COSINE) != 0;
+    if (maxc(P.sun_irr) > 0.0f) {
+        const v3 l = P.sun_dir, lL = to_local(fr, l);
+        const Eval e = eval_bsdf(P, bs, woL, lL, dc);
+        if (maxc(e.fcos) > 0.0f && visible(P, offset_of(x, l), l, 1e30f)) {
+            L = add(L, mulv(e.fcos, P.sun_irr));
+            diff = add(diff, mulv(lambert_cos(P, bs, woL, lL, dc), P.sun_irr));
+        }
+    }
+    if (P.nemit == 0) return L;
+    const R2 a = rand2(P, px, smp, base + 2), b = rand2(P, px, smp, base + 3);
+    const float target = fmul(a.a, P.area);
+    uint32_t lo = 0, hi = P.nemit;              // std::upper_bound: the first cdf > target
+    while (lo < hi) {
+        const uint32_t mid = lo + (hi - lo) / 2;
+        if (target < __ldg(P.cdf + mid)) hi = mid; else lo = mid + 1;
+    }
+    const uint32_t k = lo < P.nemit - 1 ? lo : P.nemit - 1;
+    const int et = (int)__ldg(P.emit + k);
+    const v3 ta = tri_corner(P, et, 0), tb = tri_corner(P, et, 1), tc = tri_corner(P, et, 2);
+    const float su = fsqrt(a.b);
+    const v3 q = add(add(scale(ta, fsub(1.0f, su)), scale(tb, fmul(su, fsub(1.0f, b.a)))), scale(tc, fmul(su, b.a)));
+    const v3 to = sub(q, x.p);
+    const float dist = length(to);
+    const v3 l = scale(to, fdiv(1.0f, dist)), lL = to_local(fr, l);
+    const float cosL = fabsf(dot(normalize(cross(sub(tb, ta), sub(tc, ta))), l));
+    if (cosL <= 0.0f) return L;
+    const float pl = fdiv(fmul(dist, dist), fmul(cosL, P.area));
+    const Eval e = eval_bsdf(P, bs, woL, lL, dc);
+    if (maxc(e.fcos) <= 0.0f || !visible(P, offset_of(x, l), l, fmul(dist, fsub(1.0f, 1e-3f)))) return L;
+    const float w = (P.controls & RN_PT_MIS_WEIGHT_ONE) ? 1.0f
+                                                      : fdiv(fmul(pl, pl), fadd(fmul(pl, pl), fmul(e.pdf, e.pdf)));
+    const float* em = P.mat + 7 * (size_t)__ldg(P.tritex + et) + 4;
+    const v3 Le = mk(__ldg(em), __ldg(em + 1), __ldg(em + 2));
+    const float wp = fdiv(w, pl);
+    diff = add(diff, scale(mulv(lambert_cos(P, bs, woL, lL, dc), Le), wp));
+    return add(L, scale(mulv(e.fcos, Le), wp));
+}
+
+struct Sample { v3 L, D, S, E, alb, nrm, dAlb, sAlb; };
+// rt_pt_cpu.cpp:31-97
+__device__ Sample trace_path(const PtParams& P, v3 ro, v3 rd, uint32_t px, uint32_t smp) {
+    const v3 z = mk(0.0f, 0.0f, 0.0f);
+    Sample o{z, z, z, z, z, z, z, z};
+    v3 T = mk(1.0f, 1.0f, 1.0f), tw = T, R = z, wd = z, ws = z;
+    float prevPdf = 0.0f;
+    const bool dc = (P.controls & RN_PT_DROP_LAMBERT_COSINE) != 0;
+    for (uint32_t b = 0; b <= P.max_bounces; ++b) {
+        Surf x0;
+        if (!hit(P, ro, rd, 1e30f, x0)) {
+            o.L = add(o.L, mulv(T, P.sky));
+            if (b == 0) o.E = P.sky; else R = add(R, mulv(tw, P.sky));
+            break;
+        }
+        const Bsdf bs{x0.base, __ldg(x0.m + 1), __ldg(x0.m + 2), __ldg(x0.m + 3), (P.controls & RN_PT_LEGACY_LOBE_V2) != 0};
+        if (b == 0) {
+            o.alb = x0.base; o.nrm = x0.n;
+            o.dAlb = scale(x0.base, fsub(1.0f, bs.metallic));
+            o.sAlb = spec_albedo(bs, clampf(-dot(x0.n, rd), 0.0f, 1.0f));
+        }
+        const v3 Le = mk(__ldg(x0.m + 4), __ldg(x0.m + 5), __ldg(x0.m + 6));
+        if (maxc(Le) > 0.0f) {
+            float w = 1.0f;
+            if (b > 0 && !(P.controls & RN_PT_MIS_WEIGHT_ONE)) {
+                const float cosL = fabsf(dot(x0.ng, rd)), pl = fdiv(fmul(x0.t, x0.t), fmul(cosL, P.area));
+                w = fdiv(fmul(prevPdf, prevPdf), fadd(fmul(prevPdf, prevPdf), fmul(pl, pl)));
+            }
+            o.L = add(o.L, scale(mulv(T, Le), w));
+            if (b == 0) o.E = Le; else R = add(R, scale(mulv(tw, Le), w));
+        }
+        if (b == P.max_bounces) break;
+        const Frame fr = basis(x0.n);
+        const v3 woL = to_local(fr, scale(rd, -1.0f));
+        if (woL.z <= 0.0f) break;
+        const uint32_t base = 2 + b * 4;
+        v3 nd;
+        const v3 Ln = nee(P, x0, fr, bs, woL, px, smp, base, nd);
+        o.L = add(o.L, mulv(T, Ln));
+        if (b == 0) { o.D = nd; o.S = sub(Ln, nd); } else R = add(R, mulv(tw, Ln));
+        const R2 u = rand2(P, px, smp, base), r = rand2(P, px, smp, base + 1);
+        v3 wiL;
+        if (!sample_bsdf(P, bs, woL, r.a, u.a, u.kb, wiL)) break;
+        const Eval e = eval_bsdf(P, bs, woL, wiL, dc);
+        if (e.pdf <= 0.0f) break;
+        const float ip = fdiv(1.0f, e.pdf);
+        const v3 step = scale(e.fcos, ip);
+        T = mulv(T, step);
+        if (b == 0) { wd = scale(lambert_cos(P, bs, woL, wiL, dc), ip); ws = sub(step, wd); }
+        else tw = mulv(tw, step);
+        prevPdf = e.pdf;
+        if (P.rr && b >= 3) {
+            const float q = smin(0.95f, maxc(T));
+            if (r.b >= q) break;
+            const float iq = fdiv(1.0f, q);
+            T = scale(T, iq);
+            tw = scale(tw, iq);
+        }
+        const v3 wi = to_world(fr, wiL);
+        ro = offset_of(x0, wi);
+        rd = wi;
+    }
+    o.D = add(o.D, mulv(wd, R));
+    if (!(P.controls & RN_PT_AOV_DROP_SPECULAR_INDIRECT)) o.S = add(o.S, mulv(ws, R));
+    if (P.controls & RN_PT_AOV_EMISSION_TO_DIFFUSE) { o.D = add(o.D, o.E); o.E = z; }
+    return o;
+}
+
+// rt_pt_cpu.cpp:21-24
+__device__ __forceinline__ v3 dir_of(const PtCam& c, float px, float py, int w, int h) {
+    const float nx = fsub(fmul(fdiv(px, (float)w), 2.0f), 1.0f), ny = fsub(1.0f, fmul(fdiv(py, (float)h), 2.0f));
+    return normalize(add(add(c.f, scale(c.s, fmul(fmul(nx, c.th), c.aspect))), scale(c.u, fmul(ny, c.th))));
+}
+
+// One thread per (pixel, sample of the slice): a warp takes an 8 x 4 pixel tile for one sample.
+__global__ void __launch_bounds__(128) pt_paths_kernel(const PtParams P) {
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    const uint32_t tiles_x = (P.w + kTileW - 1) / kTileW, tiles_y = (P.h + kTileH - 1) / kTileH;
+    const uint32_t ntiles = tiles_x * tiles_y;
+    if (warp >= ntiles * P.kn) return;
+    const uint32_t j = warp / ntiles, tile = warp % ntiles;
+    const int x = (int)((tile % tiles_x) * kTileW + (lane % kTileW)), y = (int)((tile / tiles_x) * kTileH + (lane / kTileW));
+    if (x >= P.w || y >= P.h) return;
+    const uint32_t px = (uint32_t)(y * P.w + x);
+    const uint32_t smp = P.spp_begin + P.k0 + j;
+    float ja = 0.5f, jb = 0.5f;
+    if (P.jitter) { const R2 r = rand2(P, px, smp, 0); ja = r.a; jb = r.b; }
+    const v3 dir = dir_of(P.cam, fadd((float)x, ja), fadd((float)y, jb), P.w, P.h);
+    const Sample o = trace_path(P, P.cam.eye, dir, px, smp);
+    const size_t stride = (size_t)P.kn * P.npix;
+    float* s = P.samp + (size_t)j * P.npix + px;
+    const v3* f = &o.L;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        s[(3 * c) * stride] = f[c].x;
+        s[(3 * c + 1) * stride] = f[c].y;
+        s[(3 * c + 2) * stride] = f[c].z;
+    }
+}
+
+// Per pixel: the slice's samples added in sample order to the running sums (rt_pt_cpu.cpp:
+// 132-141); after the last slice the means, the variances and the pixel-centre ray.
+struct PtOutDev {
+    float *radiance, *albedo, *normal, *depth, *variance;
+    int32_t* triangle;
+    float* motion;
+    float *diffuse, *specular, *emission, *diffuse_albedo, *specular_albedo, *diffuse_variance, *specular_variance;
+};
+__device__ __forceinline__ void put3(float* v, size_t p, v3 a) {
+    if (v) { v[p * 3] = a.x; v[p * 3 + 1] = a.y; v[p * 3 + 2] = a.z; }
+}
+__device__ __forceinline__ float var_of(double s1, double s2, uint32_t n) {
+    return n > 1 ? (float)(__ddiv_rn(__ddiv_rn(__dsub_rn(s2, __ddiv_rn(__dmul_rn(s1, s1), (double)n)), (double)(n - 1)),
+                                     (double)n))
+                 : 0.0f;
+}
+__global__ void __launch_bounds__(128) pt_accum_kernel(const PtParams P, const PtOutDev O) {
+    const uint32_t px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (px >= P.npix) return;
+    float a[kSampleFloats];
+    double m[6];
+    if (P.first) {
+#pragma unroll
+        for (int c = 0; c < kSampleFloats; ++c) a[c] = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) m[c] = 0.0;
+    } else {
+#pragma unroll
+        for (int c = 0; c < kSampleFloats; ++c) a[c] = P.acc[(size_t)c * P.npix + px];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) m[c] = P.mom[(size_t)c * P.npix + px];
+    }
+    const size_t stride = (size_t)P.kn * P.npix;
+    for (uint32_t j = 0; j < P.kn; ++j) {
+        const float* s = P.samp + (size_t)j * P.npix + px;
+        float v[kSampleFloats];
+#pragma unroll
+        for (int c = 0; c < kSampleFloats; ++c) { v[c] = s[c * stride]; a[c] = fadd(a[c], v[c]); }
+        // luminance of L, D and S, their moments in float64
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const double l = (double)lum(mk(v[3 * q], v[3 * q + 1], v[3 * q + 2]));
+            m[2 * q] = __dadd_rn(m[2 * q], l);
+            m[2 * q + 1] = __dadd_rn(m[2 * q + 1], __dmul_rn(l, l));
+        }
+    }
+    if (!P.last) {
+#pragma unroll
+        for (int c = 0; c < kSampleFloats; ++c) P.acc[(size_t)c * P.npix + px] = a[c];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) P.mom[(size_t)c * P.npix + px] = m[c];
+        return;
+    }
+    const float inv = P.spp ? fdiv(1.0f, (float)P.spp) : 0.0f;
+    const size_t p = px;
+    const v3 L = mk(a[0], a[1], a[2]), D = mk(a[3], a[4], a[5]), S = mk(a[6], a[7], a[8]), E = mk(a[9], a[10], a[11]);
+    const v3 alb = mk(a[12], a[13], a[14]), nrm = mk(a[15], a[16], a[17]), da = mk(a[18], a[19], a[20]),
+             sa = mk(a[21], a[22], a[23]);
+    put3(O.radiance, p, scale(L, inv)); put3(O.albedo, p, scale(alb, inv)); put3(O.normal, p, scale(nrm, inv));
+    put3(O.diffuse, p, scale(D, inv)); put3(O.specular, p, scale(S, inv)); put3(O.emission, p, scale(E, inv));
+    put3(O.diffuse_albedo, p, scale(da, inv)); put3(O.specular_albedo, p, scale(sa, inv));
+    if (O.variance) O.variance[p] = var_of(m[0], m[1], P.spp);
+    if (O.diffuse_variance) O.diffuse_variance[p] = var_of(m[2], m[3], P.spp);
+    if (O.specular_variance) O.specular_variance[p] = var_of(m[4], m[5], P.spp);
+    // the pixel-centre ray (rt_pt_cpu.cpp:111-122)
+    const int x = (int)(px % (uint32_t)P.w), y = (int)(px / (uint32_t)P.w);
+    float depth = 0.0f, mx = 0.0f, my = 0.0f;
+    int32_t tri = -1;
+    if (O.depth || O.triangle || O.motion) {
+        Surf c;
+        if (hit(P, P.cam.eye, dir_of(P.cam, fadd((float)x, 0.5f), fadd((float)y, 0.5f), P.w, P.h), 1e30f, c)) {
+            depth = dot(sub(c.p, P.cam.eye), P.cam.f);
+            tri = c.tri;
+            const v3 v = sub(c.p, P.prev.eye);
+            const float zz = dot(v, P.prev.f);
+            const float nx = fdiv(dot(v, P.prev.s), fmul(fmul(zz, P.prev.th), P.prev.aspect));
+            const float ny = fdiv(dot(v, P.prev.u), fmul(zz, P.prev.th));
+            mx = fsub(fmul(fadd(fmul(nx, 0.5f), 0.5f), (float)P.w), fadd((float)x, 0.5f));
+            my = fsub(fmul(fsub(1.0f, fadd(fmul(ny, 0.5f), 0.5f)), (float)P.h), fadd((float)y, 0.5f));
+        }
+    }
+    if (O.depth) O.depth[p] = depth;
+    if (O.triangle) O.triangle[p] = tri;
+    if (O.motion) { O.motion[p * 2] = mx; O.motion[p * 2 + 1] = my; }
+}
+
+// trianglesOf(geo) on the device: 9 floats a triangle from the indexed vertices.
+__global__ void gather_tris_kernel(const float* __restrict__ pos, const uint32_t* __restrict__ idx, uint32_t ntri,
+                                   float* __restrict__ tris) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t v = idx[3 * (size_t)t + k];
+        tris[9 * (size_t)t + 3 * k] = pos[3 * (size_t)v];
+        tris[9 * (size_t)t + 3 * k + 1] = pos[3 * (size_t)v + 1];
+        tris[9 * (size_t)t + 3 * k + 2] = pos[3 * (size_t)v + 2];
+    }
+}
+
+}  // namespace
+}  // namespace rn
+
+using namespace rn;
+
+extern "C" {
+
+int rn_pt_scene_create(const rn_pt_scene_desc* sd, rn_ptscene** out, rn_status* st) {
+    if (!out) return fail(st, RN_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (!sd) return fail(st, RN_ERR_INVALID, "null scene");
+    if (sd->ntri > 0 && (!sd->pos || !sd->nrm || !sd->uv || !sd->idx || !sd->tri_texture))
+        return fail(st, RN_ERR_INVALID, "null geometry arrays");
+    if (sd->ntri >= (1u << 28)) return fail(st, RN_ERR_INVALID, "%u triangles: at most 2^28 - 1", sd->ntri);
+    if (sd->ntex == 0 || !sd->tex_entries || !sd->texels || !sd->materials)
+        return fail(st, RN_ERR_INVALID, "a scene needs at least one texture and its material");
+    // every index in range, every texture a power of two inside the texel array
+    for (uint32_t i = 0; i < 3 * sd->ntri; ++i)
+        if (sd->idx[i] >= sd->nvert) return fail(st, RN_ERR_INVALID, "index %u of triangle %u out of range", sd->idx[i], i / 3);
+    for (uint32_t t = 0; t < sd->ntri; ++t)
+        if (sd->tri_texture[t] >= sd->ntex) return fail(st, RN_ERR_INVALID, "triangle %u: texture %u", t, sd->tri_texture[t]);
+    for (uint32_t k = 0; k < sd->ntex; ++k) {
+        const uint64_t off = sd->tex_entries[3 * k], w = sd->tex_entries[3 * k + 1], h = sd->tex_entries[3 * k + 2];
+        if (w == 0 || h == 0 || (w & (w - 1)) || (h & (h - 1)) || off + w * h > sd->ntexels)
+            return fail(st, RN_ERR_INVALID, "texture %u: %llux%llu at %llu (sizes must be powers of two inside the texels)",
+                        k, (unsigned long long)w, (unsigned long long)h, (unsigned long long)off);
+    }
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    const float* table = nullptr;
+    RN_TRY(device_table(c.device, &table, st));
+    rn_ptscene* s = new rn_ptscene();
+    s->device = c.device;
+    s->nvert = sd->nvert; s->ntri = sd->ntri; s->ntex = sd->ntex; s->ntexels = sd->ntexels;
+    std::memcpy(s->sun_dir, sd->sun_dir, sizeof s->sun_dir);
+    std::memcpy(s->sun_irr, sd->sun_irradiance, sizeof s->sun_irr);
+    std::memcpy(s->sky, sd->sky, sizeof s->sky);
+    // trianglesOf and finishPtScene's emitter list and inclusive area CDF, on the host in
+    // triangle order (a float running sum: its rounding is the reference's)
+    std::vector<float> tris((size_t)sd->ntri * 9);
+    for (uint32_t t = 0; t < sd->ntri; ++t)
+        for (int k = 0; k < 3; ++k)
+            for (int a = 0; a < 3; ++a) tris[9 * (size_t)t + 3 * k + a] = sd->pos[3 * (size_t)sd->idx[3 * (size_t)t + k] + a];
+    std::vector<uint32_t> emit;
+    std::vector<float> cdf;
+    float area = 0.0f;
+    for (uint32_t t = 0; t < sd->ntri; ++t) {
+        const float* e = sd->materials[sd->tri_texture[t]].emission;
+        if (e[0] <= 0.0f && e[1] <= 0.0f && e[2] <= 0.0f) continue;
+        const float* q = &tris[9 * (size_t)t];
+        const hv3 a{q[0], q[1], q[2]}, b{q[3], q[4], q[5]}, cc{q[6], q[7], q[8]};
+        const hv3 cr = hcross(hsub(b, a), hsub(cc, a));
+        area += 0.5f * std::sqrt(hdot(cr, cr));
+        emit.push_back(t);
+        cdf.push_back(area);
+    }
+    s->nemit = (uint32_t)emit.size();
+    s->area = area;
+    // one device block for every array
+    const size_t nv = sd->nvert, nt = sd->ntri;
+    const size_t sizes[] = {nv * 12, nv * 8, nt * 12, nt * 4, (size_t)sd->ntex * 12, (size_t)sd->ntexels * 4,
+                            (size_t)sd->ntex * 28, nt * 36, emit.size() * 4, cdf.size() * 4, nv * 12};
+    size_t offs[11], total = 0;
+    for (int i = 0; i < 11; ++i) { offs[i] = total; total += (sizes[i] + 255) & ~(size_t)255; }
+    if (cudaMalloc(&s->block, total ? total : 256) != cudaSuccess) {
+        delete s;
+        return cuda_fail(st, cudaGetLastError(), "path tracer scene allocation");
+    }
+    char* base = (char*)s->block;
+    s->nrm = (float*)(base + offs[0]); s->uv = (float*)(base + offs[1]); s->idx = (uint32_t*)(base + offs[2]);
+    s->tritex = (uint32_t*)(base + offs[3]); s->texent = (uint32_t*)(base + offs[4]);
+    s->texels = (uint32_t*)(base + offs[5]); s->mat = (float*)(base + offs[6]); s->tris = (float*)(base + offs[7]);
+    s->emit = (uint32_t*)(base + offs[8]); s->cdf = (float*)(base + offs[9]);
+    float* d_pos = (float*)(base + offs[10]);
+    std::vector<float> mats((size_t)sd->ntex * 7);
+    for (uint32_t k = 0; k < sd->ntex; ++k) {
+        const rn_pt_material& m = sd->materials[k];
+        const float v[7] = {m.base_factor, m.roughness, m.metallic, m.specular, m.emission[0], m.emission[1], m.emission[2]};
+        std::memcpy(&mats[7 * (size_t)k], v, sizeof v);
+    }
+    const struct { void* d; const void* h; size_t n; } up[] = {
+        {s->nrm, sd->nrm, sizes[0]}, {s->uv, sd->uv, sizes[1]}, {s->idx, sd->idx, sizes[2]},
+        {s->tritex, sd->tri_texture, sizes[3]}, {s->texent, sd->tex_entries, sizes[4]}, {s->texels, sd->texels, sizes[5]},
+        {s->mat, mats.data(), sizes[6]}, {s->emit, emit.data(), sizes[8]}, {s->cdf, cdf.data(), sizes[9]},
+        {d_pos, sd->pos, sizes[10]}};
+    int rc = RN_OK;
+    for (const auto& u : up)
+        if (rc == RN_OK && u.n && cudaMemcpyAsync(u.d, u.h, u.n, cudaMemcpyHostToDevice, c.stream) != cudaSuccess)
+            rc = cuda_fail(st, cudaGetLastError(), "path tracer scene upload");
+    if (rc == RN_OK && nt) {
+        gather_tris_kernel<<<(unsigned)((nt + 255) / 256), 256, 0, c.stream>>>(d_pos, s->idx, (uint32_t)nt, s->tris);
+        if (cudaGetLastError() != cudaSuccess) rc = cuda_fail(st, cudaGetLastError(), "gather_tris_kernel");
+    }
+    if (rc == RN_OK) rc = rn_accel_build(s->tris, (uint32_t)nt, RN_DEVICE_PTRS, &s->accel, st);
+    // the uploads read the host vectors above: finish them before they go out of scope
+    const cudaError_t e = cudaStreamSynchronize(c.stream);
+    if (rc == RN_OK && e != cudaSuccess) rc = cuda_fail(st, e, "rn_pt_scene_create");
+    if (rc != RN_OK) { rn_pt_scene_free(s); return rc; }
+    *out = s;
+    return ok(st);
+}
+
+void rn_pt_scene_free(rn_ptscene* s) {
+    if (!s) return;
+    if (s->accel) rn_accel_free(s->accel);
+    if (s->block) cudaFree(s->block);
+    delete s;
+}
+
+int rn_pt_scene_info(const rn_ptscene* s, uint32_t* emitters, float* emitter_area, rn_status* st) {
+    if (!s) return fail(st, RN_ERR_INVALID, "null scene");
+    if (emitters) *emitters = s->nemit;
+    if (emitter_area) *emitter_area = s->area;
+    return ok(st);
+}
+
+int rn_pathtrace(const rn_ptscene* s, const rn_pt_desc* d, int flags, rn_pt_out* out, rn_status* st) {
+    if (!s || !d || !out) return fail(st, RN_ERR_INVALID, "null argument");
+    if (d->width <= 0 || d->height <= 0 || (size_t)d->width * (size_t)d->height > ((size_t)1 << 30))
+        return fail(st, RN_ERR_INVALID, "frame size %dx%d", d->width, d->height);
+    if (d->max_bounces > 1024) return fail(st, RN_ERR_INVALID, "max_bounces %u", d->max_bounces);
+    RN_TRY(ensure_ctx(st));
+    Context& c = ctx();
+    if (s->device != c.device) return fail(st, RN_ERR_STATE, "scene belongs to device %d", s->device);
+    const float* table = nullptr;
+    RN_TRY(device_table(c.device, &table, st));
+    const bool dev = (flags & RN_DEVICE_PTRS) != 0;
+    const uint32_t npix = (uint32_t)d->width * (uint32_t)d->height;
+    PtParams P{};
+    P.nodes = s->accel->d_nodes; P.ltris = s->accel->d_tris; P.has_geometry = s->ntri > 0;
+    P.tris = s->tris; P.nrm = s->nrm; P.uv = s->uv; P.idx = s->idx; P.tritex = s->tritex; P.texent = s->texent;
+    P.texels = s->texels; P.mat = s->mat; P.emit = s->emit; P.cdf = s->cdf; P.nemit = s->nemit; P.area = s->area;
+    P.table = table; P.corr = c.trig_corr;
+    const hv3 sd = hnorm(hv3{s->sun_dir[0], s->sun_dir[1], s->sun_dir[2]});
+    P.sun_dir = v3{sd.x, sd.y, sd.z};
+    P.sun_irr = v3{s->sun_irr[0], s->sun_irr[1], s->sun_irr[2]};
+    P.sky = v3{s->sky[0], s->sky[1], s->sky[2]};
+    P.seed_lo = (uint32_t)d->seed; P.seed_hi = (uint32_t)(d->seed >> 32);
+    P.spp = d->spp; P.spp_begin = d->spp_begin; P.max_bounces = d->max_bounces; P.controls = d->controls;
+    P.w = d->width; P.h = d->height; P.jitter = d->jitter != 0; P.rr = d->russian_roulette != 0;
+    P.cam = cam_of(d->camera, d->width, d->height);
+    P.prev = cam_of(d->previous, d->width, d->height);
+    P.npix = npix;
+    P.err = c.dev_error;
+    // output planes: the caller's device arrays, or one staging block
+    const int comps[14] = {3, 3, 3, 1, 1, 1, 2, 3, 3, 3, 3, 3, 1, 1};
+    void* user[14] = {out->radiance, out->albedo, out->normal, out->depth, out->variance, out->triangle, out->motion,
+                      out->diffuse, out->specular, out->emission, out->diffuse_albedo, out->specular_albedo,
+                      out->diffuse_variance, out->specular_variance};
+    void* dplane[14] = {};
+    if (dev) {
+        for (int i = 0; i < 14; ++i) dplane[i] = user[i];
+    } else {
+        size_t total = 0, offs[14];
+        for (int i = 0; i < 14; ++i) { offs[i] = total; if (user[i]) total += ((size_t)npix * comps[i] * 4 + 255) & ~(size_t)255; }
+        void* blk = nullptr;
+        RN_TRY(ws_get(WS_PT_OUT, total ? total : 256, &blk, st));
+        for (int i = 0; i < 14; ++i) dplane[i] = user[i] ? (char*)blk + offs[i] : nullptr;
+    }
+    PtOutDev O{(float*)dplane[0], (float*)dplane[1], (float*)dplane[2], (float*)dplane[3], (float*)dplane[4],
+               (int32_t*)dplane[5], (float*)dplane[6], (float*)dplane[7], (float*)dplane[8], (float*)dplane[9],
+               (float*)dplane[10], (float*)dplane[11], (float*)dplane[12], (float*)dplane[13]};
+    // slices: at most kSliceBytes of per-sample terms at a time
+    const size_t per_sample = (size_t)npix * kSampleFloats * sizeof(float);
+    const size_t kSliceBytes = (size_t)1 << 31;
+    uint32_t kn_max = (uint32_t)std::max<size_t>(1, std::min<size_t>(d->spp ? d->spp : 1, kSliceBytes / per_sample));
+    if (c.tune.pt_slice > 0) kn_max = std::min(kn_max, (uint32_t)c.tune.pt_slice);
+    void* samp = nullptr;
+    RN_TRY(ws_get(WS_PT_SAMPLES, per_sample * kn_max, &samp, st));
+    P.samp = (float*)samp;
+    if (d->spp > kn_max) {
+        void* acc = nullptr;
+        RN_TRY(ws_get(WS_PT_ACC, (size_t)npix * (kSampleFloats * sizeof(float) + 6 * sizeof(double)), &acc, st));
+        P.mom = (double*)acc;
+        P.acc = (float*)((char*)acc + (size_t)npix * 6 * sizeof(double));
+    }
+    const uint32_t tiles = ((uint32_t)(d->width + 7) / 8) * ((uint32_t)(d->height + 3) / 4);
+    uint32_t k0 = 0;
+    do {
+        P.k0 = k0;
+        P.kn = std::min(kn_max, d->spp - k0);
+        P.first = k0 == 0;
+        P.last = k0 + P.kn >= d->spp;
+        if (P.kn > 0) {
+            const uint64_t warps = (uint64_t)tiles * P.kn;
+            pt_paths_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, c.stream>>>(P);
+            const cudaError_t le = cudaGetLastError();
+            if (le != cudaSuccess) return cuda_fail(st, le, "pt_paths_kernel");
+        }
+        pt_accum_kernel<<<(npix + 127) / 128, 128, 0, c.stream>>>(P, O);
+        const cudaError_t le = cudaGetLastError();
+        if (le != cudaSuccess) return cuda_fail(st, le, "pt_accum_kernel");
+        k0 += P.kn;
+    } while (k0 < d->spp);
+    if (!dev)
+        for (int i = 0; i < 14; ++i)
+            if (user[i]) RN_CUDA(cudaMemcpyAsync(user[i], dplane[i], (size_t)npix * comps[i] * 4, cudaMemcpyDeviceToHost,
+                                                 c.stream), st);
+    RN_CUDA(cudaStreamSynchronize(c.stream), st);
+    RN_TRY(check_device_error(st, "rn_pathtrace"));
+    return ok(st);
+}
+
+}  // extern "C"

@@ -154,6 +154,39 @@ __device__ __forceinline__ bool hit_tri(const WRay& r, v3 a, v3 b, v3 c, float& 
     return t > 1e-4f;
 }
 
+// The same test with the barycentrics the closest-hit consumers read (primitives.hpp:52-63):
+// u and v from the sheared sums where Moeller-Trumbore's determinant is unusable, else
+// Moeller-Trumbore's, clamped at 0 and renormalized when their sum passes 1.
+__device__ __forceinline__ bool hit_tri_uv(const WRay& r, v3 a, v3 b, v3 c, float& t, float& u, float& v) {
+    const v3 A = wframe(sub(a, r.o), r.kz, r.sw), B = wframe(sub(b, r.o), r.kz, r.sw),
+             C = wframe(sub(c, r.o), r.kz, r.sw);
+    const float Ax = fsub(A.x, fmul(r.sx, A.z)), Ay = fsub(A.y, fmul(r.sy, A.z));
+    const float Bx = fsub(B.x, fmul(r.sx, B.z)), By = fsub(B.y, fmul(r.sy, B.z));
+    const float Cx = fsub(C.x, fmul(r.sx, C.z)), Cy = fsub(C.y, fmul(r.sy, C.z));
+    const float U = fsub(fmul(Cx, By), fmul(Cy, Bx));
+    const float V = fsub(fmul(Ax, Cy), fmul(Ay, Cx));
+    const float W = fsub(fmul(Bx, Ay), fmul(By, Ax));
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = fadd(fadd(U, V), W);
+    if (det == 0.0f) return false;
+    const v3 e1 = sub(b, a), e2 = sub(c, a), p = cross(r.d, e2);
+    const float dm = dot(e1, p);
+    if (dm > -1e-7f && dm < 1e-7f) {
+        const float T = fadd(fadd(fmul(U, fmul(r.sz, A.z)), fmul(V, fmul(r.sz, B.z))), fmul(W, fmul(r.sz, C.z)));
+        const float inv = fdiv(1.0f, det);
+        t = fmul(T, inv); u = fmul(V, inv); v = fmul(W, inv);
+        return t > 1e-4f;
+    }
+    const float inv = fdiv(1.0f, dm);
+    const v3 tv = sub(r.o, a), q = cross(tv, e1);
+    u = smax(0.0f, fmul(dot(tv, p), inv));
+    v = smax(0.0f, fmul(dot(r.d, q), inv));
+    t = fmul(dot(e2, q), inv);
+    const float s = fadd(u, v);
+    if (s > 1.0f) { u = fdiv(u, s); v = fdiv(v, s); }
+    return t > 1e-4f;
+}
+
 // ------------------------------------------------------------------ misc
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 

@@ -43,6 +43,7 @@ enum Slot {
     WS_SUR_AO4, WS_SUR_PRED, WS_SUR_FB, WS_SUR_AOFB, WS_SUR_STATS, WS_VPOS, WS_VNRM, WS_VDEPTH, WS_GTAO,
     WS_ALB_IN, WS_ALB, WS_MOTION, WS_FRAME, WS_HDR, WS_FRAME_SMALL, WS_MIRROR,
     WS_HYB_LIT, WS_HYB_TRI, WS_HYB_T, WS_HYB_NG, WS_CLOSEST_TRI, WS_CLOSEST_T,
+    WS_PT_SAMPLES, WS_PT_ACC, WS_PT_OUT,
     WS_COUNT
 };
 
@@ -65,6 +66,7 @@ struct Tune {
     int accel_leaf_small = 4;   // ... of those with fewer than kSmallScene triangles
     int frame_direct = 1;       // host-buffer frames: the passes read and write mapped host memory
     int hybrid_min_blocks = 6;  // resident 128-thread hybrid-pass blocks per SM: 5, 6 or 8
+    int pt_slice = 0;           // path tracer: samples per slice at most (0: as many as 2 GiB of terms hold)
 };
 constexpr uint32_t kSmallScene = 1u << 16;
 

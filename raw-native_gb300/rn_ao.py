@@ -36,7 +36,8 @@ EXPORTS = ("rn_ao_version", "rn_init", "rn_set_stream", "rn_synchronize", "rn_ac
            "rn_unet_set_clip", "rn_unet_last_grad_norm", "rn_unet_backward", "rn_unet_grad_count",
            "rn_unet_grads_flat", "rn_unet_apply",
            "rn_tune_set", "rn_tune_get", "rn_tune_load", "rn_tc_conv3x3", "rn_surrogate_ao", "rn_gtao", "rn_selftest_wait_budget",
-           "rn_render_frame", "rn_device_info")
+           "rn_render_frame", "rn_device_info", "rn_pt_scene_create", "rn_pt_scene_free", "rn_pt_scene_info",
+           "rn_pathtrace")
 
 
 class RnError(RuntimeError):
@@ -191,7 +192,7 @@ TUNE_KEYS = {"trace_min_blocks": (2, 3, 4), "batch_min_blocks": (2, 3, 4), "trac
              "trace_packet": (4, 8, 16),
              "trace_stack": (48, 96), "ssao_tile_h": (4, 8, 16), "conv_bn_max": (64, 128, 256), "conv_halo": (0, 1), "conv_pair": (0, 1),
              "accel_radius": (8, 16, 32, 64), "accel_leaf": (1, 2, 4, 8), "accel_leaf_small": (1, 2, 4, 8),
-             "frame_direct": (0, 1), "hybrid_min_blocks": (5, 6, 8)}
+             "frame_direct": (0, 1), "hybrid_min_blocks": (5, 6, 8), "pt_slice": (0, 1, 4, 16)}
 
 
 def tune_set(key: str, value: int) -> None:
@@ -830,3 +831,117 @@ def hybrid(g: GBuffer, accel: LinearAccel, eye, to_sun, geo_normal=None):
                            C.cast(l, C.c_void_p), args.flags,
                            args.ptr(lit, np.float32), args.ptr(tri, np.int32), args.ptr(t, np.float32), C.byref(st)), st)
     return lit, tri, t
+
+
+# ---------------------------------------------------------------- path tracer (raw::rt, interface v4)
+PT_CONTROLS = dict(drop_lambert_cosine=0x01, mis_weight_one=0x02, aov_drop_specular_indirect=0x04,
+                   aov_emission_to_diffuse=0x08, legacy_lobe_v2=0x10)
+PT_AOVS = (("radiance", 3, np.float32), ("albedo", 3, np.float32), ("normal", 3, np.float32),
+           ("depth", 1, np.float32), ("variance", 1, np.float32), ("triangle", 1, np.int32),
+           ("motion", 2, np.float32), ("diffuse", 3, np.float32), ("specular", 3, np.float32),
+           ("emission", 3, np.float32), ("diffuse_albedo", 3, np.float32), ("specular_albedo", 3, np.float32),
+           ("diffuse_variance", 1, np.float32), ("specular_variance", 1, np.float32))
+
+
+class PtMaterial(C.Structure):
+    _fields_ = [("base_factor", C.c_float), ("roughness", C.c_float), ("metallic", C.c_float),
+                ("specular", C.c_float), ("emission", C.c_float * 3)]
+
+
+class PtSceneDesc(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("nrm", C.c_void_p), ("uv", C.c_void_p), ("nvert", C.c_uint32),
+                ("idx", C.c_void_p), ("tri_texture", C.c_void_p), ("ntri", C.c_uint32),
+                ("tex_entries", C.c_void_p), ("ntex", C.c_uint32), ("texels", C.c_void_p), ("ntexels", C.c_uint32),
+                ("materials", C.c_void_p), ("sun_dir", C.c_float * 3), ("sun_irradiance", C.c_float * 3),
+                ("sky", C.c_float * 3)]
+
+
+class PtDesc(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("spp", C.c_uint32), ("spp_begin", C.c_uint32), ("max_bounces", C.c_uint32),
+                ("width", C.c_int32), ("height", C.c_int32), ("camera", C.c_float * 10), ("previous", C.c_float * 10),
+                ("jitter", C.c_int32), ("russian_roulette", C.c_int32), ("controls", C.c_uint32)]
+
+
+class PtOut(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name, _, _ in PT_AOVS]
+
+
+def pt_desc(d: dict) -> PtDesc:
+    """A render description (raw::rt::PathTraceDesc) from a dict: seed, spp, spp_begin,
+    max_bounces, width, height, camera (10 floats), previous, jitter, russian_roulette and
+    controls (names of PT_CONTROLS)."""
+    controls = 0
+    for k in d.get("controls", ()):
+        controls |= PT_CONTROLS[k]
+    return PtDesc(int(d.get("seed", 1)), int(d.get("spp", 16)), int(d.get("spp_begin", 0)),
+                  int(d.get("max_bounces", 64)), int(d["width"]), int(d["height"]), (C.c_float * 10)(*d["camera"]),
+                  (C.c_float * 10)(*d.get("previous", d["camera"])), int(d.get("jitter", True)),
+                  int(d.get("russian_roulette", True)), controls)
+
+
+class PtScene:
+    """A path-tracer scene on the GPU (rn_pt_scene_create: raw::rt::finishPtScene). `sc` holds
+    numpy arrays: pos (n,3), nrm (n,3), uv (n,2), idx (t,3), tri_tex (t,), tex_entries (k,3),
+    texels, materials (k,7: base_factor, roughness, metallic, specular, emission), sun_dir,
+    sun_irr, sky."""
+
+    def __init__(self, sc: dict):
+        f32 = lambda a: np.ascontiguousarray(a, np.float32)  # noqa: E731
+        u32 = lambda a: np.ascontiguousarray(a, np.uint32)  # noqa: E731
+        self._keep = dict(pos=f32(sc["pos"]), nrm=f32(sc["nrm"]), uv=f32(sc["uv"]), idx=u32(sc["idx"]),
+                          tri_tex=u32(sc["tri_tex"]), tex_entries=u32(sc["tex_entries"]), texels=u32(sc["texels"]))
+        mats = np.asarray(sc["materials"], np.float32).reshape(-1, 7)
+        self._mats = (PtMaterial * len(mats))(*[PtMaterial(m[0], m[1], m[2], m[3], (C.c_float * 3)(*m[4:7])) for m in mats])
+        k = self._keep
+        p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        desc = PtSceneDesc(p(k["pos"]), p(k["nrm"]), p(k["uv"]), k["pos"].size // 3, p(k["idx"]), p(k["tri_tex"]),
+                           k["tri_tex"].size, p(k["tex_entries"]), k["tex_entries"].size // 3, p(k["texels"]),
+                           k["texels"].size, C.cast(self._mats, C.c_void_p), (C.c_float * 3)(*sc["sun_dir"]),
+                           (C.c_float * 3)(*sc["sun_irr"]), (C.c_float * 3)(*sc["sky"]))
+        self._h = C.c_void_p()
+        st = Status()
+        _check(lib().rn_pt_scene_create(C.byref(desc), C.byref(self._h), C.byref(st)), st)
+        self._keep = None
+
+    def info(self) -> dict:
+        n, a = C.c_uint32(), C.c_float()
+        st = Status()
+        _check(lib().rn_pt_scene_info(self._h, C.byref(n), C.byref(a), C.byref(st)), st)
+        return dict(emitters=n.value, emitter_area=a.value)
+
+    def close(self) -> None:
+        if self._h:
+            lib().rn_pt_scene_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def path_trace(scene: PtScene, desc: dict, device: bool = False, planes=None):
+    """rn_pathtrace: every AOV of raw::rt::pathTraceCpu as (h, w[, k]) arrays (numpy, or CUDA
+    tensors with device=True). `planes` limits the outputs to those names."""
+    h, w = int(desc["height"]), int(desc["width"])
+    names = [n for n, _, _ in PT_AOVS if planes is None or n in planes]
+    outs = {}
+    if device:
+        import torch
+        tdt = {np.float32: torch.float32, np.int32: torch.int32}
+        for name, k, dt in PT_AOVS:
+            if name in names:
+                outs[name] = torch.empty((h, w, k) if k > 1 else (h, w), dtype=tdt[dt], device="cuda")
+        _use_torch_stream()
+        ptr = lambda name: C.c_void_p(outs[name].data_ptr()) if name in outs else None  # noqa: E731
+    else:
+        for name, k, dt in PT_AOVS:
+            if name in names:
+                outs[name] = np.zeros((h, w, k) if k > 1 else (h, w), dt)
+        ptr = lambda name: outs[name].ctypes.data_as(C.c_void_p) if name in outs else None  # noqa: E731
+    o = PtOut(*[ptr(name) for name, _, _ in PT_AOVS])
+    d = pt_desc(desc)
+    st = Status()
+    _check(lib().rn_pathtrace(scene._h, C.byref(d), RN_DEVICE_PTRS if device else 0, C.byref(o), C.byref(st)), st)
+    return outs

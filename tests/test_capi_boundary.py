@@ -185,3 +185,24 @@ def test_device_info_and_gpu_renderer_without_a_device(lib):
     args = [8, 8, p, p, p, p, p, 0, None, 1, 2, C.c_float(0.12), 0] + [None] * 14 + [None, 0, msg, 512]
     assert shim.shim_render_gpu(*args) == -1
     assert msg.value.startswith(b"gpuInit: ")
+
+
+@pytest.mark.skipif(_cuda_present(), reason="checks the behaviour without a GPU")
+def test_path_tracer_arguments_and_no_device(lib):
+    """rn_pt_scene_create rejects malformed scenes before touching a device (an index out of
+    range, a texture that is not a power of two) and reports no device otherwise."""
+    import rn_ao
+    sc = dict(pos=np.zeros((3, 3), np.float32), nrm=np.zeros((3, 3), np.float32), uv=np.zeros((3, 2), np.float32),
+              idx=np.array([[0, 1, 2]], np.uint32), tri_tex=np.zeros(1, np.uint32),
+              tex_entries=np.array([[0, 4, 4]], np.uint32), texels=np.zeros(16, np.uint32),
+              materials=np.array([[1, 0.5, 0, 0.5, 0, 0, 0]], np.float32), sun_dir=(0, 1, 0), sun_irr=(1, 1, 1),
+              sky=(0, 0, 0))
+    with pytest.raises(rn_ao.RnError) as e:
+        rn_ao.PtScene(dict(sc, idx=np.array([[0, 1, 3]], np.uint32)))
+    assert e.value.code == 1 and "out of range" in e.value.message
+    with pytest.raises(rn_ao.RnError) as e:
+        rn_ao.PtScene(dict(sc, tex_entries=np.array([[0, 3, 4]], np.uint32)))
+    assert e.value.code == 1 and "powers of two" in e.value.message
+    with pytest.raises(rn_ao.RnError) as e:
+        rn_ao.PtScene(sc)
+    assert e.value.code == 2
