@@ -24,7 +24,7 @@ rasterized on the GPU by this library); no dataset is involved.
            nothing in the frame's measurement
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-    python bench.py --workload batch|large|surrogate|hybrid|build   (the other workloads)
+    python bench.py --workload batch|large|surrogate|hybrid|build|pathtrace   (the other workloads)
 """
 from __future__ import annotations
 
@@ -62,7 +62,8 @@ def parse():
                    help="run only this pass `--steps` times after `--warmup` (for ncu), print nothing")
     p.add_argument("--spp", type=int, default=SPP, help="samples per pixel (the benchmark uses 256)")
     p.add_argument("--tris", type=int, default=1000000, help="--profile build: soup triangles")
-    p.add_argument("--workload", default="4k", choices=["4k", "batch", "large", "surrogate", "hybrid", "build"],
+    p.add_argument("--workload", default="4k", choices=["4k", "batch", "large", "surrogate", "hybrid", "build",
+                                                        "pathtrace"],
                    help="4k: the benchmark (built-in scene, 3840x2160, 256 spp); batch: 64 orbit views of the "
                         "seeded 744k-triangle scene in one batch; large: 16 4K views of the 7.88M-triangle scene")
     p.add_argument("--views", type=int, default=0, help="batch/large: number of views (default 64 / 16)")
@@ -758,8 +759,74 @@ def run_build(args):
     print(json.dumps(out), flush=True)
 
 
+def pt_fixture_scene(key: str):
+    """A lit scene of the reference's path tracer from tests/golden/pt_scenes.npz (made by the
+    reference's own scene builders): (scene dict, camera)."""
+    import numpy as np
+    z = np.load(os.path.join(ROOT, "tests", "golden", "pt_scenes.npz"))
+    sc = {k.split("/", 1)[1]: z[k] for k in z.files if k.startswith(key + "/")}
+    cam = sc.pop("camera")
+    return sc, cam
+
+
+def run_pathtrace(args):
+    """The path tracer (rn_pathtrace, interface v4): retro_room (the reference's lit room: sun
+    through the open end, a ceiling lamp, textured brick, tile, plank and brass) and iso_street
+    at 1280 x 720, 64 spp, 64 bounces with Russian roulette, every AOV; timed per frame with CUDA
+    events, outputs in HBM. The CPU baseline is the oracle (a restatement of raw::rt::pathTraceCpu,
+    bit-identical to the reference build) on the host's cores, on the same frame at 4 spp.
+    Metric: path samples per second."""
+    import torch
+    import rn_ao as rn
+    torch.cuda.set_device(0)
+    rn.init()
+    stream = torch.cuda.current_stream()
+    W, H, SPPS = 1280, 720, 64
+    out = {"metric": "path-traced samples per second (interface v4, every AOV)", "unit": "M samples/s",
+           "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic: the reference's own lit scenes", "scenes": []}
+    with Clocks(0) as clk:
+        for key in ("retro_room", "iso_street"):
+            sc, cam = pt_fixture_scene(key)
+            s = rn.PtScene(sc)
+            d = dict(seed=1, spp=SPPS, width=W, height=H, camera=[float(v) for v in cam])
+            for _ in range(max(1, args.warmup)):
+                o = rn.path_trace(s, d, device=True)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                o = rn.path_trace(s, d, device=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            row = {"scene": key, "width": W, "height": H, "spp": SPPS, "ms_per_frame": ms,
+                   "msamples_per_s": W * H * SPPS / (ms * 1e-3) / 1e6, "emitters": s.info()["emitters"],
+                   "radiance_mean": float(o["radiance"].mean().item())}
+            if not os.environ.get("RN_BENCH_NO_CPU"):
+                from oracle import oracle as O
+                # the same frame at 4 of the 64 samples: a bounded CPU sample of the same work
+                dd = dict(d, spp=4)
+                t0 = time.perf_counter()
+                O.pathtrace(sc, dd, threads=os.cpu_count() or 1)
+                dt = time.perf_counter() - t0
+                row["cpu_baseline"] = {"value": W * H * 4 / dt / 1e6, "unit": "M samples/s", "cores": os.cpu_count() or 1,
+                                       "kind": "port", "sample": "the same 1280x720 frame at 4 spp (%.1f s), oracle "
+                                       "restatement of pathTraceCpu, all host threads" % dt}
+            out["scenes"].append(row)
+            s.close()
+    first = out["scenes"][0]
+    out.update(value=first["msamples_per_s"], ms_per_step=first["ms_per_frame"], clocks=clk.summary(),
+               config={"workload": "path tracer, retro_room at 1280x720, 64 spp, 64 bounces (Russian roulette)",
+                       "outputs": "every AOV in HBM"}, gpu_launches=2 * args.steps)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "pathtrace":
+        run_pathtrace(args)
+        return
     if args.workload == "build":
         run_build(args)
         return
