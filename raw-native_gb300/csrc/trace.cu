@@ -64,6 +64,212 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
     }
 }
 
+// AO-only walks with warp-level compaction. A warp takes a packet of 32 pixels and puts all
+// of its walks (every covered pixel's spp samples) in one queue: each lane runs one walk
+// (pixel, sample) at a time, a node per loop step, and whenever fewer than `refill` lanes are
+// still walking, the idle lanes take the next walks of the queue, whichever pixel they
+// belong to. A lane is therefore not held by the slowest walk of its own pixel's sample
+// round, as in trace_kernel's one-pixel-per-lane loop; only the queue's last walks leave
+// lanes idle. A walk's rays, box tests and hit test are trace_pixel's (sample_direction,
+// slab, hit_tri, the frontier start), and a pixel's AO is its count of open walks over spp:
+// an integer count, so the order the walks finish in changes no bit.
+template <int kMinBlocks, int kStackN>
+__global__ void __launch_bounds__(256, kMinBlocks) trace_ao_pool_kernel(const __grid_constant__ TraceParams p,
+                                                                        uint32_t* tile_ctr, int refill) {
+    const int pl = p.packet_log2, tw = 1 << pl, th = 32 >> pl;
+    const int tiles_x = (p.w + tw - 1) >> pl, tiles_y = (p.h + th - 1) / th;
+    const uint32_t ntiles = (uint32_t)tiles_x * tiles_y;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned below = (1u << lane) - 1u;
+    __shared__ FrontierEntry frontier[8][kFrontier];
+    __shared__ int open_sh[8][32];
+    __shared__ uint8_t lane_sh[8][32];
+    FrontierEntry* F = frontier[threadIdx.x >> 5];
+    int* opens = open_sh[threadIdx.x >> 5];
+    uint8_t* lane_of = lane_sh[threadIdx.x >> 5];   // the covered lanes in lane order
+    const size_t np = (size_t)p.w * p.h;
+    int32_t stack[kStackN];
+    while (true) {
+        uint32_t tile = 0;
+        if (lane == 0) tile = atomicAdd(tile_ctr, 1u);
+        tile = __shfl_sync(0xffffffffu, tile, 0);
+        if (tile >= ntiles) break;
+        const int x = ((int)(tile % tiles_x) << pl) + (int)(lane & (tw - 1));
+        const int y = (int)(tile / tiles_x) * th + (int)(lane >> pl);
+        const bool valid = x < p.w && y < p.h;
+        const size_t i = valid ? (size_t)y * p.w + x : 0;
+        uint8_t m = 0;
+        v3 P = mk(0.0f, 0.0f, 0.0f), n = P;
+        if (valid) {
+            m = p.mask[i];
+            P = load3(p.pos + 3 * i);
+            n = load3(p.nrm + 3 * i);
+            if (p.mirror) {
+                store3(mirror_pos(p.mirror, np) + 3 * i, P);
+                store3(mirror_nrm(p.mirror, np) + 3 * i, n);
+                mirror_mask(p.mirror, np)[i] = m;
+            }
+            if (!m) {
+                p.ao[i] = 1.0f;
+                if (p.mirror) mirror_ao(p.mirror, np)[i] = 1.0f;
+            }
+        }
+        const bool covered = valid && m;
+        // basis (ray_ao.cpp:14-17) of the lane's own pixel; other lanes read it by shuffle
+        const v3 a = fabsf(n.x) > 0.9f ? mk(0.0f, 1.0f, 0.0f) : mk(1.0f, 0.0f, 0.0f);
+        v3 T = mk(0.0f, 0.0f, 0.0f), B = T, O = T;
+        if (covered) {
+            T = normalize(cross(a, n));
+            B = cross(n, T);
+            O = add(P, scale(n, 1e-3f));
+        }
+        const int fn = (p.has_geometry && p.frontier) ? tile_frontier(p, x, y, valid, F) : 0;
+        const unsigned cov = __ballot_sync(0xffffffffu, covered);
+        const int nc = __popc(cov);
+        opens[lane] = 0;
+        if (covered) lane_of[__popc(cov & below)] = (uint8_t)lane;
+        __syncwarp();
+        const uint32_t total = (uint32_t)nc * (uint32_t)p.spp;
+        uint32_t next = 0;
+        bool active = false;
+        int q = 0;                    // the lane whose pixel the current walk belongs to
+        v3 o = O, d = O;
+        Inv iv;
+        WRay wr;
+        bool wr_ready = false;
+        int32_t cur = 0;
+        int sp = 0;
+        uint32_t guard = 0;
+        const float tmax = p.radius;
+        while (p.has_geometry && total > 0) {
+            const unsigned busy = __ballot_sync(0xffffffffu, active);
+            if (__popc(busy) < refill && next < total) {
+                // the idle lanes take the next walks of the queue, in lane order
+                const unsigned idle = ~busy;
+                const uint32_t my = next + (uint32_t)__popc(idle & below);
+                next = min(total, next + (uint32_t)__popc(idle));
+                const bool take = !active && my < total;
+                const uint32_t wi = take ? my : 0u;
+                const int src = (int)lane_of[wi % (uint32_t)nc];
+                const v3 pt = mk(__shfl_sync(0xffffffffu, T.x, src), __shfl_sync(0xffffffffu, T.y, src),
+                                 __shfl_sync(0xffffffffu, T.z, src));
+                const v3 pb = mk(__shfl_sync(0xffffffffu, B.x, src), __shfl_sync(0xffffffffu, B.y, src),
+                                 __shfl_sync(0xffffffffu, B.z, src));
+                const v3 pn = mk(__shfl_sync(0xffffffffu, n.x, src), __shfl_sync(0xffffffffu, n.y, src),
+                                 __shfl_sync(0xffffffffu, n.z, src));
+                const v3 po = mk(__shfl_sync(0xffffffffu, O.x, src), __shfl_sync(0xffffffffu, O.y, src),
+                                 __shfl_sync(0xffffffffu, O.z, src));
+                const int qx = __shfl_sync(0xffffffffu, x, src), qy = __shfl_sync(0xffffffffu, y, src);
+                if (take) {
+                    q = src;
+                    o = po;
+                    d = sample_direction(pt, pb, pn, (uint32_t)qx, (uint32_t)qy, wi / (uint32_t)nc, p.corr);
+                    iv = make_inv(o, d);
+                    wr_ready = false;
+                    sp = 0;
+                    guard = 0;
+                    active = true;
+                    // start: the frontier's entries stand in for the root (walk(), trace_device.cuh)
+                    cur = 0;
+                    if (fn > 0) {
+                        int32_t nearest = -1;
+                        float tbest = 3.0e38f;
+                        bool hit = false;
+                        for (int e = 0; e < fn && !hit; ++e) {
+                            float tn;
+                            if (!slab(F[e].lo[0], F[e].hi[0], F[e].lo[1], F[e].hi[1], F[e].lo[2], F[e].hi[2], o, iv,
+                                      tmax, tn))
+                                continue;
+                            const int32_t c = F[e].word;
+                            if (c < 0) {
+                                if (!wr_ready) { wr = make_wray(o, d); wr_ready = true; }
+                                const uint32_t w = (uint32_t)~c;
+                                const uint32_t first = w >> 3, count = (w & 7u) + 1u;
+                                for (uint32_t k = 0; k < count && !hit; ++k) {
+                                    const float4* tq = reinterpret_cast<const float4*>(p.tris + first + k);
+                                    const float4 A = __ldg(tq), Bq = __ldg(tq + 1), C = __ldg(tq + 2);
+                                    float t;
+                                    if (hit_tri(wr, mk(A.x, A.y, A.z), mk(Bq.x, Bq.y, Bq.z), mk(C.x, C.y, C.z), t) &&
+                                        t < tmax)
+                                        hit = true;
+                                }
+                                continue;
+                            }
+                            if (nearest < 0) { nearest = c; tbest = tn; continue; }
+                            int32_t push = c;
+                            if (tn < tbest) { push = nearest; nearest = c; tbest = tn; }
+                            stack[sp++] = push;                  // fn <= kFrontier < kStackN
+                        }
+                        if (hit) active = false;                 // occluded: not open
+                        else if (nearest >= 0) cur = nearest;
+                        else if (sp > 0) cur = stack[--sp];
+                        else { active = false; atomicAdd(&opens[q], 1); }
+                    }
+                }
+            }
+            if (!__any_sync(0xffffffffu, active)) {
+                if (next >= total) break;
+                continue;
+            }
+            if (!active) continue;
+            // one node of the lane's walk
+            const float4* nq = reinterpret_cast<const float4*>(p.nodes + cur);
+            const float4 lx = __ldg(nq + 0), hx = __ldg(nq + 1), ly = __ldg(nq + 2), hy = __ldg(nq + 3);
+            const float4 lz = __ldg(nq + 4), hz = __ldg(nq + 5);
+            const int4 ch = __ldg(reinterpret_cast<const int4*>(nq + 6));
+            const int cnt = __ldg(reinterpret_cast<const int*>(nq + 7));
+            const float LX[4] = {lx.x, lx.y, lx.z, lx.w}, HX[4] = {hx.x, hx.y, hx.z, hx.w};
+            const float LY[4] = {ly.x, ly.y, ly.z, ly.w}, HY[4] = {hy.x, hy.y, hy.z, hy.w};
+            const float LZ[4] = {lz.x, lz.y, lz.z, lz.w}, HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+            const int32_t CH[4] = {ch.x, ch.y, ch.z, ch.w};
+            int32_t nearest = -1;
+            float tbest = 3.0e38f;
+            bool hit = false, overflow = false;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float tn;
+                if (hit || k >= cnt || !slab(LX[k], HX[k], LY[k], HY[k], LZ[k], HZ[k], o, iv, tmax, tn)) continue;
+                const int32_t c = CH[k];
+                if (c < 0) {
+                    if (!wr_ready) { wr = make_wray(o, d); wr_ready = true; }
+                    const uint32_t w = (uint32_t)~c;
+                    const uint32_t first = w >> 3, count = (w & 7u) + 1u;
+                    for (uint32_t j = 0; j < count; ++j) {
+                        const float4* tq = reinterpret_cast<const float4*>(p.tris + first + j);
+                        const float4 A = __ldg(tq), Bq = __ldg(tq + 1), C = __ldg(tq + 2);
+                        float t;
+                        if (hit_tri(wr, mk(A.x, A.y, A.z), mk(Bq.x, Bq.y, Bq.z), mk(C.x, C.y, C.z), t) && t < tmax) {
+                            hit = true;
+                            break;
+                        }
+                    }
+                    continue;
+                }
+                if (nearest < 0) { nearest = c; tbest = tn; continue; }
+                int32_t push = c;
+                if (tn < tbest) { push = nearest; nearest = c; tbest = tn; }
+                if (sp >= kStackN) { overflow = true; continue; }
+                stack[sp++] = push;
+            }
+            if (overflow) { atomicOr(p.err_word, DEV_STACK_OVERFLOW); active = false; continue; }
+            if (hit) { active = false; continue; }
+            if (++guard >= kGuard) { atomicOr(p.err_word, DEV_GUARD); active = false; continue; }
+            if (nearest >= 0) { cur = nearest; continue; }
+            if (sp > 0) { cur = stack[--sp]; continue; }
+            active = false;                              // nothing within the radius: open
+            atomicAdd(&opens[q], 1);
+        }
+        __syncwarp();
+        if (covered) {
+            // no geometry: every ray is open
+            const int open = p.has_geometry ? opens[lane] : p.spp;
+            p.ao[i] = fdiv((float)open, (float)p.spp);
+            if (p.mirror) mirror_ao(p.mirror, np)[i] = p.ao[i];
+        }
+        __syncwarp();                              // the frontier and counts are reused by the next packet
+    }
+}
+
 __global__ void occluded_kernel(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, int has_geometry,
                                 const float* __restrict__ rays, const float* __restrict__ tmax, uint32_t n,
                                 uint8_t* __restrict__ hit, uint32_t* err) {
@@ -128,8 +334,11 @@ template <int kMB, int kStackN>
 void launch_variant(const TraceParams& p, int sm_count, cudaStream_t s, uint32_t* tile_ctr, unsigned long long* counts,
                     uint32_t stride) {
     const int blocks = sm_count * kMB;
+    const int pool = ctx().tune.trace_pool;
     if (counts)
         trace_kernel<true, kMB, kStack><<<blocks, 256, 0, s>>>(p, tile_ctr, counts, stride < 1 ? 1 : stride);
+    else if (pool > 0 && !p.want_sky)
+        trace_ao_pool_kernel<kMB, kStackN><<<blocks, 256, 0, s>>>(p, tile_ctr, pool);
     else
         trace_kernel<false, kMB, kStackN><<<blocks, 256, 0, s>>>(p, tile_ctr, nullptr, 1);
 }

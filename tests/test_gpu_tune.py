@@ -25,7 +25,7 @@ def _scene(rn, w, h, n_boxes=300, n_spheres=60):
 def test_trace_keys_keep_every_bit(rn, restore_tune):
     g, acc, tl = _scene(rn, 333, 197)
     defaults = {"trace_min_blocks": 3, "trace_packet": 8, "trace_stack": 96, "trace_frontier": 1,
-                "trace_frontier_min_spp": 1, "trace_frontier_tail": 0}
+                "trace_frontier_min_spp": 1, "trace_frontier_tail": 0, "trace_pool": 0}
     for k, v in defaults.items():
         rn.tune_set(k, v)
     ref_ao = rn.compute_rtao(g, acc, 16, 1.0).clone()
@@ -37,6 +37,31 @@ def test_trace_keys_keep_every_bit(rn, restore_tune):
             vis = rn.compute_rt_visibility(g, acc, 16, 1.0, tl)
             assert all(bool((a == b).all()) for a, b in zip(vis, ref_vis)), (k, v)
         rn.tune_set(k, defaults[k])
+
+
+@pytest.mark.parametrize("spp", [1, 4, 7, 16])
+def test_pooled_walks_keep_every_bit(rn, oracle, restore_tune, spp):
+    """AO-only walks from one queue per packet (trace_pool) against one pixel per lane, for
+    every refill threshold, packet shape and frontier setting, on a ragged frame; and against
+    the oracle."""
+    import numpy as np
+    g, acc, _ = _scene(rn, 211, 101)
+    rn.tune_set("trace_pool", 0)
+    ref = rn.compute_rtao(g, acc, spp, 1.0).clone()
+    for pool in (16, 24, 32):
+        for packet in (4, 8, 16):
+            for frontier in (0, 1):
+                rn.tune_set("trace_pool", pool)
+                rn.tune_set("trace_packet", packet)
+                rn.tune_set("trace_frontier", frontier)
+                rn.tune_set("trace_frontier_min_spp", 1)
+                got = rn.compute_rtao(g, acc, spp, 1.0)
+                assert bool((got == ref).all()), (pool, packet, frontier, int((got != ref).sum().item()))
+    import scene as scenes
+    sc = scenes.build_synthetic_scene(11, 300, 60)
+    want = oracle.trace(g.position.cpu().numpy(), g.normal.cpu().numpy(), g.mask.cpu().numpy(), sc.tris, spp, 1.0,
+                        threads=8)
+    assert np.array_equal(ref.cpu().numpy(), want)
 
 
 def test_ssao_tile_keeps_every_bit(rn, restore_tune):
