@@ -58,7 +58,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-row-stride", type=int, default=4, help="rows of the CPU sample: every n-th")
-    p.add_argument("--profile", choices=["frame", "trace", "ssao", "reconcile", "build", "unet", "surrogate"],
+    p.add_argument("--profile", choices=["frame", "trace", "ssao", "reconcile", "build", "unet", "surrogate",
+                                         "pathtrace"],
                    help="run only this pass `--steps` times after `--warmup` (for ncu), print nothing")
     p.add_argument("--spp", type=int, default=SPP, help="samples per pixel (the benchmark uses 256)")
     p.add_argument("--tris", type=int, default=1000000, help="--profile build: soup triangles")
@@ -366,6 +367,17 @@ def run_profile(args):
         x = torch.rand(1, *net.shape[1:], 5, device="cuda")
         for _ in range(args.warmup + args.steps):
             net.forward(x)
+        torch.cuda.synchronize()
+        return
+    if args.profile == "pathtrace":
+        # the path tracer on retro_room at --res (default 3840x2160 is too large a capture:
+        # pass e.g. --res 320x180) and --spp samples
+        fw, fh = (int(v) for v in args.res.split("x"))
+        sc, cam = pt_fixture_scene("retro_room")
+        s = rn.PtScene(sc)
+        d = dict(seed=1, spp=args.spp, width=fw, height=fh, camera=[float(v) for v in cam])
+        for _ in range(args.warmup + args.steps):
+            rn.path_trace(s, d, device=True)
         torch.cuda.synchronize()
         return
     if args.profile == "surrogate":
