@@ -16,6 +16,10 @@
 //     src/renderer/rt_pt_energy.cpp builds it, then read on the device;
 //   - per pixel the samples are summed in sample order and the moments kept in float64.
 //
+// Code size: the walks, the surface query, the lobe's evaluation and its energy terms are
+// called from several places of a path's bounce; they are kept out of line (one copy each)
+// so that the kernel fits the instruction cache (inlined, fetch stalls dominated).
+//
 // Work: samples of a slice are traced in parallel, one thread per (pixel, sample), a warp
 // on an 8 x 4 pixel tile for one sample index (coherent primary rays); each sample's eight
 // colour terms go to a slice buffer, and a second kernel adds them per pixel in sample
@@ -291,7 +295,7 @@ __device__ __forceinline__ float lambda_f(float a2, float cosT) {
     return fmul(fadd(-1.0f, fsqrt(fadd(1.0f, fdiv(fmul(a2, fsub(1.0f, c2)), c2)))), 0.5f);
 }
 // VNDF sampling (Heitz 2018); u2 = kb / 2^24, so phi is the sampler angle kb.
-__device__ v3 sample_vndf(const PtParams& P, v3 wo, float a, float u1, uint32_t kb) {
+__device__ __noinline__ v3 sample_vndf(const PtParams& P, v3 wo, float a, float u1, uint32_t kb) {
     const v3 vh = normalize(mk(fmul(a, wo.x), fmul(a, wo.y), wo.z));
     const float lensq = fadd(fmul(vh.x, vh.x), fmul(vh.y, vh.y));
     const v3 t1 = lensq > 0.0f ? scale(mk(-vh.y, vh.x, 0.0f), fdiv(1.0f, fsqrt(lensq))) : mk(1.0f, 0.0f, 0.0f);
@@ -337,7 +341,7 @@ __device__ __forceinline__ void table_avg(const float* __restrict__ t, float rou
     A = fadd(fmul(__ldg(p), gy), fmul(__ldg(p + 2), fy)); B = fadd(fmul(__ldg(p + 1), gy), fmul(__ldg(p + 3), fy));
 }
 struct Energy { float ms, wd, kd, eavg; };
-__device__ Energy energy_of(const PtParams& P, const Bsdf& m, float muO, float muI) {
+__device__ __noinline__ Energy energy_of(const PtParams& P, const Bsdf& m, float muO, float muI) {
     float oa, ob, ia, ib, aa, ab;
     table_ab(P.table, muO, m.rough, oa, ob);
     table_ab(P.table, muI, m.rough, ia, ib);
@@ -374,7 +378,7 @@ __device__ __forceinline__ Spec spec_terms(const Bsdf& m, v3 wo, v3 wi) {
 __device__ __forceinline__ float km_of(const Bsdf& m, float b, const Energy& en) {
     return fadd(fmul(m.metallic, kms(fadd(b, fdiv(fsub(1.0f, b), 21.0f)), en.eavg)), fmul(fsub(1.0f, m.metallic), en.kd));
 }
-__device__ Eval eval_bsdf(const PtParams& P, const Bsdf& m, v3 wo, v3 wi, bool dropCosine) {
+__device__ __noinline__ Eval eval_bsdf(const PtParams& P, const Bsdf& m, v3 wo, v3 wi, bool dropCosine) {
     Eval r{mk(0.0f, 0.0f, 0.0f), 0.0f};
     if (wo.z <= 0.0f || wi.z <= 0.0f) return r;
     const float ps = lobe_prob(m), cosI = dropCosine ? 1.0f : wi.z;
@@ -405,7 +409,7 @@ __device__ Eval eval_bsdf(const PtParams& P, const Bsdf& m, v3 wo, v3 wi, bool d
     r.pdf = pdf;
     return r;
 }
-__device__ v3 lambert_cos(const PtParams& P, const Bsdf& m, v3 wo, v3 wi, bool dropCosine) {
+__device__ __noinline__ v3 lambert_cos(const PtParams& P, const Bsdf& m, v3 wo, v3 wi, bool dropCosine) {
     if (wo.z <= 0.0f || wi.z <= 0.0f) return mk(0.0f, 0.0f, 0.0f);
     const float cosI = dropCosine ? 1.0f : wi.z, kd = fdiv(fsub(1.0f, m.metallic), kPiF);
     v3 f = mk(fmul(m.base.x, kd), fmul(m.base.y, kd), fmul(m.base.z, kd));
@@ -438,7 +442,7 @@ __device__ bool sample_bsdf(const PtParams& P, const Bsdf& m, v3 wo, float pick,
 struct Surf { v3 p, n, ng, base; const float* m; float t; int tri; };
 __device__ __forceinline__ v3 tri_corner(const PtParams& P, int t, int k) { return load3(P.tris + (size_t)t * 9 + 3 * k); }
 
-__device__ bool hit(const PtParams& P, v3 o, v3 d, float tmax, Surf& x) {
+__device__ __noinline__ bool hit(const PtParams& P, v3 o, v3 d, float tmax, Surf& x) {
     if (!P.has_geometry) return false;
     float t;
     const int tri = walk_closest(P.nodes, P.ltris, o, d, tmax, t, P.err);
@@ -471,7 +475,7 @@ __device__ bool hit(const PtParams& P, v3 o, v3 d, float tmax, Surf& x) {
     (void)tt;
     return true;
 }
-__device__ __forceinline__ bool visible(const PtParams& P, v3 p, v3 dir, float tmax) {
+__device__ __noinline__ bool visible(const PtParams& P, v3 p, v3 dir, float tmax) {
     if (!P.has_geometry) return true;
     Counts cn;
     return walk<false>(P.nodes, P.ltris, p, dir, tmax, tmax, P.err, cn) == 0;

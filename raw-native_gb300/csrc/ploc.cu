@@ -406,6 +406,121 @@ __global__ void ploc_scatter(const RoundState* __restrict__ st, const int32_t* _
         run += (unsigned long long)o[k] | ((unsigned long long)g[k] << 32);
     }
 }
+// The remaining rounds in one block, once few clusters are left: the round's three steps
+// (nearest neighbours, the flags' prefix sum, the scatter) are separated by block barriers
+// instead of kernel launches, and the round state lives in shared memory. Each thread takes
+// a contiguous run of positions, so the prefix sum runs in position order and node ids,
+// cluster order and boxes are ploc_nn / ploc_scatter's exactly. At most max_rounds rounds
+// (a bound, not a wait: every round either merges or sets DEV_PLOC_NO_MERGE and stops).
+constexpr int kTailThreads = 1024;
+__global__ void __launch_bounds__(kTailThreads) ploc_tail(RoundState* st, int32_t* __restrict__ cl0,
+                                                          int32_t* __restrict__ cl1, float* __restrict__ cb0,
+                                                          float* __restrict__ cb1, int32_t* __restrict__ nn,
+                                                          float* __restrict__ box, int32_t* __restrict__ left,
+                                                          int32_t* __restrict__ right, int R, uint32_t max_rounds) {
+    __shared__ uint32_t s_m, s_next, s_parity, s_rounds, s_error;
+    __shared__ unsigned long long warp_tot[kTailThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) { s_m = st->m; s_next = st->next; s_parity = st->parity; s_rounds = st->rounds; s_error = 0; }
+    __syncthreads();
+    for (uint32_t guard = 0; guard < max_rounds; ++guard) {
+        const uint32_t m = s_m;
+        if (m <= 1 || s_error) break;
+        const bool p = s_parity != 0;
+        const float* cb = p ? cb1 : cb0;
+        float* cbo = p ? cb0 : cb1;
+        const int32_t* cl = p ? cl1 : cl0;
+        int32_t* clo = p ? cl0 : cl1;
+        // nearest neighbours (ploc_nn_any)
+        for (uint32_t i = tid; i < m; i += kTailThreads) {
+            const float* A = cb + (size_t)i * 6;
+            const int ii = (int)i;
+            const int j0 = ii - R > 0 ? ii - R : 0, j1 = ii + R < (int)m - 1 ? ii + R : (int)m - 1;
+            float best = FLT_MAX;
+            int arg = -1;
+            for (int j = j0; j <= j1; ++j) {
+                if (j == ii) continue;
+                const float* B = cb + (size_t)j * 6;
+                const float d = ploc_area(smin(A[0], B[0]), smin(A[1], B[1]), smin(A[2], B[2]),
+                                          smax(A[3], B[3]), smax(A[4], B[4]), smax(A[5], B[5]));
+                if (d < best) { best = d; arg = j; }
+            }
+            nn[i] = arg;
+        }
+        __syncthreads();
+        // flags of this thread's run of positions, then their prefix sum in position order
+        const uint32_t chunk = (m + kTailThreads - 1) / kTailThreads;
+        const uint32_t b0 = min(m, (uint32_t)tid * chunk), b1 = min(m, b0 + chunk);
+        unsigned long long s = 0;
+        for (uint32_t i = b0; i < b1; ++i) {
+            uint32_t o, g;
+            ploc_flags(nn, i, o, g);
+            s += (unsigned long long)o | ((unsigned long long)g << 32);
+        }
+        unsigned long long x = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long w = warp_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_tot[lane] = w;
+        }
+        __syncthreads();
+        const unsigned long long total = warp_tot[kTailThreads / 32 - 1];
+        const uint32_t merges = (uint32_t)(total >> 32);
+        if (merges == 0) {
+            if (tid == 0) s_error = DEV_PLOC_NO_MERGE;
+            __syncthreads();
+            break;
+        }
+        unsigned long long run = (warp == 0 ? 0ull : warp_tot[warp - 1]) + x - s;
+        const uint32_t next = s_next;
+        for (uint32_t i = b0; i < b1; ++i) {
+            uint32_t o, g;
+            ploc_flags(nn, i, o, g);
+            if (o) {
+                const uint32_t pos = (uint32_t)(run & 0xFFFFFFFFull);
+                if (g) {
+                    const uint32_t id = next + (uint32_t)(run >> 32);
+                    const int32_t j = nn[i];
+                    const float* A = cb + (size_t)i * 6;
+                    const float* B = cb + (size_t)j * 6;
+                    float nb6[6];
+                    for (int a = 0; a < 3; ++a) { nb6[a] = smin(A[a], B[a]); nb6[3 + a] = smax(A[3 + a], B[3 + a]); }
+                    for (int a = 0; a < 6; ++a) { box[(size_t)id * 6 + a] = nb6[a]; cbo[(size_t)pos * 6 + a] = nb6[a]; }
+                    left[id] = cl[i];
+                    right[id] = cl[j];
+                    clo[pos] = (int32_t)id;
+                } else {
+                    for (int a = 0; a < 6; ++a) cbo[(size_t)pos * 6 + a] = cb[(size_t)i * 6 + a];
+                    clo[pos] = cl[i];
+                }
+            }
+            run += (unsigned long long)o | ((unsigned long long)g << 32);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            s_next = next + merges;
+            s_m = (uint32_t)(total & 0xFFFFFFFFull);
+            s_parity ^= 1u;
+            s_rounds += 1;
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        st->m = s_m; st->next = s_next; st->parity = s_parity; st->rounds = s_rounds;
+        if (s_error) st->error |= s_error;
+        else if (s_m > 1) st->error |= DEV_GUARD;
+    }
+}
+
 __global__ void ploc_commit(RoundState* st) {
     if (st->m <= 1 || st->merges == 0) return;
     st->next += st->merges;
@@ -650,8 +765,22 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
     uint32_t m_known = n;
     RoundState hs = init;
     const int kBatch = 6;
+    const uint32_t tail_max = (uint32_t)ctx().tune.ploc_tail;
     for (int batch = 0; m_known > 1; ++batch) {
         if (batch > 2000) return fail(st, RN_ERR_BUDGET, "PLOC: more than %d rounds", batch * kBatch);
+        if (m_known <= tail_max) {
+            // the last rounds in one block (at most one round per cluster: each merges one pair or more)
+            ploc_tail<<<1, kTailThreads, 0, s>>>(state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right,
+                                                 radius, m_known + 1);
+            RN_CUDA(cudaGetLastError(), st);
+            RN_CUDA(cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, s), st);
+            RN_CUDA(cudaStreamSynchronize(s), st);
+            if (hs.error & DEV_PLOC_NO_MERGE)
+                return fail(st, RN_ERR_STATE, "PLOC round %u made no merge (%u clusters)", hs.rounds, hs.m);
+            if (hs.error & DEV_GUARD) return fail(st, RN_ERR_BUDGET, "PLOC: rounds left %u clusters", hs.m);
+            m_known = hs.m;
+            break;
+        }
         const uint32_t nbn = cdiv(m_known, kThreads), nbc = cdiv(m_known, kTile);
         for (int r = 0; r < kBatch; ++r) {
             if (radius == 16)
