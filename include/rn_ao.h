@@ -358,6 +358,8 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *                                    clusters on run in one block (0: a launch per step)
  *   trace_pool        0|16|24|32     AO-only walks: one queue of a packet's walks, idle lanes
  *                                    refilled when fewer than this many walk (0: one pixel per lane)
+ *   pt_regen          0|4|8|16       rn_pathtrace: persistent threads that start a new path when
+ *                                    theirs ends, this many 128-thread blocks per SM (0: a thread a sample)
  *   pt_slice          0|1|4|16       rn_pathtrace: samples traced per slice at most (0: as many
  *                                    as 2 GiB of per-sample terms hold)
  * Process-wide; RN_TUNE_<KEY> environment variables apply before the first call.

@@ -128,6 +128,7 @@ const TuneKey kTuneKeys[] = {
     {"frame_direct", "RN_TUNE_FRAME_DIRECT", &Tune::frame_direct, {0, 1}, 2},
     {"hybrid_min_blocks", "RN_TUNE_HYBRID_MIN_BLOCKS", &Tune::hybrid_min_blocks, {5, 6, 8}, 3},
     {"pt_slice", "RN_TUNE_PT_SLICE", &Tune::pt_slice, {0, 1, 4, 16}, 4},
+    {"pt_regen", "RN_TUNE_PT_REGEN", &Tune::pt_regen, {0, 4, 8, 16}, 4},
     {"trace_pool", "RN_TUNE_TRACE_POOL", &Tune::trace_pool, {0, 16, 24, 32}, 4},
     {"ploc_tail", "RN_TUNE_PLOC_TAIL", &Tune::ploc_tail, {0, 4096, 32768, 262144}, 4},
 };

@@ -528,77 +528,109 @@ __device__ v3 nee(const PtParams& P, const Surf& x, const Frame& fr, const Bsdf&
 }
 
 struct Sample { v3 L, D, S, E, alb, nrm, dAlb, sAlb; };
-// rt_pt_cpu.cpp:31-97
-__device__ Sample trace_path(const PtParams& P, v3 ro, v3 rd, uint32_t px, uint32_t smp) {
+// One path's state between bounces (the locals of rt_pt_cpu.cpp:31-97's loop).
+struct Path {
+    Sample o;
+    v3 ro, rd, T, tw, R, wd, ws;
+    float prevPdf;
+    uint32_t b, px, smp;
+};
+__device__ __forceinline__ void path_start(Path& s, v3 ro, v3 rd, uint32_t px, uint32_t smp) {
     const v3 z = mk(0.0f, 0.0f, 0.0f);
-    Sample o{z, z, z, z, z, z, z, z};
-    v3 T = mk(1.0f, 1.0f, 1.0f), tw = T, R = z, wd = z, ws = z;
-    float prevPdf = 0.0f;
+    s.o = Sample{z, z, z, z, z, z, z, z};
+    s.ro = ro; s.rd = rd;
+    s.T = mk(1.0f, 1.0f, 1.0f); s.tw = s.T; s.R = z; s.wd = z; s.ws = z;
+    s.prevPdf = 0.0f;
+    s.b = 0; s.px = px; s.smp = smp;
+}
+// One bounce (one iteration of rt_pt_cpu.cpp:37-91's loop); false when the path ends.
+__device__ __noinline__ bool path_bounce(const PtParams& P, Path& s) {
+    const uint32_t b = s.b;
+    if (b > P.max_bounces) return false;
     const bool dc = (P.controls & RN_PT_DROP_LAMBERT_COSINE) != 0;
-    for (uint32_t b = 0; b <= P.max_bounces; ++b) {
-        Surf x0;
-        if (!hit(P, ro, rd, 1e30f, x0)) {
-            o.L = add(o.L, mulv(T, P.sky));
-            if (b == 0) o.E = P.sky; else R = add(R, mulv(tw, P.sky));
-            break;
-        }
-        const Bsdf bs{x0.base, __ldg(x0.m + 1), __ldg(x0.m + 2), __ldg(x0.m + 3), (P.controls & RN_PT_LEGACY_LOBE_V2) != 0};
-        if (b == 0) {
-            o.alb = x0.base; o.nrm = x0.n;
-            o.dAlb = scale(x0.base, fsub(1.0f, bs.metallic));
-            o.sAlb = spec_albedo(bs, clampf(-dot(x0.n, rd), 0.0f, 1.0f));
-        }
-        const v3 Le = mk(__ldg(x0.m + 4), __ldg(x0.m + 5), __ldg(x0.m + 6));
-        if (maxc(Le) > 0.0f) {
-            float w = 1.0f;
-            if (b > 0 && !(P.controls & RN_PT_MIS_WEIGHT_ONE)) {
-                const float cosL = fabsf(dot(x0.ng, rd)), pl = fdiv(fmul(x0.t, x0.t), fmul(cosL, P.area));
-                w = fdiv(fmul(prevPdf, prevPdf), fadd(fmul(prevPdf, prevPdf), fmul(pl, pl)));
-            }
-            o.L = add(o.L, scale(mulv(T, Le), w));
-            if (b == 0) o.E = Le; else R = add(R, scale(mulv(tw, Le), w));
-        }
-        if (b == P.max_bounces) break;
-        const Frame fr = basis(x0.n);
-        const v3 woL = to_local(fr, scale(rd, -1.0f));
-        if (woL.z <= 0.0f) break;
-        const uint32_t base = 2 + b * 4;
-        v3 nd;
-        const v3 Ln = nee(P, x0, fr, bs, woL, px, smp, base, nd);
-        o.L = add(o.L, mulv(T, Ln));
-        if (b == 0) { o.D = nd; o.S = sub(Ln, nd); } else R = add(R, mulv(tw, Ln));
-        const R2 u = rand2(P, px, smp, base), r = rand2(P, px, smp, base + 1);
-        v3 wiL;
-        if (!sample_bsdf(P, bs, woL, r.a, u.a, u.kb, wiL)) break;
-        const Eval e = eval_bsdf(P, bs, woL, wiL, dc);
-        if (e.pdf <= 0.0f) break;
-        const float ip = fdiv(1.0f, e.pdf);
-        const v3 step = scale(e.fcos, ip);
-        T = mulv(T, step);
-        if (b == 0) { wd = scale(lambert_cos(P, bs, woL, wiL, dc), ip); ws = sub(step, wd); }
-        else tw = mulv(tw, step);
-        prevPdf = e.pdf;
-        if (P.rr && b >= 3) {
-            const float q = smin(0.95f, maxc(T));
-            if (r.b >= q) break;
-            const float iq = fdiv(1.0f, q);
-            T = scale(T, iq);
-            tw = scale(tw, iq);
-        }
-        const v3 wi = to_world(fr, wiL);
-        ro = offset_of(x0, wi);
-        rd = wi;
+    Surf x0;
+    if (!hit(P, s.ro, s.rd, 1e30f, x0)) {
+        s.o.L = add(s.o.L, mulv(s.T, P.sky));
+        if (b == 0) s.o.E = P.sky; else s.R = add(s.R, mulv(s.tw, P.sky));
+        return false;
     }
-    o.D = add(o.D, mulv(wd, R));
-    if (!(P.controls & RN_PT_AOV_DROP_SPECULAR_INDIRECT)) o.S = add(o.S, mulv(ws, R));
-    if (P.controls & RN_PT_AOV_EMISSION_TO_DIFFUSE) { o.D = add(o.D, o.E); o.E = z; }
-    return o;
+    const Bsdf bs{x0.base, __ldg(x0.m + 1), __ldg(x0.m + 2), __ldg(x0.m + 3), (P.controls & RN_PT_LEGACY_LOBE_V2) != 0};
+    if (b == 0) {
+        s.o.alb = x0.base; s.o.nrm = x0.n;
+        s.o.dAlb = scale(x0.base, fsub(1.0f, bs.metallic));
+        s.o.sAlb = spec_albedo(bs, clampf(-dot(x0.n, s.rd), 0.0f, 1.0f));
+    }
+    const v3 Le = mk(__ldg(x0.m + 4), __ldg(x0.m + 5), __ldg(x0.m + 6));
+    if (maxc(Le) > 0.0f) {
+        float w = 1.0f;
+        if (b > 0 && !(P.controls & RN_PT_MIS_WEIGHT_ONE)) {
+            const float cosL = fabsf(dot(x0.ng, s.rd)), pl = fdiv(fmul(x0.t, x0.t), fmul(cosL, P.area));
+            w = fdiv(fmul(s.prevPdf, s.prevPdf), fadd(fmul(s.prevPdf, s.prevPdf), fmul(pl, pl)));
+        }
+        s.o.L = add(s.o.L, scale(mulv(s.T, Le), w));
+        if (b == 0) s.o.E = Le; else s.R = add(s.R, scale(mulv(s.tw, Le), w));
+    }
+    if (b == P.max_bounces) return false;
+    const Frame fr = basis(x0.n);
+    const v3 woL = to_local(fr, scale(s.rd, -1.0f));
+    if (woL.z <= 0.0f) return false;
+    const uint32_t base = 2 + b * 4;
+    v3 nd;
+    const v3 Ln = nee(P, x0, fr, bs, woL, s.px, s.smp, base, nd);
+    s.o.L = add(s.o.L, mulv(s.T, Ln));
+    if (b == 0) { s.o.D = nd; s.o.S = sub(Ln, nd); } else s.R = add(s.R, mulv(s.tw, Ln));
+    const R2 u = rand2(P, s.px, s.smp, base), r = rand2(P, s.px, s.smp, base + 1);
+    v3 wiL;
+    if (!sample_bsdf(P, bs, woL, r.a, u.a, u.kb, wiL)) return false;
+    const Eval e = eval_bsdf(P, bs, woL, wiL, dc);
+    if (e.pdf <= 0.0f) return false;
+    const float ip = fdiv(1.0f, e.pdf);
+    const v3 step = scale(e.fcos, ip);
+    s.T = mulv(s.T, step);
+    if (b == 0) { s.wd = scale(lambert_cos(P, bs, woL, wiL, dc), ip); s.ws = sub(step, s.wd); }
+    else s.tw = mulv(s.tw, step);
+    s.prevPdf = e.pdf;
+    if (P.rr && b >= 3) {
+        const float q = smin(0.95f, maxc(s.T));
+        if (r.b >= q) return false;
+        const float iq = fdiv(1.0f, q);
+        s.T = scale(s.T, iq);
+        s.tw = scale(s.tw, iq);
+    }
+    const v3 wi = to_world(fr, wiL);
+    s.ro = offset_of(x0, wi);
+    s.rd = wi;
+    s.b = b + 1;
+    return true;
+}
+// rt_pt_cpu.cpp:92-96: the split's last terms.
+__device__ __forceinline__ void path_finish(const PtParams& P, Path& s) {
+    s.o.D = add(s.o.D, mulv(s.wd, s.R));
+    if (!(P.controls & RN_PT_AOV_DROP_SPECULAR_INDIRECT)) s.o.S = add(s.o.S, mulv(s.ws, s.R));
+    if (P.controls & RN_PT_AOV_EMISSION_TO_DIFFUSE) { s.o.D = add(s.o.D, s.o.E); s.o.E = mk(0.0f, 0.0f, 0.0f); }
+}
+__device__ __forceinline__ void store_sample(const PtParams& P, uint32_t j, uint32_t px, const Sample& o) {
+    const size_t stride = (size_t)P.kn * P.npix;
+    float* s = P.samp + (size_t)j * P.npix + px;
+    const v3* f = &o.L;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        s[(3 * c) * stride] = f[c].x;
+        s[(3 * c + 1) * stride] = f[c].y;
+        s[(3 * c + 2) * stride] = f[c].z;
+    }
 }
 
 // rt_pt_cpu.cpp:21-24
 __device__ __forceinline__ v3 dir_of(const PtCam& c, float px, float py, int w, int h) {
     const float nx = fsub(fmul(fdiv(px, (float)w), 2.0f), 1.0f), ny = fsub(1.0f, fmul(fdiv(py, (float)h), 2.0f));
     return normalize(add(add(c.f, scale(c.s, fmul(fmul(nx, c.th), c.aspect))), scale(c.u, fmul(ny, c.th))));
+}
+
+__device__ __forceinline__ v3 camera_ray(const PtParams& P, int x, int y, uint32_t px, uint32_t smp) {
+    float ja = 0.5f, jb = 0.5f;
+    if (P.jitter) { const R2 r = rand2(P, px, smp, 0); ja = r.a; jb = r.b; }
+    return dir_of(P.cam, fadd((float)x, ja), fadd((float)y, jb), P.w, P.h);
 }
 
 // One thread per (pixel, sample of the slice): a warp takes an 8 x 4 pixel tile for one sample.
@@ -612,18 +644,46 @@ __global__ void __launch_bounds__(128) pt_paths_kernel(const PtParams P) {
     if (x >= P.w || y >= P.h) return;
     const uint32_t px = (uint32_t)(y * P.w + x);
     const uint32_t smp = P.spp_begin + P.k0 + j;
-    float ja = 0.5f, jb = 0.5f;
-    if (P.jitter) { const R2 r = rand2(P, px, smp, 0); ja = r.a; jb = r.b; }
-    const v3 dir = dir_of(P.cam, fadd((float)x, ja), fadd((float)y, jb), P.w, P.h);
-    const Sample o = trace_path(P, P.cam.eye, dir, px, smp);
-    const size_t stride = (size_t)P.kn * P.npix;
-    float* s = P.samp + (size_t)j * P.npix + px;
-    const v3* f = &o.L;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        s[(3 * c) * stride] = f[c].x;
-        s[(3 * c + 1) * stride] = f[c].y;
-        s[(3 * c + 2) * stride] = f[c].z;
+    Path s;
+    path_start(s, P.cam.eye, camera_ray(P, x, y, px, smp), px, smp);
+    while (path_bounce(P, s)) {}
+    path_finish(P, s);
+    store_sample(P, j, px, s.o);
+}
+
+// Path regeneration: persistent threads, each taking the next (pixel, sample) of the slice
+// from a counter whenever its path ends, so a warp's lanes are not held by its longest path
+// (Russian roulette gives paths of very different lengths). Items run tile-major (a warp's
+// first items are one 8 x 4 tile for one sample index); the per-sample terms and their sum
+// in sample order are the per-sample kernel's, so the bits are the same.
+__global__ void __launch_bounds__(128) pt_regen_kernel(const PtParams P, uint32_t* ctr) {
+    const uint32_t tiles_x = (P.w + kTileW - 1) / kTileW, tiles_y = (P.h + kTileH - 1) / kTileH;
+    const uint32_t ntiles = tiles_x * tiles_y;
+    const unsigned long long total = (unsigned long long)ntiles * 32ull * P.kn;
+    Path s;
+    uint32_t j = 0;
+    bool live = false;
+    for (;;) {
+        if (!live) {
+            const unsigned long long item = atomicAdd(reinterpret_cast<unsigned long long*>(ctr), 1ull);
+            if (item >= total) break;
+            const uint32_t lane = (uint32_t)(item & 31u);
+            const unsigned long long w = item >> 5;
+            j = (uint32_t)(w / ntiles);
+            const uint32_t tile = (uint32_t)(w % ntiles);
+            const int x = (int)((tile % tiles_x) * kTileW + (lane % kTileW)),
+                      y = (int)((tile / tiles_x) * kTileH + (lane / kTileW));
+            if (x >= P.w || y >= P.h) continue;
+            const uint32_t px = (uint32_t)(y * P.w + x);
+            const uint32_t smp = P.spp_begin + P.k0 + j;
+            path_start(s, P.cam.eye, camera_ray(P, x, y, px, smp), px, smp);
+            live = true;
+        }
+        if (!path_bounce(P, s)) {
+            path_finish(P, s);
+            store_sample(P, j, s.px, s.o);
+            live = false;
+        }
     }
 }
 
@@ -903,13 +963,24 @@ int rn_pathtrace(const rn_ptscene* s, const rn_pt_desc* d, int flags, rn_pt_out*
         P.acc = (float*)((char*)acc + (size_t)npix * 6 * sizeof(double));
     }
     const uint32_t tiles = ((uint32_t)(d->width + 7) / 8) * ((uint32_t)(d->height + 3) / 4);
+    uint32_t* ctr = nullptr;                       // the regeneration kernel's item counter (8 bytes)
+    if (c.tune.pt_regen) {
+        void* cp = nullptr;
+        RN_TRY(ws_get(WS_PT_CTR, 8, &cp, st));
+        ctr = (uint32_t*)cp;
+    }
     uint32_t k0 = 0;
     do {
         P.k0 = k0;
         P.kn = std::min(kn_max, d->spp - k0);
         P.first = k0 == 0;
         P.last = k0 + P.kn >= d->spp;
-        if (P.kn > 0) {
+        if (P.kn > 0 && c.tune.pt_regen) {
+            RN_CUDA(cudaMemsetAsync(ctr, 0, 8, c.stream), st);
+            pt_regen_kernel<<<c.sm_count * c.tune.pt_regen, 128, 0, c.stream>>>(P, ctr);
+            const cudaError_t le = cudaGetLastError();
+            if (le != cudaSuccess) return cuda_fail(st, le, "pt_regen_kernel");
+        } else if (P.kn > 0) {
             const uint64_t warps = (uint64_t)tiles * P.kn;
             pt_paths_kernel<<<(unsigned)((warps + 3) / 4), 128, 0, c.stream>>>(P);
             const cudaError_t le = cudaGetLastError();

@@ -7,7 +7,8 @@ Parity is bit for bit:
 - on a seeded synthetic scene with emitters, metals, glossy and rough dielectrics and textures,
   every AOV equals the oracle's (rno_pathtrace, pinned to the reference by
   tests/test_oracle_pt.py), for several controls, several slice sizes (samples traced in
-  parallel and summed in sample order), device and host output pointers.
+  parallel and summed in sample order), both kernels (a thread a sample, or persistent
+  threads regenerating paths), device and host output pointers.
 
 Then the reference's own checks of its GPU path tracer (src/renderer/gpu/rt_pt_parity.cpp,
 src/renderer/rt_pt_checks.cpp), with its statistics and bounds:
@@ -67,22 +68,25 @@ def _synthetic():
     return importlib.import_module("test_oracle_pt").synthetic_scene(), importlib.import_module("test_oracle_pt").SYNTH_CAMERA
 
 
-@pytest.mark.parametrize("controls,slice_", [([], 0), (["legacy_lobe_v2"], 1), (["drop_lambert_cosine"], 4),
-                                             (["aov_emission_to_diffuse", "mis_weight_one"], 16),
-                                             (["aov_drop_specular_indirect"], 0)])
-def test_gpu_equals_oracle_on_a_synthetic_scene(rn, oracle, controls, slice_):
+@pytest.mark.parametrize("controls,slice_,regen", [([], 0, 0), ([], 0, 4), (["legacy_lobe_v2"], 1, 8),
+                                                   (["drop_lambert_cosine"], 4, 0),
+                                                   (["aov_emission_to_diffuse", "mis_weight_one"], 16, 16),
+                                                   (["aov_drop_specular_indirect"], 0, 4)])
+def test_gpu_equals_oracle_on_a_synthetic_scene(rn, oracle, controls, slice_, regen):
     sc, cam = _synthetic()
     d = dict(seed=(11 << 32) | 3, spp=24, width=73, height=41, camera=cam, controls=controls,
              previous=(0.3, 2.4, 5.6, 0.0, 1.0, -1.0, 0.0, 1.0, 0.0, 1.1))
     ref = oracle.pathtrace(sc, d, threads=THREADS)
     s = rn.PtScene(sc)
     assert s.info()["emitters"] == ref["emitters"] == 2
-    old = rn.tune_get("pt_slice")
+    old = (rn.tune_get("pt_slice"), rn.tune_get("pt_regen"))
     rn.tune_set("pt_slice", slice_)
+    rn.tune_set("pt_regen", regen)
     try:
         out = rn.path_trace(s, d)
     finally:
-        rn.tune_set("pt_slice", old)
+        rn.tune_set("pt_slice", old[0])
+        rn.tune_set("pt_regen", old[1])
     for k, _, _ in rn.PT_AOVS:
         assert np.array_equal(out[k], ref[k]), (k, int((out[k] != ref[k]).sum()))
 
