@@ -59,7 +59,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--cpu-row-stride", type=int, default=4, help="rows of the CPU sample: every n-th")
     p.add_argument("--profile", choices=["frame", "trace", "ssao", "reconcile", "build", "unet", "surrogate",
-                                         "pathtrace"],
+                                         "pathtrace", "train"],
                    help="run only this pass `--steps` times after `--warmup` (for ncu), print nothing")
     p.add_argument("--spp", type=int, default=SPP, help="samples per pixel (the benchmark uses 256)")
     p.add_argument("--tris", type=int, default=1000000, help="--profile build: soup triangles")
@@ -367,6 +367,17 @@ def run_profile(args):
         x = torch.rand(1, *net.shape[1:], 5, device="cuda")
         for _ in range(args.warmup + args.steps):
             net.forward(x)
+        torch.cuda.synchronize()
+        return
+    if args.profile == "train":
+        # surrogate training steps at the training recipe's shape (batch 64 of 128 x 128 crops,
+        # Adam): forward, backward (dgrad on the implicit convolution, wgrad on tc_gemm), Adam
+        net = rn.UNet(64, 128, 128, seed=1)
+        g = torch.Generator(device="cuda").manual_seed(1)
+        x = torch.rand(64, 128, 128, 5, device="cuda", generator=g)
+        y = torch.rand(64, 128, 128, device="cuda", generator=g)
+        for _ in range(args.warmup + args.steps):
+            net.train_step(x, y, 1e-3)
         torch.cuda.synchronize()
         return
     if args.profile == "pathtrace":

@@ -591,6 +591,27 @@ __device__ __forceinline__ void padded(const float* b, float* lo, float* hi) {
     }
 }
 
+// Reserve `n` consecutive slots of a global counter for each lane of the warp (every lane
+// calls it; `am` is the full warp) with one atomic for the warp: returns the lane's first
+// slot. The counters hand out node ids, queue positions and leaf
+// triangle ranges; their order does not matter to any answer (the tree is the same), and
+// one atomic per warp instead of one per child keeps a level of millions of tasks from
+// queueing on three addresses.
+__device__ __forceinline__ uint32_t warp_reserve(uint32_t* ctr, uint32_t n, unsigned am) {
+    const int lane = threadIdx.x & 31;
+    uint32_t incl = n;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(am, incl, off);
+        if (lane >= off) incl += y;
+    }
+    const int last = 31 - __clz(am);
+    const uint32_t total = __shfl_sync(am, incl, last);
+    uint32_t base = 0;
+    if (lane == last && total) base = atomicAdd(ctr, total);
+    base = __shfl_sync(am, base, last);
+    return base + incl - n;
+}
+
 __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __restrict__ nin,
                                Task* __restrict__ out, uint32_t* __restrict__ nout, uint32_t out_cap,
                                uint32_t* __restrict__ node_ctr, uint32_t node_cap,
@@ -600,14 +621,21 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
                                const uint32_t* __restrict__ count, const float* __restrict__ tris,
                                Node4* __restrict__ nodes, LeafTri* __restrict__ leaf, uint32_t leaf_max,
                                uint32_t* err) {
-    // grid-stride over the level's tasks: the grid is fixed, the count is read on the device
+    // grid-stride over the level's tasks: the grid is fixed, the count is read on the device.
+    // Whole warps step together (the base is warp-uniform), so every lane takes part in the
+    // reservations; lanes past the end reserve nothing.
     const uint32_t m = *nin;
-    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x) {
-        const Task task = in[t];
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < m; base += gridDim.x * blockDim.x) {
+        const uint32_t t = base + lane;
+        const bool valid = t < m;
+        const Task task = valid ? in[t] : Task{0, 0};
         int32_t C[4];
         int nc = 0;
         const int32_t b = task.bnode;
-        if (tri[b] >= 0 || count[b] <= leaf_max) {
+        if (!valid) {
+            nc = 0;
+        } else if (tri[b] >= 0 || count[b] <= leaf_max) {
             C[nc++] = b;
         } else {
             C[nc++] = left[b];
@@ -627,6 +655,17 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
                 C[nc++] = right[c];
             }
         }
+        // this task's leaf triangles and interior children, reserved for the warp at once
+        uint32_t ntri = 0, nint = 0;
+        for (int k = 0; k < nc; ++k) {
+            const int32_t c = C[k];
+            if (tri[c] >= 0 || count[c] <= leaf_max) ntri += count[c];
+            else ++nint;
+        }
+        uint32_t tri_next = warp_reserve(tri_ctr, ntri, 0xffffffffu);
+        uint32_t id_next = warp_reserve(node_ctr, nint, 0xffffffffu);
+        uint32_t q_next = warp_reserve(nout, nint, 0xffffffffu);
+        if (!valid) continue;
         Node4 nd;
         for (int k = 0; k < 4; ++k) {
             nd.lox[k] = nd.loy[k] = nd.loz[k] = 1e30f;
@@ -643,7 +682,8 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
             nd.hix[k] = hi[0]; nd.hiy[k] = hi[1]; nd.hiz[k] = hi[2];
             if (tri[c] >= 0 || count[c] <= leaf_max) {
                 const uint32_t cnt = count[c];
-                const uint32_t first = atomicAdd(tri_ctr, cnt);
+                const uint32_t first = tri_next;
+                tri_next += cnt;
                 // the subtree's leaves, left to right
                 int32_t stack[2 * kLeafCap];
                 int sp = 0, w = 0;
@@ -666,8 +706,8 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
                 }
                 nd.child[k] = ~(int32_t)((first << 3) | (cnt - 1));
             } else {
-                const uint32_t id = atomicAdd(node_ctr, 1u);
-                const uint32_t q = atomicAdd(nout, 1u);
+                const uint32_t id = id_next++;
+                const uint32_t q = q_next++;
                 if (id >= node_cap || q >= out_cap) { atomicOr(err, DEV_QUEUE_OVERFLOW); nd.child[k] = 0; continue; }
                 out[q] = Task{c, (int32_t)id};
                 nd.child[k] = (int32_t)id;
@@ -785,6 +825,10 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
         for (int r = 0; r < kBatch; ++r) {
             if (radius == 16)
                 ploc_nn<16><<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn);
+            else if (radius == 8)
+                ploc_nn<8><<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn);
+            else if (radius == 32)
+                ploc_nn<32><<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn);
             else
                 ploc_nn_any<<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn, radius);
             ploc_count<<<nbc, kThreads, 0, s>>>(state, nn, bs64);
