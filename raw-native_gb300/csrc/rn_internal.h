@@ -68,7 +68,7 @@ struct Tune {
     int hybrid_min_blocks = 6;  // resident 128-thread hybrid-pass blocks per SM: 5, 6 or 8
     int ploc_tail = 4096;       // PLOC: the rounds from this many clusters on run in one block (0: never)
     int trace_pool = 0;         // AO-only walks from a per-packet queue, lanes refilled below this many busy (0: off)
-    int pt_regen = 0;           // path tracer: persistent threads regenerating paths, blocks of 128 per SM (0: one thread a sample)
+    int pt_regen = 4;           // path tracer: persistent threads regenerating paths, blocks of 128 per SM (0: one thread a sample)
     int pt_slice = 0;           // path tracer: samples per slice at most (0: as many as 2 GiB of terms hold)
 };
 constexpr uint32_t kSmallScene = 1u << 16;
