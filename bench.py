@@ -347,6 +347,17 @@ def run_ours(args):
     if world == 1 and os.path.exists(SURROGATE_WEIGHTS) and not os.environ.get("RN_BENCH_NO_SURROGATE"):
         # the metric's other half: surrogate vs plain GPU RT at 4K on the 7.88M-triangle scene
         out["surrogate_4k"] = surrogate_headtohead(max(2, args.steps // 4), max(1, args.warmup // 3))
+    if world == 1 and not os.environ.get("RN_BENCH_NO_EXTRA"):
+        # the secondary workloads, short runs after the frame's timed region (each with its own
+        # CUDA-event timing; the full runs are `--workload batch|build|pathtrace`)
+        short = argparse.Namespace(steps=2, warmup=1, views=0, spp=SPP, workload="batch")
+        b = views_report(short)
+        out["batch_config3"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "ms_per_view", "config", "clocks")}
+        out["accel_build"] = {k: v for k, v in build_report(argparse.Namespace(steps=3, warmup=1)).items()
+                              if k in ("value", "unit", "ms_per_step", "builds", "config")}
+        os.environ["RN_BENCH_NO_CPU"] = "1"
+        p = pathtrace_report(argparse.Namespace(steps=2, warmup=1), spp=16)
+        out["pathtrace"] = {k: p[k] for k in ("value", "unit", "ms_per_step", "scenes", "config")}
     print(json.dumps(out), flush=True)
 
 
@@ -442,6 +453,10 @@ def run_profile(args):
 def run_views(args):
     """The batched-views and large-scene workloads: one batch frame = every view's AO (radius 1),
     SSAO and reconcile, from one traversal launch and one SSAO launch (a CUDA graph)."""
+    print(json.dumps(views_report(args)), flush=True)
+
+
+def views_report(args) -> dict:
     import numpy as np
     import torch
     import rn_ao as rn
@@ -491,7 +506,7 @@ def run_views(args):
            "ms_per_view": ms / len(views),
            "rmse_mean": float(np.mean([r.rmse for r in res])), "clocks": clk.summary(),
            "gpu_launches": 2 * args.steps}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 # the network trained on mixed-density scenes (the 200-box recipe's network is
@@ -736,6 +751,10 @@ def run_hybrid(args):
 
 
 def run_build(args):
+    print(json.dumps(build_report(args)), flush=True)
+
+
+def build_report(args) -> dict:
     """The accelerator build (rn_accel_build: PLOC on the GPU, then the collapse to 4-wide
     nodes) from device-resident triangles: the 7.88M-triangle and 744k-triangle seeded scenes,
     a 1M-triangle random soup and the reference's 20,000-triangle PLOC check soup. Each build is timed with CUDA events around the call (it
@@ -779,7 +798,7 @@ def run_build(args):
     out.update(value=big["mtris_per_s"], ms_per_step=big["ms_per_build"], clocks=clk.summary(),
                config={"workload": "accelerator build, seeded 7.88M-triangle scene (median of the timed builds)",
                        "inputs": "triangles resident in HBM (284 MB, larger than L2)"})
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def pt_fixture_scene(key: str):
@@ -793,6 +812,10 @@ def pt_fixture_scene(key: str):
 
 
 def run_pathtrace(args):
+    print(json.dumps(pathtrace_report(args)), flush=True)
+
+
+def pathtrace_report(args, spp: int = 64) -> dict:
     """The path tracer (rn_pathtrace, interface v4): retro_room (the reference's lit room: sun
     through the open end, a ceiling lamp, textured brick, tile, plank and brass) and iso_street
     at 1280 x 720, 64 spp, 64 bounces with Russian roulette, every AOV; timed per frame with CUDA
@@ -804,7 +827,7 @@ def run_pathtrace(args):
     torch.cuda.set_device(0)
     rn.init()
     stream = torch.cuda.current_stream()
-    W, H, SPPS = 1280, 720, 64
+    W, H, SPPS = 1280, 720, spp
     out = {"metric": "path-traced samples per second (interface v4, every AOV)", "unit": "M samples/s",
            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic: the reference's own lit scenes", "scenes": []}
@@ -840,9 +863,9 @@ def run_pathtrace(args):
             s.close()
     first = out["scenes"][0]
     out.update(value=first["msamples_per_s"], ms_per_step=first["ms_per_frame"], clocks=clk.summary(),
-               config={"workload": "path tracer, retro_room at 1280x720, 64 spp, 64 bounces (Russian roulette)",
+               config={"workload": "path tracer, retro_room at 1280x720, %d spp, 64 bounces (Russian roulette)" % SPPS,
                        "outputs": "every AOV in HBM"}, gpu_launches=2 * args.steps)
-    print(json.dumps(out), flush=True)
+    return out
 
 
 def main():

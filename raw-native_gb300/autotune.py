@@ -1,6 +1,6 @@
 """Autotuner for the library's launch shapes (rn_tune_* keys): the traversal's packet shape,
 stack depth, residency and frontier; the accelerator's shape; the SSAO tile; the convolution
-GEMM's tile width; the hybrid pass's residency.
+GEMM's tile width; the hybrid pass's residency; the PLOC tail; the path tracer's kernel.
 
 Every candidate is timed with CUDA events on the library's stream over representative
 workloads, after a check that it reproduces the default configuration's outputs bit for bit
@@ -29,6 +29,9 @@ Workloads:
   trace/tail     the same view at 16, 64 and 256 spp (trace_frontier_tail)
   hybrid         the hybrid pass (shadow + mirror ray per pixel) on the built-in scene and
                  the 744k scene at 4K (hybrid_min_blocks)
+  ploc_tail      accelerator builds of the 744k scene, a 1M soup and the 20,000-triangle check
+                 soup (the cluster count from which the PLOC rounds run in one block)
+  pt             the path tracer on retro_room and iso_street at 640 x 360, 16 spp (pt_regen)
 The traversal keys are searched jointly (every combination); the others one at a time.
 """
 from __future__ import annotations
@@ -354,6 +357,75 @@ def tune_conv(quick: bool, reps: int, log):
     return best["cfg"], rows
 
 
+def tune_ploc_tail(quick: bool, reps: int, log):
+    """From how many clusters on the PLOC rounds run in one block: builds of the 744k scene,
+    a 1M-triangle soup and the reference's 20,000-triangle check soup (the trees checked node
+    for node against the first candidate's); scored by the geometric mean of the ratios."""
+    import torch
+    rng = np.random.default_rng(1)
+    n = 200000 if quick else 1000000
+    c = rng.uniform(-50, 50, (n, 1, 3)).astype(np.float32)
+    soup = (c + rng.uniform(-1, 1, (n, 3, 3)).astype(np.float32)).reshape(-1, 9)
+    inputs = [("build/744k", scenes.build_synthetic_scene(1, 500 if quick else 2000, 100 if quick else 500).tris),
+              ("build/soup", soup), ("build/20k", scenes.soup(20000, 7))]
+    inputs = [(name, torch.from_numpy(np.ascontiguousarray(t)).cuda()) for name, t in inputs]
+    current = rn.tune_get("ploc_tail")
+    rows, ref = [], None
+    for v in rn.TUNE_KEYS["ploc_tail"]:
+        rn.tune_set("ploc_tail", v)
+        trees = [rn.build_ploc(t)[0].cpu() for _, t in inputs]
+        if ref is None:
+            ref = trees
+        elif not all(bool((a == b).all()) for a, b in zip(trees, ref)):
+            raise RuntimeError("ploc_tail %d changed a tree" % v)
+        ms = {name: _time(lambda t=t: rn.LinearAccel(t).close(), reps) for name, t in inputs}
+        rows.append(dict(cfg={"ploc_tail": v}, ms=ms))
+        log("ploc_tail %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    base = next(r for r in rows if r["cfg"]["ploc_tail"] == current)["ms"]
+    for r in rows:
+        r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
+    best = min(rows, key=lambda r: r["score"])
+    rn.tune_set("ploc_tail", best["cfg"]["ploc_tail"])
+    return best["cfg"], rows
+
+
+def tune_pt(quick: bool, reps: int, log):
+    """The path tracer's kernel: a thread per sample, or persistent threads regenerating paths
+    (4, 8, 16 blocks per SM): retro_room and iso_street (the reference's lit scenes, from the
+    test fixtures) at 640 x 360, 16 spp, every AOV checked bit for bit."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden",
+                             "pt_scenes.npz"))
+    wls = []
+    for key in ("retro_room", "iso_street"):
+        sc = {k.split("/", 1)[1]: z[k] for k in z.files if k.startswith(key + "/")}
+        cam = [float(v) for v in sc.pop("camera")]
+        s = rn.PtScene(sc)
+        d = dict(seed=1, spp=4 if quick else 16, width=320 if quick else 640, height=180 if quick else 360, camera=cam)
+        wls.append(("pt/" + key, s, d))
+    current = rn.tune_get("pt_regen")
+    rows, ref = [], None
+    for v in rn.TUNE_KEYS["pt_regen"]:
+        rn.tune_set("pt_regen", v)
+        outs = [rn.path_trace(s, d, device=True, planes=("radiance", "variance", "diffuse")) for _, s, d in wls]
+        if ref is None:
+            ref = outs
+        elif not all(bool((o[k] == r[k]).all()) for o, r in zip(outs, ref) for k in o):
+            raise RuntimeError("pt_regen %d changed a path-traced result" % v)
+        ms = {name: _time(lambda s=s, d=d: rn.path_trace(s, d, device=True, planes=("radiance",)), reps)
+              for name, s, d in wls}
+        rows.append(dict(cfg={"pt_regen": v}, ms=ms))
+        log("pt_regen %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    base = next(r for r in rows if r["cfg"]["pt_regen"] == current)["ms"]
+    for r in rows:
+        r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
+    best = min(rows, key=lambda r: r["score"])
+    rn.tune_set("pt_regen", best["cfg"]["pt_regen"])
+    for _, s, _ in wls:
+        s.close()
+    return best["cfg"], rows
+
+
 def write_tune_file(path: str, cfg: dict, note: str) -> None:
     with open(path, "w") as f:
         f.write("# launch shapes picked by autotune.py: %s\n" % note)
@@ -389,6 +461,10 @@ def main(argv=None):
     c, report["conv"] = tune_conv(a.quick, a.reps, log)
     cfg.update(c)
     c, report["hybrid"] = tune_hybrid(a.quick, a.reps, log)
+    cfg.update(c)
+    c, report["ploc_tail"] = tune_ploc_tail(a.quick, a.reps, log)
+    cfg.update(c)
+    c, report["pt"] = tune_pt(a.quick, a.reps, log)
     cfg.update(c)
     dev = torch.cuda.get_device_name(0)
     note = "%s, %d SMs, %s workloads, %.0f s" % (dev, torch.cuda.get_device_properties(0).multi_processor_count,
