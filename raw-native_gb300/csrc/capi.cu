@@ -131,6 +131,7 @@ const TuneKey kTuneKeys[] = {
     {"pt_regen", "RN_TUNE_PT_REGEN", &Tune::pt_regen, {0, 4, 8, 16}, 4},
     {"trace_pool", "RN_TUNE_TRACE_POOL", &Tune::trace_pool, {0, 16, 24, 32}, 4},
     {"ploc_tail", "RN_TUNE_PLOC_TAIL", &Tune::ploc_tail, {0, 4096, 32768, 262144}, 4},
+    {"conv_tmem_a", "RN_TUNE_CONV_TMEM_A", &Tune::conv_tmem_a, {0, 1}, 2},
 };
 
 const TuneKey* find_tune_key(const char* name) {

@@ -514,6 +514,28 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+// tcgen05.cp of a 128-row x 256-bit matrix (128 pixels x 16 BF16 channels, K-major, the
+// descriptor's canonical layout) from shared memory into TMEM columns [taddr, taddr + 8).
+__device__ __forceinline__ void tc_cp_128x256b(uint32_t taddr, uint64_t sdesc) {
+    asm volatile("tcgen05.cp.cta_group::1.128x256b [%0], %1;" ::"r"(taddr), "l"(sdesc) : "memory");
+}
+// tcgen05.mma.kind::f16 with the A operand read from TMEM (128 lanes = M rows, K in columns).
+__device__ __forceinline__ void tc_mma_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t b, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\ntcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "r"(tmem_a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// The A operands of one input row kept in TMEM (kTA): its three horizontal taps (the row
+// shifted by -1, 0, +1 pixel) x the K steps of its channels, 8 columns each, in a ring of
+// kTaSlots rows after the two accumulators. Each input row is copied from its shared-memory
+// slot once and read by the three output rows that need it, so shared memory serves the A
+// operand once per input row instead of once per tap of every output row; the MMAs then
+// read only the weights (B) from shared memory.
+constexpr int kTaSlots = 4;
+constexpr uint32_t kTaRowCols = 3 * 2 * 8;         // taps x K steps (at most 32 channels) x 8 columns
+
 struct HaloArgs {
     int nsrc, C0, C1, cin;
     int B, H, W;
@@ -537,14 +559,16 @@ __device__ __forceinline__ HaloItem halo_item(const HaloArgs& a, int item) {
     return it;
 }
 
-template <int BN>
+template <int BN, bool kTA>
 __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __grid_constant__ CUtensorMap map0,
                                                                        const __grid_constant__ CUtensorMap map1,
                                                                        const __grid_constant__ CUtensorMap mapW,
                                                                        const HaloArgs a, const Epilogue e) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    constexpr uint32_t kCols = 2 * BN;
+    // TMEM: two accumulators, then (kTA) the ring of input rows' A operands; a power of two
+    constexpr uint32_t kCols = kTA ? 256u : 2u * BN;
+    static_assert(!kTA || 2 * BN + kTaSlots * kTaRowCols <= 256, "the TMEM ring fits");
     const int kSt = a.stages;
     uint8_t* sB = smem;
     uint8_t* sA = smem + ((a.b_bytes + 1023) & ~1023u);
@@ -606,6 +630,62 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
             // the copies this lane issued must land before the CTA can leave
             for (uint32_t k = kc > (uint32_t)kSt ? kc - kSt : 0; k < kc; ++k) mbar_wait(full(k % kSt), (k / kSt) & 1u);
             mbar_wait(wbar, 0);
+        }
+    } else if (warp == 1 && kTA) {
+        if (lane == 0) {
+            const uint32_t idesc = instr_desc(BN);
+            const uint32_t b0 = smem_u32(sB);
+            const int q16 = a.cin / 16, g_tap = a.cin / 8;
+            const uint32_t ta0 = tmem + 2u * BN;
+            bool ok = mbar_wait_or_abort(wbar, 0, abort_flag);
+            uint32_t base = 0, i = 0;   // ring index of the item's first load; output rows so far
+            for (int item = blockIdx.x; ok && item < a.items && !*abort_flag; item += gridDim.x) {
+                const HaloItem it = halo_item(a, item);
+                for (int j = 0; ok && j < it.rows; ++j, ++i) {
+                    // output row y0 + j reads loads j, j + 1, j + 2 of the item
+                    const uint32_t buf = i & 1u, use = i >> 1;
+                    // row i - 2's MMAs are done once its accumulator is free again: the TMEM
+                    // slots they read may be overwritten
+                    if (!mbar_wait_or_abort(acc_empty(buf), (use & 1u) ^ 1u, abort_flag)) { ok = false; break; }
+                    if (j == 0 && i > 0) {
+                        // a new item reloads three rows: the previous row's MMAs must be done too
+                        const uint32_t pi = i - 1;
+                        if (!mbar_wait_or_abort(acc_full(pi & 1u), (pi >> 1) & 1u, abort_flag)) { ok = false; break; }
+                    }
+                    for (int d = (j == 0 ? 0 : 2); d < 3 && ok; ++d) {
+                        const uint32_t k = base + (uint32_t)(j + d);
+                        ok = mbar_wait_or_abort(full(k % kSt), (k / kSt) & 1u, abort_flag);
+                        if (!ok) break;
+                        tc_fence_after();
+                        const uint32_t row = smem_u32(sA + (k % kSt) * a_stride);
+                        const uint32_t slot = ta0 + (k % kTaSlots) * kTaRowCols;
+                        for (int dx = 0; dx < 3; ++dx)
+                            for (int q = 0; q < q16; ++q)
+                                tc_cp_128x256b(slot + (uint32_t)(dx * q16 + q) * 8u,
+                                               desc_plain(row + (uint32_t)dx * 16u + (uint32_t)(2 * q) * kHaloGroup,
+                                                          kHaloGroup, 128));
+                        // the shared-memory slot is free once its copies have run
+                        tc_commit(empty(k % kSt));
+                    }
+                    if (!ok) break;
+                    const uint32_t acc = tmem + buf * BN;
+                    for (int t = 0; t < 9; ++t) {
+                        const uint32_t k = base + (uint32_t)(j + t / 3);
+                        const uint32_t slot = ta0 + (k % kTaSlots) * kTaRowCols + (uint32_t)((t % 3) * q16) * 8u;
+                        for (int q = 0; q < q16; ++q) {
+                            const uint64_t db = desc_plain(b0 + (uint32_t)(t * g_tap + 2 * q) * (BN * 16), BN * 16, 128);
+                            tc_mma_ta(acc, slot + (uint32_t)q * 8u, db, idesc, (t | q) != 0 ? 1u : 0u);
+                        }
+                    }
+                    tc_commit(acc_full(buf));
+                }
+                if (!ok) break;
+                base += (uint32_t)it.rows + 2;
+            }
+            if (!ok) {
+                atomicOr(e.err, DEV_GUARD);
+                s_abort = 1;
+            }
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -833,23 +913,25 @@ bool make_map_wgroups(CUtensorMap* m, const void* base, int N, int ldw, int kgro
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int BN>
+template <int BN, bool kTA>
 int launch_conv_halo(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap& mw, const HaloArgs& a,
                      const Epilogue& e, size_t smem, cudaStream_t s) {
     static size_t attr = 0;
     if (attr < smem) {
-        if (cudaFuncSetAttribute(tc_conv_halo_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        if (cudaFuncSetAttribute(tc_conv_halo_kernel<BN, kTA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
                 cudaSuccess ||
-            cudaFuncSetAttribute(tc_conv_halo_kernel<BN>, cudaFuncAttributePreferredSharedMemoryCarveout,
+            cudaFuncSetAttribute(tc_conv_halo_kernel<BN, kTA>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return RN_ERR_CUDA;
         attr = smem;
     }
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx().device);
-    const int per_sm = std::max(1, std::min(std::min(smem_sm / (int)(smem + 1024), 512 / (2 * BN)), 3));
+    // co-resident CTAs: shared memory and TMEM (512 columns an SM) both have to fit
+    const int tmem_cols = kTA ? 256 : 2 * BN;
+    const int per_sm = std::max(1, std::min(std::min(smem_sm / (int)(smem + 1024), 512 / tmem_cols), 3));
     const int ctas = std::min(a.items, per_sm * ctx().sm_count);
-    tc_conv_halo_kernel<BN><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
+    tc_conv_halo_kernel<BN, kTA><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 
@@ -963,8 +1045,11 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
             h.a_bytes = a_bytes; h.b_bytes = b_bytes;
             h.up16 = up16;
             const size_t smem = 1024 + b_pad + (size_t)stages * a_stride + (2 * stages + 5) * 8 + 16;
-            const int rc = N == 32 ? tc::launch_conv_halo<32>(hm[0], hm[1], hw, h, epi, smem, s)
-                                   : tc::launch_conv_halo<64>(hm[0], hm[1], hw, h, epi, smem, s);
+            // A operands in TMEM for 32 output channels and at most 32 input channels
+            const bool ta = ctx().tune.conv_tmem_a && N == 32 && cin <= 32;
+            const int rc = ta ? tc::launch_conv_halo<32, true>(hm[0], hm[1], hw, h, epi, smem, s)
+                         : N == 32 ? tc::launch_conv_halo<32, false>(hm[0], hm[1], hw, h, epi, smem, s)
+                                   : tc::launch_conv_halo<64, false>(hm[0], hm[1], hw, h, epi, smem, s);
             if (rc != RN_OK) return cuda_fail(st, cudaGetLastError(), "tc_conv_halo_kernel");
             return RN_OK;
         }

@@ -66,6 +66,7 @@ struct Tune {
     int accel_leaf_small = 4;   // ... of those with fewer than kSmallScene triangles
     int frame_direct = 1;       // host-buffer frames: the passes read and write mapped host memory
     int hybrid_min_blocks = 6;  // resident 128-thread hybrid-pass blocks per SM: 5, 6 or 8
+    int conv_tmem_a = 0;        // row-ring convolutions of 32 -> 32 or 16 -> 32 channels: A operands kept in TMEM
     int ploc_tail = 4096;       // PLOC: the rounds from this many clusters on run in one block (0: never)
     int trace_pool = 0;         // AO-only walks from a per-packet queue, lanes refilled below this many busy (0: off)
     int pt_regen = 4;           // path tracer: persistent threads regenerating paths, blocks of 128 per SM (0: one thread a sample)

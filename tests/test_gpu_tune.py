@@ -97,6 +97,37 @@ def test_conv_tile_keeps_every_bit(rn, restore_tune):
             rn.tune_set(k, {"conv_bn_max": 256, "conv_pair": 0, "conv_halo": 1}[k])
 
 
+def test_conv_tmem_a_keeps_every_bit(rn, restore_tune):
+    """The row-ring convolutions with their A operands kept in TMEM (conv_tmem_a) give the
+    same network output, training loss and gradients bit for bit: the same MMAs in the same
+    order on the same operands, only read from TMEM. Frames of several heights (items of
+    1 to 16 rows, so the TMEM ring crosses item boundaries), batch 2."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(3)
+    for H, W in ((64, 128), (136, 256), (1088, 1920)):
+        net = rn.UNet(1 if H > 200 else 2, H, W, seed=5, inference=True)
+        x = torch.rand(net.shape[0], H, W, 5, device="cuda", generator=g)
+        rn.tune_set("conv_tmem_a", 0)
+        ref = net.forward(x).clone()
+        rn.tune_set("conv_tmem_a", 1)
+        got = net.forward(x)
+        assert bool((got == ref).all()), (H, W, int((got != ref).sum().item()))
+        net.close()
+    trn = rn.UNet(4, 128, 128, seed=6)
+    xb = torch.rand(4, 128, 128, 5, device="cuda", generator=g)
+    yb = torch.rand(4, 128, 128, device="cuda", generator=g)
+    p0 = trn.get_params()
+    losses, grads = [], []
+    for v in (0, 1):
+        rn.tune_set("conv_tmem_a", v)
+        trn.set_params(p0)
+        losses.append(trn.backward(xb, yb))
+        grads.append(trn.get_grads().copy())
+    assert losses[0] == losses[1]
+    import numpy as np
+    assert np.array_equal(grads[0], grads[1])
+
+
 @pytest.mark.parametrize("sky", [False, True])
 def test_host_frame_keeps_every_bit(rn, restore_tune, sky):
     """rn_ao_frame with pinned host buffers runs without copies: the traversal reads the
