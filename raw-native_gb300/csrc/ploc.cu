@@ -288,7 +288,7 @@ __global__ void ploc_nn(const RoundState* __restrict__ st, const float* __restri
     }
     nn[i] = arg;
 }
-// Generic-radius fallback (radius other than 16): reads neighbours from global memory.
+// Generic-radius fallback (a radius other than 8, 16 or 32): reads neighbours from global memory.
 __global__ void ploc_nn_any(const RoundState* __restrict__ st, const float* __restrict__ cbox0,
                             const float* __restrict__ cbox1, int32_t* __restrict__ nn, int R) {
     const uint32_t m = st->m;
