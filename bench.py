@@ -818,7 +818,8 @@ def run_pathtrace(args):
 def pathtrace_report(args, spp: int = 64) -> dict:
     """The path tracer (rn_pathtrace, interface v4): retro_room (the reference's lit room: sun
     through the open end, a ceiling lamp, textured brick, tile, plank and brass) and iso_street
-    at 1280 x 720, 64 spp, 64 bounces with Russian roulette, every AOV; timed per frame with CUDA
+    at 1920 x 1080, 64 spp, 64 bounces with Russian roulette, every AOV (the frame the reference
+    times its own GPU path tracer on: docs/rt-interface-v4.md:36-40); timed per frame with CUDA
     events, outputs in HBM. The CPU baseline is the oracle (a restatement of raw::rt::pathTraceCpu,
     bit-identical to the reference build) on the host's cores, on the same frame at 4 spp.
     Metric: path samples per second."""
@@ -827,7 +828,7 @@ def pathtrace_report(args, spp: int = 64) -> dict:
     torch.cuda.set_device(0)
     rn.init()
     stream = torch.cuda.current_stream()
-    W, H, SPPS = 1280, 720, spp
+    W, H, SPPS = 1920, 1080, spp
     out = {"metric": "path-traced samples per second (interface v4, every AOV)", "unit": "M samples/s",
            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic: the reference's own lit scenes", "scenes": []}
@@ -857,13 +858,18 @@ def pathtrace_report(args, spp: int = 64) -> dict:
                 O.pathtrace(sc, dd, threads=os.cpu_count() or 1)
                 dt = time.perf_counter() - t0
                 row["cpu_baseline"] = {"value": W * H * 4 / dt / 1e6, "unit": "M samples/s", "cores": os.cpu_count() or 1,
-                                       "kind": "port", "sample": "the same 1280x720 frame at 4 spp (%.1f s), oracle "
-                                       "restatement of pathTraceCpu, all host threads" % dt}
+                                       "kind": "port", "sample": "the same %dx%d frame at 4 spp (%.1f s), oracle "
+                                       "restatement of pathTraceCpu, all host threads" % (W, H, dt)}
+            if key == "retro_room" and SPPS == 64:
+                # context only (other hardware and API, one run): the reference's GPU path tracer
+                row["reference_gpu_context"] = {"ms_per_frame": 1638.0, "msamples_per_s": W * H * 64 / 1.638 / 1e6,
+                                                "hardware": "RTX 4090, D3D12 (WGSL), interface v4",
+                                                "source": "docs/rt-interface-v4.md:38-39"}
             out["scenes"].append(row)
             s.close()
     first = out["scenes"][0]
     out.update(value=first["msamples_per_s"], ms_per_step=first["ms_per_frame"], clocks=clk.summary(),
-               config={"workload": "path tracer, retro_room at 1280x720, %d spp, 64 bounces (Russian roulette)" % SPPS,
+               config={"workload": "path tracer, retro_room at %dx%d, %d spp, 64 bounces (Russian roulette)" % (W, H, SPPS),
                        "outputs": "every AOV in HBM"}, gpu_launches=2 * args.steps)
     return out
 

@@ -354,10 +354,14 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *   accel_leaf_small  1 | 2 | 4 | 8  ... below 65,536 triangles
  *   frame_direct      0 | 1          rn_ao_frame on pinned, mapped host buffers without copies
  *   hybrid_min_blocks 5 | 6 | 8      resident rn_hybrid blocks per SM (register budget)
+ *   trace_leaf_pass   0 | 1          rn_ao_visibility: a node's leaf children tested after its
+ *                                    four slab tests, in one loop
  *   conv_tmem_a       0 | 1          row-ring convolutions with at most 32 input and 32 output
  *                                    channels keep each input row's A operands in TMEM
  *   ploc_tail         0|4096|32768|262144  accelerator builds: the PLOC rounds from this many
  *                                    clusters on run in one block (0: a launch per step)
+ *   collapse_block    0|16384|65536|262144  accelerator builds of at most this many triangles
+ *                                    collapse to 4-wide nodes in one block (0: a launch per level)
  *   trace_pool        0|16|24|32     AO-only walks: one queue of a packet's walks, idle lanes
  *                                    refilled when fewer than this many walk (0: one pixel per lane)
  *   pt_regen          0|4|8|16       rn_pathtrace: persistent threads that start a new path when

@@ -9,6 +9,10 @@ workloads, after a check that it reproduces the default configuration's outputs 
 tune_sm103.txt when it exists.
 
   python autotune.py --out tune_sm103.txt [--report report.json] [--quick]
+                     [--stages ploc_tail,pt --merge tune_sm103.txt]
+
+--stages runs only the named stages (in the order below); --merge starts from a tune file's
+values (applied before the stages run) and writes them back with the stages' picks.
 
 Workloads:
   accel          the traversal accelerator's PLOC radius and leaf size: builds of the
@@ -20,6 +24,7 @@ Workloads:
   trace/ao       a seeded synthetic scene (2,000 boxes, 500 spheres; 744k triangles),
                  1920 x 1080 orbit view, 64 spp AO only (radius 1)
   trace/large    the 7.88M-triangle scene, one 3840 x 2160 orbit view, 16 spp AO only
+                 (the launch shape jointly, then the walk's leaf pass on the same three)
   batch          16 orbit views of the 744k scene in one captured batch (batch_min_blocks)
   ssao           the built-in scene at 4K: SSAO, 24 taps
   conv           the surrogate U-Net: a forward at 1088 x 1920 and a training step on
@@ -30,7 +35,8 @@ Workloads:
   hybrid         the hybrid pass (shadow + mirror ray per pixel) on the built-in scene and
                  the 744k scene at 4K (hybrid_min_blocks)
   ploc_tail      accelerator builds of the 744k scene, a 1M soup and the 20,000-triangle check
-                 soup (the cluster count from which the PLOC rounds run in one block)
+                 soup (the cluster count from which the PLOC rounds run in one block; then the
+                 size under which the collapse runs in one block)
   pt             the path tracer on retro_room and iso_street at 640 x 360, 16 spp (pt_regen)
 The traversal keys are searched jointly (every combination); the others one at a time.
 """
@@ -114,6 +120,29 @@ def tune_trace(quick: bool, reps: int, log):
         r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
     best = min(rows, key=lambda r: r["score"])
     _apply(best["cfg"])
+    return best["cfg"], rows
+
+
+def tune_walk(quick: bool, reps: int, log):
+    """The walk's form on the traversal workloads, after the launch shape: leaf children
+    tested inline or in one pass after the slab tests (trace_leaf_pass). Each candidate is
+    checked bit for bit; score: geometric mean of the time ratios to the inline form."""
+    wls = trace_workloads(quick)
+    rn.tune_set("trace_leaf_pass", 0)
+    ref = [fn().clone() for _, fn, _ in wls]
+    rows = []
+    for v in rn.TUNE_KEYS["trace_leaf_pass"]:
+        rn.tune_set("trace_leaf_pass", v)
+        if not all(bool((fn() == r).all()) for (_, fn, _), r in zip(wls, ref)):
+            raise RuntimeError("trace_leaf_pass %d changed a traced result" % v)
+        ms = {name: _time(fn, reps) for name, fn, _ in wls}
+        rows.append(dict(cfg={"trace_leaf_pass": v}, ms=ms))
+        log("trace_leaf_pass %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    base = rows[0]["ms"]
+    for r in rows:
+        r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
+    best = min(rows, key=lambda r: r["score"])
+    rn.tune_set("trace_leaf_pass", best["cfg"]["trace_leaf_pass"])
     return best["cfg"], rows
 
 
@@ -404,7 +433,25 @@ def tune_ploc_tail(quick: bool, reps: int, log):
         r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
     best = min(rows, key=lambda r: r["score"])
     rn.tune_set("ploc_tail", best["cfg"]["ploc_tail"])
-    return best["cfg"], rows
+    # then the size under which the collapse runs in one block (same node counts required)
+    current = rn.tune_get("collapse_block")
+    rows2, ref2 = [], None
+    for v in rn.TUNE_KEYS["collapse_block"]:
+        rn.tune_set("collapse_block", v)
+        infos = [rn.LinearAccel(t).info() for _, t in inputs]
+        if ref2 is None:
+            ref2 = infos
+        elif infos != ref2:
+            raise RuntimeError("collapse_block %d changed an accelerator: %s" % (v, infos))
+        ms = {name: _time(lambda t=t: rn.LinearAccel(t).close(), reps) for name, t in inputs}
+        rows2.append(dict(cfg={"collapse_block": v}, ms=ms))
+        log("collapse_block %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    base = next(r for r in rows2 if r["cfg"]["collapse_block"] == current)["ms"]
+    for r in rows2:
+        r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
+    best2 = min(rows2, key=lambda r: r["score"])
+    rn.tune_set("collapse_block", best2["cfg"]["collapse_block"])
+    return dict(best["cfg"], **best2["cfg"]), rows + rows2
 
 
 def tune_pt(quick: bool, reps: int, log):
@@ -444,6 +491,25 @@ def tune_pt(quick: bool, reps: int, log):
     return best["cfg"], rows
 
 
+STAGES = {"accel": tune_accel, "trace": tune_trace, "walk": tune_walk, "frontier_min_spp": tune_frontier_min_spp,
+          "frontier_tail": tune_frontier_tail, "batch": tune_batch, "ssao": tune_ssao, "conv": tune_conv,
+          "hybrid": tune_hybrid, "ploc_tail": tune_ploc_tail, "pt": tune_pt}
+
+
+def read_tune_file(path: str) -> dict:
+    """The "key = value" lines of a tune file ('#' starts a comment), as rn_tune_load reads them."""
+    out = {}
+    for line in open(path):
+        line = line.split("#", 1)[0].strip()
+        if not line:
+            continue
+        k, v = (x.strip() for x in line.split("=", 1))
+        if k not in rn.TUNE_KEYS:
+            raise ValueError("%s: unknown tune key %r" % (path, k))
+        out[k] = int(v)
+    return out
+
+
 def write_tune_file(path: str, cfg: dict, note: str) -> None:
     with open(path, "w") as f:
         f.write("# launch shapes picked by autotune.py: %s\n" % note)
@@ -458,32 +524,26 @@ def main(argv=None):
     ap.add_argument("--report", default=None, help="JSON with every candidate's timings")
     ap.add_argument("--quick", action="store_true", help="smaller workloads (a test run)")
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--stages", default=None, help="comma-separated stages to run (default: all): "
+                    + ",".join(STAGES))
+    ap.add_argument("--merge", default=None, help="tune file whose values apply first and are kept")
     a = ap.parse_args(argv)
     import torch
     rn.init(load_tune=False)
     t0 = time.time()
     log = lambda m: print(m, flush=True)
     cfg, report = {}, {}
-    c, report["accel"] = tune_accel(a.quick, a.reps, log)
-    cfg.update(c)
-    c, report["trace"] = tune_trace(a.quick, a.reps, log)
-    cfg.update(c)
-    c, report["frontier_min_spp"] = tune_frontier_min_spp(a.quick, a.reps, log)
-    cfg.update(c)
-    c, report["frontier_tail"] = tune_frontier_tail(a.quick, a.reps, log)
-    cfg.update(c)
-    c, report["batch"] = tune_batch(a.quick, a.reps, log)
-    cfg.update(c)
-    c, report["ssao"] = tune_ssao(a.quick, a.reps, log)
-    cfg.update(c)
-    c, report["conv"] = tune_conv(a.quick, a.reps, log)
-    cfg.update(c)
-    c, report["hybrid"] = tune_hybrid(a.quick, a.reps, log)
-    cfg.update(c)
-    c, report["ploc_tail"] = tune_ploc_tail(a.quick, a.reps, log)
-    cfg.update(c)
-    c, report["pt"] = tune_pt(a.quick, a.reps, log)
-    cfg.update(c)
+    if a.merge:
+        cfg.update(read_tune_file(a.merge))
+        _apply(cfg)
+    names = STAGES if not a.stages else [s.strip() for s in a.stages.split(",") if s.strip()]
+    unknown = [s for s in names if s not in STAGES]
+    if unknown:
+        ap.error("unknown stages %s (known: %s)" % (unknown, ", ".join(STAGES)))
+    for name in STAGES:
+        if name in names:
+            c, report[name] = STAGES[name](a.quick, a.reps, log)
+            cfg.update(c)
     dev = torch.cuda.get_device_name(0)
     note = "%s, %d SMs, %s workloads, %.0f s" % (dev, torch.cuda.get_device_properties(0).multi_processor_count,
                                                  "quick" if a.quick else "full", time.time() - t0)

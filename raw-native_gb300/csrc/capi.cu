@@ -131,7 +131,9 @@ const TuneKey kTuneKeys[] = {
     {"pt_regen", "RN_TUNE_PT_REGEN", &Tune::pt_regen, {0, 4, 8, 16}, 4},
     {"trace_pool", "RN_TUNE_TRACE_POOL", &Tune::trace_pool, {0, 16, 24, 32}, 4},
     {"ploc_tail", "RN_TUNE_PLOC_TAIL", &Tune::ploc_tail, {0, 4096, 32768, 262144}, 4},
+    {"collapse_block", "RN_TUNE_COLLAPSE_BLOCK", &Tune::collapse_block, {0, 16384, 65536, 262144}, 4},
     {"conv_tmem_a", "RN_TUNE_CONV_TMEM_A", &Tune::conv_tmem_a, {0, 1}, 2},
+    {"trace_leaf_pass", "RN_TUNE_TRACE_LEAF_PASS", &Tune::trace_leaf_pass, {0, 1}, 2},
 };
 
 const TuneKey* find_tune_key(const char* name) {
@@ -606,8 +608,7 @@ int rn_accel_build(const float* tris, uint32_t ntri, int flags, rn_accel** out, 
 
 void rn_accel_free(rn_accel* accel) {
     if (!accel) return;
-    if (accel->d_nodes) cudaFree(accel->d_nodes);
-    if (accel->d_tris) cudaFree(accel->d_tris);
+    if (accel->d_nodes) cudaFree(accel->d_nodes);      // d_tris lies in the same allocation
     delete accel;
 }
 

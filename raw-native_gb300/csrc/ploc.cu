@@ -612,21 +612,20 @@ __device__ __forceinline__ uint32_t warp_reserve(uint32_t* ctr, uint32_t n, unsi
     return base + incl - n;
 }
 
-__global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __restrict__ nin,
-                               Task* __restrict__ out, uint32_t* __restrict__ nout, uint32_t out_cap,
-                               uint32_t* __restrict__ node_ctr, uint32_t node_cap,
-                               uint32_t* __restrict__ tri_ctr,
-                               const float* __restrict__ box, const int32_t* __restrict__ left,
-                               const int32_t* __restrict__ right, const int32_t* __restrict__ tri,
-                               const uint32_t* __restrict__ count, const float* __restrict__ tris,
-                               Node4* __restrict__ nodes, LeafTri* __restrict__ leaf, uint32_t leaf_max,
-                               uint32_t* err) {
-    // grid-stride over the level's tasks: the grid is fixed, the count is read on the device.
-    // Whole warps step together (the base is warp-uniform), so every lane takes part in the
-    // reservations; lanes past the end reserve nothing.
-    const uint32_t m = *nin;
+// One level's tasks in[0, m), strided: this thread's warp takes bases first, first + step, ...
+// (first and step warp-uniform), so whole warps step together and every lane takes part in
+// the reservations; lanes past the end reserve nothing. `in` and `out` carry no __restrict__:
+// the single-block form reads in one level what it wrote in the previous one.
+__device__ __forceinline__ void collapse_tasks(const Task* in, uint32_t m, uint32_t first, uint32_t step, Task* out,
+                                               uint32_t* nout, uint32_t out_cap, uint32_t* node_ctr,
+                                               uint32_t node_cap, uint32_t* tri_ctr,
+                                               const float* __restrict__ box, const int32_t* __restrict__ left,
+                                               const int32_t* __restrict__ right, const int32_t* __restrict__ tri,
+                                               const uint32_t* __restrict__ count, const float* __restrict__ tris,
+                                               Node4* __restrict__ nodes, LeafTri* __restrict__ leaf,
+                                               uint32_t leaf_max, uint32_t* err) {
     const uint32_t lane = threadIdx.x & 31u;
-    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < m; base += gridDim.x * blockDim.x) {
+    for (uint32_t base = first; base < m; base += step) {
         const uint32_t t = base + lane;
         const bool valid = t < m;
         const Task task = valid ? in[t] : Task{0, 0};
@@ -717,12 +716,56 @@ __global__ void collapse_level(const Task* __restrict__ in, const uint32_t* __re
     }
 }
 
+// One level over the whole grid: a fixed grid strides over the level's tasks, whose count
+// is read on the device.
+__global__ void collapse_level(const Task* in, const uint32_t* __restrict__ nin, Task* out,
+                               uint32_t* __restrict__ nout, uint32_t out_cap, uint32_t* __restrict__ node_ctr,
+                               uint32_t node_cap, uint32_t* __restrict__ tri_ctr,
+                               const float* __restrict__ box, const int32_t* __restrict__ left,
+                               const int32_t* __restrict__ right, const int32_t* __restrict__ tri,
+                               const uint32_t* __restrict__ count, const float* __restrict__ tris,
+                               Node4* __restrict__ nodes, LeafTri* __restrict__ leaf, uint32_t leaf_max,
+                               uint32_t* err) {
+    collapse_tasks(in, *nin, blockIdx.x * blockDim.x + (threadIdx.x & ~31u), gridDim.x * blockDim.x, out, nout,
+                   out_cap, node_ctr, node_cap, tri_ctr, box, left, right, tri, count, tris, nodes, leaf, leaf_max,
+                   err);
+}
+
 // Between two levels: count the level just processed if it had tasks (ctr[5], the 4-wide
 // depth), make its output the next input (ctr[0] = ctr[1]) and restart the output count.
-__global__ void collapse_next(uint32_t* ctr) {
+__device__ __forceinline__ void collapse_advance(uint32_t* ctr) {
     if (ctr[0] > 0) ++ctr[5];
     ctr[0] = ctr[1];
     ctr[1] = 0;
+}
+__global__ void collapse_next(uint32_t* ctr) { collapse_advance(ctr); }
+
+// The whole collapse in one block, for small trees: the levels are separated by block
+// barriers instead of launches and host reads (the same tasks, reservations and nodes as
+// collapse_level / collapse_next). At most max_levels levels (a bound: a level left over
+// shows as a task count above zero, which the host reports).
+constexpr int kCollapseThreads = 1024;
+__global__ void __launch_bounds__(kCollapseThreads) collapse_block(Task* q0, Task* q1, uint32_t* ctr, uint32_t out_cap,
+                                                                   uint32_t node_cap, const float* __restrict__ box,
+                                                                   const int32_t* __restrict__ left,
+                                                                   const int32_t* __restrict__ right,
+                                                                   const int32_t* __restrict__ tri,
+                                                                   const uint32_t* __restrict__ count,
+                                                                   const float* __restrict__ tris,
+                                                                   Node4* __restrict__ nodes, LeafTri* __restrict__ leaf,
+                                                                   uint32_t leaf_max, uint32_t max_levels) {
+    volatile uint32_t* vctr = ctr;
+    for (uint32_t lv = 0; lv < max_levels; ++lv) {
+        const uint32_t m = vctr[0];
+        if (m == 0) break;                       // every thread read the same count after the barrier
+        const Task* in = (lv & 1) ? q1 : q0;
+        Task* out = (lv & 1) ? q0 : q1;
+        collapse_tasks(in, m, threadIdx.x & ~31u, kCollapseThreads, out, ctr + 1, out_cap, ctr + 2, node_cap, ctr + 3,
+                       box, left, right, tri, count, tris, nodes, leaf, leaf_max, ctr + 4);
+        __syncthreads();
+        if (threadIdx.x == 0) collapse_advance(ctr);
+        __syncthreads();
+    }
 }
 
 inline uint32_t cdiv(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
@@ -749,7 +792,8 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
     if (radius < 1 || radius > 1024) return fail(st, RN_ERR_INVALID, "PLOC radius %d outside [1, 1024]", radius);
     const size_t N = 2 * (size_t)n - 1;
     const uint32_t nbs = cdiv(n, kTile);
-    // one allocation for everything the build needs
+    // one workspace block for everything the build needs (grow-only: repeated builds allocate
+    // nothing; the tree's arrays live there until the next build)
     size_t off = 0;
     auto take = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
     const size_t o_box = take(N * 6 * 4), o_left = take(N * 4), o_right = take(N * 4), o_tri = take(N * 4);
@@ -762,7 +806,7 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
     const size_t o_nn = take((size_t)n * 4), o_bs64 = take((size_t)(nbs + 1) * 8);
     const size_t o_bounds = take(sizeof(Bounds)), o_state = take(sizeof(RoundState));
     char* mem = nullptr;
-    RN_CUDA(cudaMallocAsync((void**)&mem, off, s), st);
+    RN_TRY(ws_get(WS_PLOC, off, (void**)&mem, st));
     out->mem = mem;
     out->box = (float*)(mem + o_box);
     out->left = (int32_t*)(mem + o_left);
@@ -854,10 +898,7 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
     return ok(st);
 }
 
-void ploc_free(PlocTree* t) {
-    if (t->mem) cudaFree(t->mem);
-    *t = PlocTree{};
-}
+void ploc_free(PlocTree* t) { *t = PlocTree{}; }
 
 int ploc_export(const PlocTree& t, int32_t* d_nodes9, cudaStream_t s, rn_status* st) {
     if (t.n == 0) return ok(st);
@@ -876,21 +917,19 @@ int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, int lea
     if (n == 0) return ok(st);
     const uint32_t N = 2 * n - 1;
     const uint32_t node_cap = n;              // every 4-wide node has at least 2 children
-    RN_CUDA(cudaMalloc((void**)&acc->d_nodes, (size_t)node_cap * sizeof(Node4)), st);
-    RN_CUDA(cudaMalloc((void**)&acc->d_tris, (size_t)n * sizeof(LeafTri)), st);
+    // the accelerator's nodes and leaf triangles in one allocation (rn_accel_free frees d_nodes)
+    const size_t node_bytes = ((size_t)node_cap * sizeof(Node4) + 255) & ~size_t(255);
+    char* block = nullptr;
+    RN_CUDA(cudaMalloc((void**)&block, node_bytes + (size_t)n * sizeof(LeafTri)), st);
+    acc->d_nodes = (Node4*)block;
+    acc->d_tris = (LeafTri*)(block + node_bytes);
     size_t off = 0;
     auto take = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
     const size_t o_parent = take((size_t)N * 4), o_visits = take((size_t)N * 4), o_count = take((size_t)N * 4);
     const size_t o_q0 = take((size_t)n * sizeof(Task)), o_q1 = take((size_t)n * sizeof(Task));
     const size_t o_ctr = take(8 * 4);
     char* mem = nullptr;
-    RN_CUDA(cudaMallocAsync((void**)&mem, off, s), st);
-    // the scratch goes back to the stream's pool on every return path
-    struct ScratchGuard {
-        char* p;
-        cudaStream_t s;
-        ~ScratchGuard() { cudaFreeAsync(p, s); }
-    } guard{mem, s};
+    RN_TRY(ws_get(WS_COLLAPSE, off, (void**)&mem, st));
     int32_t* parent = (int32_t*)(mem + o_parent);
     uint32_t* visits = (uint32_t*)(mem + o_visits);
     uint32_t* count = (uint32_t*)(mem + o_count);
@@ -906,11 +945,22 @@ int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, int lea
     const uint32_t init[4] = {1u, 0u, 1u, 0u};
     RN_CUDA(cudaMemcpyAsync(q0, &root, sizeof root, cudaMemcpyHostToDevice, s), st);
     RN_CUDA(cudaMemcpyAsync(ctr, init, sizeof init, cudaMemcpyHostToDevice, s), st);
-    // levels in batches of kLevels per host read; a level after the last one finds no task
+    // levels in batches of kLevels per host read; a level after the last one finds no task.
+    // Small trees run every level in one block and are read once.
     constexpr int kLevels = 8;
     const uint32_t grid = std::max(1u, std::min(cdiv(n, 128), (uint32_t)ctx().sm_count * 16u));
     uint32_t level_tasks = 1, depth = 0;
     uint32_t hc[6] = {0, 0, 0, 0, 0, 0};
+    if (n <= (uint32_t)ctx().tune.collapse_block) {
+        collapse_block<<<1, kCollapseThreads, 0, s>>>(q0, q1, ctr, n, node_cap, t.box, t.left, t.right, t.tri, count,
+                                                      d_tris, acc->d_nodes, acc->d_tris, (uint32_t)leaf_max, 4097u);
+        RN_CUDA(cudaGetLastError(), st);
+        RN_CUDA(cudaMemcpyAsync(hc, ctr, sizeof hc, cudaMemcpyDeviceToHost, s), st);
+        RN_CUDA(cudaStreamSynchronize(s), st);
+        level_tasks = hc[0];
+        depth = hc[5];
+        if (level_tasks > 0) return fail(st, RN_ERR_BUDGET, "collapse: more than 4096 levels");
+    }
     while (level_tasks > 0) {
         if (depth > 4096) return fail(st, RN_ERR_BUDGET, "collapse: more than 4096 levels");
         for (int k = 0; k < kLevels; ++k) {

@@ -43,7 +43,7 @@ enum Slot {
     WS_SUR_AO4, WS_SUR_PRED, WS_SUR_FB, WS_SUR_AOFB, WS_SUR_STATS, WS_VPOS, WS_VNRM, WS_VDEPTH, WS_GTAO,
     WS_ALB_IN, WS_ALB, WS_MOTION, WS_FRAME, WS_HDR, WS_FRAME_SMALL, WS_MIRROR,
     WS_HYB_LIT, WS_HYB_TRI, WS_HYB_T, WS_HYB_NG, WS_CLOSEST_TRI, WS_CLOSEST_T,
-    WS_PT_SAMPLES, WS_PT_ACC, WS_PT_OUT, WS_PT_CTR,
+    WS_PT_SAMPLES, WS_PT_ACC, WS_PT_OUT, WS_PT_CTR, WS_PLOC, WS_COLLAPSE,
     WS_COUNT
 };
 
@@ -66,8 +66,10 @@ struct Tune {
     int accel_leaf_small = 4;   // ... of those with fewer than kSmallScene triangles
     int frame_direct = 1;       // host-buffer frames: the passes read and write mapped host memory
     int hybrid_min_blocks = 6;  // resident 128-thread hybrid-pass blocks per SM: 5, 6 or 8
+    int trace_leaf_pass = 1;    // traversal: a node's leaf children tested in one loop after its slab tests
     int conv_tmem_a = 0;        // row-ring convolutions of 32 -> 32 or 16 -> 32 channels: A operands kept in TMEM
     int ploc_tail = 4096;       // PLOC: the rounds from this many clusters on run in one block (0: never)
+    int collapse_block = 0;     // 4-wide collapse: trees of at most this many triangles in one block
     int trace_pool = 0;         // AO-only walks from a per-packet queue, lanes refilled below this many busy (0: off)
     int pt_regen = 4;           // path tracer: persistent threads regenerating paths, blocks of 128 per SM (0: one thread a sample)
     int pt_slice = 0;           // path tracer: samples per slice at most (0: as many as 2 GiB of terms hold)
@@ -179,7 +181,7 @@ struct PlocTree {
     int32_t* left = nullptr;   // (2n-1)
     int32_t* right = nullptr;  // (2n-1)
     int32_t* tri = nullptr;    // (2n-1)
-    void* mem = nullptr;       // the one allocation holding the arrays above
+    void* mem = nullptr;       // the workspace block holding the arrays above (not owned)
 };
 int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaStream_t s, rn_status* st);
 void ploc_free(PlocTree* t);

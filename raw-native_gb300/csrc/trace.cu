@@ -31,7 +31,7 @@ using namespace trace_dev;
 // fetches to counts[0..3] (hemisphere rays, nodes, tris, sky continuations); the outputs of
 // the other tiles are left unwritten. "Sky continuations" are the open hemisphere rays whose
 // walk went on past the radius: the same walk serves both queries.
-template <bool kCount, int kMinBlocks, int kStackN>
+template <bool kCount, int kMinBlocks, int kStackN, bool kLeafPass = false>
 __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_constant__ TraceParams p, uint32_t* tile_ctr,
                                                                 unsigned long long* counts, uint32_t stride) {
     const int pl = p.packet_log2, tw = 1 << pl, th = 32 >> pl;
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
         // no lane leaves the loop body early: the next tile fetch is a full-warp shuffle
         if (kCount && tile % stride != 0) continue;
         const int fn = (!p.want_sky && p.has_geometry && p.frontier) ? tile_frontier(p, x, y, x < p.w && y < p.h, F) : 0;
-        if (x < p.w && y < p.h) trace_pixel<kCount, kStackN>(p, x, y, toLight, cn, F, fn);
+        if (x < p.w && y < p.h) trace_pixel<kCount, kStackN, kLeafPass>(p, x, y, toLight, cn, F, fn);
         __syncwarp();                              // the frontier is rebuilt for the next tile
     }
     if (kCount) {
@@ -339,6 +339,8 @@ void launch_variant(const TraceParams& p, int sm_count, cudaStream_t s, uint32_t
         trace_kernel<true, kMB, kStack><<<blocks, 256, 0, s>>>(p, tile_ctr, counts, stride < 1 ? 1 : stride);
     else if (pool > 0 && !p.want_sky)
         trace_ao_pool_kernel<kMB, kStackN><<<blocks, 256, 0, s>>>(p, tile_ctr, pool);
+    else if (ctx().tune.trace_leaf_pass)
+        trace_kernel<false, kMB, kStackN, true><<<blocks, 256, 0, s>>>(p, tile_ctr, nullptr, 1);
     else
         trace_kernel<false, kMB, kStackN><<<blocks, 256, 0, s>>>(p, tile_ctr, nullptr, 1);
 }

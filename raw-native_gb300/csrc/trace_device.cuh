@@ -189,7 +189,12 @@ __device__ inline int build_frontier(const Node4* __restrict__ nodes, const floa
 // 1e-4 < t < tnear; HIT_FAR alone when the nearest hit it needed to find lies in
 // [tnear, tfar); 0 when nothing is hit before tfar. The any-hit query of raw::Bvh::occluded
 // (src/renderer/bvh.cpp:119-138) is tnear == tfar.
-template <bool kCount, int kStackN = kStack>
+// kLeafPass: a node's leaf children are tested after all four slab tests, in one loop over
+// the leaves that passed (lanes whose leaves sit at different child positions test them
+// together, and the triangle test exists once in the code instead of once per position).
+// Either order finds the same answers: boxes are only culled against tmax >= tnear, and a
+// far hit only lowers tmax to tnear.
+template <bool kCount, int kStackN = kStack, bool kLeafPass = false>
 __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__ tris, const v3& o, const v3& d,
                     float tnear, float tfar, uint32_t* err, Counts& cn, const FrontierEntry* F = nullptr,
                     int fn = 0) {
@@ -246,11 +251,13 @@ __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__
         const int32_t CH[4] = {ch.x, ch.y, ch.z, ch.w};
         int32_t nearest = -1;
         float tbest = 3.0e38f;
+        unsigned leaves = 0;                  // kLeafPass: child positions of leaves to test
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             float tn;
             if (k >= cnt || !slab(LX[k], HX[k], LY[k], HY[k], LZ[k], HZ[k], o, iv, tmax, tn)) continue;
             const int32_t c = CH[k];
+            if (kLeafPass && c < 0) { leaves |= 1u << k; continue; }
             if (c < 0) {
                 // a leaf: test its triangles now (a near hit ends the walk)
                 if (!wr_ready) { wr = make_wray(o, d); wr_ready = true; }
@@ -274,6 +281,24 @@ __device__ int walk(const Node4* __restrict__ nodes, const LeafTri* __restrict__
             if (sp >= kStackN) { atomicOr(err, DEV_STACK_OVERFLOW); return far_hit; }
             stack[sp++] = push;
         }
+        if (kLeafPass)
+            while (leaves) {
+                const int k = __ffs(leaves) - 1;
+                leaves &= leaves - 1u;
+                const int32_t c = k == 0 ? ch.x : k == 1 ? ch.y : k == 2 ? ch.z : ch.w;
+                if (!wr_ready) { wr = make_wray(o, d); wr_ready = true; }
+                const uint32_t w = (uint32_t)~c;
+                const uint32_t first = w >> 3, count = (w & 7u) + 1u;
+                for (uint32_t i = 0; i < count; ++i) {
+                    if (kCount) ++cn.tris;
+                    const float4* tq = reinterpret_cast<const float4*>(tris + first + i);
+                    const float4 A = __ldg(tq), B = __ldg(tq + 1), C = __ldg(tq + 2);
+                    float t;
+                    if (!hit_tri(wr, mk(A.x, A.y, A.z), mk(B.x, B.y, B.z), mk(C.x, C.y, C.z), t)) continue;
+                    if (t < tnear) return HIT_NEAR | HIT_FAR;
+                    if (t < tmax) { far_hit = HIT_FAR; tmax = tnear; }
+                }
+            }
         if (nearest >= 0) { cur = nearest; continue; }
         if (sp == 0) return far_hit;
         cur = stack[--sp];
@@ -395,7 +420,7 @@ __device__ __forceinline__ v3 sample_direction(const v3& t, const v3& b, const v
 }
 
 // One pixel: its spp cosine-weighted rays (AO and, when asked, the sky), then the sun ray.
-template <bool kCount, int kStackN = kStack>
+template <bool kCount, int kStackN = kStack, bool kLeafPass = false>
 __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, const v3& toLight, Counts& cn,
                                             const FrontierEntry* F = nullptr, int fn = 0) {
     const float kFar = 1e30f;
@@ -452,8 +477,8 @@ __device__ __forceinline__ void trace_pixel(const TraceParams& p, int x, int y, 
         }
         // AO-only walks may start from the warp's frontier; the sky and the sun need the root
         const bool local = s < p.spp && tf == p.radius;
-        const int h = p.has_geometry ? walk<kCount, kStackN>(p.nodes, p.tris, origin, dir, tn, tf, p.err_word, cn,
-                                                    local ? F : nullptr, local ? fn : 0)
+        const int h = p.has_geometry ? walk<kCount, kStackN, kLeafPass>(p.nodes, p.tris, origin, dir, tn, tf, p.err_word,
+                                                               cn, local ? F : nullptr, local ? fn : 0)
                                      : 0;
         if (s < p.spp) {
             if (kCount) { ++cn.rays; if (p.want_sky && !(h & HIT_NEAR)) ++cn.sky; }

@@ -164,6 +164,7 @@ def test_autotuner_file_round_trip(lib, tmp_path):
             rn_ao.tune_set(k, v)
         rn_ao.tune_load(str(path))
         assert rn_ao.tune_all() == pick
+        assert autotune.read_tune_file(str(path)) == pick      # --merge reads what it wrote
     finally:
         for k, v in saved.items():
             rn_ao.tune_set(k, v)
