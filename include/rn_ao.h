@@ -364,6 +364,9 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *                                    collapse to 4-wide nodes in one block (0: a launch per level)
  *   trace_pool        0|16|24|32     AO-only walks: one queue of a packet's walks, idle lanes
  *                                    refilled when fewer than this many walk (0: one pixel per lane)
+ *   pt_wave           0|1|64|256|1024|2048  rn_pathtrace: the wavefront form (a bounce as shade, shadow-ray
+ *                                    and closest-hit kernels over this many x 1024 path slots;
+ *                                    0: one kernel a path, below)
  *   pt_regen          0|4|8|16       rn_pathtrace: persistent threads that start a new path when
  *                                    theirs ends, this many 128-thread blocks per SM (0: a thread a sample)
  *   pt_slice          0|1|4|16       rn_pathtrace: samples traced per slice at most (0: as many

@@ -37,7 +37,8 @@ Workloads:
   ploc_tail      accelerator builds of the 744k scene, a 1M soup and the 20,000-triangle check
                  soup (the cluster count from which the PLOC rounds run in one block; then the
                  size under which the collapse runs in one block)
-  pt             the path tracer on retro_room and iso_street at 640 x 360, 16 spp (pt_regen)
+  pt             the path tracer on retro_room and iso_street at 1280 x 720, 16 spp (pt_regen,
+                 pt_wave)
 The traversal keys are searched jointly (every combination); the others one at a time.
 """
 from __future__ import annotations
@@ -455,9 +456,10 @@ def tune_ploc_tail(quick: bool, reps: int, log):
 
 
 def tune_pt(quick: bool, reps: int, log):
-    """The path tracer's kernel: a thread per sample, or persistent threads regenerating paths
-    (4, 8, 16 blocks per SM): retro_room and iso_street (the reference's lit scenes, from the
-    test fixtures) at 640 x 360, 16 spp, every AOV checked bit for bit."""
+    """The path tracer's form: one kernel a path (a thread a sample, or persistent threads
+    regenerating paths: 4, 8, 16 blocks per SM) or the wavefront form over 64K to 2M path
+    slots: retro_room and iso_street (the reference's lit scenes, from the test fixtures) at
+    1280 x 720, 16 spp, every candidate's radiance, variance and diffuse checked bit for bit."""
     import os
     z = np.load(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden",
                              "pt_scenes.npz"))
@@ -466,26 +468,30 @@ def tune_pt(quick: bool, reps: int, log):
         sc = {k.split("/", 1)[1]: z[k] for k in z.files if k.startswith(key + "/")}
         cam = [float(v) for v in sc.pop("camera")]
         s = rn.PtScene(sc)
-        d = dict(seed=1, spp=4 if quick else 16, width=320 if quick else 640, height=180 if quick else 360, camera=cam)
+        d = dict(seed=1, spp=4 if quick else 16, width=320 if quick else 1280, height=180 if quick else 720, camera=cam)
         wls.append(("pt/" + key, s, d))
-    current = rn.tune_get("pt_regen")
+    current = {"pt_wave": rn.tune_get("pt_wave"), "pt_regen": rn.tune_get("pt_regen")}
+    cands = [{"pt_wave": 0, "pt_regen": v} for v in rn.TUNE_KEYS["pt_regen"]]
+    cands += [{"pt_wave": v, "pt_regen": current["pt_regen"]} for v in rn.TUNE_KEYS["pt_wave"] if v >= 64]
+    if current not in cands:
+        cands.append(dict(current))
     rows, ref = [], None
-    for v in rn.TUNE_KEYS["pt_regen"]:
-        rn.tune_set("pt_regen", v)
+    for cfg in cands:
+        _apply(cfg)
         outs = [rn.path_trace(s, d, device=True, planes=("radiance", "variance", "diffuse")) for _, s, d in wls]
         if ref is None:
             ref = outs
         elif not all(bool((o[k] == r[k]).all()) for o, r in zip(outs, ref) for k in o):
-            raise RuntimeError("pt_regen %d changed a path-traced result" % v)
-        ms = {name: _time(lambda s=s, d=d: rn.path_trace(s, d, device=True, planes=("radiance",)), reps)
+            raise RuntimeError("%s changed a path-traced result" % cfg)
+        ms = {name: _time(lambda s=s, d=d: rn.path_trace(s, d, device=True, planes=("radiance",)), max(2, reps // 2))
               for name, s, d in wls}
-        rows.append(dict(cfg={"pt_regen": v}, ms=ms))
-        log("pt_regen %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
-    base = next(r for r in rows if r["cfg"]["pt_regen"] == current)["ms"]
+        rows.append(dict(cfg=dict(cfg), ms=ms))
+        log("pt %s  %s" % (cfg, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    base = next(r for r in rows if r["cfg"] == current)["ms"]
     for r in rows:
         r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
     best = min(rows, key=lambda r: r["score"])
-    rn.tune_set("pt_regen", best["cfg"]["pt_regen"])
+    _apply(best["cfg"])
     for _, s, _ in wls:
         s.close()
     return best["cfg"], rows

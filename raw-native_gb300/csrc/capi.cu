@@ -107,7 +107,7 @@ struct TuneKey {
     const char* name;
     const char* env;
     int Tune::*field;
-    int allowed[4];
+    int allowed[6];
     int nallowed;
 };
 const TuneKey kTuneKeys[] = {
@@ -129,6 +129,7 @@ const TuneKey kTuneKeys[] = {
     {"hybrid_min_blocks", "RN_TUNE_HYBRID_MIN_BLOCKS", &Tune::hybrid_min_blocks, {5, 6, 8}, 3},
     {"pt_slice", "RN_TUNE_PT_SLICE", &Tune::pt_slice, {0, 1, 4, 16}, 4},
     {"pt_regen", "RN_TUNE_PT_REGEN", &Tune::pt_regen, {0, 4, 8, 16}, 4},
+    {"pt_wave", "RN_TUNE_PT_WAVE", &Tune::pt_wave, {0, 1, 64, 256, 1024, 2048}, 6},
     {"trace_pool", "RN_TUNE_TRACE_POOL", &Tune::trace_pool, {0, 16, 24, 32}, 4},
     {"ploc_tail", "RN_TUNE_PLOC_TAIL", &Tune::ploc_tail, {0, 4096, 32768, 262144}, 4},
     {"collapse_block", "RN_TUNE_COLLAPSE_BLOCK", &Tune::collapse_block, {0, 16384, 65536, 262144}, 4},

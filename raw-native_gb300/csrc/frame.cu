@@ -41,7 +41,7 @@ __device__ __forceinline__ bool project_uv(const M16& vp, float x, float y, floa
         cs[r] = fadd(fadd(fadd(fmul(vp.m[4 * r], x), fmul(vp.m[4 * r + 1], y)), fmul(vp.m[4 * r + 2], z)),
                      fmul(vp.m[4 * r + 3], 1.0f));
     if (cs[3] <= 1e-6f) return false;
-    const float invw = fdiv(1.0f, cs[3]);
+    const float invw = frcp(cs[3]);
     const float nx = fmul(cs[0], invw), ny = fmul(cs[1], invw);
     u = fadd(fmul(nx, 0.5f), 0.5f);
     v = fsub(1.0f, fadd(fmul(ny, 0.5f), 0.5f));

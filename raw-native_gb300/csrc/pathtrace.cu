@@ -298,7 +298,7 @@ __device__ __forceinline__ float lambda_f(float a2, float cosT) {
 __device__ __noinline__ v3 sample_vndf(const PtParams& P, v3 wo, float a, float u1, uint32_t kb) {
     const v3 vh = normalize(mk(fmul(a, wo.x), fmul(a, wo.y), wo.z));
     const float lensq = fadd(fmul(vh.x, vh.x), fmul(vh.y, vh.y));
-    const v3 t1 = lensq > 0.0f ? scale(mk(-vh.y, vh.x, 0.0f), fdiv(1.0f, fsqrt(lensq))) : mk(1.0f, 0.0f, 0.0f);
+    const v3 t1 = lensq > 0.0f ? scale(mk(-vh.y, vh.x, 0.0f), frcp(fsqrt(lensq))) : mk(1.0f, 0.0f, 0.0f);
     const v3 t2 = cross(vh, t1);
     float cphi, sphi;
     sample_sincos(kb, P.corr, cphi, sphi);
@@ -340,81 +340,104 @@ __device__ __forceinline__ void table_avg(const float* __restrict__ t, float rou
     const float* p = t + kNodes + (size_t)y0 * 2;
     A = fadd(fmul(__ldg(p), gy), fmul(__ldg(p + 2), fy)); B = fadd(fmul(__ldg(p + 1), gy), fmul(__ldg(p + 3), fy));
 }
-struct Energy { float ms, wd, kd, eavg; };
-__device__ __noinline__ Energy energy_of(const PtParams& P, const Bsdf& m, float muO, float muI) {
-    float oa, ob, ia, ib, aa, ab;
-    table_ab(P.table, muO, m.rough, oa, ob);
-    table_ab(P.table, muI, m.rough, ia, ib);
-    table_avg(P.table, m.rough, aa, ab);
-    const float eo = smin(1.0f, fadd(oa, ob)), ei = smin(1.0f, fadd(ia, ib)), ea = smin(1.0f, fadd(aa, ab));
-    Energy e;
-    e.eavg = ea;
-    e.ms = ea < 1.0f ? fdiv(fmul(fsub(1.0f, eo), fsub(1.0f, ei)), fmul(kPiF, fsub(1.0f, ea))) : 0.0f;
-    const float on = m.specular > 0.0f ? 1.0f : 0.0f, d = fmul(0.04f, m.specular);
-    e.kd = kms(fmul(on, fadd(d, fdiv(fsub(1.0f, d), 21.0f))), ea);
-    const float eso = fadd(fmul(on, fadd(fmul(d, oa), ob)), fmul(e.kd, fsub(1.0f, eo)));
-    const float esi = fadd(fmul(on, fadd(fmul(d, ia), ib)), fmul(e.kd, fsub(1.0f, ei)));
-    const float esa = fadd(fmul(on, fadd(fmul(d, aa), ab)), fmul(e.kd, fsub(1.0f, ea)));
-    e.wd = fdiv(fmul(fsub(1.0f, eso), fsub(1.0f, esi)), fsub(1.0f, esa));
-    return e;
+// The lobe at one surface point for one outgoing direction: every term of energyOf,
+// evalLegacy and evalBsdf (rt_pt_math.hpp:113-183) that does not depend on the incoming
+// direction, formed once per bounce instead of once per evaluation (the operations and
+// their order are the reference's; only their repetition is gone). The bounce evaluates the
+// lobe for three incoming directions (the sun, the sampled emitter point, the sampled
+// direction), each also giving its Lambert part (lambertCos, rt_pt_math.hpp:184-190, of the
+// same pair).
+struct Lobe {
+    Bsdf m;
+    float ps;                       // lobe_prob
+    v3 fd;                          // base x (1 - metallic) / pi
+    // specular (ps > 0): F0, f90, a^2, Lambda(wo), G1 = 1 / (1 + Lambda(wo)), 4 wo.z
+    v3 F0;
+    float f90, a2, lo, G1, four_wo;
+    // energy compensation (ps > 0, v4 lobe): the table's terms at mu_o and its average
+    float on, d, kd, omeo, den_ms, omeso, omesa;
+    bool ms_on;                     // E_avg < 1
+    v3 km;
+};
+__device__ __forceinline__ float km_of(const Bsdf& m, float b, float eavg, float kd) {
+    return fadd(fmul(m.metallic, kms(fadd(b, fdiv(fsub(1.0f, b), 21.0f)), eavg)), fmul(fsub(1.0f, m.metallic), kd));
 }
-struct Eval { v3 fcos; float pdf; };
-// The shared specular part of both lobes: h, D, G1, G2, the Fresnel weight x1^5.
-struct Spec { float D, G1, G2, fw, spec; };
-__device__ __forceinline__ Spec spec_terms(const Bsdf& m, v3 wo, v3 wi) {
-    const float a = smax(1e-4f, fmul(m.rough, m.rough)), a2 = fmul(a, a);
-    const v3 h = normalize(add(wo, wi));
-    const float oh = dot(wo, h);
-    Spec s;
-    s.D = ggx_d(a2, h.z);
-    const float lo = lambda_f(a2, wo.z);
-    s.G2 = fdiv(1.0f, fadd(fadd(1.0f, lo), lambda_f(a2, wi.z)));
-    s.G1 = fdiv(1.0f, fadd(1.0f, lo));
-    const float x1 = clampf(fsub(1.0f, oh), 0.0f, 1.0f);
-    s.fw = fmul(fmul(fmul(fmul(x1, x1), x1), x1), x1);
-    s.spec = fdiv(fmul(s.D, s.G2), fmul(fmul(4.0f, wo.z), wi.z));
-    return s;
-}
-__device__ __forceinline__ float km_of(const Bsdf& m, float b, const Energy& en) {
-    return fadd(fmul(m.metallic, kms(fadd(b, fdiv(fsub(1.0f, b), 21.0f)), en.eavg)), fmul(fsub(1.0f, m.metallic), en.kd));
-}
-__device__ __noinline__ Eval eval_bsdf(const PtParams& P, const Bsdf& m, v3 wo, v3 wi, bool dropCosine) {
-    Eval r{mk(0.0f, 0.0f, 0.0f), 0.0f};
-    if (wo.z <= 0.0f || wi.z <= 0.0f) return r;
-    const float ps = lobe_prob(m), cosI = dropCosine ? 1.0f : wi.z;
+__device__ __noinline__ void lobe_setup(const PtParams& P, const Bsdf& m, float woz, Lobe& L) {
+    L.m = m;
+    L.ps = lobe_prob(m);
     const float kd = fdiv(fsub(1.0f, m.metallic), kPiF);
-    v3 f = mk(fmul(m.base.x, kd), fmul(m.base.y, kd), fmul(m.base.z, kd));
+    L.fd = mk(fmul(m.base.x, kd), fmul(m.base.y, kd), fmul(m.base.z, kd));
+    if (!(L.ps > 0.0f)) return;
+    L.F0 = f0_of(m);
+    L.f90 = fadd(m.metallic, fmul(fsub(1.0f, m.metallic), m.specular > 0.0f ? 1.0f : 0.0f));
+    const float a = smax(1e-4f, fmul(m.rough, m.rough));
+    L.a2 = fmul(a, a);
+    L.lo = lambda_f(L.a2, woz);
+    L.G1 = frcp(fadd(1.0f, L.lo));
+    L.four_wo = fmul(4.0f, woz);
+    if (m.legacy) return;
+    float oa, ob, aa, ab;
+    table_ab(P.table, woz, m.rough, oa, ob);
+    table_avg(P.table, m.rough, aa, ab);
+    const float eo = smin(1.0f, fadd(oa, ob)), ea = smin(1.0f, fadd(aa, ab));
+    L.ms_on = ea < 1.0f;
+    L.omeo = fsub(1.0f, eo);
+    L.den_ms = fmul(kPiF, fsub(1.0f, ea));
+    L.on = m.specular > 0.0f ? 1.0f : 0.0f;
+    L.d = fmul(0.04f, m.specular);
+    L.kd = kms(fmul(L.on, fadd(L.d, fdiv(fsub(1.0f, L.d), 21.0f))), ea);
+    const float eso = fadd(fmul(L.on, fadd(fmul(L.d, oa), ob)), fmul(L.kd, fsub(1.0f, eo)));
+    const float esa = fadd(fmul(L.on, fadd(fmul(L.d, aa), ab)), fmul(L.kd, fsub(1.0f, ea)));
+    L.omeso = fsub(1.0f, eso);
+    L.omesa = fsub(1.0f, esa);
+    L.km = mk(km_of(m, m.base.x, ea, L.kd), km_of(m, m.base.y, ea, L.kd), km_of(m, m.base.z, ea, L.kd));
+}
+// evalBsdf / evalLegacy (f cos and pdf) and lambertCos of one (wo, wi) pair.
+struct Eval { v3 fcos; float pdf; v3 lam; };
+__device__ __noinline__ Eval eval_lobe(const PtParams& P, const Lobe& L, v3 wo, v3 wi, bool dropCosine) {
+    const v3 z = mk(0.0f, 0.0f, 0.0f);
+    Eval r{z, 0.0f, z};
+    if (wo.z <= 0.0f || wi.z <= 0.0f) return r;
+    const Bsdf& m = L.m;
+    const float ps = L.ps, cosI = dropCosine ? 1.0f : wi.z;
+    v3 f = L.fd;
     float pdf = fdiv(fmul(fsub(1.0f, ps), wi.z), kPiF);
+    v3 lam = f;
     if (ps > 0.0f) {
-        const v3 F0 = f0_of(m);
+        // the specular terms with the per-bounce parts
+        const v3 h = normalize(add(wo, wi));
+        const float oh = dot(wo, h);
+        const float D = ggx_d(L.a2, h.z);
+        const float G2 = frcp(fadd(fadd(1.0f, L.lo), lambda_f(L.a2, wi.z)));
+        const float x1 = clampf(fsub(1.0f, oh), 0.0f, 1.0f);
+        const float fw = fmul(fmul(fmul(fmul(x1, x1), x1), x1), x1);
+        const float spec = fdiv(fmul(D, G2), fmul(L.four_wo, wi.z));
+        const v3 F0 = L.F0;
         if (m.legacy) {
-            const Spec s = spec_terms(m, wo, wi);
-            const v3 F = mk(fadd(F0.x, fmul(fsub(1.0f, F0.x), s.fw)), fadd(F0.y, fmul(fsub(1.0f, F0.y), s.fw)),
-                            fadd(F0.z, fmul(fsub(1.0f, F0.z), s.fw)));
-            f = add(f, scale(F, s.spec));
-            pdf = fadd(pdf, fmul(ps, fdiv(fmul(s.G1, s.D), fmul(4.0f, wo.z))));
+            const v3 F = mk(fadd(F0.x, fmul(fsub(1.0f, F0.x), fw)), fadd(F0.y, fmul(fsub(1.0f, F0.y), fw)),
+                            fadd(F0.z, fmul(fsub(1.0f, F0.z), fw)));
+            f = add(f, scale(F, spec));
         } else {
-            const Energy en = energy_of(P, m, wo.z, wi.z);
-            f = scale(f, en.wd);
-            const Spec s = spec_terms(m, wo, wi);
-            const float f90 = fadd(m.metallic, fmul(fsub(1.0f, m.metallic), m.specular > 0.0f ? 1.0f : 0.0f));
-            const v3 F = mk(fadd(F0.x, fmul(fsub(f90, F0.x), s.fw)), fadd(F0.y, fmul(fsub(f90, F0.y), s.fw)),
-                            fadd(F0.z, fmul(fsub(f90, F0.z), s.fw)));
-            const v3 km = mk(km_of(m, m.base.x, en), km_of(m, m.base.y, en), km_of(m, m.base.z, en));
-            f = add(add(f, scale(F, s.spec)), scale(km, en.ms));
-            pdf = fadd(pdf, fmul(ps, fdiv(fmul(s.G1, s.D), fmul(4.0f, wo.z))));
+            // energyOf's terms at mu_i
+            float ia, ib;
+            table_ab(P.table, wi.z, m.rough, ia, ib);
+            const float ei = smin(1.0f, fadd(ia, ib));
+            const float ms = L.ms_on ? fdiv(fmul(L.omeo, fsub(1.0f, ei)), L.den_ms) : 0.0f;
+            const float esi = fadd(fmul(L.on, fadd(fmul(L.d, ia), ib)), fmul(L.kd, fsub(1.0f, ei)));
+            const float wd = fdiv(fmul(L.omeso, fsub(1.0f, esi)), L.omesa);
+            f = scale(f, wd);
+            lam = f;
+            const float f90 = L.f90;
+            const v3 F = mk(fadd(F0.x, fmul(fsub(f90, F0.x), fw)), fadd(F0.y, fmul(fsub(f90, F0.y), fw)),
+                            fadd(F0.z, fmul(fsub(f90, F0.z), fw)));
+            f = add(add(f, scale(F, spec)), scale(L.km, ms));
         }
+        pdf = fadd(pdf, fmul(ps, fdiv(fmul(L.G1, D), L.four_wo)));
     }
     r.fcos = scale(f, cosI);
     r.pdf = pdf;
+    r.lam = scale(lam, cosI);
     return r;
-}
-__device__ __noinline__ v3 lambert_cos(const PtParams& P, const Bsdf& m, v3 wo, v3 wi, bool dropCosine) {
-    if (wo.z <= 0.0f || wi.z <= 0.0f) return mk(0.0f, 0.0f, 0.0f);
-    const float cosI = dropCosine ? 1.0f : wi.z, kd = fdiv(fsub(1.0f, m.metallic), kPiF);
-    v3 f = mk(fmul(m.base.x, kd), fmul(m.base.y, kd), fmul(m.base.z, kd));
-    if (!m.legacy && lobe_prob(m) > 0.0f) f = scale(f, energy_of(P, m, wo.z, wi.z).wd);
-    return scale(f, cosI);
 }
 __device__ __forceinline__ v3 spec_albedo(const Bsdf& m, float cosO) {
     if (lobe_prob(m) <= 0.0f) return mk(0.0f, 0.0f, 0.0f);
@@ -442,11 +465,9 @@ __device__ bool sample_bsdf(const PtParams& P, const Bsdf& m, v3 wo, float pick,
 struct Surf { v3 p, n, ng, base; const float* m; float t; int tri; };
 __device__ __forceinline__ v3 tri_corner(const PtParams& P, int t, int k) { return load3(P.tris + (size_t)t * 9 + 3 * k); }
 
-__device__ __noinline__ bool hit(const PtParams& P, v3 o, v3 d, float tmax, Surf& x) {
-    if (!P.has_geometry) return false;
-    float t;
-    const int tri = walk_closest(P.nodes, P.ltris, o, d, tmax, t, P.err);
-    if (tri < 0) return false;
+// The surface at the closest hit (triangle tri at t along o + t d): the hit's barycentrics,
+// position, normals, texture coordinates, texel and material (rt_pt_ctx.hpp:18-60).
+__device__ __noinline__ void surface_of(const PtParams& P, v3 o, v3 d, int tri, float t, Surf& x) {
     const v3 a = tri_corner(P, tri, 0), b = tri_corner(P, tri, 1), c = tri_corner(P, tri, 2);
     float tt, u, v;
     hit_tri_uv(make_wray(o, d), a, b, c, tt, u, v);      // the winner's u, v (its t is the walk's)
@@ -473,6 +494,13 @@ __device__ __noinline__ bool hit(const PtParams& P, v3 o, v3 d, float tmax, Surf
     if (dot(x.ng, d) > 0.0f) x.ng = scale(x.ng, -1.0f);
     if (dot(x.n, x.ng) < 0.0f) x.n = scale(x.n, -1.0f);
     (void)tt;
+}
+__device__ __noinline__ bool hit(const PtParams& P, v3 o, v3 d, float tmax, Surf& x) {
+    if (!P.has_geometry) return false;
+    float t;
+    const int tri = walk_closest(P.nodes, P.ltris, o, d, tmax, t, P.err);
+    if (tri < 0) return false;
+    surface_of(P, o, d, tri, t, x);
     return true;
 }
 __device__ __noinline__ bool visible(const PtParams& P, v3 p, v3 dir, float tmax) {
@@ -484,17 +512,17 @@ __device__ __forceinline__ v3 offset_of(const Surf& x, v3 dir) {
     const float e = fmul(2e-4f, fadd(1.0f, smax(fabsf(x.p.x), smax(fabsf(x.p.y), fabsf(x.p.z)))));
     return add(x.p, scale(x.ng, dot(x.ng, dir) > 0.0f ? e : -e));
 }
-__device__ v3 nee(const PtParams& P, const Surf& x, const Frame& fr, const Bsdf& bs, v3 woL, uint32_t px, uint32_t smp,
+__device__ v3 nee(const PtParams& P, const Surf& x, const Frame& fr, const Lobe& lb, v3 woL, uint32_t px, uint32_t smp,
                   uint32_t base, v3& diff) {
     v3 L = mk(0.0f, 0.0f, 0.0f);
     diff = L;
     const bool dc = (P.controls & RN_PT_DROP_LAMBERT_COSINE) != 0;
     if (maxc(P.sun_irr) > 0.0f) {
         const v3 l = P.sun_dir, lL = to_local(fr, l);
-        const Eval e = eval_bsdf(P, bs, woL, lL, dc);
+        const Eval e = eval_lobe(P, lb, woL, lL, dc);
         if (maxc(e.fcos) > 0.0f && visible(P, offset_of(x, l), l, 1e30f)) {
             L = add(L, mulv(e.fcos, P.sun_irr));
-            diff = add(diff, mulv(lambert_cos(P, bs, woL, lL, dc), P.sun_irr));
+            diff = add(diff, mulv(e.lam, P.sun_irr));
         }
     }
     if (P.nemit == 0) return L;
@@ -512,18 +540,18 @@ __device__ v3 nee(const PtParams& P, const Surf& x, const Frame& fr, const Bsdf&
     const v3 q = add(add(scale(ta, fsub(1.0f, su)), scale(tb, fmul(su, fsub(1.0f, b.a)))), scale(tc, fmul(su, b.a)));
     const v3 to = sub(q, x.p);
     const float dist = length(to);
-    const v3 l = scale(to, fdiv(1.0f, dist)), lL = to_local(fr, l);
+    const v3 l = scale(to, frcp(dist)), lL = to_local(fr, l);
     const float cosL = fabsf(dot(normalize(cross(sub(tb, ta), sub(tc, ta))), l));
     if (cosL <= 0.0f) return L;
     const float pl = fdiv(fmul(dist, dist), fmul(cosL, P.area));
-    const Eval e = eval_bsdf(P, bs, woL, lL, dc);
+    const Eval e = eval_lobe(P, lb, woL, lL, dc);
     if (maxc(e.fcos) <= 0.0f || !visible(P, offset_of(x, l), l, fmul(dist, fsub(1.0f, 1e-3f)))) return L;
     const float w = (P.controls & RN_PT_MIS_WEIGHT_ONE) ? 1.0f
                                                       : fdiv(fmul(pl, pl), fadd(fmul(pl, pl), fmul(e.pdf, e.pdf)));
     const float* em = P.mat + 7 * (size_t)__ldg(P.tritex + et) + 4;
     const v3 Le = mk(__ldg(em), __ldg(em + 1), __ldg(em + 2));
     const float wp = fdiv(w, pl);
-    diff = add(diff, scale(mulv(lambert_cos(P, bs, woL, lL, dc), Le), wp));
+    diff = add(diff, scale(mulv(e.lam, Le), wp));
     return add(L, scale(mulv(e.fcos, Le), wp));
 }
 
@@ -575,25 +603,27 @@ __device__ __noinline__ bool path_bounce(const PtParams& P, Path& s) {
     const v3 woL = to_local(fr, scale(s.rd, -1.0f));
     if (woL.z <= 0.0f) return false;
     const uint32_t base = 2 + b * 4;
+    Lobe lb;
+    lobe_setup(P, bs, woL.z, lb);
     v3 nd;
-    const v3 Ln = nee(P, x0, fr, bs, woL, s.px, s.smp, base, nd);
+    const v3 Ln = nee(P, x0, fr, lb, woL, s.px, s.smp, base, nd);
     s.o.L = add(s.o.L, mulv(s.T, Ln));
     if (b == 0) { s.o.D = nd; s.o.S = sub(Ln, nd); } else s.R = add(s.R, mulv(s.tw, Ln));
     const R2 u = rand2(P, s.px, s.smp, base), r = rand2(P, s.px, s.smp, base + 1);
     v3 wiL;
     if (!sample_bsdf(P, bs, woL, r.a, u.a, u.kb, wiL)) return false;
-    const Eval e = eval_bsdf(P, bs, woL, wiL, dc);
+    const Eval e = eval_lobe(P, lb, woL, wiL, dc);
     if (e.pdf <= 0.0f) return false;
-    const float ip = fdiv(1.0f, e.pdf);
+    const float ip = frcp(e.pdf);
     const v3 step = scale(e.fcos, ip);
     s.T = mulv(s.T, step);
-    if (b == 0) { s.wd = scale(lambert_cos(P, bs, woL, wiL, dc), ip); s.ws = sub(step, s.wd); }
+    if (b == 0) { s.wd = scale(e.lam, ip); s.ws = sub(step, s.wd); }
     else s.tw = mulv(s.tw, step);
     s.prevPdf = e.pdf;
     if (P.rr && b >= 3) {
         const float q = smin(0.95f, maxc(s.T));
         if (r.b >= q) return false;
-        const float iq = fdiv(1.0f, q);
+        const float iq = frcp(q);
         s.T = scale(s.T, iq);
         s.tw = scale(s.tw, iq);
     }
@@ -687,6 +717,342 @@ __global__ void __launch_bounds__(128) pt_regen_kernel(const PtParams P, uint32_
     }
 }
 
+// ================================================================ the wavefront form
+// The same paths with each bounce split over three kernels that run over a pool of path
+// slots in HBM: pt_wave_shade (the rest of a bounce after its closest hit: emission, the
+// lobe, next-event estimation up to its shadow rays, the sampled direction, Russian
+// roulette; a slot whose path ended takes the next (pixel, sample) item), pt_wave_shadow
+// (the queued shadow rays' any-hit walks) and pt_wave_extend (the closest-hit walks). A warp
+// then runs one kind of code at a time: the bounce as one kernel left warps at different
+// points of a large body (instruction-fetch stalls dominated) and its walks diverging
+// beside shading.
+//
+// Order of every float operation is path_bounce's: a bounce's estimate (the sun's and the
+// emitter's terms, kept with the throughput it is weighted by) is added once its shadow
+// rays are traced, at the start of the slot's next shade pass, before anything else touches
+// the path's sums (the next bounce's emission, or the path's end).
+namespace wave {
+// float components (each an array of Q floats)
+enum : int {
+    RO = 0, RD = 3, T = 6, TW = 9, R = 12, WD = 15, WS = 18, PREV = 21,
+    OL = 22, OD = 25, OS = 28, OE = 31, OALB = 34, ONRM = 37, ODALB = 40, OSALB = 43,   // Sample, in store_sample order
+    TP = 46, TWP = 49, LSUN = 52, DSUN = 55, LEM = 58, DEM = 61, HT = 64, NF = 65
+};
+// u32 components
+enum : int { UB = 0, UPX = 1, USMP = 2, UJ = 3, UTRI = 4, UFL = 5, NU = 6 };
+// a slot's mode (bits 0-1) and its pending estimate
+enum : uint32_t {
+    M_FRESH = 0,      // takes the next item
+    M_TRACE = 1,      // its ray was traced (or is about to be): the next shade pass continues the bounce
+    M_END = 2,        // its path ended after an estimate: finish once the estimate is added
+    M_IDLE = 3,       // no items left
+    F_NEE = 4,        // the last bounce ran next-event estimation (add it before anything else)
+    F_SUN = 8,        // ... with a sun shadow ray
+    F_EM = 16,        // ... with an emitter shadow ray
+    F_B0 = 32         // ... at bounce 0 (the estimate sets D and S instead of adding to R)
+};
+}  // namespace wave
+
+struct WaveBufs {
+    float* f;             // NF x Q
+    uint32_t* u;          // NU x Q
+    uint8_t* vis;         // 2 x Q: the sun ray and the emitter ray reached their light
+    float* qf;            // 7 x 2Q: the shadow rays' origin, direction, limit
+    uint32_t* qu;         // 2Q: slot << 1 | (emitter ray)
+    uint32_t* ctr;        // [0] shadow rays queued [1] live slots [2..3] the 64-bit item counter
+    uint32_t Q;
+};
+__device__ __forceinline__ v3 wld3(const WaveBufs& W, int c, uint32_t i) {
+    const size_t q = W.Q;
+    return mk(W.f[c * q + i], W.f[(c + 1) * q + i], W.f[(c + 2) * q + i]);
+}
+__device__ __forceinline__ void wst3(const WaveBufs& W, int c, uint32_t i, v3 v) {
+    const size_t q = W.Q;
+    W.f[c * q + i] = v.x; W.f[(c + 1) * q + i] = v.y; W.f[(c + 2) * q + i] = v.z;
+}
+__device__ __forceinline__ uint32_t& wu(const WaveBufs& W, int c, uint32_t i) { return W.u[(size_t)c * W.Q + i]; }
+__device__ __forceinline__ float& wf(const WaveBufs& W, int c, uint32_t i) { return W.f[(size_t)c * W.Q + i]; }
+
+// `n` consecutive slots of a counter for each lane of a full warp, one atomic a warp.
+__device__ __forceinline__ uint32_t wave_reserve(uint32_t* ctr, uint32_t n) {
+    const int lane = threadIdx.x & 31;
+    uint32_t incl = n;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(ctr, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + incl - n;
+}
+
+// path_finish and store_sample from the slot's arrays.
+__device__ void wave_finish(const PtParams& P, const WaveBufs& W, uint32_t i) {
+    using namespace wave;
+    Sample o;
+    o.L = wld3(W, OL, i); o.D = wld3(W, OD, i); o.S = wld3(W, OS, i); o.E = wld3(W, OE, i);
+    o.alb = wld3(W, OALB, i); o.nrm = wld3(W, ONRM, i); o.dAlb = wld3(W, ODALB, i); o.sAlb = wld3(W, OSALB, i);
+    const v3 R = wld3(W, wave::R, i);
+    o.D = add(o.D, mulv(wld3(W, WD, i), R));
+    if (!(P.controls & RN_PT_AOV_DROP_SPECULAR_INDIRECT)) o.S = add(o.S, mulv(wld3(W, WS, i), R));
+    if (P.controls & RN_PT_AOV_EMISSION_TO_DIFFUSE) { o.D = add(o.D, o.E); o.E = mk(0.0f, 0.0f, 0.0f); }
+    store_sample(P, wu(W, UJ, i), wu(W, UPX, i), o);
+}
+
+// path_start into the slot's arrays.
+__device__ void wave_start(const PtParams& P, const WaveBufs& W, uint32_t i, uint32_t j, uint32_t px, uint32_t smp,
+                           v3 rd) {
+    using namespace wave;
+    const v3 z = mk(0.0f, 0.0f, 0.0f), one = mk(1.0f, 1.0f, 1.0f);
+    wst3(W, RO, i, P.cam.eye); wst3(W, RD, i, rd);
+    wst3(W, T, i, one); wst3(W, TW, i, one);
+    wst3(W, wave::R, i, z); wst3(W, WD, i, z); wst3(W, WS, i, z);
+    wf(W, PREV, i) = 0.0f;
+    for (int c = OL; c < OL + 24; c += 3) wst3(W, c, i, z);
+    wu(W, UB, i) = 0; wu(W, UPX, i) = px; wu(W, USMP, i) = smp; wu(W, UJ, i) = j;
+}
+
+// One bounce after its closest hit, for a slot in M_TRACE (path_bounce from the hit on):
+// returns the slot's next mode; next-event estimation leaves its flags in *fl and its
+// shadow rays in the ray arguments.
+__device__ __noinline__ uint32_t wave_bounce(const PtParams& P, const WaveBufs& W, uint32_t i, uint32_t& fl,
+                                             v3& sun_o, v3& em_o, v3& em_d, float& em_t) {
+    using namespace wave;
+    const uint32_t b = wu(W, UB, i);
+    if (b > P.max_bounces) return M_FRESH;
+    const bool dc = (P.controls & RN_PT_DROP_LAMBERT_COSINE) != 0;
+    const int tri = (int)wu(W, UTRI, i);
+    const v3 ro = wld3(W, RO, i), rd = wld3(W, RD, i);
+    v3 T = wld3(W, wave::T, i), tw = wld3(W, TW, i);
+    if (tri < 0) {
+        wst3(W, OL, i, add(wld3(W, OL, i), mulv(T, P.sky)));
+        if (b == 0) wst3(W, OE, i, P.sky); else wst3(W, wave::R, i, add(wld3(W, wave::R, i), mulv(tw, P.sky)));
+        return M_FRESH;
+    }
+    Surf x0;
+    surface_of(P, ro, rd, tri, wf(W, HT, i), x0);
+    const Bsdf bs{x0.base, __ldg(x0.m + 1), __ldg(x0.m + 2), __ldg(x0.m + 3), (P.controls & RN_PT_LEGACY_LOBE_V2) != 0};
+    if (b == 0) {
+        wst3(W, OALB, i, x0.base); wst3(W, ONRM, i, x0.n);
+        wst3(W, ODALB, i, scale(x0.base, fsub(1.0f, bs.metallic)));
+        wst3(W, OSALB, i, spec_albedo(bs, clampf(-dot(x0.n, rd), 0.0f, 1.0f)));
+    }
+    const v3 Le = mk(__ldg(x0.m + 4), __ldg(x0.m + 5), __ldg(x0.m + 6));
+    if (maxc(Le) > 0.0f) {
+        float w = 1.0f;
+        if (b > 0 && !(P.controls & RN_PT_MIS_WEIGHT_ONE)) {
+            const float pp = wf(W, PREV, i);
+            const float cosL = fabsf(dot(x0.ng, rd)), pl = fdiv(fmul(x0.t, x0.t), fmul(cosL, P.area));
+            w = fdiv(fmul(pp, pp), fadd(fmul(pp, pp), fmul(pl, pl)));
+        }
+        wst3(W, OL, i, add(wld3(W, OL, i), scale(mulv(T, Le), w)));
+        if (b == 0) wst3(W, OE, i, Le); else wst3(W, wave::R, i, add(wld3(W, wave::R, i), scale(mulv(tw, Le), w)));
+    }
+    if (b == P.max_bounces) return M_FRESH;
+    const Frame fr = basis(x0.n);
+    const v3 woL = to_local(fr, scale(rd, -1.0f));
+    if (woL.z <= 0.0f) return M_FRESH;
+    const uint32_t base = 2 + b * 4;
+    Lobe lb;
+    lobe_setup(P, bs, woL.z, lb);
+    // next-event estimation (nee) up to its shadow rays: the terms each adds when its ray
+    // reaches the light
+    fl = F_NEE | (b == 0 ? F_B0 : 0u);
+    if (maxc(P.sun_irr) > 0.0f) {
+        const v3 l = P.sun_dir, lL = to_local(fr, l);
+        const Eval e = eval_lobe(P, lb, woL, lL, dc);
+        if (maxc(e.fcos) > 0.0f) {
+            wst3(W, LSUN, i, mulv(e.fcos, P.sun_irr));
+            wst3(W, DSUN, i, mulv(e.lam, P.sun_irr));
+            sun_o = offset_of(x0, l);
+            fl |= F_SUN;
+        }
+    }
+    if (P.nemit != 0) {
+        const R2 a = rand2(P, wu(W, UPX, i), wu(W, USMP, i), base + 2), bb = rand2(P, wu(W, UPX, i), wu(W, USMP, i), base + 3);
+        const float target = fmul(a.a, P.area);
+        uint32_t lo = 0, hi = P.nemit;              // std::upper_bound: the first cdf > target
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2;
+            if (target < __ldg(P.cdf + mid)) hi = mid; else lo = mid + 1;
+        }
+        const uint32_t k = lo < P.nemit - 1 ? lo : P.nemit - 1;
+        const int et = (int)__ldg(P.emit + k);
+        const v3 ta = tri_corner(P, et, 0), tb = tri_corner(P, et, 1), tc = tri_corner(P, et, 2);
+        const float su = fsqrt(a.b);
+        const v3 q = add(add(scale(ta, fsub(1.0f, su)), scale(tb, fmul(su, fsub(1.0f, bb.a)))), scale(tc, fmul(su, bb.a)));
+        const v3 to = sub(q, x0.p);
+        const float dist = length(to);
+        const v3 l = scale(to, frcp(dist)), lL = to_local(fr, l);
+        const float cosL = fabsf(dot(normalize(cross(sub(tb, ta), sub(tc, ta))), l));
+        if (cosL > 0.0f) {
+            const float pl = fdiv(fmul(dist, dist), fmul(cosL, P.area));
+            const Eval e = eval_lobe(P, lb, woL, lL, dc);
+            if (maxc(e.fcos) > 0.0f) {
+                const float w = (P.controls & RN_PT_MIS_WEIGHT_ONE)
+                                    ? 1.0f
+                                    : fdiv(fmul(pl, pl), fadd(fmul(pl, pl), fmul(e.pdf, e.pdf)));
+                const float* em = P.mat + 7 * (size_t)__ldg(P.tritex + et) + 4;
+                const v3 Lem = mk(__ldg(em), __ldg(em + 1), __ldg(em + 2));
+                const float wp = fdiv(w, pl);
+                wst3(W, DEM, i, scale(mulv(e.lam, Lem), wp));
+                wst3(W, LEM, i, scale(mulv(e.fcos, Lem), wp));
+                em_o = offset_of(x0, l);
+                em_d = l;
+                em_t = fmul(dist, fsub(1.0f, 1e-3f));
+                fl |= F_EM;
+            }
+        }
+    }
+    wst3(W, TP, i, T);
+    wst3(W, TWP, i, tw);
+    // the sampled direction
+    const R2 u = rand2(P, wu(W, UPX, i), wu(W, USMP, i), base), r = rand2(P, wu(W, UPX, i), wu(W, USMP, i), base + 1);
+    v3 wiL;
+    if (!sample_bsdf(P, bs, woL, r.a, u.a, u.kb, wiL)) return M_END;
+    const Eval e = eval_lobe(P, lb, woL, wiL, dc);
+    if (e.pdf <= 0.0f) return M_END;
+    const float ip = frcp(e.pdf);
+    const v3 step = scale(e.fcos, ip);
+    T = mulv(T, step);
+    if (b == 0) {
+        const v3 wd = scale(e.lam, ip);
+        wst3(W, WD, i, wd);
+        wst3(W, WS, i, sub(step, wd));
+    } else {
+        tw = mulv(tw, step);
+    }
+    if (P.rr && b >= 3) {
+        const float q = smin(0.95f, maxc(T));
+        if (r.b >= q) return M_END;
+        const float iq = frcp(q);
+        T = scale(T, iq);
+        tw = scale(tw, iq);
+    }
+    const v3 wi = to_world(fr, wiL);
+    wst3(W, wave::T, i, T);
+    wst3(W, TW, i, tw);
+    wf(W, PREV, i) = e.pdf;
+    wst3(W, RO, i, offset_of(x0, wi));
+    wst3(W, RD, i, wi);
+    wu(W, UB, i) = b + 1;
+    return M_TRACE;
+}
+
+__global__ void __launch_bounds__(128) pt_wave_shade(const PtParams P, const WaveBufs W, unsigned long long total) {
+    using namespace wave;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31u;
+    const bool in = i < W.Q;
+    uint32_t fl = in ? wu(W, UFL, i) : (uint32_t)M_IDLE;
+    uint32_t mode = fl & 3u;
+    // 1. the last bounce's estimate, its shadow rays now traced (nee's sums, then the
+    //    bounce's use of them: L += T Ln, then D and S at bounce 0 or R += tw Ln)
+    if (fl & F_NEE) {
+        v3 L = mk(0.0f, 0.0f, 0.0f), diff = L;
+        if ((fl & F_SUN) && W.vis[i]) { L = add(L, wld3(W, LSUN, i)); diff = add(diff, wld3(W, DSUN, i)); }
+        if ((fl & F_EM) && W.vis[W.Q + i]) { diff = add(diff, wld3(W, DEM, i)); L = add(L, wld3(W, LEM, i)); }
+        wst3(W, OL, i, add(wld3(W, OL, i), mulv(wld3(W, TP, i), L)));
+        if (fl & F_B0) { wst3(W, OD, i, diff); wst3(W, OS, i, sub(L, diff)); }
+        else wst3(W, wave::R, i, add(wld3(W, wave::R, i), mulv(wld3(W, TWP, i), L)));
+    }
+    // 2. the bounce after the closest hit, or the end of a path that ended after its estimate
+    uint32_t nfl = 0;
+    v3 sun_o = mk(0.0f, 0.0f, 0.0f), em_o = sun_o, em_d = sun_o;
+    float em_t = 0.0f;
+    if (mode == M_TRACE) {
+        mode = wave_bounce(P, W, i, nfl, sun_o, em_o, em_d, em_t);
+        // a path that ended before any estimate (a miss, the bounce limit, a surface seen
+        // from behind) is finished now; one that ended after it (M_END) in the next pass
+        if (mode == M_FRESH) wave_finish(P, W, i);
+    } else if (mode == M_END) {
+        wave_finish(P, W, i);
+        mode = M_FRESH;
+    }
+    // 3. free slots take the next items (one atomic a warp per round)
+    const uint32_t tiles_x = (P.w + kTileW - 1) / kTileW, tiles_y = (P.h + kTileH - 1) / kTileH;
+    const uint32_t ntiles = tiles_x * tiles_y;
+    for (int round = 0; round < 64; ++round) {
+        const unsigned need = __ballot_sync(0xffffffffu, in && mode == M_FRESH);
+        if (!need) break;
+        const int leader = __ffs(need) - 1;
+        unsigned long long first = 0;
+        if ((int)lane == leader)
+            first = atomicAdd(reinterpret_cast<unsigned long long*>(W.ctr + 2), (unsigned long long)__popc(need));
+        first = __shfl_sync(0xffffffffu, first, leader);
+        if (in && mode == M_FRESH) {
+            const unsigned long long item = first + __popc(need & ((1u << lane) - 1u));
+            if (item >= total) {
+                mode = M_IDLE;
+            } else {
+                const uint32_t l = (uint32_t)(item & 31u);
+                const unsigned long long w = item >> 5;
+                const uint32_t j = (uint32_t)(w / ntiles), tile = (uint32_t)(w % ntiles);
+                const int x = (int)((tile % tiles_x) * kTileW + (l % kTileW)), y = (int)((tile / tiles_x) * kTileH + (l / kTileW));
+                if (x < P.w && y < P.h) {
+                    const uint32_t px = (uint32_t)(y * P.w + x), smp = P.spp_begin + P.k0 + j;
+                    wave_start(P, W, i, j, px, smp, camera_ray(P, x, y, px, smp));
+                    mode = M_TRACE;
+                }
+            }
+        }
+    }
+    // 4. the estimate's shadow rays into the queue; the slot's state; the live count
+    const uint32_t nr = ((nfl & F_SUN) ? 1u : 0u) + ((nfl & F_EM) ? 1u : 0u);
+    uint32_t pos = wave_reserve(W.ctr, nr);
+    const size_t q2 = 2 * (size_t)W.Q;
+    if (nfl & F_SUN) {
+        W.qf[pos] = sun_o.x; W.qf[q2 + pos] = sun_o.y; W.qf[2 * q2 + pos] = sun_o.z;
+        W.qf[3 * q2 + pos] = P.sun_dir.x; W.qf[4 * q2 + pos] = P.sun_dir.y; W.qf[5 * q2 + pos] = P.sun_dir.z;
+        W.qf[6 * q2 + pos] = 1e30f;
+        W.qu[pos] = i << 1;
+        ++pos;
+    }
+    if (nfl & F_EM) {
+        W.qf[pos] = em_o.x; W.qf[q2 + pos] = em_o.y; W.qf[2 * q2 + pos] = em_o.z;
+        W.qf[3 * q2 + pos] = em_d.x; W.qf[4 * q2 + pos] = em_d.y; W.qf[5 * q2 + pos] = em_d.z;
+        W.qf[6 * q2 + pos] = em_t;
+        W.qu[pos] = (i << 1) | 1u;
+    }
+    if (in) wu(W, UFL, i) = mode | nfl;
+    const unsigned live = __ballot_sync(0xffffffffu, in && mode != M_IDLE);
+    if (lane == 0 && live) atomicAdd(W.ctr + 1, (uint32_t)__popc(live));
+}
+
+// The queued shadow rays (visible(): the any-hit walk of the AO kernel).
+__global__ void __launch_bounds__(128) pt_wave_shadow(const PtParams P, const WaveBufs W) {
+    const uint32_t n = W.ctr[0];
+    const size_t q2 = 2 * (size_t)W.Q;
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n && k < q2; k += gridDim.x * blockDim.x) {
+        const v3 o = mk(W.qf[k], W.qf[q2 + k], W.qf[2 * q2 + k]);
+        const v3 d = mk(W.qf[3 * q2 + k], W.qf[4 * q2 + k], W.qf[5 * q2 + k]);
+        const float tmax = W.qf[6 * q2 + k];
+        const uint32_t s = W.qu[k];
+        bool vis = true;
+        if (P.has_geometry) {
+            Counts cn;
+            vis = walk<false>(P.nodes, P.ltris, o, d, tmax, tmax, P.err, cn) == 0;
+        }
+        W.vis[(size_t)(s & 1u) * W.Q + (s >> 1)] = vis ? 1 : 0;
+    }
+}
+
+// The closest hits of the slots' rays (rt::closest); also restarts the queue and live counts
+// for the next shade pass.
+__global__ void __launch_bounds__(128) pt_wave_extend(const PtParams P, const WaveBufs W) {
+    using namespace wave;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) { W.ctr[0] = 0; W.ctr[1] = 0; }
+    if (i >= W.Q || (wu(W, UFL, i) & 3u) != M_TRACE) return;
+    float t = 0.0f;
+    int tri = -1;
+    if (P.has_geometry) tri = walk_closest(P.nodes, P.ltris, wld3(W, RO, i), wld3(W, RD, i), 1e30f, t, P.err);
+    wu(W, UTRI, i) = (uint32_t)tri;
+    wf(W, HT, i) = t;
+}
+
 // Per pixel: the slice's samples added in sample order to the running sums (rt_pt_cpu.cpp:
 // 132-141); after the last slice the means, the variances and the pixel-centre ray.
 struct PtOutDev {
@@ -740,7 +1106,7 @@ __global__ void __launch_bounds__(128) pt_accum_kernel(const PtParams P, const P
         for (int c = 0; c < 6; ++c) P.mom[(size_t)c * P.npix + px] = m[c];
         return;
     }
-    const float inv = P.spp ? fdiv(1.0f, (float)P.spp) : 0.0f;
+    const float inv = P.spp ? frcp((float)P.spp) : 0.0f;
     const size_t p = px;
     const v3 L = mk(a[0], a[1], a[2]), D = mk(a[3], a[4], a[5]), S = mk(a[6], a[7], a[8]), E = mk(a[9], a[10], a[11]);
     const v3 alb = mk(a[12], a[13], a[14]), nrm = mk(a[15], a[16], a[17]), da = mk(a[18], a[19], a[20]),
@@ -969,13 +1335,54 @@ int rn_pathtrace(const rn_ptscene* s, const rn_pt_desc* d, int flags, rn_pt_out*
         RN_TRY(ws_get(WS_PT_CTR, 8, &cp, st));
         ctr = (uint32_t*)cp;
     }
+    // the wavefront form's slots (pt_wave x 1024 at most)
+    WaveBufs W{};
+    if (c.tune.pt_wave) {
+        const unsigned long long most = (unsigned long long)tiles * 32ull * kn_max;
+        W.Q = (uint32_t)std::min<unsigned long long>(most, (unsigned long long)c.tune.pt_wave * 1024ull);
+        const size_t Q = W.Q;
+        size_t off = 0;
+        auto take = [&](size_t bytes) { const size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
+        const size_t o_f = take(wave::NF * Q * 4), o_u = take(wave::NU * Q * 4), o_vis = take(2 * Q);
+        const size_t o_qf = take(7 * 2 * Q * 4), o_qu = take(2 * Q * 4), o_ctr = take(16);
+        void* blk = nullptr;
+        RN_TRY(ws_get(WS_PT_WAVE, off, &blk, st));
+        char* b8 = (char*)blk;
+        W.f = (float*)(b8 + o_f); W.u = (uint32_t*)(b8 + o_u); W.vis = (uint8_t*)(b8 + o_vis);
+        W.qf = (float*)(b8 + o_qf); W.qu = (uint32_t*)(b8 + o_qu); W.ctr = (uint32_t*)(b8 + o_ctr);
+    }
     uint32_t k0 = 0;
     do {
         P.k0 = k0;
         P.kn = std::min(kn_max, d->spp - k0);
         P.first = k0 == 0;
         P.last = k0 + P.kn >= d->spp;
-        if (P.kn > 0 && c.tune.pt_regen) {
+        if (P.kn > 0 && c.tune.pt_wave) {
+            // every slot free, the counts at zero; then shade -> shadow rays -> closest hits
+            // until a shade pass leaves no live slot (read every 8 passes)
+            const unsigned long long total = (unsigned long long)tiles * 32ull * P.kn;
+            RN_CUDA(cudaMemsetAsync(W.u + (size_t)wave::UFL * W.Q, 0, (size_t)W.Q * 4, c.stream), st);
+            RN_CUDA(cudaMemsetAsync(W.ctr, 0, 16, c.stream), st);
+            const unsigned grid = (W.Q + 127) / 128, sgrid = (unsigned)c.sm_count * 8u;
+            const unsigned long long max_passes = (total / W.Q + 2) * ((unsigned long long)d->max_bounces + 3) + 64;
+            bool done = false;
+            for (unsigned long long pass = 0; !done; ++pass) {
+                if (pass > max_passes) return fail(st, RN_ERR_BUDGET, "path tracer: more than %llu passes", max_passes);
+                pt_wave_shade<<<grid, 128, 0, c.stream>>>(P, W, total);
+                if ((pass & 7) == 7) {
+                    uint32_t live = 0;
+                    RN_CUDA(cudaMemcpyAsync(&live, W.ctr + 1, 4, cudaMemcpyDeviceToHost, c.stream), st);
+                    RN_CUDA(cudaStreamSynchronize(c.stream), st);
+                    done = live == 0;
+                }
+                if (!done) {
+                    pt_wave_shadow<<<sgrid, 128, 0, c.stream>>>(P, W);
+                    pt_wave_extend<<<grid, 128, 0, c.stream>>>(P, W);
+                }
+                const cudaError_t le = cudaGetLastError();
+                if (le != cudaSuccess) return cuda_fail(st, le, "pt_wave kernels");
+            }
+        } else if (P.kn > 0 && c.tune.pt_regen) {
             RN_CUDA(cudaMemsetAsync(ctr, 0, 8, c.stream), st);
             pt_regen_kernel<<<c.sm_count * c.tune.pt_regen, 128, 0, c.stream>>>(P, ctr);
             const cudaError_t le = cudaGetLastError();

@@ -51,7 +51,7 @@ __device__ __forceinline__ ClipV lerp_v(const ClipV& a, const ClipV& b, float t)
 __device__ void setup_tri(const ClipV v[3], int w, int h, RasterTri& T) {
     T.minx = 1; T.maxx = 0; T.miny = 1; T.maxy = 0;
     for (int k = 0; k < 3; ++k) {
-        T.invw[k] = fdiv(1.0f, v[k].cs[3]);
+        T.invw[k] = frcp(v[k].cs[3]);
         const float nx = fmul(v[k].cs[0], T.invw[k]), ny = fmul(v[k].cs[1], T.invw[k]);
         T.sx[k] = fadd(fmul(fadd(fmul(nx, 0.5f), 0.5f), (float)w), 0.0f);
         T.sy[k] = fadd(fmul(fsub(1.0f, fadd(fmul(ny, 0.5f), 0.5f)), (float)h), 0.0f);

@@ -17,6 +17,9 @@ __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b)
 __device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+// 1 / a rounded once to nearest: the same value as fdiv(1.0f, a) (both are the correctly
+// rounded quotient), from the cheaper reciprocal intrinsic.
+__device__ __forceinline__ float frcp(float a) { return __frcp_rn(a); }
 // std::min / std::max on floats: (b < a) ? b : a and (a < b) ? b : a.
 __device__ __forceinline__ float smin(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float smax(float a, float b) { return (a < b) ? b : a; }
@@ -35,7 +38,7 @@ __device__ __forceinline__ v3 cross(v3 a, v3 b) {
 __device__ __forceinline__ float length(v3 v) { return fsqrt(dot(v, v)); }
 __device__ __forceinline__ v3 normalize(v3 v) {
     const float l = length(v);
-    return l > 0.0f ? scale(v, fdiv(1.0f, l)) : v;
+    return l > 0.0f ? scale(v, frcp(l)) : v;
 }
 __device__ __forceinline__ v3 load3(const float* p) { return mk(p[0], p[1], p[2]); }
 __device__ __forceinline__ void store3(float* p, const v3& v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
@@ -121,7 +124,7 @@ __device__ __forceinline__ WRay make_wray(v3 o, v3 d) {
     v3 q = wframe(d, r.kz, false);
     r.sw = q.z < 0.0f;
     if (r.sw) q = mk(q.y, q.x, q.z);
-    r.sx = fdiv(q.x, q.z); r.sy = fdiv(q.y, q.z); r.sz = fdiv(1.0f, q.z);
+    r.sx = fdiv(q.x, q.z); r.sy = fdiv(q.y, q.z); r.sz = frcp(q.z);
     return r;
 }
 
@@ -145,9 +148,9 @@ __device__ __forceinline__ bool hit_tri(const WRay& r, v3 a, v3 b, v3 c, float& 
     const float dm = dot(e1, p);
     if (dm > -1e-7f && dm < 1e-7f) {
         const float T = fadd(fadd(fmul(U, fmul(r.sz, A.z)), fmul(V, fmul(r.sz, B.z))), fmul(W, fmul(r.sz, C.z)));
-        t = fmul(T, fdiv(1.0f, det));
+        t = fmul(T, frcp(det));
     } else {
-        const float inv = fdiv(1.0f, dm);
+        const float inv = frcp(dm);
         const v3 q = cross(sub(r.o, a), e1);
         t = fmul(dot(e2, q), inv);
     }
@@ -173,11 +176,11 @@ __device__ __forceinline__ bool hit_tri_uv(const WRay& r, v3 a, v3 b, v3 c, floa
     const float dm = dot(e1, p);
     if (dm > -1e-7f && dm < 1e-7f) {
         const float T = fadd(fadd(fmul(U, fmul(r.sz, A.z)), fmul(V, fmul(r.sz, B.z))), fmul(W, fmul(r.sz, C.z)));
-        const float inv = fdiv(1.0f, det);
+        const float inv = frcp(det);
         t = fmul(T, inv); u = fmul(V, inv); v = fmul(W, inv);
         return t > 1e-4f;
     }
-    const float inv = fdiv(1.0f, dm);
+    const float inv = frcp(dm);
     const v3 tv = sub(r.o, a), q = cross(tv, e1);
     u = smax(0.0f, fmul(dot(tv, p), inv));
     v = smax(0.0f, fmul(dot(r.d, q), inv));

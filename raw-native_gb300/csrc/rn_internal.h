@@ -43,7 +43,7 @@ enum Slot {
     WS_SUR_AO4, WS_SUR_PRED, WS_SUR_FB, WS_SUR_AOFB, WS_SUR_STATS, WS_VPOS, WS_VNRM, WS_VDEPTH, WS_GTAO,
     WS_ALB_IN, WS_ALB, WS_MOTION, WS_FRAME, WS_HDR, WS_FRAME_SMALL, WS_MIRROR,
     WS_HYB_LIT, WS_HYB_TRI, WS_HYB_T, WS_HYB_NG, WS_CLOSEST_TRI, WS_CLOSEST_T,
-    WS_PT_SAMPLES, WS_PT_ACC, WS_PT_OUT, WS_PT_CTR, WS_PLOC, WS_COLLAPSE,
+    WS_PT_SAMPLES, WS_PT_ACC, WS_PT_OUT, WS_PT_CTR, WS_PT_WAVE, WS_PLOC, WS_COLLAPSE,
     WS_COUNT
 };
 
@@ -72,6 +72,7 @@ struct Tune {
     int collapse_block = 0;     // 4-wide collapse: trees of at most this many triangles in one block
     int trace_pool = 0;         // AO-only walks from a per-packet queue, lanes refilled below this many busy (0: off)
     int pt_regen = 4;           // path tracer: persistent threads regenerating paths, blocks of 128 per SM (0: one thread a sample)
+    int pt_wave = 1024;         // path tracer: the wavefront form over this many x 1024 path slots (0: off)
     int pt_slice = 0;           // path tracer: samples per slice at most (0: as many as 2 GiB of terms hold)
 };
 constexpr uint32_t kSmallScene = 1u << 16;

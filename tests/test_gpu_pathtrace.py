@@ -7,8 +7,9 @@ Parity is bit for bit:
 - on a seeded synthetic scene with emitters, metals, glossy and rough dielectrics and textures,
   every AOV equals the oracle's (rno_pathtrace, pinned to the reference by
   tests/test_oracle_pt.py), for several controls, several slice sizes (samples traced in
-  parallel and summed in sample order), both kernels (a thread a sample, or persistent
-  threads regenerating paths), device and host output pointers.
+  parallel and summed in sample order), every form (a thread a sample, persistent threads
+  regenerating paths, the wavefront form over 1,024 to 262,144 path slots), device and host
+  output pointers.
 
 Then the reference's own checks of its GPU path tracer (src/renderer/gpu/rt_pt_parity.cpp,
 src/renderer/rt_pt_checks.cpp), with its statistics and bounds:
@@ -53,11 +54,23 @@ def gpu_scene(rn, key):
     return _cache[key]
 
 
+@pytest.fixture
+def restore_pt_tune(rn):
+    old = {k: rn.tune_get(k) for k in ("pt_slice", "pt_regen", "pt_wave")}
+    yield
+    for k, v in old.items():
+        rn.tune_set(k, v)
+
+
+@pytest.mark.parametrize("wave", [0, 1, 256])
 @pytest.mark.parametrize("case", sorted(GOLD["cases"]))
-def test_gpu_equals_reference_outputs(rn, case):
+def test_gpu_equals_reference_outputs(rn, restore_pt_tune, case, wave):
+    """Every golden case with one kernel a path and in the wavefront form (1,024 slots, so
+    slots take many paths each; 262,144 slots)."""
     c = GOLD["cases"][case]
     s = gpu_scene(rn, c["scene"])
     assert s.info()["emitters"] == c["emitters"]
+    rn.tune_set("pt_wave", wave)
     out = rn.path_trace(s, c["desc"])
     bad = [k for k, h in c["sha256"].items() if sha(out[k]) != h]
     assert not bad, bad
@@ -68,25 +81,27 @@ def _synthetic():
     return importlib.import_module("test_oracle_pt").synthetic_scene(), importlib.import_module("test_oracle_pt").SYNTH_CAMERA
 
 
-@pytest.mark.parametrize("controls,slice_,regen", [([], 0, 0), ([], 0, 4), (["legacy_lobe_v2"], 1, 8),
-                                                   (["drop_lambert_cosine"], 4, 0),
-                                                   (["aov_emission_to_diffuse", "mis_weight_one"], 16, 16),
-                                                   (["aov_drop_specular_indirect"], 0, 4)])
-def test_gpu_equals_oracle_on_a_synthetic_scene(rn, oracle, controls, slice_, regen):
+@pytest.mark.parametrize("controls,slice_,regen,wave", [([], 0, 0, 0), ([], 0, 4, 0), (["legacy_lobe_v2"], 1, 8, 0),
+                                                        (["drop_lambert_cosine"], 4, 0, 0),
+                                                        (["aov_emission_to_diffuse", "mis_weight_one"], 16, 16, 0),
+                                                        (["aov_drop_specular_indirect"], 0, 4, 0),
+                                                        ([], 0, 0, 1), ([], 0, 0, 64), (["legacy_lobe_v2"], 1, 0, 1),
+                                                        (["drop_lambert_cosine"], 4, 0, 256),
+                                                        (["aov_emission_to_diffuse", "mis_weight_one"], 16, 0, 1),
+                                                        (["aov_drop_specular_indirect"], 0, 0, 1)])
+def test_gpu_equals_oracle_on_a_synthetic_scene(rn, oracle, restore_pt_tune, controls, slice_, regen, wave):
+    """The oracle's bytes with one kernel a path (a thread a sample, or regenerating threads)
+    and in the wavefront form (1,024 / 65,536 / 262,144 slots), over several slice sizes."""
     sc, cam = _synthetic()
     d = dict(seed=(11 << 32) | 3, spp=24, width=73, height=41, camera=cam, controls=controls,
              previous=(0.3, 2.4, 5.6, 0.0, 1.0, -1.0, 0.0, 1.0, 0.0, 1.1))
     ref = oracle.pathtrace(sc, d, threads=THREADS)
     s = rn.PtScene(sc)
     assert s.info()["emitters"] == ref["emitters"] == 2
-    old = (rn.tune_get("pt_slice"), rn.tune_get("pt_regen"))
     rn.tune_set("pt_slice", slice_)
     rn.tune_set("pt_regen", regen)
-    try:
-        out = rn.path_trace(s, d)
-    finally:
-        rn.tune_set("pt_slice", old[0])
-        rn.tune_set("pt_regen", old[1])
+    rn.tune_set("pt_wave", wave)
+    out = rn.path_trace(s, d)
     for k, _, _ in rn.PT_AOVS:
         assert np.array_equal(out[k], ref[k]), (k, int((out[k] != ref[k]).sum()))
 
