@@ -332,6 +332,8 @@ def run_ours(args):
                               "(the BVH is cache-resident), so frac is cache-served node bandwidth against the "
                               "HBM peak; dram_frac is the HBM share actually used, issue_active the binding limit's "
                               "fraction",
+                     "binding_limit": "instruction issue (ncu smsp__issue_active of the same kernel)",
+                     "binding_frac": prof.get("issue_active"),
                      "dram_frac": (traffic / (trace_ms * 1e-3) / 1e9 / peak) if traffic else None,
                      "issue_active": prof.get("issue_active"), "simt_efficiency": prof.get("simt_efficiency"),
                      "profile_source": prof.get("source"),

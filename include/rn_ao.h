@@ -358,8 +358,11 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *                                    four slab tests, in one loop
  *   conv_tmem_a       0 | 1          row-ring convolutions with at most 32 input and 32 output
  *                                    channels keep each input row's A operands in TMEM
- *   ploc_tail         0|4096|32768|262144  accelerator builds: the PLOC rounds from this many
- *                                    clusters on run in one block (0: a launch per step)
+ *   ploc_tail         0|4096|16384|32768|65536|262144  accelerator builds: the PLOC rounds
+ *                                    from this many clusters on run in one launch (0: a launch
+ *                                    per step)
+ *   ploc_tail_ctas    1|4|8|16       ... in one block of 1024 threads (1) or one thread-block
+ *                                    cluster of this many such blocks
  *   collapse_block    0|16384|65536|262144  accelerator builds of at most this many triangles
  *                                    collapse to 4-wide nodes in one block (0: a launch per level)
  *   trace_pool        0|16|24|32     AO-only walks: one queue of a packet's walks, idle lanes
@@ -367,6 +370,8 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *   pt_wave           0|1|64|256|1024|2048  rn_pathtrace: the wavefront form (a bounce as shade, shadow-ray
  *                                    and closest-hit kernels over this many x 1024 path slots;
  *                                    0: one kernel a path, below)
+ *   pt_shade_blocks   4|6|8          rn_pathtrace: the wavefront shade kernel's resident
+ *                                    128-thread blocks per SM (its register budget)
  *   pt_regen          0|4|8|16       rn_pathtrace: persistent threads that start a new path when
  *                                    theirs ends, this many 128-thread blocks per SM (0: a thread a sample)
  *   pt_slice          0|1|4|16       rn_pathtrace: samples traced per slice at most (0: as many

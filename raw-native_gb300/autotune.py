@@ -38,7 +38,7 @@ Workloads:
                  soup (the cluster count from which the PLOC rounds run in one block; then the
                  size under which the collapse runs in one block)
   pt             the path tracer on retro_room and iso_street at 1280 x 720, 16 spp (pt_regen,
-                 pt_wave)
+                 pt_wave, pt_shade_blocks)
 The traversal keys are searched jointly (every combination); the others one at a time.
 """
 from __future__ import annotations
@@ -417,23 +417,30 @@ def tune_ploc_tail(quick: bool, reps: int, log):
     inputs = [("build/744k", scenes.build_synthetic_scene(1, 500 if quick else 2000, 100 if quick else 500).tris),
               ("build/soup", soup), ("build/20k", scenes.soup(20000, 7))]
     inputs = [(name, torch.from_numpy(np.ascontiguousarray(t)).cuda()) for name, t in inputs]
-    current = rn.tune_get("ploc_tail")
+    current = {"ploc_tail": rn.tune_get("ploc_tail"), "ploc_tail_ctas": rn.tune_get("ploc_tail_ctas")}
     rows, ref = [], None
-    for v in rn.TUNE_KEYS["ploc_tail"]:
-        rn.tune_set("ploc_tail", v)
-        trees = [rn.build_ploc(t)[0].cpu() for _, t in inputs]
+    for tail, ctas in itertools.product(rn.TUNE_KEYS["ploc_tail"], rn.TUNE_KEYS["ploc_tail_ctas"]):
+        if tail == 0 and ctas != 1:
+            continue                                   # no tail: the CTA count is unused
+        cfg = {"ploc_tail": tail, "ploc_tail_ctas": ctas}
+        _apply(cfg)
+        try:
+            trees = [rn.build_ploc(t)[0].cpu() for _, t in inputs]
+        except rn.RnError as e:                        # a cluster this device cannot schedule
+            log("%s  not launchable: %s" % (cfg, e))
+            continue
         if ref is None:
             ref = trees
         elif not all(bool((a == b).all()) for a, b in zip(trees, ref)):
-            raise RuntimeError("ploc_tail %d changed a tree" % v)
+            raise RuntimeError("%s changed a tree" % cfg)
         ms = {name: _time(lambda t=t: rn.LinearAccel(t).close(), reps) for name, t in inputs}
-        rows.append(dict(cfg={"ploc_tail": v}, ms=ms))
-        log("ploc_tail %d  %s" % (v, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
-    base = next(r for r in rows if r["cfg"]["ploc_tail"] == current)["ms"]
+        rows.append(dict(cfg=cfg, ms=ms))
+        log("%s  %s" % (cfg, "  ".join("%s %.3f ms" % kv for kv in ms.items())))
+    base = next(r for r in rows if r["cfg"] == current)["ms"]
     for r in rows:
         r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
     best = min(rows, key=lambda r: r["score"])
-    rn.tune_set("ploc_tail", best["cfg"]["ploc_tail"])
+    _apply(best["cfg"])
     # then the size under which the collapse runs in one block (same node counts required)
     current = rn.tune_get("collapse_block")
     rows2, ref2 = [], None
@@ -458,7 +465,7 @@ def tune_ploc_tail(quick: bool, reps: int, log):
 def tune_pt(quick: bool, reps: int, log):
     """The path tracer's form: one kernel a path (a thread a sample, or persistent threads
     regenerating paths: 4, 8, 16 blocks per SM) or the wavefront form over 64K to 2M path
-    slots: retro_room and iso_street (the reference's lit scenes, from the test fixtures) at
+    slots, and the wavefront shade kernel's register budget: retro_room and iso_street (the reference's lit scenes, from the test fixtures) at
     1280 x 720, 16 spp, every candidate's radiance, variance and diffuse checked bit for bit."""
     import os
     z = np.load(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden",
@@ -470,11 +477,16 @@ def tune_pt(quick: bool, reps: int, log):
         s = rn.PtScene(sc)
         d = dict(seed=1, spp=4 if quick else 16, width=320 if quick else 1280, height=180 if quick else 720, camera=cam)
         wls.append(("pt/" + key, s, d))
-    current = {"pt_wave": rn.tune_get("pt_wave"), "pt_regen": rn.tune_get("pt_regen")}
-    cands = [{"pt_wave": 0, "pt_regen": v} for v in rn.TUNE_KEYS["pt_regen"]]
-    cands += [{"pt_wave": v, "pt_regen": current["pt_regen"]} for v in rn.TUNE_KEYS["pt_wave"] if v >= 64]
-    if current not in cands:
-        cands.append(dict(current))
+    keys = ("pt_wave", "pt_regen", "pt_shade_blocks")
+    current = {k: rn.tune_get(k) for k in keys}
+    cands = [dict(current, pt_wave=0, pt_regen=v) for v in rn.TUNE_KEYS["pt_regen"]]
+    cands += [dict(current, pt_wave=v) for v in rn.TUNE_KEYS["pt_wave"] if v >= 64]
+    cands += [dict(current, pt_shade_blocks=v) for v in rn.TUNE_KEYS["pt_shade_blocks"]]
+    uniq = []
+    for c in cands + [dict(current)]:
+        if c not in uniq:
+            uniq.append(c)
+    cands = uniq
     rows, ref = [], None
     for cfg in cands:
         _apply(cfg)

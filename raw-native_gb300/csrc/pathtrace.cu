@@ -941,7 +941,9 @@ __device__ __noinline__ uint32_t wave_bounce(const PtParams& P, const WaveBufs& 
     return M_TRACE;
 }
 
-__global__ void __launch_bounds__(128) pt_wave_shade(const PtParams P, const WaveBufs W, unsigned long long total) {
+template <int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) pt_wave_shade(const PtParams P, const WaveBufs W,
+                                                                 unsigned long long total) {
     using namespace wave;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31u;
@@ -1368,7 +1370,11 @@ int rn_pathtrace(const rn_ptscene* s, const rn_pt_desc* d, int flags, rn_pt_out*
             bool done = false;
             for (unsigned long long pass = 0; !done; ++pass) {
                 if (pass > max_passes) return fail(st, RN_ERR_BUDGET, "path tracer: more than %llu passes", max_passes);
-                pt_wave_shade<<<grid, 128, 0, c.stream>>>(P, W, total);
+                switch (c.tune.pt_shade_blocks) {   // resident blocks per SM: a register budget
+                    case 6: pt_wave_shade<6><<<grid, 128, 0, c.stream>>>(P, W, total); break;
+                    case 8: pt_wave_shade<8><<<grid, 128, 0, c.stream>>>(P, W, total); break;
+                    default: pt_wave_shade<4><<<grid, 128, 0, c.stream>>>(P, W, total); break;
+                }
                 if ((pass & 7) == 7) {
                     uint32_t live = 0;
                     RN_CUDA(cudaMemcpyAsync(&live, W.ctr + 1, 4, cudaMemcpyDeviceToHost, c.stream), st);

@@ -17,12 +17,14 @@
 //      contiguously (48-byte records).
 #include "rn_internal.h"
 #include "rn_device.cuh"
+#include <cooperative_groups.h>
 #include <cfloat>
 #include <cstring>
 #include <vector>
 
 namespace rn {
 namespace {
+namespace cg = cooperative_groups;
 
 constexpr int kThreads = 256;
 constexpr int kItems = 8;
@@ -248,7 +250,7 @@ struct RoundState {
     uint32_t m_next;     // survivors after this round (written by the top scan)
     uint32_t merges;     // merges in this round
     uint32_t error;      // DEV_PLOC_NO_MERGE when a round merged nothing
-    uint32_t pad;
+    int32_t root;        // the last cluster, written by the tail kernels when one is left
 };
 
 // rt_bvh.cpp:104-110: 2 (dy (dx + dz) + dz dx), operation for operation.
@@ -516,9 +518,171 @@ __global__ void __launch_bounds__(kTailThreads) ploc_tail(RoundState* st, int32_
     }
     if (tid == 0) {
         st->m = s_m; st->next = s_next; st->parity = s_parity; st->rounds = s_rounds;
+        st->root = s_m == 1 ? (s_parity ? cl1 : cl0)[0] : -1;
         if (s_error) st->error |= s_error;
         else if (s_m > 1) st->error |= DEV_GUARD;
     }
+}
+
+// The remaining rounds in one thread-block cluster of C CTAs (C x 1024 threads on C SMs),
+// for more clusters than one block takes well: ploc_tail's rounds with the steps separated by
+// cluster barriers (barrier.cluster, release/acquire: each step's global writes are seen by
+// every CTA of the cluster after it), the CTAs' flag totals exchanged through distributed
+// shared memory, and the round state kept, identical, in every CTA's shared memory. Global
+// thread g = rank x 1024 + tid takes a contiguous run of positions, so the prefix sum still
+// runs in position order and node ids, cluster order and boxes are ploc_nn / ploc_scatter's
+// exactly. Data another CTA wrote in this launch is read through L2 (ld.global.cg).
+template <int C>
+__global__ void __launch_bounds__(kTailThreads) ploc_tail_cluster(RoundState* st, int32_t* __restrict__ cl0,
+                                                                  int32_t* __restrict__ cl1, float* __restrict__ cb0,
+                                                                  float* __restrict__ cb1, int32_t* __restrict__ nn,
+                                                                  float* __restrict__ box, int32_t* __restrict__ left,
+                                                                  int32_t* __restrict__ right, int R,
+                                                                  uint32_t max_rounds) {
+    cg::cluster_group cluster = cg::this_cluster();
+    __shared__ uint32_t s_m, s_next, s_parity, s_rounds, s_error;
+    __shared__ unsigned long long warp_tot[kTailThreads / 32];
+    __shared__ unsigned long long s_cta_tot;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t rank = cluster.block_rank();
+    const uint32_t g = rank * kTailThreads + (uint32_t)tid, G = (uint32_t)C * kTailThreads;
+    if (tid == 0) {
+        s_m = __ldcg(&st->m); s_next = __ldcg(&st->next); s_parity = __ldcg(&st->parity);
+        s_rounds = __ldcg(&st->rounds); s_error = 0;
+    }
+    __syncthreads();
+    for (uint32_t guard = 0; guard < max_rounds; ++guard) {
+        const uint32_t m = s_m;
+        if (m <= 1 || s_error) break;            // the same in every CTA
+        const bool p = s_parity != 0;
+        const float* cb = p ? cb1 : cb0;
+        float* cbo = p ? cb0 : cb1;
+        const int32_t* cl = p ? cl1 : cl0;
+        int32_t* clo = p ? cl0 : cl1;
+        // nearest neighbours (ploc_nn_any)
+        for (uint32_t i = g; i < m; i += G) {
+            const float* A = cb + (size_t)i * 6;
+            const float a0 = __ldcg(A), a1 = __ldcg(A + 1), a2 = __ldcg(A + 2), a3 = __ldcg(A + 3), a4 = __ldcg(A + 4),
+                        a5 = __ldcg(A + 5);
+            const int ii = (int)i;
+            const int j0 = ii - R > 0 ? ii - R : 0, j1 = ii + R < (int)m - 1 ? ii + R : (int)m - 1;
+            float best = FLT_MAX;
+            int arg = -1;
+            for (int j = j0; j <= j1; ++j) {
+                if (j == ii) continue;
+                const float* B = cb + (size_t)j * 6;
+                const float d = ploc_area(smin(a0, __ldcg(B)), smin(a1, __ldcg(B + 1)), smin(a2, __ldcg(B + 2)),
+                                          smax(a3, __ldcg(B + 3)), smax(a4, __ldcg(B + 4)), smax(a5, __ldcg(B + 5)));
+                if (d < best) { best = d; arg = j; }
+            }
+            nn[i] = arg;
+        }
+        cluster.sync();
+        // flags of this thread's run of positions, then their prefix sum in position order:
+        // within the CTA by warp shuffles, across the CTAs by their totals
+        const uint32_t chunk = (m + G - 1) / G;
+        const uint32_t b0 = min(m, g * chunk), b1 = min(m, b0 + chunk);
+        unsigned long long s = 0;
+        for (uint32_t i = b0; i < b1; ++i) {
+            const int32_t j = __ldcg(nn + i);
+            const bool mutual = j >= 0 && __ldcg(nn + j) == (int32_t)i;
+            const uint32_t o = (!mutual || (int32_t)i < j) ? 1u : 0u, gm = (mutual && (int32_t)i < j) ? 1u : 0u;
+            s += (unsigned long long)o | ((unsigned long long)gm << 32);
+        }
+        unsigned long long x = s;
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            unsigned long long w = warp_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_tot[lane] = w;
+            if (lane == 31) s_cta_tot = w;
+        }
+        cluster.sync();
+        unsigned long long before = 0, total = 0;
+        for (uint32_t r = 0; r < (uint32_t)C; ++r) {
+            const unsigned long long v = *cluster.map_shared_rank(&s_cta_tot, r);
+            if (r < rank) before += v;
+            total += v;
+        }
+        const uint32_t merges = (uint32_t)(total >> 32);
+        if (merges == 0) {
+            if (tid == 0) s_error = DEV_PLOC_NO_MERGE;
+            __syncthreads();
+            break;
+        }
+        unsigned long long run = before + (warp == 0 ? 0ull : warp_tot[warp - 1]) + x - s;
+        const uint32_t next = s_next;
+        for (uint32_t i = b0; i < b1; ++i) {
+            const int32_t j = __ldcg(nn + i);
+            const bool mutual = j >= 0 && __ldcg(nn + j) == (int32_t)i;
+            const uint32_t o = (!mutual || (int32_t)i < j) ? 1u : 0u, gm = (mutual && (int32_t)i < j) ? 1u : 0u;
+            if (o) {
+                const uint32_t pos = (uint32_t)(run & 0xFFFFFFFFull);
+                if (gm) {
+                    const uint32_t id = next + (uint32_t)(run >> 32);
+                    const float* A = cb + (size_t)i * 6;
+                    const float* B = cb + (size_t)j * 6;
+                    float nb6[6];
+                    for (int a = 0; a < 3; ++a) {
+                        nb6[a] = smin(__ldcg(A + a), __ldcg(B + a));
+                        nb6[3 + a] = smax(__ldcg(A + 3 + a), __ldcg(B + 3 + a));
+                    }
+                    for (int a = 0; a < 6; ++a) { box[(size_t)id * 6 + a] = nb6[a]; cbo[(size_t)pos * 6 + a] = nb6[a]; }
+                    left[id] = __ldcg(cl + i);
+                    right[id] = __ldcg(cl + j);
+                    clo[pos] = (int32_t)id;
+                } else {
+                    for (int a = 0; a < 6; ++a) cbo[(size_t)pos * 6 + a] = __ldcg(cb + (size_t)i * 6 + a);
+                    clo[pos] = __ldcg(cl + i);
+                }
+            }
+            run += (unsigned long long)o | ((unsigned long long)gm << 32);
+        }
+        __syncthreads();
+        if (tid == 0) {
+            s_next = next + merges;
+            s_m = (uint32_t)(total & 0xFFFFFFFFull);
+            s_parity ^= 1u;
+            s_rounds += 1;
+        }
+        cluster.sync();
+    }
+    cluster.sync();                              // no CTA leaves while another reads its shared memory
+    if (rank == 0 && tid == 0) {
+        st->m = s_m; st->next = s_next; st->parity = s_parity; st->rounds = s_rounds;
+        st->root = s_m == 1 ? __ldcg((s_parity ? cl1 : cl0)) : -1;
+        if (s_error) st->error |= s_error;
+        else if (s_m > 1) st->error |= DEV_GUARD;
+    }
+}
+
+template <int C>
+cudaError_t launch_tail_cluster(cudaStream_t s, RoundState* st, int32_t* cl0, int32_t* cl1, float* cb0, float* cb1,
+                                int32_t* nn, float* box, int32_t* left, int32_t* right, int R, uint32_t max_rounds) {
+    if (C > 8) {
+        const cudaError_t e = cudaFuncSetAttribute(ploc_tail_cluster<C>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess) return e;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(kTailThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, ploc_tail_cluster<C>, st, cl0, cl1, cb0, cb1, nn, box, left, right, R, max_rounds);
 }
 
 __global__ void ploc_commit(RoundState* st) {
@@ -844,18 +1008,34 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
     RoundState init{};
     init.m = n;
     init.next = n;
+    init.root = -1;
     RN_CUDA(cudaMemcpyAsync(state, &init, sizeof init, cudaMemcpyHostToDevice, s), st);
     // 5: rounds, in batches; the host reads the state once per batch
     uint32_t m_known = n;
     RoundState hs = init;
     const int kBatch = 6;
     const uint32_t tail_max = (uint32_t)ctx().tune.ploc_tail;
+    int32_t tail_root = -1;
     for (int batch = 0; m_known > 1; ++batch) {
         if (batch > 2000) return fail(st, RN_ERR_BUDGET, "PLOC: more than %d rounds", batch * kBatch);
         if (m_known <= tail_max) {
-            // the last rounds in one block (at most one round per cluster: each merges one pair or more)
-            ploc_tail<<<1, kTailThreads, 0, s>>>(state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right,
-                                                 radius, m_known + 1);
+            // the last rounds in one block or one cluster of blocks (at most one round per
+            // cluster: each merges one pair or more)
+            const int ctas = ctx().tune.ploc_tail_ctas;
+            cudaError_t le = cudaSuccess;
+            if (ctas == 16)
+                le = launch_tail_cluster<16>(s, state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right, radius,
+                                             m_known + 1);
+            else if (ctas == 8)
+                le = launch_tail_cluster<8>(s, state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right, radius,
+                                            m_known + 1);
+            else if (ctas == 4)
+                le = launch_tail_cluster<4>(s, state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right, radius,
+                                            m_known + 1);
+            else
+                ploc_tail<<<1, kTailThreads, 0, s>>>(state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right,
+                                                     radius, m_known + 1);
+            RN_CUDA(le, st);
             RN_CUDA(cudaGetLastError(), st);
             RN_CUDA(cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, s), st);
             RN_CUDA(cudaStreamSynchronize(s), st);
@@ -863,6 +1043,7 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
                 return fail(st, RN_ERR_STATE, "PLOC round %u made no merge (%u clusters)", hs.rounds, hs.m);
             if (hs.error & DEV_GUARD) return fail(st, RN_ERR_BUDGET, "PLOC: rounds left %u clusters", hs.m);
             m_known = hs.m;
+            tail_root = hs.root;
             break;
         }
         const uint32_t nbn = cdiv(m_known, kThreads), nbc = cdiv(m_known, kTile);
@@ -890,9 +1071,11 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
     }
     if (hs.next != 2 * n - 1)
         return fail(st, RN_ERR_STATE, "PLOC made %u nodes, expected %u", hs.next, 2 * n - 1);
-    int32_t root = 0;
-    RN_CUDA(cudaMemcpyAsync(&root, hs.parity ? cl1 : cl0, 4, cudaMemcpyDeviceToHost, s), st);
-    RN_CUDA(cudaStreamSynchronize(s), st);
+    int32_t root = tail_root;                // the tail kernels leave the root in the state
+    if (root < 0) {
+        RN_CUDA(cudaMemcpyAsync(&root, hs.parity ? cl1 : cl0, 4, cudaMemcpyDeviceToHost, s), st);
+        RN_CUDA(cudaStreamSynchronize(s), st);
+    }
     out->root = root;
     out->rounds = hs.rounds;
     return ok(st);

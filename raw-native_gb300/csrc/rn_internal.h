@@ -68,11 +68,13 @@ struct Tune {
     int hybrid_min_blocks = 6;  // resident 128-thread hybrid-pass blocks per SM: 5, 6 or 8
     int trace_leaf_pass = 1;    // traversal: a node's leaf children tested in one loop after its slab tests
     int conv_tmem_a = 0;        // row-ring convolutions of 32 -> 32 or 16 -> 32 channels: A operands kept in TMEM
-    int ploc_tail = 4096;       // PLOC: the rounds from this many clusters on run in one block (0: never)
+    int ploc_tail = 4096;       // PLOC: the rounds from this many clusters on run in one launch (0: never)
+    int ploc_tail_ctas = 1;     // ... in one block (1) or one thread-block cluster of this many CTAs
     int collapse_block = 0;     // 4-wide collapse: trees of at most this many triangles in one block
     int trace_pool = 0;         // AO-only walks from a per-packet queue, lanes refilled below this many busy (0: off)
     int pt_regen = 4;           // path tracer: persistent threads regenerating paths, blocks of 128 per SM (0: one thread a sample)
     int pt_wave = 1024;         // path tracer: the wavefront form over this many x 1024 path slots (0: off)
+    int pt_shade_blocks = 4;    // ... its shade kernel's resident blocks of 128 per SM (register budget)
     int pt_slice = 0;           // path tracer: samples per slice at most (0: as many as 2 GiB of terms hold)
 };
 constexpr uint32_t kSmallScene = 1u << 16;

@@ -193,8 +193,9 @@ TUNE_KEYS = {"trace_min_blocks": (2, 3, 4), "batch_min_blocks": (2, 3, 4), "trac
              "trace_stack": (48, 96), "ssao_tile_h": (4, 8, 16), "conv_bn_max": (64, 128, 256), "conv_halo": (0, 1), "conv_pair": (0, 1),
              "accel_radius": (8, 16, 32, 64), "accel_leaf": (1, 2, 4, 8), "accel_leaf_small": (1, 2, 4, 8),
              "frame_direct": (0, 1), "hybrid_min_blocks": (5, 6, 8), "pt_slice": (0, 1, 4, 16), "pt_regen": (0, 4, 8, 16),
-             "pt_wave": (0, 1, 64, 256, 1024, 2048),
-             "trace_pool": (0, 16, 24, 32), "ploc_tail": (0, 4096, 32768, 262144),
+             "pt_wave": (0, 1, 64, 256, 1024, 2048), "pt_shade_blocks": (4, 6, 8),
+             "trace_pool": (0, 16, 24, 32), "ploc_tail": (0, 4096, 16384, 32768, 65536, 262144),
+             "ploc_tail_ctas": (1, 4, 8, 16),
              "collapse_block": (0, 16384, 65536, 262144),
              "conv_tmem_a": (0, 1), "trace_leaf_pass": (0, 1)}
 

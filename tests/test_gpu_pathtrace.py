@@ -106,6 +106,24 @@ def test_gpu_equals_oracle_on_a_synthetic_scene(rn, oracle, restore_pt_tune, con
         assert np.array_equal(out[k], ref[k]), (k, int((out[k] != ref[k]).sum()))
 
 
+@pytest.mark.parametrize("blocks", [6, 8])
+def test_wave_shade_register_budget_keeps_every_bit(rn, oracle, restore_pt_tune, blocks):
+    """The wavefront shade kernel built for 6 or 8 resident blocks (fewer registers) gives the
+    oracle's bytes."""
+    sc, cam = _synthetic()
+    d = dict(seed=7, spp=16, width=57, height=33, camera=cam, controls=["aov_emission_to_diffuse"])
+    ref = oracle.pathtrace(sc, d, threads=THREADS)
+    rn.tune_set("pt_wave", 1)
+    old = rn.tune_get("pt_shade_blocks")
+    rn.tune_set("pt_shade_blocks", blocks)
+    try:
+        out = rn.path_trace(rn.PtScene(sc), d)
+    finally:
+        rn.tune_set("pt_shade_blocks", old)
+    for k, _, _ in rn.PT_AOVS:
+        assert np.array_equal(out[k], ref[k]), (k, int((out[k] != ref[k]).sum()))
+
+
 def test_gpu_device_pointers_equal_host_pointers(rn):
     import torch
     c = GOLD["cases"]["retro_room_motion_nojitter"]

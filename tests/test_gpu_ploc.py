@@ -42,13 +42,16 @@ def test_ploc_equals_oracle(rn, oracle, n, seed):
     assert np.array_equal(nodes, rn_nodes), int((nodes != rn_nodes).any(axis=1).sum())
 
 
-@pytest.mark.parametrize("tail", [4096, 32768, 262144])
+@pytest.mark.parametrize("tail,ctas", [(4096, 1), (32768, 1), (262144, 1), (4096, 4), (65536, 8), (262144, 8),
+                                       (262144, 16)])
 @pytest.mark.parametrize("n,seed,radius", [(2, 2, 16), (17, 5, 16), (4097, 7, 16), (65536, 8, 16), (300001, 9, 16),
                                            (20000, 7, 8), (5000, 12, 32)])
-def test_ploc_tail_in_one_block_equals_oracle(rn, oracle, tail, n, seed, radius):
-    """The last rounds in one block (ploc_tail) build the same tree, node for node."""
-    old = rn.tune_get("ploc_tail")
+def test_ploc_tail_in_one_launch_equals_oracle(rn, oracle, tail, ctas, n, seed, radius):
+    """The last rounds in one block or one thread-block cluster (ploc_tail, ploc_tail_ctas)
+    build the same tree, node for node."""
+    old = rn.tune_get("ploc_tail"), rn.tune_get("ploc_tail_ctas")
     rn.tune_set("ploc_tail", tail)
+    rn.tune_set("ploc_tail_ctas", ctas)
     try:
         tris = oracle.soup(n, seed)
         nodes, root, rounds = rn.build_ploc(tris, radius)
@@ -56,7 +59,8 @@ def test_ploc_tail_in_one_block_equals_oracle(rn, oracle, tail, n, seed, radius)
         assert root == rroot and rounds == rrounds
         assert np.array_equal(nodes, rn_nodes), int((nodes != rn_nodes).any(axis=1).sum())
     finally:
-        rn.tune_set("ploc_tail", old)
+        rn.tune_set("ploc_tail", old[0])
+        rn.tune_set("ploc_tail_ctas", old[1])
 
 
 def test_ploc_radius_8_differs(rn, oracle):
