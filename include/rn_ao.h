@@ -367,6 +367,8 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *                                    collapse to 4-wide nodes in one block (0: a launch per level)
  *   trace_pool        0|16|24|32     AO-only walks: one queue of a packet's walks, idle lanes
  *                                    refilled when fewer than this many walk (0: one pixel per lane)
+ *   trace_pool_sort   0 | 1          ... the queue ordered by the walks' direction octant (at most
+ *                                    16 spp)
  *   pt_wave           0|1|64|256|1024|2048  rn_pathtrace: the wavefront form (a bounce as shade, shadow-ray
  *                                    and closest-hit kernels over this many x 1024 path slots;
  *                                    0: one kernel a path, below)

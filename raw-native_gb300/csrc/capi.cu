@@ -137,6 +137,7 @@ const TuneKey kTuneKeys[] = {
     {"collapse_block", "RN_TUNE_COLLAPSE_BLOCK", &Tune::collapse_block, {0, 16384, 65536, 262144}, 4},
     {"conv_tmem_a", "RN_TUNE_CONV_TMEM_A", &Tune::conv_tmem_a, {0, 1}, 2},
     {"trace_leaf_pass", "RN_TUNE_TRACE_LEAF_PASS", &Tune::trace_leaf_pass, {0, 1}, 2},
+    {"trace_pool_sort", "RN_TUNE_TRACE_POOL_SORT", &Tune::trace_pool_sort, {0, 1}, 2},
 };
 
 const TuneKey* find_tune_key(const char* name) {
@@ -240,6 +241,15 @@ int ensure_ctx(rn_status* st) {
     c.stream = c.own_stream;
     RN_CUDA(cudaMalloc((void**)&c.dev_error, 64), st);
     RN_CUDA(cudaMemsetAsync(c.dev_error, 0, 64, c.stream), st);
+    // the library's own pool for accelerators (rebuilt per scene, often per frame): a freed
+    // accelerator's memory stays mapped for the next build instead of going back to the driver
+    cudaMemPoolProps pp = {};
+    pp.allocType = cudaMemAllocationTypePinned;
+    pp.location.type = cudaMemLocationTypeDevice;
+    pp.location.id = dev;
+    RN_CUDA(cudaMemPoolCreate(&c.accel_pool, &pp), st);
+    uint64_t keep = (uint64_t)4 << 30;
+    RN_CUDA(cudaMemPoolSetAttribute(c.accel_pool, cudaMemPoolAttrReleaseThreshold, &keep), st);
     RN_TRY(build_trig_correction(c, st));
     c.ready = true;
     return RN_OK;
@@ -611,7 +621,12 @@ int rn_accel_build(const float* tris, uint32_t ntri, int flags, rn_accel** out, 
 
 void rn_accel_free(rn_accel* accel) {
     if (!accel) return;
-    if (accel->d_nodes) cudaFree(accel->d_nodes);      // d_tris lies in the same allocation
+    if (accel->d_nodes) {
+        // d_tris lies in the same block. Any stream may still be reading it: wait for the
+        // device (as cudaFree would), then hand the block back to the library's pool.
+        cudaDeviceSynchronize();
+        cudaFreeAsync(accel->d_nodes, ctx().stream);
+    }
     delete accel;
 }
 

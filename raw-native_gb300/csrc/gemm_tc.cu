@@ -690,8 +690,11 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     } else if (warp == 1) {
         if (lane == 0) {
             const uint32_t idesc = instr_desc(BN);
-            const uint32_t b0 = smem_u32(sB);
             const int q16 = a.cin / 16, g_tap = a.cin / 8;
+            const uint64_t db0 = desc_plain(smem_u32(sB), BN * 16, 128);
+            const uint64_t dq_a = (2u * kHaloGroup) >> 4;                 // the next 16 channels of A
+            const uint64_t dq_b = (2u * BN * 16u) >> 4;                   // ... of B
+            const uint64_t dtap_b = ((uint32_t)g_tap * BN * 16u) >> 4;    // the next tap of B
             bool ok = mbar_wait_or_abort(wbar, 0, abort_flag);
             uint32_t base = 0, i = 0;   // ring index of the item's first load; output rows so far
             for (int item = blockIdx.x; ok && item < a.items && !*abort_flag; item += gridDim.x) {
@@ -709,13 +712,24 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                     if (!ok) break;
                     tc_fence_after();
                     const uint32_t acc = tmem + buf * BN;
+                    // a descriptor is affine in its address (the 14-bit field holds address / 16
+                    // and no offset here carries out of it): each MMA's operands are the row's or
+                    // the weights' base descriptor plus a constant, so the issuing thread spends
+                    // a few instructions per MMA instead of forming two descriptors
+                    const uint64_t da_row[3] = {desc_plain(row_addr[0], kHaloGroup, 128),
+                                                desc_plain(row_addr[1], kHaloGroup, 128),
+                                                desc_plain(row_addr[2], kHaloGroup, 128)};
+                    uint64_t db_tap = db0;
+#pragma unroll
                     for (int t = 0; t < 9; ++t) {
-                        const uint32_t a_tap = row_addr[t / 3] + (uint32_t)(t % 3) * 16u;
+                        uint64_t da = da_row[t / 3] + (uint64_t)(t % 3);        // one pixel: 16 bytes
+                        uint64_t db = db_tap;
                         for (int q = 0; q < q16; ++q) {
-                            const uint64_t da = desc_plain(a_tap + (uint32_t)(2 * q) * kHaloGroup, kHaloGroup, 128);
-                            const uint64_t db = desc_plain(b0 + (uint32_t)(t * g_tap + 2 * q) * (BN * 16), BN * 16, 128);
                             tc_mma(acc, da, db, idesc, (t | q) != 0 ? 1u : 0u);
+                            da += dq_a;
+                            db += dq_b;
                         }
+                        db_tap += dtap_b;
                     }
                     tc_commit(acc_full(buf));
                     // load j (input row y0 + j - 1) has no later reader

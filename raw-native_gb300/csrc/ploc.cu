@@ -1103,7 +1103,7 @@ int collapse_bvh4(const PlocTree& t, const float* d_tris, rn_accel* acc, int lea
     // the accelerator's nodes and leaf triangles in one allocation (rn_accel_free frees d_nodes)
     const size_t node_bytes = ((size_t)node_cap * sizeof(Node4) + 255) & ~size_t(255);
     char* block = nullptr;
-    RN_CUDA(cudaMalloc((void**)&block, node_bytes + (size_t)n * sizeof(LeafTri)), st);
+    RN_CUDA(cudaMallocFromPoolAsync((void**)&block, node_bytes + (size_t)n * sizeof(LeafTri), ctx().accel_pool, s), st);
     acc->d_nodes = (Node4*)block;
     acc->d_tris = (LeafTri*)(block + node_bytes);
     size_t off = 0;

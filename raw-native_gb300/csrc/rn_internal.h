@@ -72,9 +72,10 @@ struct Tune {
     int ploc_tail_ctas = 1;     // ... in one block (1) or one thread-block cluster of this many CTAs
     int collapse_block = 0;     // 4-wide collapse: trees of at most this many triangles in one block
     int trace_pool = 0;         // AO-only walks from a per-packet queue, lanes refilled below this many busy (0: off)
+    int trace_pool_sort = 0;    // ... the queue ordered by the walks' direction octant (at most 16 spp)
     int pt_regen = 4;           // path tracer: persistent threads regenerating paths, blocks of 128 per SM (0: one thread a sample)
     int pt_wave = 1024;         // path tracer: the wavefront form over this many x 1024 path slots (0: off)
-    int pt_shade_blocks = 4;    // ... its shade kernel's resident blocks of 128 per SM (register budget)
+    int pt_shade_blocks = 6;    // ... its shade kernel's resident blocks of 128 per SM (register budget)
     int pt_slice = 0;           // path tracer: samples per slice at most (0: as many as 2 GiB of terms hold)
 };
 constexpr uint32_t kSmallScene = 1u << 16;
@@ -88,6 +89,7 @@ struct Context {
     cudaStream_t own_stream = nullptr;  // the library's own stream
     uint8_t* trig_corr = nullptr;       // 2^24 bytes: host-libm correction per sample angle
     uint32_t* dev_error = nullptr;      // one DeviceError word
+    cudaMemPool_t accel_pool = nullptr; // the accelerators' memory: freed blocks kept for reuse (up to 4 GiB)
     DevBuf ws[WS_COUNT];
 };
 

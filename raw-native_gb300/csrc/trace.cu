@@ -73,9 +73,14 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_kernel(const __grid_con
 // lanes idle. A walk's rays, box tests and hit test are trace_pixel's (sample_direction,
 // slab, hit_tri, the frontier start), and a pixel's AO is its count of open walks over spp:
 // an integer count, so the order the walks finish in changes no bit.
+// With `sort` (at most kSortSpp samples a pixel) the queue is ordered by the walks' direction
+// octant first (a counting sort of the packet's walks in shared memory), so the lanes that
+// walk together point into one or two octants: nearby origins, the same signs of the
+// direction, similar child orders and node sequences.
+constexpr int kSortSpp = 16;
 template <int kMinBlocks, int kStackN>
 __global__ void __launch_bounds__(256, kMinBlocks) trace_ao_pool_kernel(const __grid_constant__ TraceParams p,
-                                                                        uint32_t* tile_ctr, int refill) {
+                                                                        uint32_t* tile_ctr, int refill, int sort) {
     const int pl = p.packet_log2, tw = 1 << pl, th = 32 >> pl;
     const int tiles_x = (p.w + tw - 1) >> pl, tiles_y = (p.h + th - 1) / th;
     const uint32_t ntiles = (uint32_t)tiles_x * tiles_y;
@@ -84,6 +89,10 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_ao_pool_kernel(const __
     __shared__ FrontierEntry frontier[8][kFrontier];
     __shared__ int open_sh[8][32];
     __shared__ uint8_t lane_sh[8][32];
+    __shared__ uint16_t perm_sh[8][32 * kSortSpp];
+    __shared__ uint32_t oct_sh[8][8];
+    uint16_t* perm = perm_sh[threadIdx.x >> 5];
+    uint32_t* octs = oct_sh[threadIdx.x >> 5];
     FrontierEntry* F = frontier[threadIdx.x >> 5];
     int* opens = open_sh[threadIdx.x >> 5];
     uint8_t* lane_of = lane_sh[threadIdx.x >> 5];   // the covered lanes in lane order
@@ -130,6 +139,43 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_ao_pool_kernel(const __
         if (covered) lane_of[__popc(cov & below)] = (uint8_t)lane;
         __syncwarp();
         const uint32_t total = (uint32_t)nc * (uint32_t)p.spp;
+        const bool sorted = sort && p.spp <= kSortSpp && total > 0;
+        if (sorted) {
+            // the octant of every walk (wi: pixel lane_of[wi % nc], sample wi / nc), counted,
+            // then placed: perm[] lists the walks octant by octant
+            if (lane < 8) octs[lane] = 0;
+            __syncwarp();
+            uint64_t mine = 0;                       // 4 bits a walk of this lane's share
+            for (uint32_t k = 0; k < (uint32_t)kSortSpp; ++k) {
+                const uint32_t wi = lane + 32u * k;
+                const bool has = wi < total;
+                const int src = (int)lane_of[has ? wi % (uint32_t)nc : 0u];
+                const v3 pt = mk(__shfl_sync(0xffffffffu, T.x, src), __shfl_sync(0xffffffffu, T.y, src),
+                                 __shfl_sync(0xffffffffu, T.z, src));
+                const v3 pb = mk(__shfl_sync(0xffffffffu, B.x, src), __shfl_sync(0xffffffffu, B.y, src),
+                                 __shfl_sync(0xffffffffu, B.z, src));
+                const v3 pn = mk(__shfl_sync(0xffffffffu, n.x, src), __shfl_sync(0xffffffffu, n.y, src),
+                                 __shfl_sync(0xffffffffu, n.z, src));
+                const int qx = __shfl_sync(0xffffffffu, x, src), qy = __shfl_sync(0xffffffffu, y, src);
+                if (has) {
+                    const v3 dd = sample_direction(pt, pb, pn, (uint32_t)qx, (uint32_t)qy, wi / (uint32_t)nc, p.corr);
+                    const uint32_t o8 = (dd.x < 0.0f ? 1u : 0u) | (dd.y < 0.0f ? 2u : 0u) | (dd.z < 0.0f ? 4u : 0u);
+                    mine |= (uint64_t)o8 << (4 * k);
+                    atomicAdd(&octs[o8], 1u);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) {
+                uint32_t run = 0;
+                for (int o8 = 0; o8 < 8; ++o8) { const uint32_t c = octs[o8]; octs[o8] = run; run += c; }
+            }
+            __syncwarp();
+            for (uint32_t k = 0; k < (uint32_t)kSortSpp; ++k) {
+                const uint32_t wi = lane + 32u * k;
+                if (wi < total) perm[atomicAdd(&octs[(mine >> (4 * k)) & 7u], 1u)] = (uint16_t)wi;
+            }
+            __syncwarp();
+        }
         uint32_t next = 0;
         bool active = false;
         int q = 0;                    // the lane whose pixel the current walk belongs to
@@ -149,7 +195,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) trace_ao_pool_kernel(const __
                 const uint32_t my = next + (uint32_t)__popc(idle & below);
                 next = min(total, next + (uint32_t)__popc(idle));
                 const bool take = !active && my < total;
-                const uint32_t wi = take ? my : 0u;
+                const uint32_t wi = take ? (sorted ? (uint32_t)perm[my] : my) : 0u;
                 const int src = (int)lane_of[wi % (uint32_t)nc];
                 const v3 pt = mk(__shfl_sync(0xffffffffu, T.x, src), __shfl_sync(0xffffffffu, T.y, src),
                                  __shfl_sync(0xffffffffu, T.z, src));
@@ -338,7 +384,7 @@ void launch_variant(const TraceParams& p, int sm_count, cudaStream_t s, uint32_t
     if (counts)
         trace_kernel<true, kMB, kStack><<<blocks, 256, 0, s>>>(p, tile_ctr, counts, stride < 1 ? 1 : stride);
     else if (pool > 0 && !p.want_sky)
-        trace_ao_pool_kernel<kMB, kStackN><<<blocks, 256, 0, s>>>(p, tile_ctr, pool);
+        trace_ao_pool_kernel<kMB, kStackN><<<blocks, 256, 0, s>>>(p, tile_ctr, pool, ctx().tune.trace_pool_sort);
     else if (ctx().tune.trace_leaf_pass)
         trace_kernel<false, kMB, kStackN, true><<<blocks, 256, 0, s>>>(p, tile_ctr, nullptr, 1);
     else

@@ -39,11 +39,11 @@ def test_trace_keys_keep_every_bit(rn, restore_tune):
         rn.tune_set(k, defaults[k])
 
 
-@pytest.mark.parametrize("spp", [1, 4, 7, 16])
+@pytest.mark.parametrize("spp", [1, 4, 7, 16, 17])
 def test_pooled_walks_keep_every_bit(rn, oracle, restore_tune, spp):
     """AO-only walks from one queue per packet (trace_pool) against one pixel per lane, for
-    every refill threshold, packet shape and frontier setting, on a ragged frame; and against
-    the oracle."""
+    every refill threshold, packet shape and frontier setting, the queue in pixel order or
+    sorted by direction octant (trace_pool_sort), on a ragged frame; and against the oracle."""
     import numpy as np
     g, acc, _ = _scene(rn, 211, 101)
     rn.tune_set("trace_pool", 0)
@@ -51,12 +51,14 @@ def test_pooled_walks_keep_every_bit(rn, oracle, restore_tune, spp):
     for pool in (16, 24, 32):
         for packet in (4, 8, 16):
             for frontier in (0, 1):
-                rn.tune_set("trace_pool", pool)
-                rn.tune_set("trace_packet", packet)
-                rn.tune_set("trace_frontier", frontier)
-                rn.tune_set("trace_frontier_min_spp", 1)
-                got = rn.compute_rtao(g, acc, spp, 1.0)
-                assert bool((got == ref).all()), (pool, packet, frontier, int((got != ref).sum().item()))
+                for sort in (0, 1):
+                    rn.tune_set("trace_pool", pool)
+                    rn.tune_set("trace_pool_sort", sort)
+                    rn.tune_set("trace_packet", packet)
+                    rn.tune_set("trace_frontier", frontier)
+                    rn.tune_set("trace_frontier_min_spp", 1)
+                    got = rn.compute_rtao(g, acc, spp, 1.0)
+                    assert bool((got == ref).all()), (pool, sort, packet, frontier, int((got != ref).sum().item()))
     import scene as scenes
     sc = scenes.build_synthetic_scene(11, 300, 60)
     want = oracle.trace(g.position.cpu().numpy(), g.normal.cpu().numpy(), g.mask.cpu().numpy(), sc.tris, spp, 1.0,
