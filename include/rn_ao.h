@@ -363,6 +363,8 @@ int rn_selftest_wait_budget(uint32_t spin_limit, rn_status* st);
  *                                    per step)
  *   ploc_tail_ctas    1|4|8|16       ... in one block of 1024 threads (1) or one thread-block
  *                                    cluster of this many such blocks
+ *   ploc_fused        0 | 1          accelerator builds: a PLOC round's prefix sum, scatter and
+ *                                    commit in one launch (decoupled look-back) instead of four
  *   collapse_block    0|16384|65536|262144  accelerator builds of at most this many triangles
  *                                    collapse to 4-wide nodes in one block (0: a launch per level)
  *   trace_pool        0|16|24|32     AO-only walks: one queue of a packet's walks, idle lanes

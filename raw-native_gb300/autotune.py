@@ -419,10 +419,12 @@ def tune_ploc_tail(quick: bool, reps: int, log):
     inputs = [(name, torch.from_numpy(np.ascontiguousarray(t)).cuda()) for name, t in inputs]
     current = {"ploc_tail": rn.tune_get("ploc_tail"), "ploc_tail_ctas": rn.tune_get("ploc_tail_ctas")}
     rows, ref = [], None
-    for tail, ctas in itertools.product(rn.TUNE_KEYS["ploc_tail"], rn.TUNE_KEYS["ploc_tail_ctas"]):
+    current = dict(current, ploc_fused=rn.tune_get("ploc_fused"))
+    for tail, ctas, fused in itertools.product(rn.TUNE_KEYS["ploc_tail"], rn.TUNE_KEYS["ploc_tail_ctas"],
+                                               rn.TUNE_KEYS["ploc_fused"]):
         if tail == 0 and ctas != 1:
             continue                                   # no tail: the CTA count is unused
-        cfg = {"ploc_tail": tail, "ploc_tail_ctas": ctas}
+        cfg = {"ploc_tail": tail, "ploc_tail_ctas": ctas, "ploc_fused": fused}
         _apply(cfg)
         try:
             trees = [rn.build_ploc(t)[0].cpu() for _, t in inputs]

@@ -134,6 +134,7 @@ const TuneKey kTuneKeys[] = {
     {"trace_pool", "RN_TUNE_TRACE_POOL", &Tune::trace_pool, {0, 16, 24, 32}, 4},
     {"ploc_tail", "RN_TUNE_PLOC_TAIL", &Tune::ploc_tail, {0, 4096, 16384, 32768, 65536, 262144}, 6},
     {"ploc_tail_ctas", "RN_TUNE_PLOC_TAIL_CTAS", &Tune::ploc_tail_ctas, {1, 4, 8, 16}, 4},
+    {"ploc_fused", "RN_TUNE_PLOC_FUSED", &Tune::ploc_fused, {0, 1}, 2},
     {"collapse_block", "RN_TUNE_COLLAPSE_BLOCK", &Tune::collapse_block, {0, 16384, 65536, 262144}, 4},
     {"conv_tmem_a", "RN_TUNE_CONV_TMEM_A", &Tune::conv_tmem_a, {0, 1}, 2},
     {"trace_leaf_pass", "RN_TUNE_TRACE_LEAF_PASS", &Tune::trace_leaf_pass, {0, 1}, 2},

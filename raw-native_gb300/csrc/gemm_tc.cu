@@ -101,6 +101,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// 32 consecutive TMEM columns of this warp's 32 lanes, the load and its wait in one
+// statement (the registers are defined only once the wait has returned).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+          "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr)
+        : "memory");
+}
+
 template <int BN>
 __global__ void __launch_bounds__(kThreads, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mapP,
                                                               const __grid_constant__ CUtensorMap mapQ,
@@ -566,15 +581,18 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                                                                        const HaloArgs a, const Epilogue e) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    // TMEM: two accumulators, then (kTA) the ring of input rows' A operands; a power of two
-    constexpr uint32_t kCols = kTA ? 256u : 2u * BN;
+    // TMEM: kAcc accumulators (the MMAs of a row run while the previous row is in the
+    // epilogue; four measured no faster), then (kTA) the ring of input rows' A operands; a
+    // power of two
+    constexpr uint32_t kAcc = 2u;
+    constexpr uint32_t kCols = kTA ? 256u : kAcc * BN;
     static_assert(!kTA || 2 * BN + kTaSlots * kTaRowCols <= 256, "the TMEM ring fits");
     const int kSt = a.stages;
     uint8_t* sB = smem;
     uint8_t* sA = smem + ((a.b_bytes + 1023) & ~1023u);
     const uint32_t a_stride = (a.a_bytes + 1023) & ~1023u;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sA + kSt * a_stride);     // full[kSt], empty[kSt], acc_full[2], acc_empty[2], w
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 5);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sA + kSt * a_stride);     // full[kSt], empty[kSt], acc_full[4], acc_empty[4], w
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 9);
     __shared__ int s_abort;
     __shared__ float s_bias[512];       // the bias of every output channel, staged once
     volatile int* abort_flag = &s_abort;
@@ -582,12 +600,12 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     auto full = [&](int s) { return smem_u32(&bars[s]); };
     auto empty = [&](int s) { return smem_u32(&bars[kSt + s]); };
     auto acc_full = [&](int b) { return smem_u32(&bars[2 * kSt + b]); };
-    auto acc_empty = [&](int b) { return smem_u32(&bars[2 * kSt + 2 + b]); };
-    const uint32_t wbar = smem_u32(&bars[2 * kSt + 4]);
+    auto acc_empty = [&](int b) { return smem_u32(&bars[2 * kSt + 4 + b]); };
+    const uint32_t wbar = smem_u32(&bars[2 * kSt + 8]);
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kSt; ++s) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
-        for (int b = 0; b < 2; ++b) { mbar_init(acc_full(b), 1); mbar_init(acc_empty(b), 4); }
+        for (int b = 0; b < (int)kAcc; ++b) { mbar_init(acc_full(b), 1); mbar_init(acc_empty(b), 4); }
         mbar_init(wbar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
@@ -643,14 +661,14 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                 const HaloItem it = halo_item(a, item);
                 for (int j = 0; ok && j < it.rows; ++j, ++i) {
                     // output row y0 + j reads loads j, j + 1, j + 2 of the item
-                    const uint32_t buf = i & 1u, use = i >> 1;
+                    const uint32_t buf = i % kAcc, use = i / kAcc;
                     // row i - 2's MMAs are done once its accumulator is free again: the TMEM
                     // slots they read may be overwritten
                     if (!mbar_wait_or_abort(acc_empty(buf), (use & 1u) ^ 1u, abort_flag)) { ok = false; break; }
                     if (j == 0 && i > 0) {
                         // a new item reloads three rows: the previous row's MMAs must be done too
                         const uint32_t pi = i - 1;
-                        if (!mbar_wait_or_abort(acc_full(pi & 1u), (pi >> 1) & 1u, abort_flag)) { ok = false; break; }
+                        if (!mbar_wait_or_abort(acc_full(pi % kAcc), (pi / kAcc) & 1u, abort_flag)) { ok = false; break; }
                     }
                     for (int d = (j == 0 ? 0 : 2); d < 3 && ok; ++d) {
                         const uint32_t k = base + (uint32_t)(j + d);
@@ -701,7 +719,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                 const HaloItem it = halo_item(a, item);
                 for (int j = 0; ok && j < it.rows; ++j, ++i) {
                     // output row y0 + j reads loads j, j + 1, j + 2 of the item
-                    const uint32_t buf = i & 1u, use = i >> 1;
+                    const uint32_t buf = i % kAcc, use = i / kAcc;
                     if (!mbar_wait_or_abort(acc_empty(buf), (use & 1u) ^ 1u, abort_flag)) { ok = false; break; }
                     uint32_t row_addr[3];
                     for (int d = 0; d < 3 && ok; ++d) {
@@ -754,7 +772,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
         for (int item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
             const HaloItem it = halo_item(a, item);
             for (int j = 0; j < it.rows; ++j, ++i) {
-                const uint32_t buf = i & 1u, use = i >> 1;
+                const uint32_t buf = i % kAcc, use = i / kAcc;
                 ok = __all_sync(0xffffffffu, mbar_wait_or_abort(acc_full(buf), use & 1u, abort_flag));
                 if (!ok) {
                     if (lane == 0) { atomicOr(e.err, DEV_GUARD); s_abort = 1; }
@@ -766,9 +784,13 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                 const uint32_t tbase = tmem + buf * BN + ((uint32_t)(q * 32) << 16);
                 float hz = e.head_out ? e.head_b[0] : 0.0f;
 #pragma unroll 1
-                for (int c0 = 0; c0 < BN; c0 += 16) {
-                    uint32_t v[16];
-                    tmem_ld16(tbase + (uint32_t)c0, v);
+                for (int c32 = 0; c32 < BN; c32 += 32) {
+                  uint32_t v32[32];
+                  tmem_ld32(tbase + (uint32_t)c32, v32);       // 32 columns, one wait
+#pragma unroll
+                  for (int h16 = 0; h16 < 32; h16 += 16) {
+                    const int c0 = c32 + h16;
+                    const uint32_t* v = v32 + h16;
                     float f[16];
 #pragma unroll
                     for (int jj = 0; jj < 16; ++jj) {
@@ -805,6 +827,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
 #pragma unroll
                         for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
                     }
+                  }
                 }
                 if (e.head_out) e.head_out[pix] = 1.0f / (1.0f + __expf(-hz));
                 tc_fence_before();
@@ -1058,7 +1081,7 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
             h.stages = stages;
             h.a_bytes = a_bytes; h.b_bytes = b_bytes;
             h.up16 = up16;
-            const size_t smem = 1024 + b_pad + (size_t)stages * a_stride + (2 * stages + 5) * 8 + 16;
+            const size_t smem = 1024 + b_pad + (size_t)stages * a_stride + (2 * stages + 9) * 8 + 16;
             // A operands in TMEM for 32 output channels and at most 32 input channels
             const bool ta = ctx().tune.conv_tmem_a && N == 32 && cin <= 32;
             const int rc = ta ? tc::launch_conv_halo<32, true>(hm[0], hm[1], hw, h, epi, smem, s)

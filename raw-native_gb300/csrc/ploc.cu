@@ -251,6 +251,7 @@ struct RoundState {
     uint32_t merges;     // merges in this round
     uint32_t error;      // DEV_PLOC_NO_MERGE when a round merged nothing
     int32_t root;        // the last cluster, written by the tail kernels when one is left
+    uint32_t stop;       // the launched rounds do nothing once m <= stop (the tail's threshold, or 1)
 };
 
 // rt_bvh.cpp:104-110: 2 (dy (dx + dz) + dz dx), operation for operation.
@@ -267,7 +268,7 @@ __global__ void ploc_nn(const RoundState* __restrict__ st, const float* __restri
     const uint32_t m = st->m;
     const float* cbox = st->parity ? cbox1 : cbox0;
     const int base = blockIdx.x * kThreads;
-    if (m <= 1 || (uint32_t)base >= m) return;
+    if (m <= st->stop || (uint32_t)base >= m) return;
     for (int q = threadIdx.x; q < kThreads + 2 * R; q += kThreads) {
         const int j = base - R + q;
         if (j >= 0 && (uint32_t)j < m)
@@ -296,7 +297,7 @@ __global__ void ploc_nn_any(const RoundState* __restrict__ st, const float* __re
     const uint32_t m = st->m;
     const float* cbox = st->parity ? cbox1 : cbox0;
     const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (m <= 1 || (uint32_t)i >= m) return;
+    if (m <= st->stop || (uint32_t)i >= m) return;
     const float* A = cbox + (size_t)i * 6;
     const int j0 = i - R > 0 ? i - R : 0, j1 = i + R < (int)m - 1 ? i + R : (int)m - 1;
     float best = FLT_MAX;
@@ -322,7 +323,7 @@ __device__ __forceinline__ void ploc_flags(const int32_t* __restrict__ nn, uint3
 __global__ void ploc_count(const RoundState* __restrict__ st, const int32_t* __restrict__ nn,
                            unsigned long long* __restrict__ bsum) {
     const uint32_t m = st->m;
-    if (m <= 1 || blockIdx.x * (uint32_t)kTile >= m) return;
+    if (m <= st->stop || blockIdx.x * (uint32_t)kTile >= m) return;
     const uint32_t base = blockIdx.x * kTile + threadIdx.x * kItems;
     unsigned long long s = 0;
     for (int k = 0; k < kItems; ++k)
@@ -338,7 +339,7 @@ __global__ void ploc_count(const RoundState* __restrict__ st, const int32_t* __r
 __global__ void ploc_top(RoundState* st, unsigned long long* __restrict__ bsum) {
     __shared__ unsigned long long carry;
     const uint32_t m = st->m;
-    if (m <= 1) return;
+    if (m <= st->stop) return;
     const uint32_t nb = (m + kTile - 1) / kTile;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
@@ -368,7 +369,7 @@ __global__ void ploc_scatter(const RoundState* __restrict__ st, const int32_t* _
                              float* __restrict__ cbo0, float* __restrict__ cbo1,
                              float* __restrict__ box, int32_t* __restrict__ left, int32_t* __restrict__ right) {
     const uint32_t m = st->m;
-    if (m <= 1 || st->merges == 0 || blockIdx.x * (uint32_t)kTile >= m) return;
+    if (m <= st->stop || st->merges == 0 || blockIdx.x * (uint32_t)kTile >= m) return;
     const bool p = st->parity != 0;
     const int32_t* cl = p ? cl1 : cl0;
     int32_t* clo = p ? clo0 : clo1;        // the other buffer of the pair
@@ -408,6 +409,127 @@ __global__ void ploc_scatter(const RoundState* __restrict__ st, const int32_t* _
         run += (unsigned long long)o[k] | ((unsigned long long)g[k] << 32);
     }
 }
+// The round's flags, their prefix sum and the scatter in one launch (ploc_count + ploc_top +
+// ploc_scatter + ploc_commit): a tile of kTile positions per block, tiles handed out by a
+// ticket so that every tile a block waits on is already running, and the prefix across tiles
+// by decoupled look-back (Merrill and Garland, 2016): each tile publishes its total, then
+// adds its predecessors' totals back to the first one that published its inclusive prefix.
+// A status word packs the round (6 bits), the kind (aggregate 1, inclusive prefix 2) and
+// the two sums (survivors, merges: 28 bits each; n < 2^28). The tile that ends the round
+// commits the state (ploc_commit's update) and clears the next launch's ticket (tickets are
+// counted per launch, `launch` numbering this build's merge launches: a block that starts
+// after the commit takes a ticket past the round's tiles and leaves). Every wait is bounded:
+// a tile that gives up sets DEV_GUARD and publishes anyway, and the build fails.
+constexpr uint64_t kLookOut = (1ull << 28) - 1;
+constexpr int kLookSpin = 1 << 22;
+__device__ __forceinline__ uint64_t look_load(const unsigned long long* p) {
+    uint64_t v;
+    asm volatile("ld.global.acquire.gpu.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void look_store(unsigned long long* p, uint64_t v) {
+    asm volatile("st.global.release.gpu.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__global__ void ploc_merge(RoundState* st, const int32_t* __restrict__ nn, unsigned long long* look, uint32_t* ticket,
+                           uint32_t launch, int32_t* __restrict__ cl0, int32_t* __restrict__ cl1, float* __restrict__ cb0,
+                           float* __restrict__ cb1, float* __restrict__ box, int32_t* __restrict__ left,
+                           int32_t* __restrict__ right) {
+    __shared__ uint32_t s_m, s_next, s_parity, s_rounds, s_stop, s_tile;
+    __shared__ unsigned long long s_prefix;
+    if (threadIdx.x == 0) {
+        s_m = st->m; s_next = st->next; s_parity = st->parity; s_rounds = st->rounds; s_stop = st->stop;
+        __threadfence();                         // the state is read before the ticket is taken
+        s_tile = s_m <= s_stop ? 0xFFFFFFFFu : atomicAdd(ticket + (launch & 1u), 1u);
+    }
+    __syncthreads();
+    const uint32_t m = s_m, tile = s_tile;
+    const uint32_t ntiles = (m + kTile - 1) / kTile;
+    if (m <= s_stop || tile >= ntiles) return;
+    const bool p = s_parity != 0;
+    const int32_t* cl = p ? cl1 : cl0;
+    int32_t* clo = p ? cl0 : cl1;
+    const float* cb = p ? cb1 : cb0;
+    float* cbo = p ? cb0 : cb1;
+    const uint32_t base = tile * kTile + threadIdx.x * kItems;
+    uint32_t o[kItems], g[kItems];
+    unsigned long long s = 0;
+    for (int k = 0; k < kItems; ++k) {
+        o[k] = g[k] = 0;
+        if (base + k < m) ploc_flags(nn, base + k, o[k], g[k]);
+        s += (unsigned long long)o[k] | ((unsigned long long)g[k] << 32);
+    }
+    unsigned long long tot;
+    const unsigned long long ex = block_exclusive_scan<unsigned long long>(s, tot);
+    if (threadIdx.x == 0) {
+        const uint64_t tag = (uint64_t)(s_rounds & 63u) << 58;
+        const uint64_t agg = (tot & 0xFFFFFFFFull) | ((tot >> 32) << 28);
+        uint64_t prefix = 0;
+        if (tile == 0) {
+            look_store(look, tag | (2ull << 56) | agg);
+        } else {
+            look_store(look + tile, tag | (1ull << 56) | agg);
+            bool ok = true;
+            for (int k = (int)tile - 1; k >= 0;) {
+                uint64_t w = 0;
+                int spin = 0;
+                for (; spin < kLookSpin; ++spin) {
+                    w = look_load(look + k);
+                    if ((w >> 58) == (tag >> 58) && ((w >> 56) & 3u) != 0) break;
+                    if (spin > 64) __nanosleep(64);
+                }
+                if (spin == kLookSpin) { ok = false; break; }
+                prefix += w & ((1ull << 56) - 1);
+                if (((w >> 56) & 3u) == 2u) break;
+                --k;
+            }
+            if (!ok) atomicOr(&st->error, DEV_GUARD);
+            look_store(look + tile, tag | (2ull << 56) | ((prefix + agg) & ((1ull << 56) - 1)));
+        }
+        // back to the block's form: survivors in the low half, merges in the high half
+        s_prefix = (prefix & kLookOut) | ((prefix >> 28) << 32);
+        if (tile == ntiles - 1) {
+            const uint64_t total = prefix + agg;
+            const uint32_t m_next = (uint32_t)(total & kLookOut), merges = (uint32_t)(total >> 28);
+            st->m_next = m_next;
+            st->merges = merges;
+            if (merges == 0) {
+                atomicOr(&st->error, DEV_PLOC_NO_MERGE);
+            } else {
+                ticket[(launch + 1) & 1u] = 0;
+                st->next = s_next + merges;
+                st->m = m_next;
+                st->parity = s_parity ^ 1u;
+                st->rounds = s_rounds + 1;
+            }
+        }
+    }
+    __syncthreads();
+    unsigned long long run = ex + s_prefix;
+    const uint32_t next = s_next;
+    for (int k = 0; k < kItems; ++k) {
+        const uint32_t i = base + k;
+        if (i < m && o[k]) {
+            const uint32_t pos = (uint32_t)(run & 0xFFFFFFFFull);
+            if (g[k]) {
+                const uint32_t id = next + (uint32_t)(run >> 32);
+                const int32_t j = nn[i];
+                const float* A = cb + (size_t)i * 6;
+                const float* B = cb + (size_t)j * 6;
+                float nb6[6];
+                for (int a = 0; a < 3; ++a) { nb6[a] = smin(A[a], B[a]); nb6[3 + a] = smax(A[3 + a], B[3 + a]); }
+                for (int a = 0; a < 6; ++a) { box[(size_t)id * 6 + a] = nb6[a]; cbo[(size_t)pos * 6 + a] = nb6[a]; }
+                left[id] = cl[i];
+                right[id] = cl[j];
+                clo[pos] = (int32_t)id;
+            } else {
+                for (int a = 0; a < 6; ++a) cbo[(size_t)pos * 6 + a] = cb[(size_t)i * 6 + a];
+                clo[pos] = cl[i];
+            }
+        }
+        run += (unsigned long long)o[k] | ((unsigned long long)g[k] << 32);
+    }
+}
+
 // The remaining rounds in one block, once few clusters are left: the round's three steps
 // (nearest neighbours, the flags' prefix sum, the scatter) are separated by block barriers
 // instead of kernel launches, and the round state lives in shared memory. Each thread takes
@@ -419,12 +541,15 @@ __global__ void __launch_bounds__(kTailThreads) ploc_tail(RoundState* st, int32_
                                                           int32_t* __restrict__ cl1, float* __restrict__ cb0,
                                                           float* __restrict__ cb1, int32_t* __restrict__ nn,
                                                           float* __restrict__ box, int32_t* __restrict__ left,
-                                                          int32_t* __restrict__ right, int R, uint32_t max_rounds) {
+                                                          int32_t* __restrict__ right, int R, uint32_t max_rounds,
+                                                          uint32_t tail_max) {
     __shared__ uint32_t s_m, s_next, s_parity, s_rounds, s_error;
     __shared__ unsigned long long warp_tot[kTailThreads / 32];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (tid == 0) { s_m = st->m; s_next = st->next; s_parity = st->parity; s_rounds = st->rounds; s_error = 0; }
     __syncthreads();
+    // launched after every batch of rounds: nothing to do until the rounds reach the threshold
+    if (s_m <= 1 || s_m > tail_max) return;
     for (uint32_t guard = 0; guard < max_rounds; ++guard) {
         const uint32_t m = s_m;
         if (m <= 1 || s_error) break;
@@ -538,7 +663,7 @@ __global__ void __launch_bounds__(kTailThreads) ploc_tail_cluster(RoundState* st
                                                                   float* __restrict__ cb1, int32_t* __restrict__ nn,
                                                                   float* __restrict__ box, int32_t* __restrict__ left,
                                                                   int32_t* __restrict__ right, int R,
-                                                                  uint32_t max_rounds) {
+                                                                  uint32_t max_rounds, uint32_t tail_max) {
     cg::cluster_group cluster = cg::this_cluster();
     __shared__ uint32_t s_m, s_next, s_parity, s_rounds, s_error;
     __shared__ unsigned long long warp_tot[kTailThreads / 32];
@@ -551,6 +676,9 @@ __global__ void __launch_bounds__(kTailThreads) ploc_tail_cluster(RoundState* st
         s_rounds = __ldcg(&st->rounds); s_error = 0;
     }
     __syncthreads();
+    // launched after every batch of rounds: nothing to do until the rounds reach the threshold
+    // (every CTA reads the same state, so all leave together, before any cluster barrier)
+    if (s_m <= 1 || s_m > tail_max) return;
     for (uint32_t guard = 0; guard < max_rounds; ++guard) {
         const uint32_t m = s_m;
         if (m <= 1 || s_error) break;            // the same in every CTA
@@ -666,7 +794,8 @@ __global__ void __launch_bounds__(kTailThreads) ploc_tail_cluster(RoundState* st
 
 template <int C>
 cudaError_t launch_tail_cluster(cudaStream_t s, RoundState* st, int32_t* cl0, int32_t* cl1, float* cb0, float* cb1,
-                                int32_t* nn, float* box, int32_t* left, int32_t* right, int R, uint32_t max_rounds) {
+                                int32_t* nn, float* box, int32_t* left, int32_t* right, int R, uint32_t max_rounds,
+                                uint32_t tail_max) {
     if (C > 8) {
         const cudaError_t e = cudaFuncSetAttribute(ploc_tail_cluster<C>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         if (e != cudaSuccess) return e;
@@ -682,11 +811,12 @@ cudaError_t launch_tail_cluster(cudaStream_t s, RoundState* st, int32_t* cl0, in
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, ploc_tail_cluster<C>, st, cl0, cl1, cb0, cb1, nn, box, left, right, R, max_rounds);
+    return cudaLaunchKernelEx(&cfg, ploc_tail_cluster<C>, st, cl0, cl1, cb0, cb1, nn, box, left, right, R, max_rounds,
+                              tail_max);
 }
 
 __global__ void ploc_commit(RoundState* st) {
-    if (st->m <= 1 || st->merges == 0) return;
+    if (st->m <= st->stop || st->merges == 0) return;
     st->next += st->merges;
     st->m = st->m_next;
     st->parity ^= 1u;
@@ -968,6 +1098,7 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
     const size_t o_cl0 = take((size_t)n * 4), o_cl1 = take((size_t)n * 4);
     const size_t o_cb0 = take((size_t)n * 24), o_cb1 = take((size_t)n * 24);
     const size_t o_nn = take((size_t)n * 4), o_bs64 = take((size_t)(nbs + 1) * 8);
+    const size_t o_look = take((size_t)(nbs + 1) * 8), o_ticket = take(8);
     const size_t o_bounds = take(sizeof(Bounds)), o_state = take(sizeof(RoundState));
     char* mem = nullptr;
     RN_TRY(ws_get(WS_PLOC, off, (void**)&mem, st));
@@ -986,6 +1117,8 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
     float *cb0 = (float*)(mem + o_cb0), *cb1 = (float*)(mem + o_cb1);
     int32_t* nn = (int32_t*)(mem + o_nn);
     unsigned long long* bs64 = (unsigned long long*)(mem + o_bs64);
+    unsigned long long* look = (unsigned long long*)(mem + o_look);
+    uint32_t* ticket = (uint32_t*)(mem + o_ticket);
     Bounds* bounds = (Bounds*)(mem + o_bounds);
     RoundState* state = (RoundState*)(mem + o_state);
 
@@ -1005,74 +1138,85 @@ int ploc_build(const float* d_tris, uint32_t n, int radius, PlocTree* out, cudaS
     // 4: leaves
     make_leaves<<<cdiv(n, 256), 256, 0, s>>>(d_tris, v0, n, out->box, out->left, out->right, out->tri, cb0, cl0);
     if (n > 1) init_internal<<<cdiv(n - 1, 256), 256, 0, s>>>(n, out->box, out->left, out->right, out->tri);
+    // 5: rounds, in batches; the host reads the state once per batch. With a tail threshold
+    // the launched rounds stop at it (stop) and every batch ends with the tail kernel, which
+    // runs the remaining rounds once the state is at or below the threshold and otherwise
+    // leaves at once: the batch that reaches the threshold also finishes the tree.
+    const uint32_t tail_max = (uint32_t)ctx().tune.ploc_tail;
     RoundState init{};
     init.m = n;
     init.next = n;
     init.root = -1;
+    init.stop = tail_max > 1 ? tail_max : 1u;
     RN_CUDA(cudaMemcpyAsync(state, &init, sizeof init, cudaMemcpyHostToDevice, s), st);
-    // 5: rounds, in batches; the host reads the state once per batch
+    const bool fused = ctx().tune.ploc_fused != 0;
+    if (fused) {
+        // the look-back words of an earlier build must not pass for this one's
+        RN_CUDA(cudaMemsetAsync(look, 0, (size_t)(nbs + 1) * 8, s), st);
+        RN_CUDA(cudaMemsetAsync(ticket, 0, 8, s), st);
+    }
+    uint32_t merge_launch = 0;
     uint32_t m_known = n;
     RoundState hs = init;
     const int kBatch = 6;
-    const uint32_t tail_max = (uint32_t)ctx().tune.ploc_tail;
-    int32_t tail_root = -1;
+    const int ctas = ctx().tune.ploc_tail_ctas;
     for (int batch = 0; m_known > 1; ++batch) {
         if (batch > 2000) return fail(st, RN_ERR_BUDGET, "PLOC: more than %d rounds", batch * kBatch);
-        if (m_known <= tail_max) {
+        if (m_known > tail_max) {
+            const uint32_t nbn = cdiv(m_known, kThreads), nbc = cdiv(m_known, kTile);
+            for (int r = 0; r < kBatch; ++r) {
+                if (radius == 16)
+                    ploc_nn<16><<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn);
+                else if (radius == 8)
+                    ploc_nn<8><<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn);
+                else if (radius == 32)
+                    ploc_nn<32><<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn);
+                else
+                    ploc_nn_any<<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn, radius);
+                if (fused) {
+                    ploc_merge<<<nbc, kThreads, 0, s>>>(state, nn, look, ticket, merge_launch++, cl0, cl1, cb0, cb1,
+                                                        out->box, out->left, out->right);
+                    continue;
+                }
+                ploc_count<<<nbc, kThreads, 0, s>>>(state, nn, bs64);
+                ploc_top<<<1, kThreads, 0, s>>>(state, bs64);
+                ploc_scatter<<<nbc, kThreads, 0, s>>>(state, nn, bs64, cl0, cl1, cl0, cl1, cb0, cb1, cb0, cb1,
+                                                      out->box, out->left, out->right);
+                ploc_commit<<<1, 1, 0, s>>>(state);
+            }
+        }
+        if (tail_max > 1) {
             // the last rounds in one block or one cluster of blocks (at most one round per
             // cluster: each merges one pair or more)
-            const int ctas = ctx().tune.ploc_tail_ctas;
+            const uint32_t rounds_max = tail_max + 1;
             cudaError_t le = cudaSuccess;
             if (ctas == 16)
                 le = launch_tail_cluster<16>(s, state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right, radius,
-                                             m_known + 1);
+                                             rounds_max, tail_max);
             else if (ctas == 8)
                 le = launch_tail_cluster<8>(s, state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right, radius,
-                                            m_known + 1);
+                                            rounds_max, tail_max);
             else if (ctas == 4)
                 le = launch_tail_cluster<4>(s, state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right, radius,
-                                            m_known + 1);
+                                            rounds_max, tail_max);
             else
                 ploc_tail<<<1, kTailThreads, 0, s>>>(state, cl0, cl1, cb0, cb1, nn, out->box, out->left, out->right,
-                                                     radius, m_known + 1);
+                                                     radius, rounds_max, tail_max);
             RN_CUDA(le, st);
-            RN_CUDA(cudaGetLastError(), st);
-            RN_CUDA(cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, s), st);
-            RN_CUDA(cudaStreamSynchronize(s), st);
-            if (hs.error & DEV_PLOC_NO_MERGE)
-                return fail(st, RN_ERR_STATE, "PLOC round %u made no merge (%u clusters)", hs.rounds, hs.m);
-            if (hs.error & DEV_GUARD) return fail(st, RN_ERR_BUDGET, "PLOC: rounds left %u clusters", hs.m);
-            m_known = hs.m;
-            tail_root = hs.root;
-            break;
-        }
-        const uint32_t nbn = cdiv(m_known, kThreads), nbc = cdiv(m_known, kTile);
-        for (int r = 0; r < kBatch; ++r) {
-            if (radius == 16)
-                ploc_nn<16><<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn);
-            else if (radius == 8)
-                ploc_nn<8><<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn);
-            else if (radius == 32)
-                ploc_nn<32><<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn);
-            else
-                ploc_nn_any<<<nbn, kThreads, 0, s>>>(state, cb0, cb1, nn, radius);
-            ploc_count<<<nbc, kThreads, 0, s>>>(state, nn, bs64);
-            ploc_top<<<1, kThreads, 0, s>>>(state, bs64);
-            ploc_scatter<<<nbc, kThreads, 0, s>>>(state, nn, bs64, cl0, cl1, cl0, cl1, cb0, cb1, cb0, cb1,
-                                                  out->box, out->left, out->right);
-            ploc_commit<<<1, 1, 0, s>>>(state);
         }
         RN_CUDA(cudaGetLastError(), st);
         RN_CUDA(cudaMemcpyAsync(&hs, state, sizeof hs, cudaMemcpyDeviceToHost, s), st);
         RN_CUDA(cudaStreamSynchronize(s), st);
         if (hs.error & DEV_PLOC_NO_MERGE)
             return fail(st, RN_ERR_STATE, "PLOC round %u made no merge (%u clusters)", hs.rounds, hs.m);
+        if (hs.error & DEV_GUARD) return fail(st, RN_ERR_BUDGET, "PLOC: rounds left %u clusters", hs.m);
         m_known = hs.m;
     }
+    const int32_t tail_root = hs.root;
     if (hs.next != 2 * n - 1)
         return fail(st, RN_ERR_STATE, "PLOC made %u nodes, expected %u", hs.next, 2 * n - 1);
     int32_t root = tail_root;                // the tail kernels leave the root in the state
-    if (root < 0) {
+    if (root < 0 || n == 1) {
         RN_CUDA(cudaMemcpyAsync(&root, hs.parity ? cl1 : cl0, 4, cudaMemcpyDeviceToHost, s), st);
         RN_CUDA(cudaStreamSynchronize(s), st);
     }

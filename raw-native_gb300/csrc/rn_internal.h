@@ -70,6 +70,7 @@ struct Tune {
     int conv_tmem_a = 0;        // row-ring convolutions of 32 -> 32 or 16 -> 32 channels: A operands kept in TMEM
     int ploc_tail = 4096;       // PLOC: the rounds from this many clusters on run in one launch (0: never)
     int ploc_tail_ctas = 1;     // ... in one block (1) or one thread-block cluster of this many CTAs
+    int ploc_fused = 1;         // PLOC: a round's prefix sum and scatter in one launch (decoupled look-back)
     int collapse_block = 0;     // 4-wide collapse: trees of at most this many triangles in one block
     int trace_pool = 0;         // AO-only walks from a per-packet queue, lanes refilled below this many busy (0: off)
     int trace_pool_sort = 0;    // ... the queue ordered by the walks' direction octant (at most 16 spp)

@@ -63,6 +63,28 @@ def test_ploc_tail_in_one_launch_equals_oracle(rn, oracle, tail, ctas, n, seed, 
         rn.tune_set("ploc_tail_ctas", old[1])
 
 
+@pytest.mark.parametrize("tail", [0, 4096, 32768])
+@pytest.mark.parametrize("n,seed,radius", [(2, 2, 16), (17, 5, 16), (4097, 7, 16), (65536, 8, 16), (300001, 9, 16),
+                                           (20000, 7, 8), (5000, 12, 32), (1000000, 3, 8)])
+def test_ploc_fused_rounds_equal_oracle(rn, oracle, tail, n, seed, radius):
+    """A round's prefix sum, scatter and commit in one launch (ploc_fused: tiles by ticket,
+    decoupled look-back) build the same tree, node for node, with and without the tail, twice
+    in a row (the look-back words of the first build must not pass for the second's)."""
+    old = rn.tune_get("ploc_tail"), rn.tune_get("ploc_fused")
+    rn.tune_set("ploc_tail", tail)
+    rn.tune_set("ploc_fused", 1)
+    try:
+        tris = oracle.soup(n, seed)
+        rn_nodes, rroot, rrounds = oracle.ploc(tris, radius)
+        for _ in range(2):
+            nodes, root, rounds = rn.build_ploc(tris, radius)
+            assert root == rroot and rounds == rrounds
+            assert np.array_equal(nodes, rn_nodes), int((nodes != rn_nodes).any(axis=1).sum())
+    finally:
+        rn.tune_set("ploc_tail", old[0])
+        rn.tune_set("ploc_fused", old[1])
+
+
 def test_ploc_radius_8_differs(rn, oracle):
     tris = oracle.soup(5000, 12)
     a = rn.build_ploc(tris, 16)[0]
