@@ -165,7 +165,7 @@ def cpu_frame_sample(row_stride: int, threads: int):
 
 
 def frame_config(world: int, covered: int) -> dict:
-    """The workload's config, the same dict on both arms (the driver compares them)."""
+    """The workload's config, the same dict on both arms (the two lines describe one workload)."""
     return {"workload": WORKLOAD, "width": W_PX, "height": H_PX, "spp": SPP, "radius": RADIUS,
             "ss_samples": SS_SAMPLES, "tolerance": TOL, "covered_px": covered, "ao_rays_per_step": covered * SPP,
             "parallelism": "replicas (one full frame per GPU)" if world > 1 else "single GPU",
@@ -354,7 +354,7 @@ def run_ours(args):
         # CUDA-event timing; the full runs are `--workload batch|build|pathtrace`)
         short = argparse.Namespace(steps=2, warmup=1, views=0, spp=SPP, workload="batch")
         b = views_report(short)
-        out["batch_config3"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "ms_per_view", "config", "clocks")}
+        out["batch_views"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "ms_per_view", "config", "clocks")}
         out["accel_build"] = {k: v for k, v in build_report(argparse.Namespace(steps=3, warmup=1)).items()
                               if k in ("value", "unit", "ms_per_step", "builds", "config")}
         os.environ["RN_BENCH_NO_CPU"] = "1"

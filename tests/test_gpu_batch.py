@@ -79,7 +79,7 @@ def test_big_scene_ao_matches_oracle(rn, oracle, big_scene):
     assert 0.0 < ao[cov].mean() < 1.0
 
 
-def test_config3_batch_on_big_scene(rn, oracle, big_scene):
+def test_batched_views_on_big_scene(rn, oracle, big_scene):
     """The batched-views config at a reduced scale: 8 orbit views (resolutions /8, spp as drawn),
     batch == single frames, and every 16th row of the first view == the oracle."""
     import torch

@@ -1,5 +1,5 @@
 """The large 4K head-to-head's scene at full size: the seeded 7.88M-triangle scene (the
-config-3 generator with 10,000 boxes and 6,000 subdivision-3 icospheres), 3840 x 2160 orbit
+batched-views scene generator with 10,000 boxes and 6,000 subdivision-3 icospheres), 3840 x 2160 orbit
 views, AO radius 1, the oracle's SAH BVH (the reference's `trace`, src/renderer/ray_ao.cpp:20-63,
 whose any-hit answer is the triangle scan's).
 
