@@ -28,7 +28,7 @@ Workloads:
   batch          16 orbit views of the 744k scene in one captured batch (batch_min_blocks)
   ssao           the built-in scene at 4K: SSAO, 24 taps
   conv           the surrogate U-Net: a forward at 1088 x 1920 and a training step on
-                 64 crops of 128 x 128 (conv_bn_max, then conv_tmem_a)
+                 64 crops of 128 x 128 (conv_bn_max, then conv_tmem_a / conv_fan)
   trace/low-spp  the synthetic scene's view at 4, 8, 16 and 32 spp, and a 4K view of the
                  7.88M-triangle scene at 4 and 16 spp (trace_frontier_min_spp)
   trace/tail     the same view at 16, 64 and 256 spp (trace_frontier_tail)
@@ -382,24 +382,28 @@ def tune_conv(quick: bool, reps: int, log):
         r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
     best = min(rows, key=lambda r: r["score"])
     rn.tune_set("conv_bn_max", best["cfg"]["conv_bn_max"])
-    # then the A operands of the narrow row-ring layers in TMEM or in shared memory
+    # then the MMA form of the row-ring layers: row by row with A from shared memory, row by
+    # row with A from TMEM, or fanned out (each input row feeding its three output rows)
     rows2, ref2 = [], None
-    for v in rn.TUNE_KEYS["conv_tmem_a"]:
-        rn.tune_set("conv_tmem_a", v)
+    for cfg in ({"conv_tmem_a": 0, "conv_fan": 0}, {"conv_tmem_a": 1, "conv_fan": 0}, {"conv_tmem_a": 0, "conv_fan": 1}):
+        for k, v in cfg.items():
+            rn.tune_set(k, v)
         out = inf.forward(x)
         if ref2 is None:
             ref2 = out.clone()
         elif not bool((out == ref2).all()):
-            raise RuntimeError("conv_tmem_a %d changed the network's output" % v)
+            raise RuntimeError("%s changed the network's output" % cfg)
         ms_f = _time(lambda: inf.forward(x), reps)
         ms_t = _time(lambda: trn.train_step(xb, yb, 0.0), max(2, reps // 2))
-        rows2.append(dict(cfg={"conv_tmem_a": v}, ms={"forward": ms_f, "train_step": ms_t}))
-        log("conv_tmem_a %d  forward %.3f ms  train step %.3f ms" % (v, ms_f, ms_t))
+        rows2.append(dict(cfg=dict(cfg), ms={"forward": ms_f, "train_step": ms_t}))
+        log("conv_tmem_a %d conv_fan %d  forward %.3f ms  train step %.3f ms"
+            % (cfg["conv_tmem_a"], cfg["conv_fan"], ms_f, ms_t))
     base = rows2[0]["ms"]
     for r in rows2:
         r["score"] = float(np.exp(np.mean([np.log(r["ms"][k] / base[k]) for k in base])))
     best2 = min(rows2, key=lambda r: r["score"])
-    rn.tune_set("conv_tmem_a", best2["cfg"]["conv_tmem_a"])
+    for k, v in best2["cfg"].items():
+        rn.tune_set(k, v)
     inf.close()
     trn.close()
     return dict(best["cfg"], **best2["cfg"]), rows + rows2

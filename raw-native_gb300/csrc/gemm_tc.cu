@@ -574,7 +574,22 @@ __device__ __forceinline__ HaloItem halo_item(const HaloArgs& a, int item) {
     return it;
 }
 
-template <int BN, bool kTA>
+// Fan-out (kFan): the MMAs follow the input rows instead of the output rows. Input row r is
+// read by output rows r + 1, r and r - 1 (vertical taps 0, 1, 2), so one MMA of N = 3 x BN
+// (A: the row shifted by dx, K16 channels; B: the three vertical taps' weights stacked along
+// N) adds its products to all three rows' accumulators at once. An output row's accumulator
+// lives in a ring of kAcc = 256 / BN TMEM slots, ring index i at columns (kAcc - 1 - i % kAcc)
+// x BN: ascending columns hold descending rows, so the three rows r + 1, r, r - 1 sit in
+// ascending columns and their taps 0, 1, 2 in ascending B rows (where the ring wraps, the MMA
+// splits in two). The weights are staged as [dx][channel group][dy][n][8 channels] by a 5-D
+// box. Per output row the K16 steps still run tap by tap (dy, then dx) and channel by channel
+// within a tap, as in the row-by-row MMAs: the first step of a row (load r + 1 ... its tap 0,
+// dx 0, channels 0-15) starts its accumulator and every later step adds to it, so both forms
+// give the same bits. Each row slot in shared memory is read by the MMAs of its own input row
+// only; the row's A operand crosses from shared memory three times (dx) instead of nine.
+constexpr int kFanMaxAcc = 8;   // accumulator slots (BN 32: 8; BN 64: 4)
+
+template <int BN, bool kTA, bool kFan>
 __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __grid_constant__ CUtensorMap map0,
                                                                        const __grid_constant__ CUtensorMap map1,
                                                                        const __grid_constant__ CUtensorMap mapW,
@@ -583,16 +598,19 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     // TMEM: kAcc accumulators (the MMAs of a row run while the previous row is in the
     // epilogue; four measured no faster), then (kTA) the ring of input rows' A operands; a
-    // power of two
-    constexpr uint32_t kAcc = 2u;
-    constexpr uint32_t kCols = kTA ? 256u : kAcc * BN;
+    // power of two. Fan-out: a ring of 256 / BN accumulators.
+    static_assert(!(kTA && kFan), "one form at a time");
+    static_assert(!kFan || (3 * BN <= 256 && 256 / BN <= kFanMaxAcc), "three rows' accumulators in one MMA");
+    constexpr uint32_t kAcc = kFan ? 256u / BN : 2u;
+    constexpr uint32_t kCols = (kTA || kFan) ? 256u : kAcc * BN;
     static_assert(!kTA || 2 * BN + kTaSlots * kTaRowCols <= 256, "the TMEM ring fits");
     const int kSt = a.stages;
     uint8_t* sB = smem;
     uint8_t* sA = smem + ((a.b_bytes + 1023) & ~1023u);
     const uint32_t a_stride = (a.a_bytes + 1023) & ~1023u;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sA + kSt * a_stride);     // full[kSt], empty[kSt], acc_full[4], acc_empty[4], w
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 9);
+    // full[kSt], empty[kSt], acc_full[8], acc_empty[8], w
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sA + kSt * a_stride);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 2 * kFanMaxAcc + 1);
     __shared__ int s_abort;
     __shared__ float s_bias[512];       // the bias of every output channel, staged once
     volatile int* abort_flag = &s_abort;
@@ -600,8 +618,10 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     auto full = [&](int s) { return smem_u32(&bars[s]); };
     auto empty = [&](int s) { return smem_u32(&bars[kSt + s]); };
     auto acc_full = [&](int b) { return smem_u32(&bars[2 * kSt + b]); };
-    auto acc_empty = [&](int b) { return smem_u32(&bars[2 * kSt + 4 + b]); };
-    const uint32_t wbar = smem_u32(&bars[2 * kSt + 8]);
+    auto acc_empty = [&](int b) { return smem_u32(&bars[2 * kSt + kFanMaxAcc + b]); };
+    const uint32_t wbar = smem_u32(&bars[2 * kSt + 2 * kFanMaxAcc]);
+    // first TMEM column of the accumulator of output row i (counted over the CTA's items)
+    auto acc_col = [&](uint32_t i) -> uint32_t { return kFan ? (kAcc - 1u - i % kAcc) * BN : (i % kAcc) * BN; };
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kSt; ++s) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
@@ -628,7 +648,8 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
         if (lane == 0) {
             // loads in ring order: item by item, input rows y0 - 1 .. y0 + rows
             mbar_expect_tx(wbar, a.b_bytes);
-            tma_load_3d(smem_u32(sB), &mapW, 0, 0, 0, wbar);
+            if (kFan) tma_load_5d(smem_u32(sB), &mapW, 0, 0, 0, 0, 0, wbar);
+            else tma_load_3d(smem_u32(sB), &mapW, 0, 0, 0, wbar);
             uint32_t kc = 0;
             for (int item = blockIdx.x; item < a.items && !*abort_flag; item += gridDim.x) {
                 const HaloItem it = halo_item(a, item);
@@ -648,6 +669,67 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
             // the copies this lane issued must land before the CTA can leave
             for (uint32_t k = kc > (uint32_t)kSt ? kc - kSt : 0; k < kc; ++k) mbar_wait(full(k % kSt), (k / kSt) & 1u);
             mbar_wait(wbar, 0);
+        }
+    } else if (warp == 1 && kFan) {
+        if (lane == 0) {
+            const int q16 = a.cin / 16, G = a.cin / 8;
+            const uint32_t b0 = smem_u32(sB);
+            const uint32_t b_grp = 3u * BN * 16u;                         // next channel group of B (LBO)
+            const uint64_t dq_a = (2u * kHaloGroup) >> 4;                 // the next 16 channels of A
+            bool ok = mbar_wait_or_abort(wbar, 0, abort_flag);
+            uint32_t base = 0, i0 = 0;  // ring index of the item's first load; output rows of earlier items
+            for (int item = blockIdx.x; ok && item < a.items && !*abort_flag; item += gridDim.x) {
+                const HaloItem it = halo_item(a, item);
+                // load k is input row y0 - 1 + k; it feeds output rows j = k - 2 .. k of the item
+                for (int k = 0; ok && k <= it.rows + 1; ++k) {
+                    const int jlo = max(0, k - 2), jhi = min(it.rows - 1, k);
+                    const bool starts = k <= it.rows - 1;                 // output row k's first load
+                    if (starts) {
+                        const uint32_t i = i0 + (uint32_t)k;
+                        if (!mbar_wait_or_abort(acc_empty(i % kAcc), ((i / kAcc) & 1u) ^ 1u, abort_flag)) {
+                            ok = false;
+                            break;
+                        }
+                    }
+                    const uint32_t kk = base + (uint32_t)k;
+                    if (!mbar_wait_or_abort(full(kk % kSt), (kk / kSt) & 1u, abort_flag)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint64_t da_row = desc_plain(smem_u32(sA + (kk % kSt) * a_stride), kHaloGroup, 128);
+                    // output rows lo..hi (ring indices i0 + lo .. i0 + hi) in as few MMAs as the
+                    // ring's wrap allows; row j's block of B is its vertical tap k - j
+                    auto fan = [&](int lo, int hi, uint64_t da, uint32_t bq, uint32_t acc) {
+                        while (lo <= hi) {
+                            const uint32_t ih = i0 + (uint32_t)hi;
+                            const int l = max(lo, hi - (int)(ih % kAcc));
+                            const int n = (hi - l + 1) * BN;
+                            const uint64_t db = desc_plain(bq + (uint32_t)(k - hi) * (BN * 16u), b_grp, 128);
+                            tc_mma(tmem + acc_col(ih), da, db, instr_desc(n), acc);
+                            hi = l - 1;
+                        }
+                    };
+                    for (int dx = 0; dx < 3; ++dx)
+                        for (int q = 0; q < q16; ++q) {
+                            const uint64_t da = da_row + (uint64_t)dx + (uint64_t)q * dq_a;
+                            const uint32_t bq = b0 + (uint32_t)(dx * G + 2 * q) * b_grp;
+                            if (dx == 0 && q == 0 && starts) {
+                                fan(k, k, da, bq, 0u);                    // row k's first step
+                                fan(jlo, k - 1, da, bq, 1u);
+                            } else {
+                                fan(jlo, jhi, da, bq, 1u);
+                            }
+                        }
+                    // the row slot is free once its MMAs have read it; output row k - 2 is complete
+                    tc_commit(empty(kk % kSt));
+                    if (k >= 2) tc_commit(acc_full((i0 + (uint32_t)(k - 2)) % kAcc));
+                }
+                if (!ok) break;
+                base += (uint32_t)it.rows + 2;
+                i0 += (uint32_t)it.rows;
+            }
+            if (!ok) {
+                atomicOr(e.err, DEV_GUARD);
+                s_abort = 1;
+            }
         }
     } else if (warp == 1 && kTA) {
         if (lane == 0) {
@@ -781,7 +863,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                 tc_fence_after();
                 const int y = it.y0 + j, x = it.tx * 128 + r;
                 const size_t pix = ((size_t)it.b * a.H + y) * a.W + x;
-                const uint32_t tbase = tmem + buf * BN + ((uint32_t)(q * 32) << 16);
+                const uint32_t tbase = tmem + acc_col(i) + ((uint32_t)(q * 32) << 16);
                 float hz = e.head_out ? e.head_b[0] : 0.0f;
 #pragma unroll 1
                 for (int c32 = 0; c32 < BN; c32 += 32) {
@@ -950,14 +1032,29 @@ bool make_map_wgroups(CUtensorMap* m, const void* base, int N, int ldw, int kgro
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int BN, bool kTA>
+// The resident weights in the fan-out order: a 5-D view (8 columns, N rows, vertical tap dy,
+// channel group, horizontal tap dx) of the [N][ldw] matrix whose column is
+// (3 dy + dx) cin + channel, one box of all of it: shared memory [dx][group][dy][n][8].
+bool make_map_wfan(CUtensorMap* m, const void* base, int N, int ldw, int cin) {
+    auto fn = encoder();
+    if (!fn) return false;
+    const cuuint64_t dims[5] = {8, (cuuint64_t)N, 3, (cuuint64_t)(cin / 8), 3};
+    const cuuint64_t strides[4] = {(cuuint64_t)ldw * 2, (cuuint64_t)cin * 6, 16, (cuuint64_t)cin * 2};
+    const cuuint32_t box[5] = {8, (cuuint32_t)N, 3, (cuuint32_t)(cin / 8), 3};
+    const cuuint32_t elem[5] = {1, 1, 1, 1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, elem,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN, bool kTA, bool kFan>
 int launch_conv_halo(const CUtensorMap& m0, const CUtensorMap& m1, const CUtensorMap& mw, const HaloArgs& a,
                      const Epilogue& e, size_t smem, cudaStream_t s) {
     static size_t attr = 0;
     if (attr < smem) {
-        if (cudaFuncSetAttribute(tc_conv_halo_kernel<BN, kTA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(tc_conv_halo_kernel<BN, kTA>, cudaFuncAttributePreferredSharedMemoryCarveout,
+        if (cudaFuncSetAttribute(tc_conv_halo_kernel<BN, kTA, kFan>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess ||
+            cudaFuncSetAttribute(tc_conv_halo_kernel<BN, kTA, kFan>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return RN_ERR_CUDA;
         attr = smem;
@@ -965,10 +1062,10 @@ int launch_conv_halo(const CUtensorMap& m0, const CUtensorMap& m1, const CUtenso
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx().device);
     // co-resident CTAs: shared memory and TMEM (512 columns an SM) both have to fit
-    const int tmem_cols = kTA ? 256 : 2 * BN;
+    const int tmem_cols = (kTA || kFan) ? 256 : 2 * BN;
     const int per_sm = std::max(1, std::min(std::min(smem_sm / (int)(smem + 1024), 512 / tmem_cols), 3));
     const int ctas = std::min(a.items, per_sm * ctx().sm_count);
-    tc_conv_halo_kernel<BN, kTA><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
+    tc_conv_halo_kernel<BN, kTA, kFan><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
 }
 
@@ -1063,11 +1160,18 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
         const uint32_t a_stride = (a_bytes + 1023) & ~1023u, b_pad = (b_bytes + 1023) & ~1023u;
         const size_t budget = 220 * 1024;
         int stages = (int)std::min<size_t>(8, (budget - std::min<size_t>(budget, b_pad + 2048)) / a_stride);
+        // A operands in TMEM for 32 output channels and at most 32 input channels; else
+        // (conv_fan) each input row's MMAs feeding its three output rows at once
+        const bool ta = ctx().tune.conv_tmem_a && N == 32 && cin <= 32;
+        const bool fan = !ta && ctx().tune.conv_fan;
+        // fan-out: a row slot is busy only until its own MMAs have run; four slots, and
+        // shared memory for two CTAs per SM where the weights allow
+        if (fan && stages > 4) stages = 4;
         CUtensorMap hm[2], hw;
         bool maps = stages >= 4;
         for (int i = 0; maps && i < nsrc; ++i) maps = tc::make_map_halo(&hm[i], src[i].ptr, B, H, W, src[i].C);
         if (maps && nsrc == 1) hm[1] = hm[0];
-        maps = maps && tc::make_map_wgroups(&hw, w, N, ldw, 9 * cin / 8);
+        maps = maps && (fan ? tc::make_map_wfan(&hw, w, N, ldw, cin) : tc::make_map_wgroups(&hw, w, N, ldw, 9 * cin / 8));
         if (maps) {
             tc::HaloArgs h{};
             h.nsrc = nsrc; h.C0 = src[0].C; h.C1 = nsrc > 1 ? src[1].C : 0; h.cin = cin;
@@ -1081,12 +1185,12 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
             h.stages = stages;
             h.a_bytes = a_bytes; h.b_bytes = b_bytes;
             h.up16 = up16;
-            const size_t smem = 1024 + b_pad + (size_t)stages * a_stride + (2 * stages + 9) * 8 + 16;
-            // A operands in TMEM for 32 output channels and at most 32 input channels
-            const bool ta = ctx().tune.conv_tmem_a && N == 32 && cin <= 32;
-            const int rc = ta ? tc::launch_conv_halo<32, true>(hm[0], hm[1], hw, h, epi, smem, s)
-                         : N == 32 ? tc::launch_conv_halo<32, false>(hm[0], hm[1], hw, h, epi, smem, s)
-                                   : tc::launch_conv_halo<64, false>(hm[0], hm[1], hw, h, epi, smem, s);
+            const size_t smem = 1024 + b_pad + (size_t)stages * a_stride + (2 * stages + 2 * tc::kFanMaxAcc + 1) * 8 + 16;
+            const int rc = ta    ? tc::launch_conv_halo<32, true, false>(hm[0], hm[1], hw, h, epi, smem, s)
+                         : fan   ? (N == 32 ? tc::launch_conv_halo<32, false, true>(hm[0], hm[1], hw, h, epi, smem, s)
+                                            : tc::launch_conv_halo<64, false, true>(hm[0], hm[1], hw, h, epi, smem, s))
+                         : N == 32 ? tc::launch_conv_halo<32, false, false>(hm[0], hm[1], hw, h, epi, smem, s)
+                                   : tc::launch_conv_halo<64, false, false>(hm[0], hm[1], hw, h, epi, smem, s);
             if (rc != RN_OK) return cuda_fail(st, cudaGetLastError(), "tc_conv_halo_kernel");
             return RN_OK;
         }

@@ -133,6 +133,25 @@ def test_conv_tmem_a_keeps_every_bit(rn, restore_tune):
     assert np.allclose(grads[0], grads[1], rtol=1e-3, atol=1e-5 * scale)
 
 
+def test_conv_fan_keeps_every_bit(rn, restore_tune):
+    """The row-ring convolutions in fan-out form (conv_fan: each input row's MMAs add to the
+    three output rows that read it, N = 3 x 32 or 3 x 64) give the same network output bit for
+    bit: every output row still starts with its first K16 step and adds the other steps in
+    the same tap and channel order. Frames of several heights (items of 1 to 16 rows, so the
+    accumulator ring wraps inside MMAs and crosses item boundaries), batch 2."""
+    import torch
+    g = torch.Generator(device="cuda").manual_seed(4)
+    for H, W in ((64, 128), (144, 256), (1088, 1920)):
+        net = rn.UNet(1 if H > 200 else 2, H, W, seed=7, inference=True)
+        x = torch.rand(net.shape[0], H, W, 5, device="cuda", generator=g)
+        rn.tune_set("conv_fan", 0)
+        ref = net.forward(x).clone()
+        rn.tune_set("conv_fan", 1)
+        got = net.forward(x)
+        assert bool((got == ref).all()), (H, W, int((got != ref).sum().item()))
+        net.close()
+
+
 @pytest.mark.parametrize("sky", [False, True])
 def test_host_frame_keeps_every_bit(rn, restore_tune, sky):
     """rn_ao_frame with pinned host buffers runs without copies: the traversal reads the
