@@ -101,6 +101,25 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// 64 consecutive TMEM columns of this warp's 32 lanes in one load and one wait.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&v)[64]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];\n"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31]), "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]), "=r"(v[38]), "=r"(v[39]), "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]), "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]), "=r"(v[48]), "=r"(v[49]), "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]), "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]), "=r"(v[62]), "=r"(v[63])
+        : "r"(taddr)
+        : "memory");
+}
+// Zeros into 32 consecutive TMEM columns of this warp's 32 lanes (its wait is separate:
+// tcgen05.wait::st before the columns are handed to the MMAs).
+__device__ __forceinline__ void tmem_zero32(uint32_t taddr) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+        "%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(taddr), "r"(0u)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 // 32 consecutive TMEM columns of this warp's 32 lanes, the load and its wait in one
 // statement (the registers are defined only once the wait has returned).
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
@@ -583,14 +602,31 @@ __device__ __forceinline__ HaloItem halo_item(const HaloArgs& a, int item) {
 // ascending columns and their taps 0, 1, 2 in ascending B rows (where the ring wraps, the MMA
 // splits in two). The weights are staged as [dx][channel group][dy][n][8 channels] by a 5-D
 // box. Per output row the K16 steps still run tap by tap (dy, then dx) and channel by channel
-// within a tap, as in the row-by-row MMAs: the first step of a row (load r + 1 ... its tap 0,
-// dx 0, channels 0-15) starts its accumulator and every later step adds to it, so both forms
-// give the same bits. Each row slot in shared memory is read by the MMAs of its own input row
-// only; the row's A operand crosses from shared memory three times (dx) instead of nine.
+// within a tap, as in the row-by-row MMAs; the accumulators start at zero (the epilogue warps
+// clear each one after reading it, and the whole ring at the start) and every MMA adds, so
+// both forms give the same values (0 + x = x; at most the sign of an all-zero sum differs).
+// Each row slot in shared memory is read by the MMAs of its own input row only; the row's A
+// operand crosses from shared memory three times (dx) instead of nine.
 constexpr int kFanMaxAcc = 8;   // accumulator slots (BN 32: 8; BN 64: 4)
+constexpr int kFanCases = 6;    // which of a load's three output rows exist
+// Fan-out accumulator ring and residency: 256 TMEM columns (eight rows' accumulators at BN
+// 32, four at BN 64) and two CTAs per SM. Three CTAs of a four-row ring at BN 32 (128
+// columns, 96 registers) measured slower on every layer (32 -> 32 at 1088 x 1920: 94.0 us
+// against 88.7).
+__host__ __device__ constexpr int fan_acc(int bn) { return 256 / bn; }
+__host__ __device__ constexpr int fan_ctas(int bn) { return 2; }
+// The MMAs of one K16 step of one load in fan-out form: n pieces (two where the accumulator
+// ring wraps), each (accumulator address, instruction descriptor, B offset in 16-byte units).
+struct FanPlan { uint4 p[2]; int n, pad0, pad1, pad2; };
+// Static shared memory of tc_conv_halo_kernel<BN>, rounded up: the bias (512 floats), the
+// abort flag, the epilogue's stage (4 warps x 32 pixels x BN BF16 channels) and the fan-out
+// MMA plans.
+__host__ __device__ constexpr size_t halo_static_smem(int bn) {
+    return 2048 + 64 + (size_t)4 * 32 * bn * 2 + sizeof(FanPlan) * kFanCases * kFanMaxAcc;
+}
 
 template <int BN, bool kTA, bool kFan>
-__global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __grid_constant__ CUtensorMap map0,
+__global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv_halo_kernel(const __grid_constant__ CUtensorMap map0,
                                                                        const __grid_constant__ CUtensorMap map1,
                                                                        const __grid_constant__ CUtensorMap mapW,
                                                                        const HaloArgs a, const Epilogue e) {
@@ -601,7 +637,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     // power of two. Fan-out: a ring of 256 / BN accumulators.
     static_assert(!(kTA && kFan), "one form at a time");
     static_assert(!kFan || (3 * BN <= 256 && 256 / BN <= kFanMaxAcc), "three rows' accumulators in one MMA");
-    constexpr uint32_t kAcc = kFan ? 256u / BN : 2u;
+    constexpr uint32_t kAcc = kFan ? (uint32_t)fan_acc(BN) : 2u;
     constexpr uint32_t kCols = (kTA || kFan) ? 256u : kAcc * BN;
     static_assert(!kTA || 2 * BN + kTaSlots * kTaRowCols <= 256, "the TMEM ring fits");
     const int kSt = a.stages;
@@ -613,6 +649,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 2 * kFanMaxAcc + 1);
     __shared__ int s_abort;
     __shared__ float s_bias[512];       // the bias of every output channel, staged once
+    __shared__ FanPlan s_fan[kFanCases][kFanMaxAcc];
     volatile int* abort_flag = &s_abort;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     auto full = [&](int s) { return smem_u32(&bars[s]); };
@@ -643,6 +680,16 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     const uint32_t src1_off = (uint32_t)(a.C0 / 8) * kHaloGroup;
+    if (kFan) {
+        // fan-out accumulators start at zero and every MMA adds to them: each epilogue warp
+        // clears its lane quarter of the ring now and of each row again once it has read it
+        if (warp >= 2)
+            for (uint32_t c = 0; c < kCols; c += 32) tmem_zero32(tmem + c + ((uint32_t)((warp & 3) * 32) << 16));
+        tmem_wait_st();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
 
     if (warp == 0) {
         if (lane == 0) {
@@ -650,12 +697,15 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
             mbar_expect_tx(wbar, a.b_bytes);
             if (kFan) tma_load_5d(smem_u32(sB), &mapW, 0, 0, 0, 0, 0, wbar);
             else tma_load_3d(smem_u32(sB), &mapW, 0, 0, 0, wbar);
-            uint32_t kc = 0;
+            // kc counts loads; s and ph are its ring slot and the slot's phase (kc % kSt and
+            // kc / kSt mod 2, kept by increment: kSt is a launch argument, and a division per
+            // load would sit on this thread's path)
+            uint32_t kc = 0, ph = 0;
+            int s = 0;
             for (int item = blockIdx.x; item < a.items && !*abort_flag; item += gridDim.x) {
                 const HaloItem it = halo_item(a, item);
                 for (int r = -1; r <= it.rows && !*abort_flag; ++r, ++kc) {
-                    const int s = kc % kSt;
-                    if (!mbar_wait_or_abort(empty(s), ((kc / kSt) & 1u) ^ 1u, abort_flag)) {
+                    if (!mbar_wait_or_abort(empty(s), ph ^ 1u, abort_flag)) {
                         atomicOr(e.err, DEV_GUARD);
                         s_abort = 1;
                         break;
@@ -664,6 +714,7 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                     const uint32_t dst = smem_u32(sA + s * a_stride);
                     tma_load_5d(dst, &map0, 0, it.tx * 128 - 1, it.y0 + r, it.b, 0, full(s));
                     if (a.nsrc > 1) tma_load_5d(dst + src1_off, &map1, 0, it.tx * 128 - 1, it.y0 + r, it.b, 0, full(s));
+                    if (++s == kSt) { s = 0; ph ^= 1u; }
                 }
             }
             // the copies this lane issued must land before the CTA can leave
@@ -671,59 +722,87 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
             mbar_wait(wbar, 0);
         }
     } else if (warp == 1 && kFan) {
+        // The MMAs of a load depend only on which of its three output rows exist (the load's
+        // case: lo = max(0, k - 2) - k and hi = min(rows - 1, k) - k, six cases) and on the
+        // ring residue of its row k, so the warp tabulates them once: per case and residue the
+        // one or two pieces (two where the ring wraps) of every K16 step, each an accumulator
+        // address, an instruction descriptor (N) and the offset of its first B row (vertical
+        // tap k - h for its top row h, in 16-byte units). The issuing thread then spends two
+        // shared loads per load instead of forming pieces: it is blocked while the tensor
+        // pipe takes each MMA, so its other work adds directly to the layer's time.
+        for (int e_ = lane; e_ < kFanCases * (int)kAcc; e_ += 32) {
+            const int cs = e_ / (int)kAcc, r = e_ % (int)kAcc;
+            const int lo = cs == 0 ? 0 : cs <= 2 ? -1 : -2;                       // relative to k
+            const int hi = cs == 0 || cs == 1 || cs == 3 ? 0 : cs == 2 || cs == 4 ? -1 : -2;
+            // ring index of row k + x is r + x (mod kAcc); the piece holding the top row first
+            FanPlan& pl = s_fan[cs][r];
+            int n = 0;
+            for (int h = hi; h >= lo;) {
+                const uint32_t ih = (uint32_t)(r + h + (int)kAcc) % kAcc;
+                const int b = max(lo, h - (int)ih);
+                pl.p[n++] = make_uint4(tmem + (kAcc - 1u - ih) * BN, instr_desc((h - b + 1) * BN), (uint32_t)(-h * BN), 0u);
+                h = b - 1;
+            }
+            pl.n = n;
+        }
+        __syncwarp();
         if (lane == 0) {
             const int q16 = a.cin / 16, G = a.cin / 8;
-            const uint32_t b0 = smem_u32(sB);
             const uint32_t b_grp = 3u * BN * 16u;                         // next channel group of B (LBO)
+            const uint64_t db0 = desc_plain(smem_u32(sB), b_grp, 128);
             const uint64_t dq_a = (2u * kHaloGroup) >> 4;                 // the next 16 channels of A
+            const uint64_t dq_b = (2u * b_grp) >> 4;                      // ... of B
+            const uint64_t dx_b = ((uint32_t)G * b_grp) >> 4;             // the next horizontal tap of B
             bool ok = mbar_wait_or_abort(wbar, 0, abort_flag);
-            uint32_t base = 0, i0 = 0;  // ring index of the item's first load; output rows of earlier items
+            uint32_t i0 = 0;            // output rows of earlier items
+            // the current load's ring slot, its phase and its shared-memory row (kept by increment)
+            int slot = 0;
+            uint32_t phase = 0, row_smem = smem_u32(sA);
+            // Descriptors are affine in their address (the 14-bit field holds address / 16, and
+            // no offset here carries out of it): every MMA is a base descriptor plus a constant.
             for (int item = blockIdx.x; ok && item < a.items && !*abort_flag; item += gridDim.x) {
                 const HaloItem it = halo_item(a, item);
-                // load k is input row y0 - 1 + k; it feeds output rows j = k - 2 .. k of the item
+                // load k is input row y0 - 1 + k; it feeds output rows k - 2 .. k of the item
                 for (int k = 0; ok && k <= it.rows + 1; ++k) {
-                    const int jlo = max(0, k - 2), jhi = min(it.rows - 1, k);
-                    const bool starts = k <= it.rows - 1;                 // output row k's first load
-                    if (starts) {
+                    const int lo = max(0, k - 2) - k, hi = min(it.rows - 1, k) - k;
+                    const int cs = -lo * (1 - lo) / 2 - hi;               // (0,0) 0; (-1,0) 1; (-1,-1) 2; (-2,0) 3; ...
+                    const FanPlan& pl = s_fan[cs][(i0 + (uint32_t)k) % kAcc];
+                    const uint4 c0 = pl.p[0], c1 = pl.p[1];
+                    const int nc = pl.n;
+                    if (hi == 0) {
+                        // output row k's first load: its accumulator must be free
                         const uint32_t i = i0 + (uint32_t)k;
                         if (!mbar_wait_or_abort(acc_empty(i % kAcc), ((i / kAcc) & 1u) ^ 1u, abort_flag)) {
                             ok = false;
                             break;
                         }
                     }
-                    const uint32_t kk = base + (uint32_t)k;
-                    if (!mbar_wait_or_abort(full(kk % kSt), (kk / kSt) & 1u, abort_flag)) { ok = false; break; }
+                    if (!mbar_wait_or_abort(full(slot), phase, abort_flag)) { ok = false; break; }
                     tc_fence_after();
-                    const uint64_t da_row = desc_plain(smem_u32(sA + (kk % kSt) * a_stride), kHaloGroup, 128);
-                    // output rows lo..hi (ring indices i0 + lo .. i0 + hi) in as few MMAs as the
-                    // ring's wrap allows; row j's block of B is its vertical tap k - j
-                    auto fan = [&](int lo, int hi, uint64_t da, uint32_t bq, uint32_t acc) {
-                        while (lo <= hi) {
-                            const uint32_t ih = i0 + (uint32_t)hi;
-                            const int l = max(lo, hi - (int)(ih % kAcc));
-                            const int n = (hi - l + 1) * BN;
-                            const uint64_t db = desc_plain(bq + (uint32_t)(k - hi) * (BN * 16u), b_grp, 128);
-                            tc_mma(tmem + acc_col(ih), da, db, instr_desc(n), acc);
-                            hi = l - 1;
-                        }
-                    };
-                    for (int dx = 0; dx < 3; ++dx)
+                    const uint64_t da_row = desc_plain(row_smem, kHaloGroup, 128);
+#pragma unroll
+                    for (int dx = 0; dx < 3; ++dx) {
+                        uint64_t da = da_row + (uint64_t)dx;                      // one pixel: 16 bytes
+                        uint64_t db = db0 + (uint64_t)dx * dx_b;
                         for (int q = 0; q < q16; ++q) {
-                            const uint64_t da = da_row + (uint64_t)dx + (uint64_t)q * dq_a;
-                            const uint32_t bq = b0 + (uint32_t)(dx * G + 2 * q) * b_grp;
-                            if (dx == 0 && q == 0 && starts) {
-                                fan(k, k, da, bq, 0u);                    // row k's first step
-                                fan(jlo, k - 1, da, bq, 1u);
-                            } else {
-                                fan(jlo, jhi, da, bq, 1u);
-                            }
+                            tc_mma(c0.x, da, db + c0.z, c0.y, 1u);
+                            if (nc > 1) tc_mma(c1.x, da, db + c1.z, c1.y, 1u);
+                            da += dq_a;
+                            db += dq_b;
                         }
+                    }
                     // the row slot is free once its MMAs have read it; output row k - 2 is complete
-                    tc_commit(empty(kk % kSt));
+                    tc_commit(empty(slot));
                     if (k >= 2) tc_commit(acc_full((i0 + (uint32_t)(k - 2)) % kAcc));
+                    if (++slot == kSt) {
+                        slot = 0;
+                        phase ^= 1u;
+                        row_smem = smem_u32(sA);
+                    } else {
+                        row_smem += a_stride;
+                    }
                 }
                 if (!ok) break;
-                base += (uint32_t)it.rows + 2;
                 i0 += (uint32_t)it.rows;
             }
             if (!ok) {
@@ -849,6 +928,16 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
     } else {
         const int q = warp & 3;
         const int r = q * 32 + lane;
+        // BF16 outputs pass through shared memory: a lane converts its pixel's BN channels
+        // into 16-byte chunks of its warp's stage, then the warp stores the stage's 32 pixels
+        // as whole 512-byte runs (16 contiguous bytes a lane) instead of one 16-byte piece a
+        // lane 2 x BN bytes apart. Chunk c of pixel p sits at slot p kCh + (c ^ swz(p)): a
+        // quarter-warp's eight 16-byte accesses then fall in eight different bank groups
+        // both when lanes write their own pixels and when they read consecutive chunks.
+        constexpr int kCh = BN / 8;
+        __shared__ __align__(16) uint4 s_stage[4][32 * kCh];
+        uint4* stage = s_stage[q];
+        auto slot = [](int p, int c) { return p * kCh + (c ^ ((kCh == 4 ? (p >> 1) : p) & (kCh - 1))); };
         uint32_t i = 0;
         bool ok = true;
         for (int item = blockIdx.x; ok && item < a.items; item += gridDim.x) {
@@ -865,14 +954,16 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                 const size_t pix = ((size_t)it.b * a.H + y) * a.W + x;
                 const uint32_t tbase = tmem + acc_col(i) + ((uint32_t)(q * 32) << 16);
                 float hz = e.head_out ? e.head_b[0] : 0.0f;
-#pragma unroll 1
-                for (int c32 = 0; c32 < BN; c32 += 32) {
-                  uint32_t v32[32];
-                  tmem_ld32(tbase + (uint32_t)c32, v32);       // 32 columns, one wait
+                // the row's BN columns in one TMEM load and one wait
+                uint32_t vv[BN];
+                if constexpr (BN == 64) tmem_ld64(tbase, vv);
+                else tmem_ld32(tbase, vv);
+                if (kFan)                                      // the row's next use starts from zero
 #pragma unroll
-                  for (int h16 = 0; h16 < 32; h16 += 16) {
-                    const int c0 = c32 + h16;
-                    const uint32_t* v = v32 + h16;
+                    for (int c32 = 0; c32 < BN; c32 += 32) tmem_zero32(tbase + (uint32_t)c32);
+#pragma unroll
+                for (int c0 = 0; c0 < BN; c0 += 16) {
+                    const uint32_t* v = vv + c0;
                     float f[16];
 #pragma unroll
                     for (int jj = 0; jj < 16; ++jj) {
@@ -891,30 +982,42 @@ __global__ void __launch_bounds__(kConvThreads, 1) tc_conv_halo_kernel(const __g
                         __nv_bfloat16* ob = reinterpret_cast<__nv_bfloat16*>(out);
 #pragma unroll
                         for (int jj = 0; jj < 16; ++jj) ob[jj] = __float2bfloat16_rn(f[jj]);
-                        uint4* d4 = reinterpret_cast<uint4*>(e.c16 + o);
-                        d4[0] = out[0];
-                        d4[1] = out[1];
-                        if (a.up16) {
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) {
-                                const size_t up = ((size_t)it.b * 2 * a.H + 2 * y + (u >> 1)) * (2 * a.W) + 2 * x + (u & 1);
-                                uint4* d = reinterpret_cast<uint4*>(a.up16 + up * e.ldc + c0);
-                                d[0] = out[0];
-                                d[1] = out[1];
-                            }
-                        }
+                        stage[slot(lane, c0 / 8)] = out[0];
+                        stage[slot(lane, c0 / 8 + 1)] = out[1];
                     }
                     if (e.c32) {
                         float4* d4 = reinterpret_cast<float4*>(e.c32 + o);
 #pragma unroll
                         for (int h = 0; h < 4; ++h) d4[h] = make_float4(f[4 * h], f[4 * h + 1], f[4 * h + 2], f[4 * h + 3]);
                     }
-                  }
                 }
                 if (e.head_out) e.head_out[pix] = 1.0f / (1.0f + __expf(-hz));
+                if (kFan) tmem_wait_st();
                 tc_fence_before();
                 __syncwarp();
+                // the accumulator is read (and, fan-out, cleared): the MMAs may refill it while
+                // the warp stores
                 if (lane == 0) mbar_arrive(acc_empty(buf));
+                if (e.c16) {
+                    const size_t pix0 = pix - lane;                       // the warp's first pixel
+#pragma unroll 1
+                    for (int k = 0; k < kCh; ++k) {
+                        const int idx = k * 32 + lane, p = idx / kCh, c = idx % kCh;
+                        *reinterpret_cast<uint4*>(e.c16 + (pix0 + p) * e.ldc + c * 8) = stage[slot(p, c)];
+                    }
+                    if (a.up16) {
+                        // rows 2y and 2y + 1 of the 2x copy: 64 pixels, each source pixel twice
+                        const size_t up0 = ((size_t)it.b * 2 * a.H + 2 * y) * (2 * a.W) + 2 * (x - lane);
+#pragma unroll 1
+                        for (int k = 0; k < 2 * kCh; ++k) {
+                            const int idx = k * 32 + lane, P = idx / kCh, c = idx % kCh;
+                            const uint4 v = stage[slot(P >> 1, c)];
+                            *reinterpret_cast<uint4*>(a.up16 + (up0 + P) * e.ldc + c * 8) = v;
+                            *reinterpret_cast<uint4*>(a.up16 + (up0 + 2 * a.W + P) * e.ldc + c * 8) = v;
+                        }
+                    }
+                    __syncwarp();                                         // the stage is free again
+                }
             }
         }
     }
@@ -1061,9 +1164,11 @@ int launch_conv_halo(const CUtensorMap& m0, const CUtensorMap& m1, const CUtenso
     }
     int smem_sm = 0;
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, ctx().device);
-    // co-resident CTAs: shared memory and TMEM (512 columns an SM) both have to fit
-    const int tmem_cols = (kTA || kFan) ? 256 : 2 * BN;
-    const int per_sm = std::max(1, std::min(std::min(smem_sm / (int)(smem + 1024), 512 / tmem_cols), 3));
+    // co-resident CTAs: shared memory (dynamic, static and 1 KB reserved) and TMEM (512
+    // columns an SM) both have to fit
+    const int tmem_cols = kTA ? 256 : kFan ? fan_acc(BN) * BN : 2 * BN;
+    const int per_cta = (int)(smem + halo_static_smem(BN) + 1024);
+    const int per_sm = std::max(1, std::min(std::min(smem_sm / per_cta, 512 / tmem_cols), 3));
     const int ctas = std::min(a.items, per_sm * ctx().sm_count);
     tc_conv_halo_kernel<BN, kTA, kFan><<<ctas, kConvThreads, smem, s>>>(m0, m1, mw, a, e);
     return cudaGetLastError() == cudaSuccess ? RN_OK : RN_ERR_CUDA;
@@ -1158,17 +1263,25 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
         const uint32_t b_bytes = (uint32_t)N * 9 * cin * 2;
         const uint32_t a_bytes = (uint32_t)cin / 8 * tc::kHaloGroup;
         const uint32_t a_stride = (a_bytes + 1023) & ~1023u, b_pad = (b_bytes + 1023) & ~1023u;
-        const size_t budget = 220 * 1024;
+        // dynamic shared memory: 227 KB a block less the kernel's static arrays (the bias,
+        // the abort flag and the epilogue's BF16 stage of 4 x 32 pixels x N channels)
+        const size_t stat = tc::halo_static_smem(N);
+        const size_t budget = 220 * 1024 - stat;
         int stages = (int)std::min<size_t>(8, (budget - std::min<size_t>(budget, b_pad + 2048)) / a_stride);
         // A operands in TMEM for 32 output channels and at most 32 input channels; else
         // (conv_fan) each input row's MMAs feeding its three output rows at once
         const bool ta = ctx().tune.conv_tmem_a && N == 32 && cin <= 32;
         const bool fan = !ta && ctx().tune.conv_fan;
-        // fan-out: a row slot is busy only until its own MMAs have run; four slots, and
-        // shared memory for two CTAs per SM where the weights allow
-        if (fan && stages > 4) stages = 4;
+        // fan-out: a row slot is busy only until its own MMAs have run; four slots at most (4,
+        // 6 and 8 measured alike), and no more than leave shared memory for fan_ctas(N) CTAs
+        // per SM (228 KB less 1 KB reserved each), at least two
+        if (fan) {
+            const size_t per_cta = 228 * 1024 / tc::fan_ctas(N) - 1024 - stat;
+            const int fit = (int)((per_cta - std::min<size_t>(per_cta, b_pad + 2048)) / a_stride);
+            stages = std::min(stages, std::max(2, std::min(fit, 4)));
+        }
         CUtensorMap hm[2], hw;
-        bool maps = stages >= 4;
+        bool maps = stages >= (fan ? 2 : 4);
         for (int i = 0; maps && i < nsrc; ++i) maps = tc::make_map_halo(&hm[i], src[i].ptr, B, H, W, src[i].C);
         if (maps && nsrc == 1) hm[1] = hm[0];
         maps = maps && (fan ? tc::make_map_wfan(&hw, w, N, ldw, cin) : tc::make_map_wgroups(&hw, w, N, ldw, 9 * cin / 8));
