@@ -2,8 +2,8 @@
 
 Loads ``oracle/librn_oracle.so`` (the C restatement in ``rn_oracle.c``) and, where it was
 built, ``oracle/_ref/libref_ao.so`` (the reference's own sources). Only the tests, the
-smoke check and the benchmark's CPU-baseline leg import this module: it is the checker,
-never the thing measured or shipped.
+smoke check and the benchmark's CPU-baseline leg import this module: it is what results
+are compared against, never the thing measured or shipped.
 
 File encodings follow src/core/image.cpp:34-106 of the reference: ``Pf`` PFM with rows
 bottom-to-top, the coverage mask as P5 PGM 255/0, and 8-bit previews ``v*255+0.5``.

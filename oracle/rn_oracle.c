@@ -1,8 +1,8 @@
 /*
  * rn_oracle.c -- CPU restatement of raw-native's ambient-occlusion path.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker that the CUDA path is compared
- * against: only the tests, the smoke check and the CPU-baseline leg of the benchmark load
+ * TEST INFRASTRUCTURE ONLY. This file is the oracle the CUDA path is compared against:
+ * only the tests, the smoke check and the CPU-baseline leg of the benchmark load
  * it. No product code links it, calls it or falls back to it.
  *
  * Every function restates the reference's algorithm in plain C, in the same float32

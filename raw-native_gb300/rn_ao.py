@@ -114,7 +114,7 @@ def lib() -> C.CDLL:
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
-            raise RnError(2, "librn_ao.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+            raise RnError(2, "librn_ao.so is not built (%s); build it with raw-native_gb300/rn_build.py" % LIB_PATH)
         L = C.CDLL(LIB_PATH)
         vp, st = C.c_void_p, C.POINTER(Status)
         L.rn_ao_version.restype = C.c_int

@@ -1,7 +1,7 @@
 """Test configuration: the `gpu` marker and import paths.
 
 Tests marked `gpu` need a GB300 and the built librn_ao.so; everything else runs on a CPU
-host. The oracle (oracle/) is the checker the GPU results are compared against.
+host. The oracle (oracle/) is what the GPU results are compared against.
 """
 import os
 import sys

@@ -55,7 +55,7 @@ def test_oracle_equals_reference_outputs(oracle, table, case):
 
 def synthetic_scene(seed=5, boxes=40):
     """A seeded room of boxes: emissive ceiling quads, metals, rough and smooth dielectrics,
-    a checker texture (power-of-two sizes), smooth normals on a few boxes."""
+    a checkerboard texture (power-of-two sizes), smooth normals on a few boxes."""
     rng = np.random.default_rng(seed)
     pos, nrm, uv, idx, tex = [], [], [], [], []
 
@@ -73,7 +73,7 @@ def synthetic_scene(seed=5, boxes=40):
         tex.extend([t, t])
 
     s = 6.0
-    quad((-s, 0, -s), (-s, 0, s), (s, 0, s), (s, 0, -s), 0)                       # floor (checker)
+    quad((-s, 0, -s), (-s, 0, s), (s, 0, s), (s, 0, -s), 0)                       # floor (checkerboard)
     quad((-s, 4, -s), (s, 4, -s), (s, 4, s), (-s, 4, s), 1)                       # ceiling
     quad((-1, 3.99, -1), (1, 3.99, -1), (1, 3.99, 1), (-1, 3.99, 1), 2)          # lamp, facing down
     quad((-s, 0, -s), (s, 0, -s), (s, 4, -s), (-s, 4, -s), 1)                     # back wall
@@ -88,13 +88,13 @@ def synthetic_scene(seed=5, boxes=40):
         quad((x0, 0, z1), (x0, h, z1), (x1, h, z1), (x1, 0, z1), t)
         quad((x0, 0, z0), (x0, h, z0), (x0, h, z1), (x0, 0, z1), t)
         quad((x1, 0, z0), (x1, 0, z1), (x1, h, z1), (x1, h, z0), t)
-    checker = np.array([0xff3050a0 if ((x // 4 + y // 4) % 2) else 0xffe0e0e0 for y in range(16) for x in range(16)],
+    board = np.array([0xff3050a0 if ((x // 4 + y // 4) % 2) else 0xffe0e0e0 for y in range(16) for x in range(16)],
                        np.uint32)
     white = np.full(16, 0xffffffff, np.uint32)
     rough = np.array([(0xff000000 | int(v)) for v in rng.integers(0, 2 ** 24, 64)], np.uint32)
-    texels = np.concatenate([checker, white, white, rough, white, rough])
+    texels = np.concatenate([board, white, white, rough, white, rough])
     entries = np.array([(0, 16, 16), (256, 4, 4), (272, 4, 4), (288, 8, 8), (352, 4, 4), (368, 8, 8)], np.uint32)
-    materials = np.array([(1.0, 0.7, 0.0, 0.5, 0, 0, 0),          # checker floor
+    materials = np.array([(1.0, 0.7, 0.0, 0.5, 0, 0, 0),          # checkerboard floor
                           (0.8, 0.9, 0.0, 0.3, 0, 0, 0),          # walls
                           (1.0, 1.0, 0.0, 0.0, 8.0, 7.0, 6.0),    # lamp
                           (1.0, 0.3, 1.0, 1.0, 0, 0, 0),          # rough metal
