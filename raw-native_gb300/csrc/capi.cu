@@ -138,6 +138,7 @@ const TuneKey kTuneKeys[] = {
     {"collapse_block", "RN_TUNE_COLLAPSE_BLOCK", &Tune::collapse_block, {0, 16384, 65536, 262144}, 4},
     {"conv_tmem_a", "RN_TUNE_CONV_TMEM_A", &Tune::conv_tmem_a, {0, 1}, 2},
     {"conv_fan", "RN_TUNE_CONV_FAN", &Tune::conv_fan, {0, 1}, 2},
+    {"conv_fan_bn", "RN_TUNE_CONV_FAN_BN", &Tune::conv_fan_bn, {32, 64}, 2},
     {"trace_leaf_pass", "RN_TUNE_TRACE_LEAF_PASS", &Tune::trace_leaf_pass, {0, 1}, 2},
     {"trace_pool_sort", "RN_TUNE_TRACE_POOL_SORT", &Tune::trace_pool_sort, {0, 1}, 2},
 };

@@ -574,17 +574,21 @@ struct HaloArgs {
     int nsrc, C0, C1, cin;
     int B, H, W;
     int chunk, chunks_y;        // output rows per work item; items per strip column
-    int items;                  // (W / 128) x chunks_y x B
-    int stages;                 // row slots in the ring (>= 4)
+    int items;                  // n_slices x slice_items
+    int n_slices, slice_items;  // output-channel slices of BN (fan-out; else 1) and items per slice,
+                                // (W / 128) x chunks_y x B
+    int stages;                 // row slots in the ring (>= 4; fan-out >= 2)
     uint32_t a_bytes, b_bytes;  // one row slot (all sources), the resident weights
     __nv_bfloat16* up16;
 };
 
-// Work item -> (image, strip, first row, rows).
-struct HaloItem { int b, tx, y0, rows; };
+// Work item -> (output-channel slice, image, strip, first row, rows); items run slice by slice.
+struct HaloItem { int slice, b, tx, y0, rows; };
 __device__ __forceinline__ HaloItem halo_item(const HaloArgs& a, int item) {
     const int tiles_x = a.W >> 7;
     HaloItem it;
+    it.slice = item / a.slice_items;
+    item -= it.slice * a.slice_items;
     it.tx = item % tiles_x;
     const int c = (item / tiles_x) % a.chunks_y;
     it.b = item / (tiles_x * a.chunks_y);
@@ -644,9 +648,10 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
     uint8_t* sB = smem;
     uint8_t* sA = smem + ((a.b_bytes + 1023) & ~1023u);
     const uint32_t a_stride = (a.a_bytes + 1023) & ~1023u;
-    // full[kSt], empty[kSt], acc_full[8], acc_empty[8], w
+    // full[kSt], empty[kSt], acc_full[8], acc_empty[8], w (weights landed), wfree (the weights'
+    // last MMAs done: a slice's weights may be replaced)
     uint64_t* bars = reinterpret_cast<uint64_t*>(sA + kSt * a_stride);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 2 * kFanMaxAcc + 1);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSt + 2 * kFanMaxAcc + 2);
     __shared__ int s_abort;
     __shared__ float s_bias[512];       // the bias of every output channel, staged once
     __shared__ FanPlan s_fan[kFanCases][kFanMaxAcc];
@@ -657,6 +662,7 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
     auto acc_full = [&](int b) { return smem_u32(&bars[2 * kSt + b]); };
     auto acc_empty = [&](int b) { return smem_u32(&bars[2 * kSt + kFanMaxAcc + b]); };
     const uint32_t wbar = smem_u32(&bars[2 * kSt + 2 * kFanMaxAcc]);
+    const uint32_t wfree = smem_u32(&bars[2 * kSt + 2 * kFanMaxAcc + 1]);
     // first TMEM column of the accumulator of output row i (counted over the CTA's items)
     auto acc_col = [&](uint32_t i) -> uint32_t { return kFan ? (kAcc - 1u - i % kAcc) * BN : (i % kAcc) * BN; };
 
@@ -664,11 +670,12 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
         for (int s = 0; s < kSt; ++s) { mbar_init(full(s), 1); mbar_init(empty(s), 1); }
         for (int b = 0; b < (int)kAcc; ++b) { mbar_init(acc_full(b), 1); mbar_init(acc_empty(b), 4); }
         mbar_init(wbar, 1);
+        mbar_init(wfree, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         s_abort = 0;
     }
     if (e.bias)
-        for (int i = threadIdx.x; i < BN; i += blockDim.x) s_bias[i] = e.bias[i];
+        for (int i = threadIdx.x; i < a.n_slices * BN; i += blockDim.x) s_bias[i] = e.bias[i];
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(kCols)
@@ -694,8 +701,12 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
     if (warp == 0) {
         if (lane == 0) {
             // loads in ring order: item by item, input rows y0 - 1 .. y0 + rows
+            // the weights of the first item's slice; a later slice's replace them once the MMA
+            // thread reports the last MMAs that read them done (wfree)
+            int wslice = a.items > (int)blockIdx.x ? (int)blockIdx.x / a.slice_items : 0;
+            uint32_t wfree_ph = 0;
             mbar_expect_tx(wbar, a.b_bytes);
-            if (kFan) tma_load_5d(smem_u32(sB), &mapW, 0, 0, 0, 0, 0, wbar);
+            if (kFan) tma_load_5d(smem_u32(sB), &mapW, 0, wslice * BN, 0, 0, 0, wbar);
             else tma_load_3d(smem_u32(sB), &mapW, 0, 0, 0, wbar);
             // kc counts loads; s and ph are its ring slot and the slot's phase (kc % kSt and
             // kc / kSt mod 2, kept by increment: kSt is a launch argument, and a division per
@@ -704,6 +715,17 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
             int s = 0;
             for (int item = blockIdx.x; item < a.items && !*abort_flag; item += gridDim.x) {
                 const HaloItem it = halo_item(a, item);
+                if (kFan && it.slice != wslice) {
+                    if (!mbar_wait_or_abort(wfree, wfree_ph, abort_flag)) {
+                        atomicOr(e.err, DEV_GUARD);
+                        s_abort = 1;
+                        break;
+                    }
+                    wfree_ph ^= 1u;
+                    wslice = it.slice;
+                    mbar_expect_tx(wbar, a.b_bytes);
+                    tma_load_5d(smem_u32(sB), &mapW, 0, wslice * BN, 0, 0, 0, wbar);
+                }
                 for (int r = -1; r <= it.rows && !*abort_flag; ++r, ++kc) {
                     if (!mbar_wait_or_abort(empty(s), ph ^ 1u, abort_flag)) {
                         atomicOr(e.err, DEV_GUARD);
@@ -719,7 +741,7 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
             }
             // the copies this lane issued must land before the CTA can leave
             for (uint32_t k = kc > (uint32_t)kSt ? kc - kSt : 0; k < kc; ++k) mbar_wait(full(k % kSt), (k / kSt) & 1u);
-            mbar_wait(wbar, 0);
+            mbar_wait(wbar, wfree_ph);      // the last weights load (one more than the reloads)
         }
     } else if (warp == 1 && kFan) {
         // The MMAs of a load depend only on which of its three output rows exist (the load's
@@ -754,6 +776,8 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
             const uint64_t dq_b = (2u * b_grp) >> 4;                      // ... of B
             const uint64_t dx_b = ((uint32_t)G * b_grp) >> 4;             // the next horizontal tap of B
             bool ok = mbar_wait_or_abort(wbar, 0, abort_flag);
+            int wslice = a.items > (int)blockIdx.x ? (int)blockIdx.x / a.slice_items : 0;
+            uint32_t w_ph = 0;
             uint32_t i0 = 0;            // output rows of earlier items
             // the current load's ring slot, its phase and its shared-memory row (kept by increment)
             int slot = 0;
@@ -762,6 +786,13 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
             // no offset here carries out of it): every MMA is a base descriptor plus a constant.
             for (int item = blockIdx.x; ok && item < a.items && !*abort_flag; item += gridDim.x) {
                 const HaloItem it = halo_item(a, item);
+                if (it.slice != wslice) {
+                    // the next slice's weights: once this slice's MMAs have read theirs
+                    tc_commit(wfree);
+                    w_ph ^= 1u;
+                    if (!mbar_wait_or_abort(wbar, w_ph, abort_flag)) { ok = false; break; }
+                    wslice = it.slice;
+                }
                 // load k is input row y0 - 1 + k; it feeds output rows k - 2 .. k of the item
                 for (int k = 0; ok && k <= it.rows + 1; ++k) {
                     const int lo = max(0, k - 2) - k, hi = min(it.rows - 1, k) - k;
@@ -953,6 +984,7 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
                 const int y = it.y0 + j, x = it.tx * 128 + r;
                 const size_t pix = ((size_t)it.b * a.H + y) * a.W + x;
                 const uint32_t tbase = tmem + acc_col(i) + ((uint32_t)(q * 32) << 16);
+                const int n0 = it.slice * BN;                  // the item's first output channel
                 float hz = e.head_out ? e.head_b[0] : 0.0f;
                 // the row's BN columns in one TMEM load and one wait
                 uint32_t vv[BN];
@@ -968,7 +1000,7 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
 #pragma unroll
                     for (int jj = 0; jj < 16; ++jj) {
                         float t = __uint_as_float(v[jj]);
-                        if (e.bias) t += s_bias[c0 + jj];
+                        if (e.bias) t += s_bias[n0 + c0 + jj];
                         if (e.relu) t = fmaxf(t, 0.0f);
                         f[jj] = t;
                     }
@@ -976,7 +1008,7 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
 #pragma unroll
                         for (int jj = 0; jj < 16; ++jj)
                             hz += __bfloat162float(__float2bfloat16_rn(f[jj])) * e.head_w[c0 + jj];
-                    const size_t o = pix * e.ldc + c0;
+                    const size_t o = pix * e.ldc + n0 + c0;
                     if (e.c16) {
                         uint4 out[2];
                         __nv_bfloat16* ob = reinterpret_cast<__nv_bfloat16*>(out);
@@ -1003,7 +1035,7 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
 #pragma unroll 1
                     for (int k = 0; k < kCh; ++k) {
                         const int idx = k * 32 + lane, p = idx / kCh, c = idx % kCh;
-                        *reinterpret_cast<uint4*>(e.c16 + (pix0 + p) * e.ldc + c * 8) = stage[slot(p, c)];
+                        *reinterpret_cast<uint4*>(e.c16 + (pix0 + p) * e.ldc + n0 + c * 8) = stage[slot(p, c)];
                     }
                     if (a.up16) {
                         // rows 2y and 2y + 1 of the 2x copy: 64 pixels, each source pixel twice
@@ -1012,8 +1044,8 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
                         for (int k = 0; k < 2 * kCh; ++k) {
                             const int idx = k * 32 + lane, P = idx / kCh, c = idx % kCh;
                             const uint4 v = stage[slot(P >> 1, c)];
-                            *reinterpret_cast<uint4*>(a.up16 + (up0 + P) * e.ldc + c * 8) = v;
-                            *reinterpret_cast<uint4*>(a.up16 + (up0 + 2 * a.W + P) * e.ldc + c * 8) = v;
+                            *reinterpret_cast<uint4*>(a.up16 + (up0 + P) * e.ldc + n0 + c * 8) = v;
+                            *reinterpret_cast<uint4*>(a.up16 + (up0 + 2 * a.W + P) * e.ldc + n0 + c * 8) = v;
                         }
                     }
                     __syncwarp();                                         // the stage is free again
@@ -1137,13 +1169,13 @@ bool make_map_wgroups(CUtensorMap* m, const void* base, int N, int ldw, int kgro
 
 // The resident weights in the fan-out order: a 5-D view (8 columns, N rows, vertical tap dy,
 // channel group, horizontal tap dx) of the [N][ldw] matrix whose column is
-// (3 dy + dx) cin + channel, one box of all of it: shared memory [dx][group][dy][n][8].
-bool make_map_wfan(CUtensorMap* m, const void* base, int N, int ldw, int cin) {
+// (3 dy + dx) cin + channel, one box of a slice of bn rows: shared memory [dx][group][dy][n][8].
+bool make_map_wfan(CUtensorMap* m, const void* base, int N, int ldw, int cin, int bn) {
     auto fn = encoder();
     if (!fn) return false;
     const cuuint64_t dims[5] = {8, (cuuint64_t)N, 3, (cuuint64_t)(cin / 8), 3};
     const cuuint64_t strides[4] = {(cuuint64_t)ldw * 2, (cuuint64_t)cin * 6, 16, (cuuint64_t)cin * 2};
-    const cuuint32_t box[5] = {8, (cuuint32_t)N, 3, (cuuint32_t)(cin / 8), 3};
+    const cuuint32_t box[5] = {8, (cuuint32_t)bn, 3, (cuuint32_t)(cin / 8), 3};
     const cuuint32_t elem[5] = {1, 1, 1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<void*>(base), dims, strides, box, elem,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -1255,36 +1287,52 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
     if (N % bn || N > 512) return fail(st, RN_ERR_INVALID, "tc_conv3x3 N %d", N);
     while (bn > ctx().tune.conv_bn_max && bn > 32) bn /= 2;
     if (up16 && !epi.c16) return fail(st, RN_ERR_INVALID, "tc_conv3x3: the upsampled copy needs a BF16 output");
-    // row-ring tiles: rows of 128 pixels, channels in groups of 16, N 32 or 64 in one slice,
-    // the weights and a ring of at least four row slots in shared memory. Sources of 16
-    // channels have only this kernel (the per-tap boxes take 32 or 64 channels).
-    if ((ctx().tune.conv_halo || !all32) && t.tw_log2 == 7 && (N == 32 || N == 64) && (9 * cin) / 8 <= 256 &&
-        cin % 16 == 0) {
-        const uint32_t b_bytes = (uint32_t)N * 9 * cin * 2;
+    // row-ring tiles: rows of 128 pixels, channels in groups of 16, the weights resident in
+    // shared memory. Row by row (conv_fan 0, conv_tmem_a): N 32 or 64 in one slice and a ring of
+    // at least four row slots. Fan-out (conv_fan 1): N 32 or 64 in one slice where that fits,
+    // else slices of 32 output channels (N a multiple of 32 up to 512), at least two slots, and
+    // two CTAs per SM where shared memory allows, one otherwise. Sources of 16 channels have
+    // only this kernel (the per-tap boxes take 32 or 64 channels).
+    const bool ta = ctx().tune.conv_tmem_a && N == 32 && cin <= 32;
+    const bool fan = !ta && ctx().tune.conv_fan;
+    const bool ring_shape = t.tw_log2 == 7 && (9 * cin) / 8 <= 256 && cin % 16 == 0;
+    const bool one_slice = N == 32 || N == 64;
+    if ((ctx().tune.conv_halo || !all32) && ring_shape && (one_slice || (fan && N % 32 == 0 && N <= 512))) {
         const uint32_t a_bytes = (uint32_t)cin / 8 * tc::kHaloGroup;
-        const uint32_t a_stride = (a_bytes + 1023) & ~1023u, b_pad = (b_bytes + 1023) & ~1023u;
-        // dynamic shared memory: 227 KB a block less the kernel's static arrays (the bias,
-        // the abort flag and the epilogue's BF16 stage of 4 x 32 pixels x N channels)
-        const size_t stat = tc::halo_static_smem(N);
-        const size_t budget = 220 * 1024 - stat;
-        int stages = (int)std::min<size_t>(8, (budget - std::min<size_t>(budget, b_pad + 2048)) / a_stride);
-        // A operands in TMEM for 32 output channels and at most 32 input channels; else
-        // (conv_fan) each input row's MMAs feeding its three output rows at once
-        const bool ta = ctx().tune.conv_tmem_a && N == 32 && cin <= 32;
-        const bool fan = !ta && ctx().tune.conv_fan;
-        // fan-out: a row slot is busy only until its own MMAs have run; four slots at most (4,
-        // 6 and 8 measured alike), and no more than leave shared memory for fan_ctas(N) CTAs
-        // per SM (228 KB less 1 KB reserved each), at least two
-        if (fan) {
-            const size_t per_cta = 228 * 1024 / tc::fan_ctas(N) - 1024 - stat;
-            const int fit = (int)((per_cta - std::min<size_t>(per_cta, b_pad + 2048)) / a_stride);
-            stages = std::min(stages, std::max(2, std::min(fit, 4)));
+        const uint32_t a_stride = (a_bytes + 1023) & ~1023u;
+        const size_t bars = (size_t)(2 * 8 + 2 * tc::kFanMaxAcc + 2) * 8 + 16;
+        int bn = one_slice && (N == 32 || !fan || ctx().tune.conv_fan_bn == 64) ? N : 32, stages = 0;
+        uint32_t b_bytes = 0, b_pad = 0;
+        auto fit = [&](int bnf) {
+            b_bytes = (uint32_t)bnf * 9 * cin * 2;
+            b_pad = (b_bytes + 1023) & ~1023u;
+            const size_t stat = tc::halo_static_smem(bnf);
+            if (!fan) {
+                // dynamic shared memory: 227 KB a block less the kernel's static arrays (the
+                // bias, the abort flag and the epilogue's BF16 stage of 4 x 32 pixels x N)
+                const size_t budget = 220 * 1024 - stat;
+                return (int)std::min<size_t>(8, (budget - std::min<size_t>(budget, b_pad + 2048)) / a_stride);
+            }
+            // fan-out: a slot is busy only until its own MMAs have run: four at most (4, 6 and 8
+            // measured alike); two CTAs per SM (228 KB less 1 KB reserved each) where two slots
+            // fit, else one CTA with the whole 227 KB of a block
+            const size_t fixed = stat + 1024 + bars + b_pad;
+            for (const size_t cta : {(size_t)228 * 1024 / 2 - 1024, (size_t)227 * 1024}) {
+                const size_t room = cta > fixed ? (cta - fixed) / a_stride : 0;
+                if (room >= 2) return (int)std::min<size_t>(4, room);
+            }
+            return 0;
+        };
+        stages = fit(bn);
+        if (fan && bn == 64 && stages < 2) {
+            bn = 32;
+            stages = fit(bn);
         }
         CUtensorMap hm[2], hw;
-        bool maps = stages >= (fan ? 2 : 4);
+        bool maps = stages >= (fan ? 2 : 4) && (fan || one_slice);
         for (int i = 0; maps && i < nsrc; ++i) maps = tc::make_map_halo(&hm[i], src[i].ptr, B, H, W, src[i].C);
         if (maps && nsrc == 1) hm[1] = hm[0];
-        maps = maps && (fan ? tc::make_map_wfan(&hw, w, N, ldw, cin) : tc::make_map_wgroups(&hw, w, N, ldw, 9 * cin / 8));
+        maps = maps && (fan ? tc::make_map_wfan(&hw, w, N, ldw, cin, bn) : tc::make_map_wgroups(&hw, w, N, ldw, 9 * cin / 8));
         if (maps) {
             tc::HaloArgs h{};
             h.nsrc = nsrc; h.C0 = src[0].C; h.C1 = nsrc > 1 ? src[1].C : 0; h.cin = cin;
@@ -1294,14 +1342,16 @@ int tc_conv3x3(const tc::ConvSrc* src, int nsrc, int B, int H, int W, const __nv
             h.chunk = 16;
             while (h.chunk > 4 && (long)(W / 128) * B * ((H + h.chunk - 1) / h.chunk) < 2L * ctx().sm_count) h.chunk /= 2;
             h.chunks_y = (H + h.chunk - 1) / h.chunk;
-            h.items = (W / 128) * h.chunks_y * B;
+            h.n_slices = N / bn;
+            h.slice_items = (W / 128) * h.chunks_y * B;
+            h.items = h.n_slices * h.slice_items;
             h.stages = stages;
             h.a_bytes = a_bytes; h.b_bytes = b_bytes;
             h.up16 = up16;
-            const size_t smem = 1024 + b_pad + (size_t)stages * a_stride + (2 * stages + 2 * tc::kFanMaxAcc + 1) * 8 + 16;
+            const size_t smem = 1024 + b_pad + (size_t)stages * a_stride + bars;
             const int rc = ta    ? tc::launch_conv_halo<32, true, false>(hm[0], hm[1], hw, h, epi, smem, s)
-                         : fan   ? (N == 32 ? tc::launch_conv_halo<32, false, true>(hm[0], hm[1], hw, h, epi, smem, s)
-                                            : tc::launch_conv_halo<64, false, true>(hm[0], hm[1], hw, h, epi, smem, s))
+                         : fan   ? (bn == 32 ? tc::launch_conv_halo<32, false, true>(hm[0], hm[1], hw, h, epi, smem, s)
+                                             : tc::launch_conv_halo<64, false, true>(hm[0], hm[1], hw, h, epi, smem, s))
                          : N == 32 ? tc::launch_conv_halo<32, false, false>(hm[0], hm[1], hw, h, epi, smem, s)
                                    : tc::launch_conv_halo<64, false, false>(hm[0], hm[1], hw, h, epi, smem, s);
             if (rc != RN_OK) return cuda_fail(st, cudaGetLastError(), "tc_conv_halo_kernel");

@@ -69,6 +69,7 @@ struct Tune {
     int trace_leaf_pass = 1;    // traversal: a node's leaf children tested in one loop after its slab tests
     int conv_tmem_a = 0;        // row-ring convolutions of 32 -> 32 or 16 -> 32 channels: A operands kept in TMEM
     int conv_fan = 1;           // row-ring convolutions: each input row's MMAs feed its three output rows (N = 3 x BN)
+    int conv_fan_bn = 64;       // ... widest output-channel slice: 64 (where its weights fit, else 32) or 32
     int ploc_tail = 4096;       // PLOC: the rounds from this many clusters on run in one launch (0: never)
     int ploc_tail_ctas = 1;     // ... in one block (1) or one thread-block cluster of this many CTAs
     int ploc_fused = 1;         // PLOC: a round's prefix sum and scatter in one launch (decoupled look-back)

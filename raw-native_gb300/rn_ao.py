@@ -197,7 +197,7 @@ TUNE_KEYS = {"trace_min_blocks": (2, 3, 4), "batch_min_blocks": (2, 3, 4), "trac
              "trace_pool": (0, 16, 24, 32), "ploc_tail": (0, 4096, 16384, 32768, 65536, 262144),
              "ploc_tail_ctas": (1, 4, 8, 16), "ploc_fused": (0, 1),
              "collapse_block": (0, 16384, 65536, 262144),
-             "conv_tmem_a": (0, 1), "conv_fan": (0, 1), "trace_leaf_pass": (0, 1),
+             "conv_tmem_a": (0, 1), "conv_fan": (0, 1), "conv_fan_bn": (32, 64), "trace_leaf_pass": (0, 1),
              "trace_pool_sort": (0, 1)}
 
 

@@ -118,12 +118,18 @@ def test_conv_halo_tiles_match_the_general_kernel(rn, B, H, W, c0, c1, N):
 @pytest.mark.parametrize("B,H,W,c0,c1,N", [(2, 8, 128, 32, 0, 32), (1, 6, 256, 32, 0, 64), (1, 4, 1920, 16, 0, 32),
                                             (2, 8, 128, 32, 32, 32), (1, 5, 384, 64, 0, 64), (1, 1, 128, 32, 0, 32),
                                             (1, 2, 128, 16, 0, 64), (1, 37, 256, 32, 0, 32), (2, 70, 128, 32, 64, 32),
-                                            (1, 333, 1920, 32, 0, 64), (3, 19, 640, 32, 16, 64)])
+                                            (1, 333, 1920, 32, 0, 64), (3, 19, 640, 32, 16, 64),
+                                            # output channels in slices of 32 (the weights of a
+                                            # 64-wide slice do not fit; N beyond 64)
+                                            (1, 8, 128, 128, 64, 64), (1, 37, 384, 128, 64, 64),
+                                            (1, 6, 256, 64, 0, 128), (2, 9, 128, 32, 32, 256)])
 def test_conv_fan_matches_row_by_row(rn, B, H, W, c0, c1, N):
     """Fan-out MMAs (conv_fan 1: one MMA of N = 3 x BN per input row, shift and channel step,
     feeding the three output rows that read the row) against the row-by-row MMAs (conv_fan 0):
     identical FP32 and BF16 outputs, bias, ReLU and the upsampled copy included, on frames of
-    1 to 333 rows (items of 1 to 16 rows: the accumulator ring wraps inside an MMA)."""
+    1 to 333 rows (items of 1 to 16 rows: the accumulator ring wraps inside an MMA). Shapes the
+    row-by-row form cannot take (weights too large, N beyond 64) compare with the per-tap
+    kernel, whose K steps run in the same order (tap, then channel)."""
     import torch
     saved = (rn.tune_get("conv_fan"), rn.tune_get("conv_halo"))
     try:
@@ -150,3 +156,33 @@ def test_conv_fan_matches_row_by_row(rn, B, H, W, c0, c1, N):
     finally:
         rn.tune_set("conv_fan", saved[0])
         rn.tune_set("conv_halo", saved[1])
+
+
+@pytest.mark.parametrize("B,H,W,c0,c1,N", [(1, 8, 128, 32, 0, 64), (2, 21, 256, 64, 0, 64), (1, 5, 384, 32, 32, 64)])
+def test_conv_fan_slices_of_32_match(rn, B, H, W, c0, c1, N):
+    """64-channel layers as two 32-channel slices (conv_fan_bn 32: each CTA reloads the weights
+    when its items cross into the next slice) give the 64-wide fan-out's outputs bit for bit."""
+    import torch
+    saved = (rn.tune_get("conv_fan"), rn.tune_get("conv_fan_bn"))
+    try:
+        rn.tune_set("conv_fan", 1)
+        g = torch.Generator(device="cuda").manual_seed(11 * B + H + W + c0 + c1 + N)
+        x0 = torch.randn(B, H, W, c0, device="cuda", generator=g).to(torch.bfloat16)
+        x1 = torch.randn(B, H, W, c1, device="cuda", generator=g).to(torch.bfloat16) if c1 else None
+        cin = c0 + c1
+        ldw = (9 * cin + 127) // 128 * 128
+        w = torch.zeros(N, ldw, device="cuda", dtype=torch.bfloat16)
+        w[:, :9 * cin] = (torch.randn(N, 9 * cin, device="cuda", generator=g) / (9 * cin) ** 0.5).to(torch.bfloat16)
+        bias = torch.randn(N, device="cuda", generator=g)
+        outs = []
+        for bn in (64, 32):
+            rn.tune_set("conv_fan_bn", bn)
+            o, u = rn.tc_conv3x3(x0, w, x1, bias=bias, relu=True, upsampled=True)
+            f = rn.tc_conv3x3(x0, w, x1, bias=bias, relu=False)
+            torch.cuda.synchronize()
+            outs.append((o.clone(), u.clone(), f.clone()))
+        for a, b in zip(*outs):
+            assert torch.equal(a, b), int((a != b).sum().item())
+    finally:
+        rn.tune_set("conv_fan", saved[0])
+        rn.tune_set("conv_fan_bn", saved[1])

@@ -138,7 +138,8 @@ def test_conv_fan_keeps_every_bit(rn, restore_tune):
     three output rows that read it, N = 3 x 32 or 3 x 64) give the same network output bit for
     bit: every output row still starts with its first K16 step and adds the other steps in
     the same tap and channel order. Frames of several heights (items of 1 to 16 rows, so the
-    accumulator ring wraps inside MMAs and crosses item boundaries), batch 2."""
+    accumulator ring wraps inside MMAs and crosses item boundaries), batch 2; also with every
+    fan-out layer in 32-channel slices (conv_fan_bn 32)."""
     import torch
     g = torch.Generator(device="cuda").manual_seed(4)
     for H, W in ((64, 128), (144, 256), (1088, 1920)):
@@ -147,8 +148,11 @@ def test_conv_fan_keeps_every_bit(rn, restore_tune):
         rn.tune_set("conv_fan", 0)
         ref = net.forward(x).clone()
         rn.tune_set("conv_fan", 1)
-        got = net.forward(x)
-        assert bool((got == ref).all()), (H, W, int((got != ref).sum().item()))
+        for bn in (64, 32):
+            rn.tune_set("conv_fan_bn", bn)
+            got = net.forward(x)
+            assert bool((got == ref).all()), (H, W, bn, int((got != ref).sum().item()))
+        rn.tune_set("conv_fan_bn", 64)
         net.close()
 
 
