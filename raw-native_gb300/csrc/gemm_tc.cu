@@ -582,13 +582,16 @@ struct HaloArgs {
     __nv_bfloat16* up16;
 };
 
-// Work item -> (output-channel slice, image, strip, first row, rows); items run slice by slice.
+// Work item -> (output-channel slice, image, strip, first row, rows). The slices of one strip
+// chunk are consecutive items: with a grid that is a multiple of the slice count every CTA
+// keeps one slice (its weights load once), and the CTAs that hold a chunk's slices read its
+// input rows at about the same time, so the second read finds them in L2.
 struct HaloItem { int slice, b, tx, y0, rows; };
 __device__ __forceinline__ HaloItem halo_item(const HaloArgs& a, int item) {
     const int tiles_x = a.W >> 7;
     HaloItem it;
-    it.slice = item / a.slice_items;
-    item -= it.slice * a.slice_items;
+    it.slice = item % a.n_slices;
+    item /= a.n_slices;
     it.tx = item % tiles_x;
     const int c = (item / tiles_x) % a.chunks_y;
     it.b = item / (tiles_x * a.chunks_y);
@@ -703,7 +706,7 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
             // loads in ring order: item by item, input rows y0 - 1 .. y0 + rows
             // the weights of the first item's slice; a later slice's replace them once the MMA
             // thread reports the last MMAs that read them done (wfree)
-            int wslice = a.items > (int)blockIdx.x ? (int)blockIdx.x / a.slice_items : 0;
+            int wslice = (int)blockIdx.x % a.n_slices;
             uint32_t wfree_ph = 0;
             mbar_expect_tx(wbar, a.b_bytes);
             if (kFan) tma_load_5d(smem_u32(sB), &mapW, 0, wslice * BN, 0, 0, 0, wbar);
@@ -776,7 +779,7 @@ __global__ void __launch_bounds__(kConvThreads, kFan ? fan_ctas(BN) : 1) tc_conv
             const uint64_t dq_b = (2u * b_grp) >> 4;                      // ... of B
             const uint64_t dx_b = ((uint32_t)G * b_grp) >> 4;             // the next horizontal tap of B
             bool ok = mbar_wait_or_abort(wbar, 0, abort_flag);
-            int wslice = a.items > (int)blockIdx.x ? (int)blockIdx.x / a.slice_items : 0;
+            int wslice = (int)blockIdx.x % a.n_slices;
             uint32_t w_ph = 0;
             uint32_t i0 = 0;            // output rows of earlier items
             // the current load's ring slot, its phase and its shared-memory row (kept by increment)
